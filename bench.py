@@ -1,0 +1,288 @@
+"""Benchmark of the Kohn-Sham XC build on one GB300 (one JSON line on stdout).
+
+Workload: cyclo[18]carbon, restricted B3LYP / def2-TZVP (558 functions),
+SG-2 grid (140 220 points, 2048 blocks).  A step is one XC build: density
+(rho, grad rho) -> B3LYP functional -> E_xc -> V_xc, on an SCF-shaped
+density matrix resident in HBM.  Synthetic geometry and density (seeded).
+
+  python bench.py [--steps K] [--warmup W] [--precision fp64|mixed]
+  python bench.py --impl reference   # the CPU XC path (oracle port of the
+                                     # reference's per-block einsum loops)
+
+Under torchrun (N > 1) every rank runs an independent replica of the same
+build (the path does not need a collective: replicas only).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "XC grid-pts/s (one B3LYP/def2-TZVP XC build of C18 on SG-2)"
+UNIT = "grid-points/s"
+
+
+def workload():
+    from chinium_gb300 import molecules as M
+    Z, xyz = M.c18()
+    return dict(name="C18 RKS B3LYP/def2-TZVP SG-2", Z=Z, xyz=xyz, basis="def2-tzvp", grid="SG-2",
+                functional="B3LYP", ids=[402], nocc=54)
+
+
+def model_density(nbasis, nocc, seed=0):
+    """Closed-shell SCF-shaped total density 2 C C^T from random orthonormal
+    orbitals mixed onto a diagonal occupation profile (keeps rho > 0)."""
+    rng = np.random.default_rng(seed)
+    A = rng.normal(size=(nbasis, nocc)) * 0.05
+    A[np.arange(nocc), np.arange(nocc)] += 1.0
+    Q, _ = np.linalg.qr(A)
+    return 2.0 * Q @ Q.T
+
+
+def clocks_start(path):
+    try:
+        f = open(path, "w")
+        p = subprocess.Popen(
+            ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+             "--format=csv,noheader,nounits", "-lms", "200"], stdout=f, stderr=subprocess.DEVNULL)
+        return p, f
+    except Exception:
+        return None, None
+
+
+def clocks_stop(p, f, path):
+    if p is None:
+        return None
+    p.terminate()
+    try:
+        p.wait(timeout=5)
+    except Exception:
+        p.kill()
+    f.close()
+    rows = []
+    for ln in open(path):
+        t = [x.strip() for x in ln.split(",")]
+        if len(t) >= 9:
+            try:
+                rows.append((float(t[1]), float(t[2]), t[5:9]))
+            except ValueError:
+                pass
+    if not rows:
+        return None
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    reasons = sorted({names[i] for _, _, r in rows for i, v in enumerate(r) if v.lower() == "active"})
+    return {"sm_mhz": float(np.median([r[0] for r in rows])), "sm_max_mhz": max(r[1] for r in rows),
+            "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
+def fp64_gemm_peak(torch):
+    """cuBLAS DGEMM throughput (TFLOP/s), the FP64 denominator of the plain path."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        a @ b
+    torch.cuda.synchronize()
+    best = 1e30
+    for _ in range(3):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        a @ b
+        e.record()
+        e.synchronize()
+        best = min(best, s.elapsed_time(e) / 1e3)
+    return 2 * n ** 3 / best / 1e12
+
+
+def cpu_baseline(wl, D, sample_blocks, threads):
+    """The oracle (CPU restatement of the reference's per-block einsum loops,
+    OpenMP) on the first sample_blocks blocks of the same workload."""
+    from oracle import oracle as O
+    basis = O.Basis(wl["Z"], wl["xyz"], wl["basis"])
+    px, py, pz, w = O.grid_points(wl["Z"], wl["xyz"], wl["grid"])
+    blocks = O.padded_blocks(px, py, pz, w)[:sample_blocks]
+
+    class G:
+        pass
+
+    g = O.OracleGrid.__new__(O.OracleGrid)
+    g.basis = basis
+    g.blocks = blocks
+    g.ao = [basis.ao(b[0], b[1], b[2], 1) for b in blocks]
+    g.npoints = sum(len(b[0]) for b in blocks)
+    npts = sum(int((b[3] != 0).sum()) for b in blocks)
+    g.build([D], wl["ids"], 1, nblocks=1, nthreads=threads)  # warm
+    t = time.perf_counter()
+    g.build([D], wl["ids"], 1, nthreads=threads)
+    dt = time.perf_counter() - t
+    npad = sum(len(b[0]) for b in blocks)
+    return {"value": npad / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "%d of 2048 blocks (%d padded points), one build, %.2f s" % (len(blocks), npad, dt)}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    wl = workload()
+    import chinium_gb300 as cg  # basis size only (host side)
+    nb = cg.Basis(wl["Z"], wl["xyz"], wl["basis"]).nbasis
+    D = model_density(nb, wl["nocc"])
+    threads = os.cpu_count() or 1
+    vals = []
+    for i in range(args.warmup + args.steps):
+        cb = cpu_baseline(wl, D, args.cpu_blocks, threads)
+        if i >= args.warmup:
+            vals.append(cb["value"])
+    v = float(np.median(vals))
+    cb["value"] = v
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 147456 / v * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": wl["name"], "sample_blocks": args.cpu_blocks},
+            "cpu_baseline": cb, "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--cpu-blocks", type=int, default=96)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    import chinium_gb300 as cg
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+
+    wl = workload()
+    basis = cg.Basis(wl["Z"], wl["xyz"], wl["basis"])
+    n = basis.nbasis
+    grid = cg.Grid(basis, wl["grid"], nspin=1, screen_threshold=0.0)
+    xc = cg.ExchangeCorrelation().Read(wl["functional"])
+    grid.setType(xc.type)
+    grid.getAO(0)
+    info = grid.info()
+    stream = torch.cuda.Stream()
+    grid.set_stream(stream.cuda_stream)
+    precision = cg.PRECISION_FP64 if args.precision == "fp64" else cg.PRECISION_MIXED
+
+    D = model_density(n, wl["nocc"])
+    dD = torch.from_numpy(np.ascontiguousarray(D.T)).cuda()
+    dE = torch.zeros(1, dtype=torch.float64, device="cuda")
+    dV = torch.zeros((n, n), dtype=torch.float64, device="cuda")
+
+    for _ in range(args.warmup):
+        grid.build_device(xc, dD, dE, dV, precision)
+    stream.synchronize()
+
+    # stage timing of one build (CUDA events on the build stream)
+    grid.profile(True)
+    grid.build_device(xc, dD, dE, dV, precision)
+    stage = grid.stage_ms()
+    grid.profile(False)
+
+    clk_path = os.path.join(REPO, "gpurun_out" if os.path.isdir(os.path.join(REPO, "gpurun_out")) else "_work", "clocks_bench.csv")
+    os.makedirs(os.path.dirname(clk_path), exist_ok=True)
+    cp, cf = clocks_start(clk_path) if rank == 0 else (None, None)
+    time.sleep(0.4)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        grid.build_device(xc, dD, dE, dV, precision)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    t_dev = ev0.elapsed_time(ev1) / 1e3
+    t = torch.tensor([t_dev], dtype=torch.float64, device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    t_dev = float(t.item())
+    clocks = clocks_stop(cp, cf, clk_path) if rank == 0 else None
+
+    # end to end through the public host-buffer call: pinned D in, E and V out
+    Dh = torch.from_numpy(np.ascontiguousarray(D)).pin_memory()
+    Vh = torch.zeros((n, n), dtype=torch.float64).pin_memory()
+    import ctypes
+    from chinium_gb300._lib import check, lib
+    Eh = ctypes.c_double()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        check(lib().xc_build(grid._h, xc._h, ctypes.c_void_p(Dh.data_ptr()), 1, precision, ctypes.byref(Eh),
+                             ctypes.c_void_p(Vh.data_ptr())))
+    torch.cuda.synchronize()
+    t_e2e = time.perf_counter() - t0
+
+    G = info["npoints_padded"]
+    value = world * G * args.steps / t_dev
+    e2e = world * G * args.steps / t_e2e
+    Exc = float(dE.item())
+
+    # roofline of the dominant stage (density or V assembly): FP64 FLOPs
+    # 2 g n_b^2 per block and contraction, over the stage's event time
+    flops_ctr = 2.0 * info["screened_pairs"] * (G / info["nblocks"])  # per contraction, all blocks
+    ms_den, ms_fock = stage[0], stage[3]
+    dom = "fock" if ms_fock >= ms_den else "density"
+    dom_ms = max(ms_den, ms_fock)
+    flops = flops_ctr * (1.0 if dom == "density" else 1.0)
+    peak = fp64_gemm_peak(torch)
+    achieved = flops / (dom_ms / 1e3) / 1e12
+    roof = {"bound": "fp64", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak, "traffic": None,
+            "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (MEASURED_PEAKS.json has no FP64 entry)",
+            "stage_ms": {"density": stage[0], "functional": stage[1], "energy": stage[2], "fock": stage[3]}}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_dev / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "bf16x3+f64",
+            "data": "synthetic",
+            "config": {"workload": wl["name"], "precision": args.precision, "npoints": info["npoints"],
+                       "npoints_padded": G, "nblocks": info["nblocks"], "nbasis": n,
+                       "l2": "inputs larger than L2 (AO store %.2f GB)" % (info["ao_elements"] * 4 * 8 / 1e9),
+                       "E_xc": Exc},
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 8 * n * n, "d2h_bytes_per_step": 8 * n * n + 8},
+            "gpu_launches": args.steps * 5,
+            "roofline": roof, "clocks": clocks}
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(wl, D, args.cpu_blocks, os.cpu_count() or 1)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

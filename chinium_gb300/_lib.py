@@ -1,0 +1,117 @@
+"""ctypes binding of the C ABI in include/chinium_xc.h.
+
+The library is built in-tree (``chinium_gb300/_build/libchinium_xc.so``).  A
+missing or unloadable library is an error: there is no fallback path.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libchinium_xc.so")
+DATA_PATH = os.path.join(HERE, "data")
+
+XC_OK = 0
+STATUS = {
+    -1: "XC_ERR_ARG", -2: "XC_ERR_IO", -3: "XC_ERR_CUDA", -4: "XC_ERR_STATE", -5: "XC_ERR_NOMEM",
+    -6: "XC_ERR_UNSUPPORTED", -7: "XC_ERR_NUMERIC", -8: "XC_ERR_TIMEOUT", -9: "XC_ERR_INTERNAL",
+}
+PRECISION_FP64 = 0
+PRECISION_MIXED = 1
+
+
+class XCError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s: %s" % (STATUS.get(code, code), msg))
+        self.code = code
+
+
+class GridInfo(ctypes.Structure):
+    _fields_ = [("npoints", ctypes.c_long), ("npoints_padded", ctypes.c_long), ("nblocks", ctypes.c_int),
+                ("nbasis", ctypes.c_int), ("nspin", ctypes.c_int), ("type", ctypes.c_int),
+                ("ao_elements", ctypes.c_long), ("screened_pairs", ctypes.c_long)]
+
+
+_P = ctypes.c_void_p
+_I = ctypes.c_int
+_D = ctypes.c_double
+_L = ctypes.c_long
+_S = ctypes.c_char_p
+_PP = ctypes.POINTER(ctypes.c_void_p)
+
+SIGNATURES = {
+    "xc_last_error": [_P, ctypes.c_size_t],
+    "xc_set_data_path": [_S],
+    "xc_basis_create": [_I, _P, _P, _S, _PP],
+    "xc_basis_nbasis": [_P, _P],
+    "xc_basis_nshells": [_P, _P],
+    "xc_basis_shells": [_P, _P, _P, _P, _P],
+    "xc_basis_primitives": [_P, _P, _P],
+    "xc_basis_destroy": [_P],
+    "xc_grid_create": [_P, _S, _I, _D, _PP],
+    "xc_grid_destroy": [_P],
+    "xc_grid_set_stream": [_P, _P],
+    "xc_grid_set_type": [_P, _I],
+    "xc_grid_get_ao": [_P, _I],
+    "xc_grid_num_electrons": [_P, _P],
+    "xc_grid_get_density": [_P, _P, _I],
+    "xc_grid_get_energy": [_P, _P],
+    "xc_grid_get_fock": [_P, _P],
+    "xc_grid_info_get": [_P, _P],
+    "xc_grid_points": [_P, _P, _P, _P, _P, _P, _P, _P, _P],
+    "xc_grid_density_values": [_P, _P, _P, _P, _P],
+    "xc_grid_potential_values": [_P, _P, _P, _P, _P],
+    "xc_grid_block_ao": [_P, _I, _P, _P, _P],
+    "xc_functional_read": [_S, _I, _PP],
+    "xc_functional_create": [_P, _I, _I, _PP],
+    "xc_functional_destroy": [_P],
+    "xc_functional_exx": [_P, _P],
+    "xc_functional_family": [_P, _P],
+    "xc_evaluate": [_P, _P, _S],
+    "xc_functional_eval_points": [_P, _L, _P, _P, _P, _P, _P, _P, _P],
+    "xc_build": [_P, _P, _P, _I, _I, _P, _P],
+    "xc_build_device": [_P, _P, _P, _I, _I, _P, _P],
+    "xc_sap_fock": [_P, _P],
+    "xc_grid_profile": [_P, _I],
+    "xc_grid_stage_ms": [_P, _P],
+}
+
+_lib = None
+
+
+def header_symbols():
+    """Function names declared in include/chinium_xc.h."""
+    import re
+    path = os.path.join(os.path.dirname(HERE), "include", "chinium_xc.h")
+    with open(path) as f:
+        txt = f.read()
+    return sorted(set(re.findall(r"^int\s+(xc_\w+)\s*\(", txt, flags=re.M)))
+
+
+def lib():
+    """Load the library (building it first if absent).  Raises on failure."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        from . import build as _build
+        _build.build()
+    L = ctypes.CDLL(LIB_PATH)
+    for name, args in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = ctypes.c_int
+    L.xc_set_data_path(DATA_PATH.encode())
+    _lib = L
+    return L
+
+
+def last_error():
+    buf = ctypes.create_string_buffer(1024)
+    lib().xc_last_error(buf, 1024)
+    return buf.value.decode(errors="replace")
+
+
+def check(status):
+    if status != XC_OK:
+        raise XCError(status, last_error())
+    return status

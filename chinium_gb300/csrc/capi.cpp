@@ -1,0 +1,759 @@
+// C-ABI implementation: the Grid / ExchangeCorrelation objects and every
+// extern "C" entry point of include/chinium_xc.h.
+#include <cmath>
+#include <cstring>
+#include <fstream>
+#include <functional>
+#include <map>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "common.h"
+#include "kernels.h"
+#include "model.h"
+#include "xc_state.h"
+
+namespace cgb {
+
+namespace {
+thread_local std::string g_last_error;
+std::once_flag g_sh_once;
+}  // namespace
+
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+
+void ensure_device() {
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0)
+        throw Error(XC_ERR_CUDA, std::string("no CUDA device available: ") + cudaGetErrorString(e));
+    std::call_once(g_sh_once, [] { upload_solid_harmonics(); });
+}
+
+// ------------------------------------------------------------ grid build
+// SphericalGrid (GridGeneration.cpp:73-133) for one atom: points in
+// generation order with radial * 4 pi * Lebedev weights.
+static void atom_points(const std::string& grid, int Z, const double* c, int atom, std::vector<double>& X,
+                        std::vector<double>& Y, std::vector<double>& Zc, std::vector<double>& W, std::vector<int>& owner) {
+    const GridRecipe& r = grid_recipe(grid, Z);
+    const int nt = r.nshells_total;
+    std::function<double(double)> ri, rw;
+    if (r.formula == "de2") {
+        CGB_CHECK(r.params.size() >= 3, XC_ERR_IO, "corrupt de2 recipe");
+        const double a = r.params[0], t2 = r.params[1], t3 = r.params[2];
+        const double h = (t3 - t2) / (double)(nt - 1);
+        ri = [=](double i) {
+            const double xi = h * i + t2;
+            return std::exp(a * xi - std::exp(-xi));
+        };
+        rw = [=](double i) {
+            const double xi = h * i + t2;
+            return std::exp(3 * a * xi - 3 * std::exp(-xi)) * (a + std::exp(-xi)) * h;
+        };
+    } else if (r.formula == "em") {
+        CGB_CHECK(r.params.size() >= 1, XC_ERR_IO, "corrupt em recipe");
+        const double R = r.params[0];
+        ri = [=](double i) {
+            const double ii = i + 1;
+            return R * std::pow(ii / (nt + 1 - ii), 2);
+        };
+        rw = [=](double i) {
+            const double ii = i + 1;
+            return 2 * std::pow(R, 3) * (nt + 1) * std::pow(ii, 5) / std::pow(nt + 1 - ii, 7);
+        };
+    } else {
+        throw Error(XC_ERR_IO, "Unrecognized radial formula!");
+    }
+    int ish = 0;
+    for (auto [npts, nsh] : r.groups) {
+        const std::vector<double>& leb = lebedev_rule(npts);
+        for (int s = 0; s < nsh; s++, ish++) {
+            const double rad = ri(ish), wr = rw(ish);
+            for (int k = 0; k < npts; k++) {
+                X.push_back(leb[4 * k] * rad + c[0]);
+                Y.push_back(leb[4 * k + 1] * rad + c[1]);
+                Zc.push_back(leb[4 * k + 2] * rad + c[2]);
+                W.push_back(wr * (4 * M_PI * leb[4 * k + 3]));
+                owner.push_back(atom);
+            }
+        }
+    }
+}
+
+// RecursiveCut (GridGeneration.cpp:177-210) as it behaves: leaves are
+// recursive halves of generation order (its partition step only reorders
+// the first four points, which stay in the left half).
+static void halve(long lo, long n, std::vector<std::pair<long, long>>& out) {
+    if (n <= kMaxBlockPts) {
+        out.emplace_back(lo, n);
+        return;
+    }
+    const long h = n / 2;
+    halve(lo, h, out);
+    halve(lo + h, n - h, out);
+}
+
+void Grid::build(const BasisSet& bs, const std::string& grid_name, int ns, double thr) {
+    basis = bs;
+    nspin = ns;
+    screen_thr = thr;
+    const int natoms = bs.natoms();
+    std::vector<double> X, Y, Z, Win;
+    std::vector<int> own;
+    for (int a = 0; a < natoms; a++) atom_points(grid_name, bs.Z[a], &bs.xyz[3 * a], a, X, Y, Z, Win, own);
+    npoints = (long)X.size();
+    std::vector<std::pair<long, long>> ranges;
+    halve(0, npoints, ranges);
+    // SubGrid::SubGrid (GridGeneration.cpp:212-230): pad to a multiple of 8,
+    // padded coordinates copy the first points, padded weights zero.
+    hx.clear(); hy.clear(); hz.clear();
+    std::vector<double> hw;
+    std::vector<int> hown;
+    blocks.clear();
+    for (auto [lo, n] : ranges) {
+        BlockDesc bd{};
+        bd.pt_off = (int)hx.size();
+        bd.nreal = (int)n;
+        bd.ng = (int)((n + 7) & ~7L);
+        for (int k = 0; k < bd.ng; k++) {
+            const long src = lo + (k < n ? k : k - n);
+            hx.push_back(X[src]);
+            hy.push_back(Y[src]);
+            hz.push_back(Z[src]);
+            hw.push_back(k < n ? Win[src] : 0.0);
+            hown.push_back(own[src]);
+        }
+        blocks.push_back(bd);
+    }
+    Gp = (long)hx.size();
+    // shell screening per block: bounding sphere of the block's real points
+    std::vector<double> ext(bs.shells.size());
+    for (size_t s = 0; s < bs.shells.size(); s++) ext[s] = shell_extent(bs, bs.shells[s], thr);
+    basis_lists.clear();
+    shell_lists.clear();
+    max_nb = 0;
+    screened_pairs = 0;
+    for (auto& bd : blocks) {
+        double cx = 0, cy = 0, cz = 0;
+        for (int k = 0; k < bd.nreal; k++) {
+            cx += hx[bd.pt_off + k];
+            cy += hy[bd.pt_off + k];
+            cz += hz[bd.pt_off + k];
+        }
+        cx /= bd.nreal; cy /= bd.nreal; cz /= bd.nreal;
+        double rad = 0;
+        for (int k = 0; k < bd.ng; k++) {
+            const double dx = hx[bd.pt_off + k] - cx, dy = hy[bd.pt_off + k] - cy, dz = hz[bd.pt_off + k] - cz;
+            rad = std::max(rad, std::sqrt(dx * dx + dy * dy + dz * dz));
+        }
+        bd.sh_off = (int)shell_lists.size();
+        bd.bas_off = (int)basis_lists.size();
+        int nb = 0, nsh = 0;
+        for (size_t s = 0; s < bs.shells.size(); s++) {
+            const Shell& sh = bs.shells[s];
+            const double d = std::sqrt((sh.x - cx) * (sh.x - cx) + (sh.y - cy) * (sh.y - cy) + (sh.z - cz) * (sh.z - cz));
+            if (thr > 0 && d - rad > ext[s]) continue;
+            shell_lists.push_back((int)s);
+            for (int f = 0; f < shell_size(sh.type); f++) basis_lists.push_back(sh.first + f);
+            nb += shell_size(sh.type);
+            nsh++;
+        }
+        bd.nb = nb;
+        bd.nsh = nsh;
+        max_nb = std::max(max_nb, nb);
+        screened_pairs += (long)nb * nb;
+    }
+    // device: points, Becke weights
+    ensure_device();
+    d_x.upload(hx.data(), Gp, stream);
+    d_y.upload(hy.data(), Gp, stream);
+    d_z.upload(hz.data(), Gp, stream);
+    DevBuf<double> d_win;
+    DevBuf<int> d_own;
+    d_win.upload(hw.data(), Gp, stream);
+    d_own.upload(hown.data(), Gp, stream);
+    d_atoms.upload(bs.xyz.data(), bs.xyz.size(), stream);
+    d_w.alloc(Gp);
+    launch_becke(natoms, d_atoms.p, Gp, d_x.p, d_y.p, d_z.p, d_own.p, d_win.p, d_w.p, stream);
+    // shells
+    std::vector<int> st, sl, snp, spo, sf;
+    std::vector<double> sxyz;
+    for (auto& sh : bs.shells) {
+        st.push_back(sh.type);
+        sl.push_back(sh.l);
+        snp.push_back(sh.nprim);
+        spo.push_back(sh.prim_off);
+        sf.push_back(sh.first);
+        sxyz.push_back(sh.x);
+        sxyz.push_back(sh.y);
+        sxyz.push_back(sh.z);
+    }
+    d_sh_type.upload(st.data(), st.size(), stream);
+    d_sh_l.upload(sl.data(), sl.size(), stream);
+    d_sh_nprim.upload(snp.data(), snp.size(), stream);
+    d_sh_poff.upload(spo.data(), spo.size(), stream);
+    d_sh_first.upload(sf.data(), sf.size(), stream);
+    d_sh_xyz.upload(sxyz.data(), sxyz.size(), stream);
+    d_exps.upload(bs.exps.data(), bs.exps.size(), stream);
+    d_coefs.upload(bs.coefs.data(), bs.coefs.size(), stream);
+    d_lists.upload(basis_lists.data(), basis_lists.size(), stream);
+    d_shell_lists.upload(shell_lists.data(), shell_lists.size(), stream);
+    CGB_CUDA(cudaStreamSynchronize(stream));
+}
+
+DevShells Grid::dev_shells() const {
+    DevShells s;
+    s.nshell = (int)basis.shells.size();
+    s.type = d_sh_type.p;
+    s.l = d_sh_l.p;
+    s.nprim = d_sh_nprim.p;
+    s.prim_off = d_sh_poff.p;
+    s.first = d_sh_first.p;
+    s.xyz = d_sh_xyz.p;
+    s.exps = d_exps.p;
+    s.coefs = d_coefs.p;
+    return s;
+}
+
+void Grid::get_ao(int derivative) {
+    CGB_CHECK(derivative >= 0, XC_ERR_ARG, "negative derivative order");
+    const int order = type + derivative;
+    CGB_CHECK(order <= 2, XC_ERR_UNSUPPORTED, "AO derivative order above 2 is not stored by this build");
+    ncomp = order >= 1 ? 4 : 1;
+    long long off = 0;
+    for (auto& bd : blocks) {
+        bd.ao_off = off;
+        off += (long long)ncomp * bd.nb * bd.ng;
+    }
+    ao_elements = off / ncomp;
+    d_blocks.upload(blocks.data(), blocks.size(), stream);
+    d_ao.alloc((size_t)off);
+    launch_ao((int)blocks.size(), d_blocks.p, d_shell_lists.p, dev_shells(), d_x.p, d_y.p, d_z.p, ncomp, d_ao.p, stream);
+    ao_order = order;
+    CGB_CUDA(cudaStreamSynchronize(stream));
+}
+
+void Grid::ensure_work() {
+    const int nsig = nspin == 1 ? 1 : 3;
+    d_rho.alloc(nspin * Gp);
+    d_rho1.alloc(3 * nspin * Gp);
+    d_tau.alloc(nspin * Gp);
+    d_sigma.alloc(nsig * Gp);
+    d_eps.alloc(Gp);
+    d_vrho.alloc(nspin * Gp);
+    d_vsigma.alloc(nsig * Gp);
+    d_vtau.alloc(nspin * Gp);
+    d_fcoef.alloc(5 * nspin * Gp);
+    d_partial.alloc((Gp + 127) / 128 + 1);
+    d_scalar.alloc(2);
+    const size_t nn = (size_t)basis.nbasis * basis.nbasis * nspin;
+    d_D.alloc(nn);
+    d_V.alloc(nn);
+}
+
+void Grid::mark(int i) {
+    if (profiling) CGB_CUDA(cudaEventRecord(ev[i], stream));
+}
+
+Grid::~Grid() {
+    for (auto& e : ev)
+        if (e) cudaEventDestroy(e);
+}
+
+void Grid::density_device(const double* dD) {
+    CGB_CHECK(ao_order >= type, XC_ERR_STATE, "getAO must run (for the current type) before getDensity");
+    ensure_work();
+    mark(0);
+    launch_density_fp64((int)blocks.size(), d_blocks.p, d_lists.p, basis.nbasis, nspin, type, dD, d_ao.p, Gp,
+                        d_rho.p, d_rho1.p, d_tau.p, stream);
+    have_density = true;
+    have_potential = false;
+}
+
+void Grid::evaluate(const Functional& f) {
+    CGB_CHECK(have_density, XC_ERR_STATE, "Evaluate needs a density (getDensity first)");
+    CGB_CHECK(f.nspin == nspin, XC_ERR_ARG, "functional and grid disagree on the number of spins");
+    CGB_CHECK(f.family <= type, XC_ERR_STATE, "grid type is below the functional family (setType/getAO)");
+    mark(1);
+    launch_functional_fp64(f.desc, f.family, nspin, Gp, d_w.p, d_rho.p, d_rho1.p, d_tau.p, d_sigma.p, d_eps.p,
+                           d_vrho.p, d_vsigma.p, d_vtau.p, d_fcoef.p, d_partial.p, &n_partial, stream);
+    eval_family = f.family;
+    have_potential = true;
+}
+
+void Grid::energy_device(double* dE) {
+    CGB_CHECK(have_potential, XC_ERR_STATE, "getEnergy needs Evaluate first");
+    mark(2);
+    launch_reduce_sum(d_partial.p, n_partial, dE, stream);
+}
+
+void Grid::fock_device(double* dV, int fam) {
+    const size_t nn = (size_t)basis.nbasis * basis.nbasis * nspin;
+    mark(3);
+    CGB_CUDA(cudaMemsetAsync(dV, 0, nn * sizeof(double), stream));
+    launch_fock_fp64((int)blocks.size(), d_blocks.p, d_lists.p, max_nb, basis.nbasis, nspin, fam, d_ao.p, Gp,
+                     d_fcoef.p, dV, stream);
+    mark(4);
+}
+
+// ------------------------------------------------------------ functional
+static std::vector<int> functional_ids_by_name(const std::string& name) {
+    std::ifstream f(data_path() + "/functionals.txt");
+    if (!f.good()) throw Error(XC_ERR_IO, "Density functional file is missing!");
+    std::string line;
+    while (std::getline(f, line)) {
+        if (line.empty() || line[0] == '#') continue;
+        std::stringstream ss(line);
+        std::string nm;
+        ss >> nm;
+        if (nm != name) continue;
+        std::vector<int> ids;
+        int id;
+        while (ss >> id) ids.push_back(id);
+        return ids;
+    }
+    throw Error(XC_ERR_IO, "Density functional file is missing! (" + name + ")");
+}
+
+void Functional::init(const std::vector<int>& ids_, int ns) {
+    CGB_CHECK(ns == 1 || ns == 2, XC_ERR_ARG, "nspin must be 1 or 2");
+    CGB_CHECK(!ids_.empty() && ids_.size() <= 4, XC_ERR_ARG, "between 1 and 4 functional ids");
+    ids = ids_;
+    nspin = ns;
+    family = 0;
+    exx = 0;
+    desc.nids = (int)ids.size();
+    for (size_t i = 0; i < ids.size(); i++) {
+        const int fam = xcf::family_of_id(ids[i]);
+        CGB_CHECK(fam >= 0, XC_ERR_UNSUPPORTED, "functional id " + std::to_string(ids[i]) + " is not implemented");
+        family = std::max(family, fam);
+        exx = std::max(exx, xcf::exx_of_id(ids[i]));  // ExchangeCorrelation.cpp:63-64
+        desc.ids[i] = ids[i];
+    }
+}
+
+}  // namespace cgb
+
+using namespace cgb;
+
+// ================================================================== C ABI
+extern "C" {
+
+int xc_last_error(char* buf, size_t len) {
+    if (!buf || len == 0) return XC_ERR_ARG;
+    std::strncpy(buf, g_last_error.c_str(), len - 1);
+    buf[len - 1] = 0;
+    return XC_OK;
+}
+
+int xc_set_data_path(const char* path) {
+    return guard([&] {
+        CGB_CHECK(path, XC_ERR_ARG, "null path");
+        set_data_path(path);
+    });
+}
+
+int xc_basis_create(int natoms, const int* Z, const double* xyz, const char* name, xc_basis** out) {
+    return guard([&] {
+        CGB_CHECK(natoms > 0 && Z && xyz && name && out, XC_ERR_ARG, "bad basis arguments");
+        std::vector<int> z(Z, Z + natoms);
+        std::vector<double> c(xyz, xyz + 3 * natoms);
+        for (double v : c) CGB_CHECK(std::isfinite(v), XC_ERR_NUMERIC, "non-finite coordinate");
+        auto* b = new xc_basis;
+        try {
+            b->b = load_basis(name, z, c);
+        } catch (...) {
+            delete b;
+            throw;
+        }
+        *out = b;
+    });
+}
+
+int xc_basis_nbasis(const xc_basis* b, int* n) {
+    return guard([&] {
+        CGB_CHECK(b && n, XC_ERR_ARG, "null argument");
+        *n = b->b.nbasis;
+    });
+}
+
+int xc_basis_nshells(const xc_basis* b, int* n) {
+    return guard([&] {
+        CGB_CHECK(b && n, XC_ERR_ARG, "null argument");
+        *n = (int)b->b.shells.size();
+    });
+}
+
+int xc_basis_shells(const xc_basis* b, int* atom, int* type, int* first, int* nprim) {
+    return guard([&] {
+        CGB_CHECK(b, XC_ERR_ARG, "null basis");
+        for (size_t i = 0; i < b->b.shells.size(); i++) {
+            const Shell& s = b->b.shells[i];
+            if (atom) atom[i] = s.atom;
+            if (type) type[i] = s.type;
+            if (first) first[i] = s.first;
+            if (nprim) nprim[i] = s.nprim;
+        }
+    });
+}
+
+int xc_basis_primitives(const xc_basis* b, double* exps, double* coefs) {
+    return guard([&] {
+        CGB_CHECK(b, XC_ERR_ARG, "null basis");
+        if (exps) std::memcpy(exps, b->b.exps.data(), b->b.exps.size() * sizeof(double));
+        if (coefs) std::memcpy(coefs, b->b.coefs.data(), b->b.coefs.size() * sizeof(double));
+    });
+}
+
+int xc_basis_destroy(xc_basis* b) {
+    delete b;
+    return XC_OK;
+}
+
+int xc_grid_create(const xc_basis* b, const char* grid_name, int nspin, double thr, xc_grid** out) {
+    return guard([&] {
+        CGB_CHECK(b && grid_name && out, XC_ERR_ARG, "bad grid arguments");
+        CGB_CHECK(nspin == 1 || nspin == 2, XC_ERR_ARG, "nspin must be 1 or 2");
+        CGB_CHECK(thr >= 0 && std::isfinite(thr), XC_ERR_ARG, "screen threshold must be >= 0");
+        auto* g = new xc_grid;
+        try {
+            g->g.build(b->b, grid_name, nspin, thr);
+        } catch (...) {
+            delete g;
+            throw;
+        }
+        *out = g;
+    });
+}
+
+int xc_grid_destroy(xc_grid* g) {
+    delete g;
+    return XC_OK;
+}
+
+int xc_grid_set_stream(xc_grid* g, void* stream) {
+    return guard([&] {
+        CGB_CHECK(g, XC_ERR_ARG, "null grid");
+        g->g.stream = (cudaStream_t)stream;
+    });
+}
+
+int xc_grid_set_type(xc_grid* g, int type) {
+    return guard([&] {
+        CGB_CHECK(g, XC_ERR_ARG, "null grid");
+        CGB_CHECK(type >= 0 && type <= 2, XC_ERR_ARG, "type must be 0, 1 or 2");
+        g->g.type = type;
+    });
+}
+
+int xc_grid_get_ao(xc_grid* g, int derivative) {
+    return guard([&] {
+        CGB_CHECK(g, XC_ERR_ARG, "null grid");
+        g->g.get_ao(derivative);
+    });
+}
+
+int xc_grid_num_electrons(xc_grid* g, double* n) {
+    return guard([&] {
+        CGB_CHECK(g && n, XC_ERR_ARG, "null argument");
+        Grid& G = g->g;
+        CGB_CHECK(G.have_density, XC_ERR_STATE, "getNumElectrons needs a density");
+        int np = 0;
+        launch_num_electrons(G.Gp, G.nspin, G.d_w.p, G.d_rho.p, G.d_partial.p, &np, G.stream);
+        launch_reduce_sum(G.d_partial.p, np, G.d_scalar.p + 1, G.stream);
+        CGB_CUDA(cudaMemcpyAsync(n, G.d_scalar.p + 1, sizeof(double), cudaMemcpyDeviceToHost, G.stream));
+        CGB_CUDA(cudaStreamSynchronize(G.stream));
+        G.have_potential = false;  // partials reused
+    });
+}
+
+int xc_grid_get_density(xc_grid* g, const double* D, int nspin) {
+    return guard([&] {
+        CGB_CHECK(g && D, XC_ERR_ARG, "null argument");
+        Grid& G = g->g;
+        CGB_CHECK(nspin == G.nspin, XC_ERR_ARG, "Wrong number of spin types!");
+        G.ensure_work();
+        const size_t nn = (size_t)G.basis.nbasis * G.basis.nbasis * nspin;
+        CGB_CUDA(cudaMemcpyAsync(G.d_D.p, D, nn * sizeof(double), cudaMemcpyHostToDevice, G.stream));
+        G.density_device(G.d_D.p);
+        CGB_CUDA(cudaStreamSynchronize(G.stream));
+    });
+}
+
+int xc_grid_get_energy(xc_grid* g, double* E) {
+    return guard([&] {
+        CGB_CHECK(g && E, XC_ERR_ARG, "null argument");
+        Grid& G = g->g;
+        G.energy_device(G.d_scalar.p);
+        CGB_CUDA(cudaMemcpyAsync(E, G.d_scalar.p, sizeof(double), cudaMemcpyDeviceToHost, G.stream));
+        CGB_CUDA(cudaStreamSynchronize(G.stream));
+    });
+}
+
+int xc_grid_get_fock(xc_grid* g, double* V) {
+    return guard([&] {
+        CGB_CHECK(g && V, XC_ERR_ARG, "null argument");
+        Grid& G = g->g;
+        CGB_CHECK(G.have_potential, XC_ERR_STATE, "getFock needs Evaluate first");
+        G.fock_device(G.d_V.p, G.eval_family);
+        const size_t nn = (size_t)G.basis.nbasis * G.basis.nbasis * G.nspin;
+        CGB_CUDA(cudaMemcpyAsync(V, G.d_V.p, nn * sizeof(double), cudaMemcpyDeviceToHost, G.stream));
+        CGB_CUDA(cudaStreamSynchronize(G.stream));
+    });
+}
+
+int xc_grid_info_get(const xc_grid* g, xc_grid_info* info) {
+    return guard([&] {
+        CGB_CHECK(g && info, XC_ERR_ARG, "null argument");
+        const Grid& G = g->g;
+        info->npoints = G.npoints;
+        info->npoints_padded = G.Gp;
+        info->nblocks = (int)G.blocks.size();
+        info->nbasis = G.basis.nbasis;
+        info->nspin = G.nspin;
+        info->type = G.type;
+        info->ao_elements = G.ao_elements;
+        info->screened_pairs = G.screened_pairs;
+    });
+}
+
+int xc_grid_points(const xc_grid* g, double* x, double* y, double* z, double* w, int* off, int* ng, int* nreal,
+                   int* nb) {
+    return guard([&] {
+        CGB_CHECK(g, XC_ERR_ARG, "null grid");
+        const Grid& G = g->g;
+        if (x) std::memcpy(x, G.hx.data(), G.Gp * sizeof(double));
+        if (y) std::memcpy(y, G.hy.data(), G.Gp * sizeof(double));
+        if (z) std::memcpy(z, G.hz.data(), G.Gp * sizeof(double));
+        if (w) {
+            CGB_CUDA(cudaMemcpyAsync(w, G.d_w.p, G.Gp * sizeof(double), cudaMemcpyDeviceToHost, G.stream));
+            CGB_CUDA(cudaStreamSynchronize(G.stream));
+        }
+        for (size_t b = 0; b < G.blocks.size(); b++) {
+            if (off) off[b] = G.blocks[b].pt_off;
+            if (ng) ng[b] = G.blocks[b].ng;
+            if (nreal) nreal[b] = G.blocks[b].nreal;
+            if (nb) nb[b] = G.blocks[b].nb;
+        }
+    });
+}
+
+static void d2h(void* dst, const void* src, size_t bytes, cudaStream_t s) {
+    if (dst && src && bytes) CGB_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s));
+}
+
+int xc_grid_density_values(const xc_grid* g, double* rho, double* rho1, double* sigma, double* tau) {
+    return guard([&] {
+        CGB_CHECK(g, XC_ERR_ARG, "null grid");
+        const Grid& G = g->g;
+        CGB_CHECK(G.have_density, XC_ERR_STATE, "no density");
+        const size_t B = sizeof(double) * G.Gp;
+        d2h(rho, G.d_rho.p, B * G.nspin, G.stream);
+        if (G.type >= 1) d2h(rho1, G.d_rho1.p, B * 3 * G.nspin, G.stream);
+        if (G.type >= 1 && G.have_potential) d2h(sigma, G.d_sigma.p, B * (G.nspin == 1 ? 1 : 3), G.stream);
+        if (G.type >= 2) d2h(tau, G.d_tau.p, B * G.nspin, G.stream);
+        CGB_CUDA(cudaStreamSynchronize(G.stream));
+    });
+}
+
+int xc_grid_potential_values(const xc_grid* g, double* eps, double* vrho, double* vsigma, double* vtau) {
+    return guard([&] {
+        CGB_CHECK(g, XC_ERR_ARG, "null grid");
+        const Grid& G = g->g;
+        CGB_CHECK(G.have_potential, XC_ERR_STATE, "no potential (Evaluate first)");
+        const size_t B = sizeof(double) * G.Gp;
+        d2h(eps, G.d_eps.p, B, G.stream);
+        d2h(vrho, G.d_vrho.p, B * G.nspin, G.stream);
+        if (G.eval_family >= 1) d2h(vsigma, G.d_vsigma.p, B * (G.nspin == 1 ? 1 : 3), G.stream);
+        if (G.eval_family >= 2) d2h(vtau, G.d_vtau.p, B * G.nspin, G.stream);
+        CGB_CUDA(cudaStreamSynchronize(G.stream));
+    });
+}
+
+int xc_grid_block_ao(const xc_grid* g, int block, double* ao, double* ao1, int* list) {
+    return guard([&] {
+        CGB_CHECK(g, XC_ERR_ARG, "null grid");
+        const Grid& G = g->g;
+        CGB_CHECK(block >= 0 && block < (int)G.blocks.size(), XC_ERR_ARG, "block index out of range");
+        CGB_CHECK(G.ao_order >= 0, XC_ERR_STATE, "getAO first");
+        const BlockDesc& bd = G.blocks[block];
+        const size_t cs = (size_t)bd.nb * bd.ng;
+        d2h(ao, G.d_ao.p + bd.ao_off, cs * sizeof(double), G.stream);
+        if (G.ncomp == 4) d2h(ao1, G.d_ao.p + bd.ao_off + cs, 3 * cs * sizeof(double), G.stream);
+        if (list) std::memcpy(list, G.basis_lists.data() + bd.bas_off, bd.nb * sizeof(int));
+        CGB_CUDA(cudaStreamSynchronize(G.stream));
+    });
+}
+
+int xc_functional_read(const char* name, int nspin, xc_functional** out) {
+    return guard([&] {
+        CGB_CHECK(name && out, XC_ERR_ARG, "null argument");
+        auto ids = functional_ids_by_name(name);
+        auto* f = new xc_functional;
+        try {
+            f->f.init(ids, nspin);
+        } catch (...) {
+            delete f;
+            throw;
+        }
+        *out = f;
+    });
+}
+
+int xc_functional_create(const int* ids, int nids, int nspin, xc_functional** out) {
+    return guard([&] {
+        CGB_CHECK(ids && nids > 0 && out, XC_ERR_ARG, "bad functional arguments");
+        auto* f = new xc_functional;
+        try {
+            f->f.init(std::vector<int>(ids, ids + nids), nspin);
+        } catch (...) {
+            delete f;
+            throw;
+        }
+        *out = f;
+    });
+}
+
+int xc_functional_destroy(xc_functional* f) {
+    delete f;
+    return XC_OK;
+}
+
+int xc_functional_exx(const xc_functional* f, double* exx) {
+    return guard([&] {
+        CGB_CHECK(f && exx, XC_ERR_ARG, "null argument");
+        *exx = f->f.exx;
+    });
+}
+
+int xc_functional_family(const xc_functional* f, int* fam) {
+    return guard([&] {
+        CGB_CHECK(f && fam, XC_ERR_ARG, "null argument");
+        *fam = f->f.family;
+    });
+}
+
+int xc_evaluate(xc_functional* f, xc_grid* g, const char* order) {
+    return guard([&] {
+        CGB_CHECK(f && g && order, XC_ERR_ARG, "null argument");
+        const std::string o = order;
+        CGB_CHECK(o == "e" || o == "v" || o == "ev", XC_ERR_UNSUPPORTED, "order must be e, v or ev");
+        g->g.evaluate(f->f);
+        CGB_CUDA(cudaStreamSynchronize(g->g.stream));
+    });
+}
+
+int xc_functional_eval_points(xc_functional* f, long n, const double* rho, const double* sigma, const double* tau,
+                              double* eps, double* vrho, double* vsigma, double* vtau) {
+    return guard([&] {
+        CGB_CHECK(f && rho && eps && vrho && n > 0, XC_ERR_ARG, "bad arguments");
+        ensure_device();
+        const Functional& F = f->f;
+        const int ns = F.nspin, nsig = ns == 1 ? 1 : 3;
+        CGB_CHECK(F.family < 1 || (sigma && vsigma), XC_ERR_ARG, "sigma arrays required for GGA");
+        CGB_CHECK(F.family < 2 || (tau && vtau), XC_ERR_ARG, "tau arrays required for meta-GGA");
+        DevBuf<double> dr, ds, dt, de, dvr, dvs, dvt;
+        dr.upload(rho, ns * n);
+        ds.alloc(nsig * n);
+        dt.alloc(ns * n);
+        if (F.family >= 1) ds.upload(sigma, nsig * n);
+        if (F.family >= 2) dt.upload(tau, ns * n);
+        de.alloc(n);
+        dvr.alloc(ns * n);
+        dvs.alloc(nsig * n);
+        dvt.alloc(ns * n);
+        launch_functional_points(F.desc, F.family, ns, n, dr.p, ds.p, dt.p, de.p, dvr.p, dvs.p, dvt.p, 0);
+        CGB_CUDA(cudaMemcpy(eps, de.p, n * sizeof(double), cudaMemcpyDeviceToHost));
+        CGB_CUDA(cudaMemcpy(vrho, dvr.p, ns * n * sizeof(double), cudaMemcpyDeviceToHost));
+        if (F.family >= 1) CGB_CUDA(cudaMemcpy(vsigma, dvs.p, nsig * n * sizeof(double), cudaMemcpyDeviceToHost));
+        if (F.family >= 2) CGB_CUDA(cudaMemcpy(vtau, dvt.p, ns * n * sizeof(double), cudaMemcpyDeviceToHost));
+    });
+}
+
+int xc_build_device(xc_grid* g, xc_functional* f, const double* dD, int nspin, int precision, double* dE, double* dV) {
+    return guard([&] {
+        CGB_CHECK(g && f && dD && dE && dV, XC_ERR_ARG, "null argument");
+        Grid& G = g->g;
+        CGB_CHECK(nspin == G.nspin, XC_ERR_ARG, "Wrong number of spin types!");
+        CGB_CHECK(precision == XC_PRECISION_FP64 || precision == XC_PRECISION_MIXED, XC_ERR_ARG, "bad precision");
+        CGB_CHECK(precision == XC_PRECISION_FP64, XC_ERR_UNSUPPORTED, "mixed precision path not built yet");
+        G.density_device(dD);
+        G.evaluate(f->f);
+        G.energy_device(dE);
+        G.fock_device(dV, f->f.family);
+    });
+}
+
+int xc_build(xc_grid* g, xc_functional* f, const double* D, int nspin, int precision, double* E, double* V) {
+    return guard([&] {
+        CGB_CHECK(g && f && D && E && V, XC_ERR_ARG, "null argument");
+        Grid& G = g->g;
+        CGB_CHECK(nspin == G.nspin, XC_ERR_ARG, "Wrong number of spin types!");
+        G.ensure_work();
+        const size_t nn = (size_t)G.basis.nbasis * G.basis.nbasis * nspin;
+        CGB_CUDA(cudaMemcpyAsync(G.d_D.p, D, nn * sizeof(double), cudaMemcpyHostToDevice, G.stream));
+        const int st = xc_build_device(g, f, G.d_D.p, nspin, precision, G.d_scalar.p, G.d_V.p);
+        if (st) throw Error(st, g_last_error);
+        CGB_CUDA(cudaMemcpyAsync(E, G.d_scalar.p, sizeof(double), cudaMemcpyDeviceToHost, G.stream));
+        CGB_CUDA(cudaMemcpyAsync(V, G.d_V.p, nn * sizeof(double), cudaMemcpyDeviceToHost, G.stream));
+        CGB_CUDA(cudaStreamSynchronize(G.stream));
+    });
+}
+
+int xc_grid_profile(xc_grid* g, int enable) {
+    return guard([&] {
+        CGB_CHECK(g, XC_ERR_ARG, "null grid");
+        Grid& G = g->g;
+        if (enable)
+            for (auto& e : G.ev)
+                if (!e) CGB_CUDA(cudaEventCreate(&e));
+        G.profiling = enable != 0;
+    });
+}
+
+int xc_grid_stage_ms(xc_grid* g, double* ms) {
+    return guard([&] {
+        CGB_CHECK(g && ms, XC_ERR_ARG, "null argument");
+        Grid& G = g->g;
+        CGB_CHECK(G.profiling, XC_ERR_STATE, "profiling is off (xc_grid_profile)");
+        CGB_CUDA(cudaEventSynchronize(G.ev[4]));
+        for (int i = 0; i < 4; i++) {
+            float t = 0;
+            CGB_CUDA(cudaEventElapsedTime(&t, G.ev[i], G.ev[i + 1]));
+            ms[i] = t;
+        }
+    });
+}
+
+int xc_sap_fock(xc_grid* g, double* V) {
+    return guard([&] {
+        CGB_CHECK(g && V, XC_ERR_ARG, "null argument");
+        Grid& G = g->g;
+        CGB_CHECK(G.ao_order >= 0, XC_ERR_STATE, "getAO must run before the SAP guess");
+        G.ensure_work();
+        const int natoms = G.basis.natoms();
+        std::vector<double> radii, table((size_t)natoms * 751), rv;
+        for (int a = 0; a < natoms; a++) {
+            sap_table(G.basis.Z[a], radii, rv);
+            CGB_CHECK(rv.size() == 751 && radii.size() == 751, XC_ERR_IO, "corrupt SAP table");
+            std::memcpy(&table[(size_t)a * 751], rv.data(), 751 * sizeof(double));
+        }
+        DevBuf<double> d_table, d_radii;
+        d_table.upload(table.data(), table.size(), G.stream);
+        d_radii.upload(radii.data(), radii.size(), G.stream);
+        // GuessSCF.cpp:19-37: pretend LDA, one spin; V = sum_g w v phi phi
+        launch_sap_coef(G.Gp, natoms, G.d_atoms.p, d_table.p, d_radii.p, G.d_x.p, G.d_y.p, G.d_z.p, G.d_w.p,
+                        G.d_fcoef.p, G.stream);
+        const size_t nn = (size_t)G.basis.nbasis * G.basis.nbasis;
+        CGB_CUDA(cudaMemsetAsync(G.d_V.p, 0, nn * sizeof(double), G.stream));
+        launch_fock_fp64((int)G.blocks.size(), G.d_blocks.p, G.d_lists.p, G.max_nb, G.basis.nbasis, 1, 0, G.d_ao.p,
+                         G.Gp, G.d_fcoef.p, G.d_V.p, G.stream);
+        CGB_CUDA(cudaMemcpyAsync(V, G.d_V.p, nn * sizeof(double), cudaMemcpyDeviceToHost, G.stream));
+        CGB_CUDA(cudaStreamSynchronize(G.stream));
+        G.have_potential = false;  // fcoef overwritten
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,70 @@
+// Launch wrappers for the XC kernels (implemented in k_*.cu).  All take raw
+// device pointers and a stream; none allocates.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "functional.cuh"
+#include "model.h"
+
+namespace cgb {
+
+// Shells on the device (struct of arrays).
+struct DevShells {
+    int nshell;
+    const int* type;
+    const int* l;
+    const int* nprim;
+    const int* prim_off;
+    const int* first;
+    const double* xyz;  // nshell x 3
+    const double* exps;
+    const double* coefs;
+};
+
+// Upload the solid-harmonic table to constant memory (once per process/device).
+void upload_solid_harmonics();
+
+// Becke partition weights (GridGeneration.cpp:134-153), one thread per point.
+void launch_becke(int natoms, const double* d_atoms, long npts, const double* x, const double* y,
+                  const double* z, const int* owner, const double* w_in, double* w_out, cudaStream_t s);
+
+// AO values (ncomp = 1) or values + gradients (ncomp = 4) for every block.
+void launch_ao(int nblocks, const BlockDesc* d_blocks, const int* d_block_shells, DevShells sh,
+               const double* x, const double* y, const double* z, int ncomp, double* ao, cudaStream_t s);
+
+// rho (s, G), rho1 (s, 3, G) and tau (s, G) from D (s, n, n) column-major.
+void launch_density_fp64(int nblocks, const BlockDesc* d_blocks, const int* d_basis_lists, int nbasis,
+                         int nspin, int type, const double* D, const double* ao, long Gp, double* rho,
+                         double* rho1, double* tau, cudaStream_t s);
+
+// Functional on every point: eps, vrho, vsigma, vtau, sigma, the Fock
+// coefficients fcoef (s, 5, G) and per-CTA partial energies.
+void launch_functional_fp64(const xcf::FuncDesc& f, int family, int nspin, long Gp, const double* w,
+                            const double* rho, const double* rho1, const double* tau, double* sigma,
+                            double* eps, double* vrho, double* vsigma, double* vtau, double* fcoef,
+                            double* e_partial, int* n_partial, cudaStream_t s);
+
+// Deterministic sum of n partials into out[0] (single CTA, fixed order).
+void launch_reduce_sum(const double* partial, int n, double* out, cudaStream_t s);
+
+// Number of electrons partials: sum_g w_g sum_s rho_gs.
+void launch_num_electrons(long Gp, int nspin, const double* w, const double* rho, double* partial,
+                          int* n_partial, cudaStream_t s);
+
+// V (s, n, n) += per-block phi^T A + A^T phi (+ gradient terms), FP64 atomics.
+void launch_fock_fp64(int nblocks, const BlockDesc* d_blocks, const int* d_basis_lists, int max_nb,
+                      int nbasis, int nspin, int type, const double* ao, long Gp, const double* fcoef,
+                      double* V, cudaStream_t s);
+
+// SAP potential times weight into fcoef (s = 1, LDA layout): fcoef[0] = 1/2 w v_SAP.
+void launch_sap_coef(long Gp, int natoms, const double* d_atoms, const double* d_table /* natoms x 751 */,
+                     const double* d_radii, const double* x, const double* y, const double* z,
+                     const double* w, double* fcoef, cudaStream_t s);
+
+// Pointwise functional on caller arrays (parity tests).
+void launch_functional_points(const xcf::FuncDesc& f, int family, int nspin, long n, const double* rho,
+                              const double* sigma, const double* tau, double* eps, double* vrho,
+                              double* vsigma, double* vtau, cudaStream_t s);
+
+}  // namespace cgb

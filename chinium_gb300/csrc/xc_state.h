@@ -1,0 +1,80 @@
+// State behind the opaque C handles: the Grid (SubGrid blocks, AO store and
+// per-point work arrays, all resident in HBM) and the functional.
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "common.h"
+#include "kernels.h"
+#include "model.h"
+
+namespace cgb {
+
+void ensure_device();
+
+struct Functional {
+    std::vector<int> ids;
+    int nspin = 1;
+    int family = 0;
+    double exx = 0;
+    xcf::FuncDesc desc{};
+    void init(const std::vector<int>& ids, int nspin);
+};
+
+struct Grid {
+    BasisSet basis;
+    int nspin = 1;
+    int type = 0;
+    double screen_thr = 0;
+    cudaStream_t stream = nullptr;
+
+    long npoints = 0, Gp = 0;
+    std::vector<BlockDesc> blocks;
+    std::vector<int> basis_lists, shell_lists;
+    std::vector<double> hx, hy, hz;
+    int max_nb = 0;
+    long screened_pairs = 0;
+    long ao_elements = 0;
+    int ncomp = 0;
+    int ao_order = -1;
+    bool have_density = false, have_potential = false;
+    int eval_family = 0;
+    int n_partial = 0;
+
+    DevBuf<double> d_x, d_y, d_z, d_w, d_atoms;
+    DevBuf<int> d_sh_type, d_sh_l, d_sh_nprim, d_sh_poff, d_sh_first;
+    DevBuf<double> d_sh_xyz, d_exps, d_coefs;
+    DevBuf<BlockDesc> d_blocks;
+    DevBuf<int> d_lists, d_shell_lists;
+    DevBuf<double> d_ao;
+    DevBuf<double> d_rho, d_rho1, d_tau, d_sigma, d_eps, d_vrho, d_vsigma, d_vtau, d_fcoef, d_partial, d_scalar;
+    DevBuf<double> d_D, d_V;
+
+    // stage timing: events bracket density, functional, energy, fock
+    bool profiling = false;
+    cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    void mark(int i);
+    ~Grid();
+
+    void build(const BasisSet& b, const std::string& grid_name, int nspin, double thr);
+    DevShells dev_shells() const;
+    void get_ao(int derivative);
+    void ensure_work();
+    void density_device(const double* dD);
+    void evaluate(const Functional& f);
+    void energy_device(double* dE);
+    void fock_device(double* dV, int family);
+};
+
+}  // namespace cgb
+
+struct xc_basis {
+    cgb::BasisSet b;
+};
+struct xc_grid {
+    cgb::Grid g;
+};
+struct xc_functional {
+    cgb::Functional f;
+};

@@ -1,0 +1,264 @@
+"""Python mirror of the reference's XC interface over the C ABI.
+
+``Grid`` mirrors ``Grid`` (src/Grid/Grid.h:90-116) and ``ExchangeCorrelation``
+mirrors ``ExchangeCorrelation`` (src/ExchangeCorrelation.h:8-17): same member
+names, argument meaning and call order, so SCF code written against the
+reference reads the same:
+
+    grid = Grid(basis, "SG-1", nspin=1); xc = ExchangeCorrelation(); xc.Read("PBE")
+    grid.setType(xc.type); grid.getAO(0)
+    grid.getDensity([2 * D]); xc.Evaluate("ev", grid)
+    Exc = grid.getEnergy(); Vxc = grid.getFock()[0]
+
+Matrices are numpy float64 (n, n); errors raise ``XCError`` (status code +
+message), where the reference throws std::runtime_error or asserts.
+"""
+import ctypes
+
+import numpy as np
+
+from ._lib import GridInfo, PRECISION_FP64, PRECISION_MIXED, XCError, check, lib
+
+__all__ = ["Basis", "Grid", "ExchangeCorrelation", "XCError", "PRECISION_FP64", "PRECISION_MIXED"]
+
+
+def _p(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+class Basis:
+    """Centres plus libint2-normalised contracted shells for a named basis
+    set (the Mwfn basis after Normalize(), Representation.cpp:30-53)."""
+
+    def __init__(self, Z, xyz_bohr, name):
+        Z = np.ascontiguousarray(Z, dtype=np.int32)
+        xyz = np.ascontiguousarray(np.asarray(xyz_bohr, dtype=np.float64).reshape(-1, 3))
+        if len(Z) != len(xyz):
+            raise ValueError("Z and coordinates differ in length")
+        self.Z = Z
+        self.xyz = xyz
+        self.name = name
+        h = ctypes.c_void_p()
+        check(lib().xc_basis_create(len(Z), _p(Z), _p(xyz), name.encode(), ctypes.byref(h)))
+        self._h = h
+        n = ctypes.c_int()
+        check(lib().xc_basis_nbasis(h, ctypes.byref(n)))
+        self.nbasis = n.value
+
+    def shells(self):
+        L = lib()
+        ns = ctypes.c_int()
+        check(L.xc_basis_nshells(self._h, ctypes.byref(ns)))
+        atom, typ, first, nprim = (np.zeros(ns.value, dtype=np.int32) for _ in range(4))
+        check(L.xc_basis_shells(self._h, _p(atom), _p(typ), _p(first), _p(nprim)))
+        exps = np.zeros(int(nprim.sum()))
+        coefs = np.zeros(int(nprim.sum()))
+        check(L.xc_basis_primitives(self._h, _p(exps), _p(coefs)))
+        return dict(atom=atom, type=typ, first=first, nprim=nprim, exps=exps, coefs=coefs)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().xc_basis_destroy(h)
+            self._h = None
+
+
+class Grid:
+    """Grid::Grid(Mwfn*, grid, nthreads, output) on the GPU.
+
+    screen_threshold: AO magnitude below which a shell is dropped from a block
+    (0 keeps every shell in every block, as the reference does)."""
+
+    def __init__(self, basis, grid="SG-1", nspin=1, screen_threshold=0.0):
+        self.basis = basis
+        self.nspin = nspin
+        h = ctypes.c_void_p()
+        check(lib().xc_grid_create(basis._h, grid.encode(), nspin, float(screen_threshold), ctypes.byref(h)))
+        self._h = h
+        self.nbasis = basis.nbasis
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().xc_grid_destroy(h)
+            self._h = None
+
+    # -- reference members ------------------------------------------------
+    def setType(self, type_):
+        check(lib().xc_grid_set_type(self._h, int(type_)))
+
+    def getAO(self, derivative=0, output=0):
+        check(lib().xc_grid_get_ao(self._h, int(derivative)))
+
+    def getDensity(self, D):
+        D = self._stack(D)
+        check(lib().xc_grid_get_density(self._h, _p(D), self.nspin))
+
+    def getNumElectrons(self):
+        n = ctypes.c_double()
+        check(lib().xc_grid_num_electrons(self._h, ctypes.byref(n)))
+        return n.value
+
+    def getEnergy(self):
+        e = ctypes.c_double()
+        check(lib().xc_grid_get_energy(self._h, ctypes.byref(e)))
+        return e.value
+
+    def getFock(self):
+        n = self.nbasis
+        V = np.zeros((self.nspin, n, n))  # column-major per spin == transposed row-major
+        check(lib().xc_grid_get_fock(self._h, _p(V)))
+        return [V[s].T.copy() for s in range(self.nspin)]
+
+    # -- fused build --------------------------------------------------------
+    def build(self, xc, D, precision=PRECISION_FP64):
+        """getDensity + Evaluate("ev") + getEnergy + getFock in one call."""
+        D = self._stack(D)
+        n = self.nbasis
+        V = np.zeros((self.nspin, n, n))
+        e = ctypes.c_double()
+        check(lib().xc_build(self._h, xc._h, _p(D), self.nspin, int(precision), ctypes.byref(e), _p(V)))
+        return e.value, [V[s].T.copy() for s in range(self.nspin)]
+
+    def build_device(self, xc, d_D, d_E, d_V, precision=PRECISION_FP64):
+        """Device-pointer variant (ints or torch tensors); no synchronisation."""
+        ptr = lambda t: ctypes.c_void_p(t if isinstance(t, int) else t.data_ptr())
+        check(lib().xc_build_device(self._h, xc._h, ptr(d_D), self.nspin, int(precision), ptr(d_E), ptr(d_V)))
+
+    def profile(self, enable=True):
+        check(lib().xc_grid_profile(self._h, int(bool(enable))))
+
+    def stage_ms(self):
+        """[density, functional, energy, fock] device milliseconds of the last build."""
+        ms = np.zeros(4)
+        check(lib().xc_grid_stage_ms(self._h, _p(ms)))
+        return ms
+
+    def set_stream(self, stream_ptr):
+        check(lib().xc_grid_set_stream(self._h, ctypes.c_void_p(stream_ptr)))
+
+    def sap_fock(self):
+        """SuperpositionAtomicPotential (GuessSCF.cpp:17-75)."""
+        n = self.nbasis
+        V = np.zeros((n, n))
+        check(lib().xc_sap_fock(self._h, _p(V)))
+        return V.T.copy()
+
+    # -- inspection -----------------------------------------------------------
+    def info(self):
+        i = GridInfo()
+        check(lib().xc_grid_info_get(self._h, ctypes.byref(i)))
+        return {k: getattr(i, k) for k, _ in GridInfo._fields_}
+
+    def points(self):
+        inf = self.info()
+        G, nb = inf["npoints_padded"], inf["nblocks"]
+        x, y, z, w = (np.zeros(G) for _ in range(4))
+        off, ng, nreal, nbas = (np.zeros(nb, dtype=np.int32) for _ in range(4))
+        check(lib().xc_grid_points(self._h, _p(x), _p(y), _p(z), _p(w), _p(off), _p(ng), _p(nreal), _p(nbas)))
+        return dict(x=x, y=y, z=z, w=w, off=off, ng=ng, nreal=nreal, nb=nbas)
+
+    def density_values(self):
+        inf = self.info()
+        G, s = inf["npoints_padded"], self.nspin
+        rho = np.zeros((s, G))
+        rho1 = np.zeros((s, 3, G))
+        sigma = np.zeros((1 if s == 1 else 3, G))
+        tau = np.zeros((s, G))
+        check(lib().xc_grid_density_values(self._h, _p(rho), _p(rho1), _p(sigma), _p(tau)))
+        return dict(rho=rho, rho1=rho1, sigma=sigma, tau=tau)
+
+    def potential_values(self):
+        inf = self.info()
+        G, s = inf["npoints_padded"], self.nspin
+        eps = np.zeros(G)
+        vrho = np.zeros((s, G))
+        vsigma = np.zeros((1 if s == 1 else 3, G))
+        vtau = np.zeros((s, G))
+        check(lib().xc_grid_potential_values(self._h, _p(eps), _p(vrho), _p(vsigma), _p(vtau)))
+        return dict(eps=eps, vrho=vrho, vsigma=vsigma, vtau=vtau)
+
+    def block_ao(self, b):
+        p = self.points()
+        ng, nb = int(p["ng"][b]), int(p["nb"][b])
+        ao = np.zeros((nb, ng))
+        ao1 = np.zeros((3, nb, ng))
+        lst = np.zeros(nb, dtype=np.int32)
+        check(lib().xc_grid_block_ao(self._h, int(b), _p(ao), _p(ao1), _p(lst)))
+        return ao, ao1, lst
+
+    def _stack(self, D):
+        if isinstance(D, np.ndarray) and D.ndim == 2:
+            D = [D]
+        D = [np.asarray(d, dtype=np.float64) for d in D]
+        if len(D) != self.nspin:
+            raise XCError(-1, "Wrong number of spin types!")
+        # column-major per spin: store D^T row-major
+        return np.ascontiguousarray(np.stack([d.T for d in D]))
+
+
+class ExchangeCorrelation:
+    """ExchangeCorrelation (src/ExchangeCorrelation.h:8-17)."""
+
+    def __init__(self, spin=1):
+        self.Spin = spin
+        self.Codes = []
+        self.EXX = 1.0
+        self.Family = ""
+        self._h = None
+
+    def Read(self, df, output=False):
+        h = ctypes.c_void_p()
+        check(lib().xc_functional_read(df.encode(), self.Spin, ctypes.byref(h)))
+        self._adopt(h)
+        return self
+
+    @classmethod
+    def from_ids(cls, ids, spin=1):
+        self = cls(spin)
+        ids = np.ascontiguousarray(ids, dtype=np.int32)
+        h = ctypes.c_void_p()
+        check(lib().xc_functional_create(_p(ids), len(ids), spin, ctypes.byref(h)))
+        self._adopt(h)
+        self.Codes = [int(i) for i in ids]
+        return self
+
+    def _adopt(self, h):
+        if self._h:
+            lib().xc_functional_destroy(self._h)
+        self._h = h
+        e = ctypes.c_double()
+        check(lib().xc_functional_exx(h, ctypes.byref(e)))
+        f = ctypes.c_int()
+        check(lib().xc_functional_family(h, ctypes.byref(f)))
+        self.EXX = e.value
+        self.type = f.value
+        self.Family = ["LDA", "GGA", "mGGA"][f.value]
+
+    def Evaluate(self, order, grid):
+        check(lib().xc_evaluate(self._h, grid._h, order.encode()))
+
+    def eval_points(self, rho, sigma=None, tau=None):
+        """Pointwise evaluation on host arrays (reference per-point layout)."""
+        s = self.Spin
+        rho = np.ascontiguousarray(rho, dtype=np.float64).reshape(s, -1)
+        n = rho.shape[1]
+        nsig = 1 if s == 1 else 3
+        sigma = np.zeros((nsig, n)) if sigma is None else np.ascontiguousarray(sigma, dtype=np.float64).reshape(nsig, n)
+        tau = np.zeros((s, n)) if tau is None else np.ascontiguousarray(tau, dtype=np.float64).reshape(s, n)
+        eps = np.zeros(n)
+        vrho = np.zeros((s, n))
+        vsigma = np.zeros((nsig, n))
+        vtau = np.zeros((s, n))
+        check(lib().xc_functional_eval_points(self._h, n, _p(rho), _p(sigma), _p(tau), _p(eps), _p(vrho),
+                                              _p(vsigma), _p(vtau)))
+        return eps, vrho, vsigma, vtau
+
+    def __bool__(self):
+        return self._h is not None
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().xc_functional_destroy(h)
+            self._h = None

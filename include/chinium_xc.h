@@ -1,0 +1,190 @@
+/*
+ * chinium_xc.h -- C ABI of the GB300 Kohn-Sham exchange-correlation build.
+ *
+ * Drop-in boundary for Chinium's XC path: the `Grid` class
+ * (src/Grid/Grid.h:90-116) and `ExchangeCorrelation` (src/ExchangeCorrelation.h:8-17)
+ * that the SCF drivers call once per iteration (src/HartreeFockKohnSham/
+ * Restricted/SP.cpp:51-56, Unrestricted/SP.cpp:64-71, Universal.cpp:49-73,
+ * GuessSCF.cpp:60).  Each entry point names the member it replaces.
+ *
+ * Conventions
+ *   - Every function returns an int status: XC_OK (0) or a negative XC_ERR_*;
+ *     xc_last_error() copies the calling thread's last message.  No exception
+ *     crosses the ABI.
+ *   - Matrices are n x n FP64 column-major (Eigen's default), one per spin,
+ *     spins concatenated: element (mu, nu, s) at D[s*n*n + nu*n + mu].
+ *   - Host buffers are caller-owned.  Device buffers are library-owned, except
+ *     in the *_device entry points, which take caller-owned device pointers.
+ *   - A handle is used by one host thread at a time.  Work is issued on the
+ *     handle's CUDA stream (xc_grid_set_stream); host-buffer calls return
+ *     after their results are in host memory.
+ *   - Coordinates are in bohr.
+ */
+#ifndef CHINIUM_XC_H
+#define CHINIUM_XC_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum xc_status {
+    XC_OK = 0,
+    XC_ERR_ARG = -1,         /* bad argument (null, size, range) */
+    XC_ERR_IO = -2,          /* missing or corrupt data file (grid, basis, .df) */
+    XC_ERR_CUDA = -3,        /* CUDA runtime error, or no usable GPU */
+    XC_ERR_STATE = -4,       /* call order violated (e.g. energy before density) */
+    XC_ERR_NOMEM = -5,       /* host or device allocation failed */
+    XC_ERR_UNSUPPORTED = -6, /* functional id / shell type not implemented */
+    XC_ERR_NUMERIC = -7,     /* non-finite values detected in inputs or results */
+    XC_ERR_TIMEOUT = -8,     /* a bounded device-side wait gave up */
+    XC_ERR_INTERNAL = -9
+};
+
+enum xc_precision {
+    XC_PRECISION_FP64 = 0,  /* plain path: every stage in FP64 */
+    XC_PRECISION_MIXED = 1  /* tensor-core split-precision contractions, FP64 accumulation */
+};
+
+enum xc_family { XC_FAMILY_LDA = 0, XC_FAMILY_GGA = 1, XC_FAMILY_MGGA = 2 };
+
+typedef struct xc_basis xc_basis;           /* centres + contracted shells (libmwfn Mwfn role) */
+typedef struct xc_grid xc_grid;             /* Grid */
+typedef struct xc_functional xc_functional; /* ExchangeCorrelation */
+
+/* Copies the calling thread's last error message (NUL-terminated). */
+int xc_last_error(char* buf, size_t len);
+
+/* Directory holding lebedev.txt, grids/, basis/, sap.txt (the role of
+ * $CHINIUM_PATH in GridGeneration.cpp:234 and ExchangeCorrelation.cpp:21). */
+int xc_set_data_path(const char* path);
+
+/* ------------------------------------------------------------------ basis */
+
+/* Centres and shells from a basis-set name (Representation.cpp:30-37 +
+ * Normalization.cpp:11-18: libint2-normalised contractions).  P shells are
+ * Cartesian (x, y, z); d and higher are pure (m = -l..l). */
+int xc_basis_create(int natoms, const int* Z, const double* xyz_bohr, const char* basis_name,
+                    xc_basis** out);
+int xc_basis_nbasis(const xc_basis* b, int* nbasis);
+/* Shell layout: per shell its atom, type (0 S, 1 Cartesian P, -l pure l),
+ * first function index and primitive count; arrays of length nshells. */
+int xc_basis_nshells(const xc_basis* b, int* nshells);
+int xc_basis_shells(const xc_basis* b, int* atom, int* type, int* first, int* nprim);
+/* Normalised primitive data; exps/coefs of length sum(nprim). */
+int xc_basis_primitives(const xc_basis* b, double* exps, double* coefs);
+int xc_basis_destroy(xc_basis* b);
+
+/* ------------------------------------------------------------------- grid */
+
+/* Grid::Grid(Mwfn*, grid, nthreads, output) (GridGeneration.cpp:232-310):
+ * SG-n atom grids, Becke partition (FP64, on the GPU), blocks of <= 128
+ * points by recursive halving in generation order, padded to a multiple of
+ * 8.  nspin is 1 (restricted) or 2 (unrestricted) (SubGrid::Spin).
+ * screen_threshold: AO magnitude below which a shell is dropped from a block
+ * (0 keeps every shell in every block, as the reference does). */
+int xc_grid_create(const xc_basis* b, const char* grid_name, int nspin, double screen_threshold,
+                   xc_grid** out);
+int xc_grid_destroy(xc_grid* g);
+/* Optional CUDA stream (cudaStream_t passed as void*); NULL = legacy default. */
+int xc_grid_set_stream(xc_grid* g, void* stream);
+
+/* Grid::setType (Grid.cpp:14-20): 0 LDA, 1 GGA, 2 meta-GGA. */
+int xc_grid_set_type(xc_grid* g, int type);
+
+/* Grid::getAO(derivative, output) (Grid.cpp:22-33): evaluates and stores AO
+ * values to order type+derivative (<= 1 here) for every block. */
+int xc_grid_get_ao(xc_grid* g, int derivative);
+
+/* Grid::getNumElectrons (Grid.cpp:51-61). */
+int xc_grid_num_electrons(xc_grid* g, double* n);
+
+/* Grid::getDensity(std::vector<EigenMatrix>) (Grid.cpp:35-49): D is nspin
+ * n x n matrices; restricted callers pass the total density 2*C_occ C_occ^T. */
+int xc_grid_get_density(xc_grid* g, const double* D, int nspin);
+
+/* Grid::getEnergy (Grid.cpp:112-122): E_xc = sum_g w_g (sum_s rho_gs) eps_g. */
+int xc_grid_get_energy(xc_grid* g, double* E);
+
+/* Grid::getFock (Grid.cpp:156-171): V_xc, nspin matrices into V. */
+int xc_grid_get_fock(xc_grid* g, double* V);
+
+/* Sizes and per-block layout, for inspection and parity tests. */
+typedef struct xc_grid_info {
+    long npoints;        /* real points (sum of unpadded block sizes) */
+    long npoints_padded; /* sum of padded block sizes */
+    int nblocks;
+    int nbasis;
+    int nspin;
+    int type;
+    long ao_elements;    /* stored AO values per component */
+    long screened_pairs; /* sum over blocks of n_b^2 */
+} xc_grid_info;
+int xc_grid_info_get(const xc_grid* g, xc_grid_info* info);
+/* Padded points in block order: x, y, z, w (each npoints_padded) and
+ * per-block (offset, padded size, real size, n_b). */
+int xc_grid_points(const xc_grid* g, double* x, double* y, double* z, double* w, int* blk_off,
+                   int* blk_ng, int* blk_nreal, int* blk_nbasis);
+/* Per-point densities in block order: rho (s, G), rho1 (s, 3, G),
+ * sigma (ns(ns+1)/2, G), tau (s, G); NULL skips an array. */
+int xc_grid_density_values(const xc_grid* g, double* rho, double* rho1, double* sigma,
+                           double* tau);
+/* Per-point functional outputs: eps (G), vrho (s, G), vsigma (ns(ns+1)/2, G),
+ * vtau (s, G); NULL skips an array. */
+int xc_grid_potential_values(const xc_grid* g, double* eps, double* vrho, double* vsigma,
+                             double* vtau);
+/* AO values of one block: ao (n_b, ng) and, if stored, ao1 (3, n_b, ng);
+ * basis_list (n_b) gives the global function index of each row. */
+int xc_grid_block_ao(const xc_grid* g, int block, double* ao, double* ao1, int* basis_list);
+
+/* ------------------------------------------------------------- functional */
+
+/* ExchangeCorrelation::Read(df, output) (ExchangeCorrelation.cpp:18-84):
+ * reads the libxc ids of a named functional (PBE, B3LYP, TPSS, R2SCAN, ...). */
+int xc_functional_read(const char* df_name, int nspin, xc_functional** out);
+/* Same, from explicit libxc ids. */
+int xc_functional_create(const int* ids, int nids, int nspin, xc_functional** out);
+int xc_functional_destroy(xc_functional* f);
+/* Public fields EXX and Family (ExchangeCorrelation.h:10-12). */
+int xc_functional_exx(const xc_functional* f, double* exx);
+int xc_functional_family(const xc_functional* f, int* family);
+
+/* ExchangeCorrelation::Evaluate(order, grid) (ExchangeCorrelation.cpp:165-248):
+ * order "e", "v" or "ev" on the grid's current density. */
+int xc_evaluate(xc_functional* f, xc_grid* g, const char* order);
+
+/* Pointwise evaluation on caller data (host arrays, layout as
+ * xc_grid_density_values/xc_grid_potential_values), for parity tests. */
+int xc_functional_eval_points(xc_functional* f, long npoints, const double* rho,
+                              const double* sigma, const double* tau, double* eps, double* vrho,
+                              double* vsigma, double* vtau);
+
+/* ------------------------------------------------------------ fused build */
+
+/* getDensity + Evaluate("ev") + getEnergy + getFock in one call
+ * (the sequence at Restricted/SP.cpp:52-55).  Host buffers in and out. */
+int xc_build(xc_grid* g, xc_functional* f, const double* D, int nspin, int precision, double* E,
+             double* V);
+
+/* Same with caller-owned device pointers (d_D in, d_E scalar and d_V out),
+ * issued on the grid's stream; does not synchronise. */
+int xc_build_device(xc_grid* g, xc_functional* f, const double* d_D, int nspin, int precision,
+                    double* d_E, double* d_V);
+
+/* Per-stage device timing of the last build (the reference's __now__ /
+ * __duration__ printouts around its stages, src/Macro/Time.h:1-2, as CUDA
+ * events on the grid's stream).  enable != 0 records events from the next
+ * build on; xc_grid_stage_ms waits for them and returns milliseconds of
+ * [density, functional, energy, fock] in ms[0..3]. */
+int xc_grid_profile(xc_grid* g, int enable);
+int xc_grid_stage_ms(xc_grid* g, double* ms);
+
+/* SAP potential matrix (GuessSCF.cpp:17-75): V_mu,nu = sum_g w v_SAP(r_g)
+ * phi_mu phi_nu with v_SAP the nearest-radius tabulated atomic potentials. */
+int xc_sap_fock(xc_grid* g, double* V);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,82 @@
+/*
+ * ORACLE -- test infrastructure only.  A CPU FP64 restatement of Chinium's
+ * Kohn-Sham XC build (src/Grid + src/ExchangeCorrelation.cpp).  Only tests/,
+ * __graft_entry__.smoke() and bench.py's CPU-baseline leg may load it; the
+ * product never links or calls it.
+ *
+ * Parity status: the grid, AO, density, energy and Fock stages restate the
+ * reference line by line (citations per function).  The functional stage
+ * restates libxc's published functionals (libxc is absent; the reference
+ * points at the libxc 6.2.2 list, DensityFunctionals/README.md:1): parity
+ * with libxc is unpinned.  The reference ships no golden XC vectors.
+ *
+ * Layouts follow the reference: per block, AO(g, mu) column-major with g
+ * fastest, AO1(g, mu, r), Rho(g, s), Rho1(g, r, s), Sigma(g, s(s+1)/2),
+ * Tau(g, s); matrices n x n column-major.
+ */
+#ifndef XC_ORACLE_H
+#define XC_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Becke-partitioned weights of raw atom-centred points.
+ * GridGeneration.cpp:134-153 with s_p_mu at :50-71.  owner[k] is the atom
+ * whose sphere generated point k; w_in is radial*Lebedev*4pi weight. */
+void oracle_becke(int natoms, const double* atom_xyz, long npts, const double* px,
+                  const double* py, const double* pz, const int* owner, const double* w_in,
+                  double* w_out);
+
+/* AO values (deriv=0) or values+gradients (deriv=1) for one block of points.
+ * GridAO.cpp:14-215 (radial part, product rule) and AO/{S,CartP,PureP,PureD,
+ * PureF,PureG}.hpp (angular part).  Shell arrays: shell_type uses the
+ * reference's convention (0 S, 1 Cartesian P, -1 pure P, -l pure l>=2).
+ * Output: ao[mu*ng + g]; ao1[(r*nbasis + mu)*ng + g]. */
+void oracle_ao(int nshells, const int* shell_type, const int* shell_nprim,
+               const int* shell_prim_off, const double* shell_center, const double* exps,
+               const double* coefs, int nbasis, int ng, const double* x, const double* y,
+               const double* z, int deriv, double* ao, double* ao1);
+
+/* rho, grad rho (x2), sigma, tau (x1/2) for one block.  GridDensity.cpp:12-41
+ * with the Rho / Rho1 / Sigma / Tau einsums, loop order kept. D is (n,n,s). */
+void oracle_density(int ng, int nbasis, int nspin, int type, const double* D, const double* ao,
+                    const double* ao1, double* rho, double* rho1, double* sigma, double* tau);
+
+/* Sum over functional ids of eps, vrho, vsigma, vtau on ng points
+ * (ExchangeCorrelation.cpp:165-248, order "ev").  Inputs/outputs use the
+ * reference's per-block layout (g fastest).  Returns 0, or -1 on an unknown id. */
+int oracle_functional(int nids, const int* ids, int nspin, int ng, const double* rho,
+                      const double* sigma, const double* tau, double* eps, double* vrho,
+                      double* vsigma, double* vtau);
+
+/* Per-block E_xc contribution, GridEnergy.cpp:11-13 einsum W,Rho,Eps->E. */
+double oracle_energy(int ng, int nspin, const double* w, const double* rho, const double* eps);
+
+/* Per-block V_xc accumulated into F (n,n,s) through basis_list.
+ * GridFock.cpp:11-49 with the F0 / F1 / F2 einsums; lapl terms are zero for
+ * the laplacian-free functionals served here. */
+void oracle_fock(int ng, int nbasis_block, int nbasis_total, const int* basis_list, int nspin,
+                 int type, const double* w, const double* ao, const double* ao1,
+                 const double* rho1, const double* vrho, const double* vsigma,
+                 const double* vtau, double* F);
+
+/* SAP potential on points (GuessSCF.cpp:38-57): sum over atoms of the
+ * nearest-radius tabulated value divided by r (r += 1e-12). */
+void oracle_sap(int natoms, const double* atom_xyz, const double* atom_table /* natoms x 751 */,
+                const double* radii, int nradii, long npts, const double* px, const double* py,
+                const double* pz, double* v);
+
+/* Whole build over a list of blocks (density -> functional -> energy ->
+ * Fock), OpenMP over blocks, mirroring Grid::getDensity / Evaluate /
+ * getEnergy / getFock.  Used as the timed CPU baseline.  Blocks are given as
+ * offsets into concatenated per-block arrays. */
+int oracle_build(int nblocks, const int* blk_ng, const long* blk_pt_off, const long* blk_ao_off,
+                 const double* w, const double* ao, const double* ao1, int nbasis, int nspin,
+                 int type, const double* D, int nids, const int* ids, int nthreads,
+                 double* E_out, double* F_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

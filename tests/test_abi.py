@@ -1,0 +1,105 @@
+"""CPU tests of the C ABI and host logic (no GPU computation)."""
+import ctypes
+import subprocess
+
+import numpy as np
+import pytest
+
+import chinium_gb300 as cg
+from chinium_gb300 import molecules as M
+from chinium_gb300._lib import LIB_PATH, header_symbols, lib
+from conftest import has_gpu
+from oracle import oracle as O
+
+
+def test_library_exports_every_header_symbol():
+    L = lib()
+    syms = header_symbols()
+    assert len(syms) >= 30
+    for s in syms:
+        assert hasattr(L, s), s
+    out = subprocess.run(["nm", "-D", "--defined-only", LIB_PATH], capture_output=True, text=True).stdout
+    exported = {ln.split()[-1] for ln in out.splitlines() if " T " in ln}
+    assert set(syms) <= exported
+
+
+@pytest.mark.parametrize("mol,basis,n", [("h2o", "def2-svp", 24), ("c18", "def2-tzvp", 558), ("fe4s4", "def2-tzvp", 328)])
+def test_basis_sizes(mol, basis, n):
+    Z, xyz = getattr(M, mol)()
+    assert cg.Basis(Z, xyz, basis).nbasis == n
+
+
+def test_basis_normalisation_matches_oracle():
+    Z, xyz = M.fe4s4()
+    b = cg.Basis(Z, xyz, "def2-tzvp")
+    ob = O.Basis(Z, xyz, "def2-tzvp")
+    sh = b.shells()
+    assert np.array_equal(sh["type"], ob.types)
+    assert np.array_equal(sh["nprim"], ob.nprim)
+    assert np.allclose(sh["exps"], ob.exps, rtol=0, atol=0)
+    assert np.allclose(sh["coefs"], ob.coefs, rtol=1e-14)
+
+
+def test_alkane_batch_shapes():
+    mols = M.alkane_batch(64, seed=0)
+    assert len(mols) == 64
+    for Z, xyz in mols:
+        nC = Z.count(6)
+        assert Z.count(1) == 2 * nC + 2
+        d = np.linalg.norm(xyz[:, None] - xyz[None], axis=-1) + np.eye(len(Z)) * 10
+        assert d.min() > 0.9 * M.ANGSTROM2BOHR
+
+
+def test_c18_and_fe4s4_geometry():
+    Z, xyz = M.c18()
+    r = np.linalg.norm(xyz, axis=1) / M.ANGSTROM2BOHR
+    assert np.allclose(r, 3.88)
+    d = np.linalg.norm(np.roll(xyz, -1, 0) - xyz, axis=1) / M.ANGSTROM2BOHR
+    assert np.allclose(d[0::2] / d[1::2], 1.22 / 1.35)
+    Z, xyz = M.fe4s4()
+    dfs = [np.linalg.norm(xyz[i] - xyz[j]) / M.ANGSTROM2BOHR for i in range(4) for j in range(4, 8)]
+    assert sorted(dfs)[:12] == pytest.approx([2.28] * 12, abs=1e-9)
+
+
+def test_functional_read_fields():
+    for name, ids, exx, fam in [("PBE", [321, 322], 0.0, "GGA"), ("B3LYP", [402], 0.2, "GGA"),
+                                ("TPSS", [202, 231], 0.0, "mGGA"), ("R2SCAN", [497, 498], 0.0, "mGGA"),
+                                ("SVWN5", [1, 7], 0.0, "LDA"), ("TPSSH", [457], 0.1, "mGGA")]:
+        xc = cg.ExchangeCorrelation().Read(name)
+        assert xc.EXX == pytest.approx(exx)
+        assert xc.Family == fam
+        assert bool(xc)
+
+
+def test_error_codes():
+    with pytest.raises(cg.XCError) as e:
+        cg.ExchangeCorrelation().Read("NO_SUCH_FUNCTIONAL")
+    assert e.value.code == -2
+    with pytest.raises(cg.XCError) as e:
+        cg.ExchangeCorrelation().Read("M06-2X")  # ids present in the data, functional not implemented
+    assert e.value.code == -6
+    with pytest.raises(cg.XCError) as e:
+        cg.ExchangeCorrelation.from_ids([402], spin=3)
+    assert e.value.code == -1
+    with pytest.raises(cg.XCError) as e:
+        cg.Basis([8, 1, 1], np.zeros((3, 3)), "no-such-basis")
+    assert e.value.code == -2
+    with pytest.raises(cg.XCError) as e:
+        cg.Basis([54], np.zeros((1, 3)), "def2-svp")  # element outside the packaged tables
+    assert e.value.code == -2
+    Z, xyz = M.fe4s4()
+    b = cg.Basis(Z, xyz, "def2-tzvp")
+    with pytest.raises(cg.XCError) as e:
+        cg.Grid(b, "SG-1")  # SG-1 has no Fe recipe (the reference throws the same)
+    assert e.value.code in (-2, -3)
+    buf = ctypes.create_string_buffer(8)
+    assert lib().xc_last_error(buf, 8) == 0
+
+
+@pytest.mark.skipif(has_gpu(), reason="checks the no-GPU error path")
+def test_grid_without_gpu_fails_loudly():
+    Z, xyz = M.h2o()
+    b = cg.Basis(Z, xyz, "def2-svp")
+    with pytest.raises(cg.XCError) as e:
+        cg.Grid(b, "SG-1")
+    assert e.value.code == -3
