@@ -274,7 +274,7 @@ def main():
                        "l2": "inputs larger than L2 (AO store %.2f GB)" % (info["ao_elements"] * 4 * 8 / 1e9),
                        "E_xc": Exc},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 8 * n * n, "d2h_bytes_per_step": 8 * n * n + 8},
-            "gpu_launches": args.steps * 5,
+            "gpu_launches": args.steps * 4,
             "roofline": roof, "clocks": clocks}
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(wl, D, args.cpu_blocks, os.cpu_count() or 1)

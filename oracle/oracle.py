@@ -221,7 +221,7 @@ def atom_points(z, xyz, recipes, lebedev):
     return np.concatenate(xs), np.concatenate(ys), np.concatenate(zs), np.concatenate(ws)
 
 
-def grid_points(Z, xyz_bohr, grid_name):
+def grid_points(Z, xyz_bohr, grid_name, return_unpartitioned=False):
     """All points (x, y, z, w) in the reference's generation order with
     Becke-partitioned weights."""
     lebedev = load_lebedev()
@@ -236,6 +236,8 @@ def grid_points(Z, xyz_bohr, grid_name):
     w = np.empty_like(w_in)
     lib().oracle_becke(ctypes.c_int(len(Z)), _p(np.ascontiguousarray(xyz.ravel())), ctypes.c_long(len(px)),
                        _p(px), _p(py), _p(pz), _p(owner), _p(w_in), _p(w))
+    if return_unpartitioned:
+        return px, py, pz, w, w_in
     return px, py, pz, w
 
 
@@ -325,9 +327,11 @@ class OracleGrid:
 
     def __init__(self, basis, grid_name, Z, xyz_bohr, deriv=1):
         self.basis = basis
-        px, py, pz, w = grid_points(Z, xyz_bohr, grid_name)
+        px, py, pz, w, w_in = grid_points(Z, xyz_bohr, grid_name, return_unpartitioned=True)
         self.npoints = len(px)
         self.blocks = padded_blocks(px, py, pz, w)
+        # radial * 4 pi * Lebedev weight before the Becke factor, padded like w
+        self.w_unpartitioned = np.concatenate([b[3] for b in padded_blocks(px, py, pz, w_in)])
         self.deriv = deriv
         self.ao = []
         for bx, by, bz, bw in self.blocks:

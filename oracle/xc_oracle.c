@@ -121,7 +121,7 @@ void oracle_ao(int nshells, const int* shell_type, const int* shell_nprim,
             }
             const double A = tmp0;
             const double Ax = -2 * x * tmp1, Ay = -2 * y * tmp1, Az = -2 * z * tmp1;
-            cplx Q[16], Qx[16], Qy[16], Qz[16];
+            cplx Q[16] = {0}, Qx[16] = {0}, Qy[16] = {0}, Qz[16] = {0};
             size = angular(type, x, y, z, Q);
             if (deriv) {
                 const double h = 1e-30;
