@@ -16,7 +16,7 @@ LIB = os.path.join(OUT, "libchinium_xc.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
-              "-Xcompiler", "-Wall,-Wno-unused-function"]
+              "-Xcompiler", "-Wall,-Wno-unused-function,-Wno-unknown-pragmas"]
 
 
 def _nvcc():

@@ -678,7 +678,12 @@ int xc_build_device(xc_grid* g, xc_functional* f, const double* dD, int nspin, i
         Grid& G = g->g;
         CGB_CHECK(nspin == G.nspin, XC_ERR_ARG, "Wrong number of spin types!");
         CGB_CHECK(precision == XC_PRECISION_FP64 || precision == XC_PRECISION_MIXED, XC_ERR_ARG, "bad precision");
-        CGB_CHECK(precision == XC_PRECISION_FP64, XC_ERR_UNSUPPORTED, "mixed precision path not built yet");
+        CGB_CHECK(f->f.nspin == G.nspin, XC_ERR_ARG, "functional and grid disagree on the number of spins");
+        CGB_CHECK(f->f.family <= G.type, XC_ERR_STATE, "grid type is below the functional family (setType/getAO)");
+        if (precision == XC_PRECISION_MIXED) {
+            G.build_mixed(dD, f->f, dE, dV);
+            return;
+        }
         G.density_device(dD);
         G.evaluate(f->f);
         G.energy_device(dE);
@@ -699,6 +704,8 @@ int xc_build(xc_grid* g, xc_functional* f, const double* D, int nspin, int preci
         CGB_CUDA(cudaMemcpyAsync(E, G.d_scalar.p, sizeof(double), cudaMemcpyDeviceToHost, G.stream));
         CGB_CUDA(cudaMemcpyAsync(V, G.d_V.p, nn * sizeof(double), cudaMemcpyDeviceToHost, G.stream));
         CGB_CUDA(cudaStreamSynchronize(G.stream));
+        if (precision == XC_PRECISION_MIXED && G.mixed_error())
+            throw Error(XC_ERR_TIMEOUT, "a bounded wait of the tensor-core pipeline gave up");
     });
 }
 

@@ -7,11 +7,15 @@
 
 #include "common.h"
 #include "kernels.h"
+#include "mixed.h"
 #include "model.h"
 
 namespace cgb {
 
 void ensure_device();
+
+// Default AO screening threshold of the mixed-precision tiles (|phi|, |grad phi|).
+constexpr double kMixedScreen = 1e-11;
 
 struct Functional {
     std::vector<int> ids;
@@ -65,6 +69,12 @@ struct Grid {
     void evaluate(const Functional& f);
     void energy_device(double* dE);
     void fock_device(double* dV, int family);
+
+    // mixed-precision (tensor-core) path; tiles and stores are prepared on first use
+    MixedState mx;
+    void prepare_mixed(double thr);
+    void build_mixed(const double* dD, const Functional& f, double* dE, double* dV);
+    int mixed_error();
 };
 
 }  // namespace cgb

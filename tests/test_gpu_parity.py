@@ -198,14 +198,29 @@ def test_sap_fock(h2o):
     assert np.abs(V - F).max() < 1e-10
 
 
-def test_mixed_precision_not_silently_plain(h2o):
-    """Until the tensor-core path exists, asking for it is an error, never a
-    silent FP64 run."""
+MIXED_E_TOL = 1e-6   # Eh, split-BF16 (~FP32) contractions with FP64 accumulation
+MIXED_V_TOL = 1e-6
+
+
+@pytest.mark.parametrize("name,type_,nspin", [("SVWN5", 0, 1), ("PBE", 1, 1), ("B3LYP", 1, 1), ("TPSS", 2, 1),
+                                              ("R2SCAN", 2, 1), ("PBE", 1, 2), ("TPSS", 2, 2)])
+def test_mixed_precision_against_fp64(h2o, name, type_, nspin):
+    """Tensor-core path vs the FP64 path on the same grid and density."""
     Z, xyz, b, ob, og = h2o
-    D = model_density(og, 5)
-    xc = cg.ExchangeCorrelation().Read("PBE")
-    g = make_grid(b)
-    try:
-        E, V = g.build(xc, [D], precision=cg.PRECISION_MIXED)
-    except cg.XCError as e:
-        assert e.code == -6
+    if nspin == 1:
+        D = [model_density(og, 5)]
+    else:
+        D = list(model_density(og, (5, 4), nspin=2, seed=2))
+    xc = cg.ExchangeCorrelation(spin=nspin).Read(name)
+    g = make_grid(b, nspin=nspin, type_=type_)
+    E64, V64 = g.build(xc, D)
+    E32, V32 = g.build(xc, D, precision=cg.PRECISION_MIXED)
+    dE = abs(E32 - E64)
+    dV = max(np.abs(V32[s] - V64[s]).max() for s in range(nspin))
+    print("mixed vs fp64 %s ns=%d: |dE|=%.3e max|dV|=%.3e" % (name, nspin, dE, dV))
+    assert dE < MIXED_E_TOL and dV < MIXED_V_TOL, (dE, dV)
+    for s in range(nspin):
+        assert np.allclose(V32[s], V32[s].T, atol=1e-14)
+    # a second call reuses the prepared tiles and gives the same result
+    E32b, V32b = g.build(xc, D, precision=cg.PRECISION_MIXED)
+    assert E32b == E32
