@@ -5,7 +5,7 @@ SG-2 grid (140 220 points, 2048 blocks).  A step is one XC build: density
 (rho, grad rho) -> B3LYP functional -> E_xc -> V_xc, on an SCF-shaped
 density matrix resident in HBM.  Synthetic geometry and density (seeded).
 
-  python bench.py [--steps K] [--warmup W] [--precision fp64|mixed]
+  python bench.py [--steps K] [--warmup W] [--precision mixed|fp64]
   python bench.py --impl reference   # the CPU XC path (oracle port of the
                                      # reference's per-block einsum loops)
 
@@ -159,21 +159,36 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def time_builds(torch, grid, xc, dD, dE, dV, precision, steps, stream):
+    """Device time of `steps` back-to-back builds on the build stream (s)."""
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(steps):
+        grid.build_device(xc, dD, dE, dV, precision)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    return ev0.elapsed_time(ev1) / 1e3
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--cpu-blocks", type=int, default=96)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
 
+    import ctypes
     import torch
     import chinium_gb300 as cg
+    from chinium_gb300._lib import check, lib
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -190,19 +205,27 @@ def main():
     xc = cg.ExchangeCorrelation().Read(wl["functional"])
     grid.setType(xc.type)
     grid.getAO(0)
-    info = grid.info()
     stream = torch.cuda.Stream()
     grid.set_stream(stream.cuda_stream)
-    precision = cg.PRECISION_FP64 if args.precision == "fp64" else cg.PRECISION_MIXED
+    P64, PMX = cg.PRECISION_FP64, cg.PRECISION_MIXED
+    precision = P64 if args.precision == "fp64" else PMX
 
     D = model_density(n, wl["nocc"])
     dD = torch.from_numpy(np.ascontiguousarray(D.T)).cuda()
     dE = torch.zeros(1, dtype=torch.float64, device="cuda")
     dV = torch.zeros((n, n), dtype=torch.float64, device="cuda")
 
+    # plain FP64 path on the same density: reference numbers and throughput
+    grid.build_device(xc, dD, dE, dV, P64)
+    stream.synchronize()
+    E64, V64 = float(dE.item()), dV.clone()
+    t_plain = time_builds(torch, grid, xc, dD, dE, dV, P64, args.plain_steps, stream)
+
     for _ in range(args.warmup):
         grid.build_device(xc, dD, dE, dV, precision)
     stream.synchronize()
+    Emx, Vmx = float(dE.item()), dV.clone()
+    info = grid.info()
 
     # stage timing of one build (CUDA events on the build stream)
     grid.profile(True)
@@ -210,33 +233,24 @@ def main():
     stage = grid.stage_ms()
     grid.profile(False)
 
-    clk_path = os.path.join(REPO, "gpurun_out" if os.path.isdir(os.path.join(REPO, "gpurun_out")) else "_work", "clocks_bench.csv")
-    os.makedirs(os.path.dirname(clk_path), exist_ok=True)
+    clk_dir = os.path.join(REPO, "gpurun_out") if os.path.isdir(os.path.join(REPO, "gpurun_out")) else os.path.join(REPO, "_work")
+    os.makedirs(clk_dir, exist_ok=True)
+    clk_path = os.path.join(clk_dir, "clocks_bench.csv")
     cp, cf = clocks_start(clk_path) if rank == 0 else (None, None)
     time.sleep(0.4)
     if world > 1:
         torch.distributed.barrier()
-    torch.cuda.synchronize()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ev0.record(stream)
-    for _ in range(args.steps):
-        grid.build_device(xc, dD, dE, dV, precision)
-    ev1.record(stream)
-    torch.cuda.synchronize()
+    t_dev = time_builds(torch, grid, xc, dD, dE, dV, precision, args.steps, stream)
     if world > 1:
         torch.distributed.barrier()
-    t_dev = ev0.elapsed_time(ev1) / 1e3
-    t = torch.tensor([t_dev], dtype=torch.float64, device="cuda")
-    if world > 1:
+        t = torch.tensor([t_dev], dtype=torch.float64, device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    t_dev = float(t.item())
+        t_dev = float(t.item())
     clocks = clocks_stop(cp, cf, clk_path) if rank == 0 else None
 
     # end to end through the public host-buffer call: pinned D in, E and V out
     Dh = torch.from_numpy(np.ascontiguousarray(D)).pin_memory()
     Vh = torch.zeros((n, n), dtype=torch.float64).pin_memory()
-    import ctypes
-    from chinium_gb300._lib import check, lib
     Eh = ctypes.c_double()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -249,32 +263,50 @@ def main():
     G = info["npoints_padded"]
     value = world * G * args.steps / t_dev
     e2e = world * G * args.steps / t_e2e
-    Exc = float(dE.item())
+    plain = G * args.plain_steps / t_plain
+    peaks = measured_peaks()
 
-    # roofline of the dominant stage (density or V assembly): FP64 FLOPs
-    # 2 g n_b^2 per block and contraction, over the stage's event time
-    flops_ctr = 2.0 * info["screened_pairs"] * (G / info["nblocks"])  # per contraction, all blocks
-    ms_den, ms_fock = stage[0], stage[3]
-    dom = "fock" if ms_fock >= ms_den else "density"
-    dom_ms = max(ms_den, ms_fock)
-    flops = flops_ctr * (1.0 if dom == "density" else 1.0)
-    peak = fp64_gemm_peak(torch)
-    achieved = flops / (dom_ms / 1e3) / 1e12
-    roof = {"bound": "fp64", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-            "frac": achieved / peak, "traffic": None,
-            "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (MEASURED_PEAKS.json has no FP64 entry)",
-            "stage_ms": {"density": stage[0], "functional": stage[1], "energy": stage[2], "fock": stage[3]}}
+    if precision == PMX:
+        # algorithmic FLOPs of one contraction: 2 * 128 * sum_t n_t^2 (screened tile sizes);
+        # the tensor core executes 6x that (three-term split cross products)
+        flops = 2.0 * 128 * info["mixed_pairs"]
+        ms_den, ms_fock = stage[0], stage[3]
+        dom, dom_ms = ("density_tc", ms_den) if ms_den >= ms_fock else ("fock_tc", ms_fock)
+        achieved = flops / (dom_ms / 1e3) / 1e12
+        peak = peaks.get("bf16_tflops", 1900.0)
+        roof = {"bound": "tensor", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "traffic": None,
+                "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst) -- of measured",
+                "executed_tensor_tflops": 6 * achieved,
+                "stage_ms": {"density": stage[0], "functional": stage[1], "energy": stage[2], "fock": stage[3]}}
+    else:
+        flops = 2.0 * info["screened_pairs"] * (G / info["nblocks"])
+        ms_den, ms_fock = stage[0], stage[3]
+        dom, dom_ms = ("density_fp64", ms_den) if ms_den >= ms_fock else ("fock_fp64", ms_fock)
+        peak = fp64_gemm_peak(torch)
+        achieved = flops / (dom_ms / 1e3) / 1e12
+        roof = {"bound": "fp64", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "traffic": None,
+                "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (no FP64 entry in MEASURED_PEAKS.json)",
+                "stage_ms": {"density": stage[0], "functional": stage[1], "energy": stage[2], "fock": stage[3]}}
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_dev / args.steps * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "bf16x3+f64",
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if precision == P64 else "bf16x3 (split) + f64 accumulation",
             "data": "synthetic",
             "config": {"workload": wl["name"], "precision": args.precision, "npoints": info["npoints"],
                        "npoints_padded": G, "nblocks": info["nblocks"], "nbasis": n,
-                       "l2": "inputs larger than L2 (AO store %.2f GB)" % (info["ao_elements"] * 4 * 8 / 1e9),
-                       "E_xc": Exc},
+                       "mixed_tiles": info["mixed_tiles"],
+                       "l2": "inputs larger than L2 (FP64 AO store %.2f GB; split-BF16 stores larger)"
+                             % (info["ao_elements"] * 4 * 8 / 1e9),
+                       "plain_fp64_pts_per_s": plain, "plain_fp64_ms_per_build": t_plain / args.plain_steps * 1e3,
+                       "speedup_vs_plain_fp64": value / world / plain,
+                       "E_xc_fp64": E64, "E_xc": Emx if precision == PMX else E64,
+                       "abs_dE_xc_vs_fp64": abs(Emx - E64),
+                       "max_abs_dV_xc_vs_fp64": float((Vmx - V64).abs().max().item())},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 8 * n * n, "d2h_bytes_per_step": 8 * n * n + 8},
-            "gpu_launches": args.steps * 4,
+            "gpu_launches": args.steps * (7 if precision == PMX else 4),
             "roofline": roof, "clocks": clocks}
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(wl, D, args.cpu_blocks, os.cpu_count() or 1)

@@ -28,7 +28,8 @@ class XCError(RuntimeError):
 class GridInfo(ctypes.Structure):
     _fields_ = [("npoints", ctypes.c_long), ("npoints_padded", ctypes.c_long), ("nblocks", ctypes.c_int),
                 ("nbasis", ctypes.c_int), ("nspin", ctypes.c_int), ("type", ctypes.c_int),
-                ("ao_elements", ctypes.c_long), ("screened_pairs", ctypes.c_long)]
+                ("ao_elements", ctypes.c_long), ("screened_pairs", ctypes.c_long),
+                ("mixed_tiles", ctypes.c_int), ("mixed_pairs", ctypes.c_long)]
 
 
 _P = ctypes.c_void_p

@@ -516,6 +516,8 @@ int xc_grid_info_get(const xc_grid* g, xc_grid_info* info) {
         info->type = G.type;
         info->ao_elements = G.ao_elements;
         info->screened_pairs = G.screened_pairs;
+        info->mixed_tiles = G.mx.ready ? G.mx.md.ntiles : 0;
+        info->mixed_pairs = G.mx.ready ? G.mx.kept_pairs : 0;
     });
 }
 

@@ -120,6 +120,8 @@ typedef struct xc_grid_info {
     int type;
     long ao_elements;    /* stored AO values per component */
     long screened_pairs; /* sum over blocks of n_b^2 */
+    int mixed_tiles;     /* 128-point tiles of the mixed-precision path (0 before its first build) */
+    long mixed_pairs;    /* sum over tiles of (kept functions)^2 */
 } xc_grid_info;
 int xc_grid_info_get(const xc_grid* g, xc_grid_info* info);
 /* Padded points in block order: x, y, z, w (each npoints_padded) and
