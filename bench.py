@@ -219,7 +219,8 @@ def main():
     grid.build_device(xc, dD, dE, dV, P64)
     stream.synchronize()
     E64, V64 = float(dE.item()), dV.clone()
-    t_plain = time_builds(torch, grid, xc, dD, dE, dV, P64, args.plain_steps, stream)
+    plain_steps = max(1, args.plain_steps)
+    t_plain = time_builds(torch, grid, xc, dD, dE, dV, P64, plain_steps, stream)
 
     for _ in range(args.warmup):
         grid.build_device(xc, dD, dE, dV, precision)
@@ -263,7 +264,7 @@ def main():
     G = info["npoints_padded"]
     value = world * G * args.steps / t_dev
     e2e = world * G * args.steps / t_e2e
-    plain = G * args.plain_steps / t_plain
+    plain = G * plain_steps / t_plain
     peaks = measured_peaks()
 
     if precision == PMX:
@@ -300,7 +301,7 @@ def main():
                        "mixed_tiles": info["mixed_tiles"],
                        "l2": "inputs larger than L2 (FP64 AO store %.2f GB; split-BF16 stores larger)"
                              % (info["ao_elements"] * 4 * 8 / 1e9),
-                       "plain_fp64_pts_per_s": plain, "plain_fp64_ms_per_build": t_plain / args.plain_steps * 1e3,
+                       "plain_fp64_pts_per_s": plain, "plain_fp64_ms_per_build": t_plain / plain_steps * 1e3,
                        "speedup_vs_plain_fp64": value / world / plain,
                        "E_xc_fp64": E64, "E_xc": Emx if precision == PMX else E64,
                        "abs_dE_xc_vs_fp64": abs(Emx - E64),

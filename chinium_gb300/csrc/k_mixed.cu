@@ -5,17 +5,24 @@
 // that its screening test marks significant, packed into "slots".  Operands
 // are three-term BF16 splits (x = h + m + l); a product sums the six
 // cross terms of order <= 2 (hh, hm, mh, hl, mm, lh) in FP32 on the tensor
-// core, ~FP32 accuracy.  Cross-tile sums (V_xc partials, rho epilogue
-// reductions) are FP64.
+// core, ~FP32 accuracy.  The leading hh term and the five corrections go to
+// separate TMEM accumulators, and every accumulation unit (one K-chunk of the
+// density product, one point tile of the V_xc product) starts a fresh
+// accumulator that the epilogue warps drain into round-to-nearest FP32
+// registers: tensor-core accumulation chains stay a few instructions long.
+// Cross-unit sums of the final quantities are FP64.
 //
 // HBM layouts (bf16, all rows 16-byte aligned, TMA 128-byte swizzle):
 //   PF  (point-major): row (c*3+p)*Gt + t*128 + g, col slot*64 + f      [c: phi, d/dx, d/dy, d/dz]
 //   FP  (function-major): row (c*3+p)*T*K + t*K + slot*64 + f, col g     (+64 zero rows)
 //   R   (function-major, per build): row (c*3+p)*T*K + t*K + slot*64 + f, col g (+64 zero rows)
 //   Dp  (density planes): row (s*3+p)*npad + nu, col mu
-// Kernels: density T = Phi D (tile x 128 functions per MMA chain) with the
-// rho / grad-rho / tau epilogue from TMEM; V partials W = L^T R per
-// (128 x 128 function block, split of tiles); a reduction V = sum W + W^T.
+//
+// CTA roles (192 threads): warp 0 issues TMA loads into a 2-stage ring,
+// warp 1 issues tcgen05.mma into one of two TMEM buffers (256 columns each:
+// hh | corrections), warps 2-5 drain TMEM (lane quadrant = warp % 4) and
+// run the epilogue.  Every wait is bounded (2 s of %globaltimer) and a
+// timeout sets XC_ERR_TIMEOUT in a global flag instead of hanging.
 #include <cstdio>
 
 #include "common.h"
@@ -28,19 +35,21 @@ namespace {
 
 using bf16 = __nv_bfloat16;
 
-constexpr int kThreads = 128;
+constexpr int kThreads = 192;
 constexpr int kStages = 2;
-constexpr uint32_t kPlaneA = 128 * 64 * 2;  // bytes of one 128x64 bf16 operand plane
+constexpr uint32_t kPlaneA = 128 * 64 * 2;     // bytes of one 128x64 bf16 operand plane
 constexpr uint32_t kStageBytes = 6 * kPlaneA;  // A (3 planes) + B (3 planes)
 constexpr uint32_t kIdesc = tc::idesc_bf16(128, 128);
-// cross terms (i, j) of the three-term splits with i + j <= 2
+constexpr uint32_t kTmemCols = 512;            // 2 buffers x (hh 128 | corrections 128)
+// cross terms (i, j) of the three-term splits with i + j <= 2; term 0 is hh
 __constant__ int c_prod_a[6] = {0, 0, 1, 0, 1, 2};
 __constant__ int c_prod_b[6] = {0, 1, 0, 2, 1, 0};
 
 struct Smem {
     uint64_t full[kStages];
     uint64_t empty[kStages];
-    uint64_t done;
+    uint64_t tfull[2];
+    uint64_t tempty[2];
     uint32_t tmem;
     int abort;
 };
@@ -52,24 +61,67 @@ __device__ __forceinline__ void flag_timeout(int* err, Smem* sm) {
     atomicExch(&sm->abort, 1);
 }
 
-// Issue the six split products of one stage: D += sum A_i B_j^T, K = 64.
-__device__ __forceinline__ void mma_stage(uint32_t tmem, uint8_t* st, bool first) {
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_u32(bar)) : "memory");
+}
+
+__device__ void init_cta(Smem& sm) {
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; s++) {
+            tc::mbar_init(&sm.full[s], 1);
+            tc::mbar_init(&sm.empty[s], 1);
+        }
+        for (int b = 0; b < 2; b++) {
+            tc::mbar_init(&sm.tfull[b], 1);
+            tc::mbar_init(&sm.tempty[b], 128);
+        }
+        sm.abort = 0;
+        tc::fence_mbar_init();
+    }
+    if ((threadIdx.x >> 5) == 0) tc::tmem_alloc(&sm.tmem, kTmemCols);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+}
+
+// The six split products of one stage into TMEM buffer `buf`: term hh into
+// the hh accumulator, the five corrections into the correction accumulator.
+// `first` starts both accumulators (unit boundary).
+__device__ __forceinline__ void mma_stage(uint32_t tmem, int buf, uint8_t* st, bool first) {
     const uint32_t a0 = tc::smem_u32(st), b0 = a0 + 3 * kPlaneA;
+    const uint32_t d_hh = tmem + buf * 256, d_corr = tmem + buf * 256 + 128;
 #pragma unroll
     for (int q = 0; q < 6; q++) {
         const uint64_t ad = tc::smem_desc_sw128(a0 + c_prod_a[q] * kPlaneA);
         const uint64_t bd = tc::smem_desc_sw128(b0 + c_prod_b[q] * kPlaneA);
+        const uint32_t d = q == 0 ? d_hh : d_corr;
 #pragma unroll
-        for (int k = 0; k < 4; k++)  // K = 16 per instruction: +32 bytes in the swizzled row
-            tc::mma_bf16(tmem, ad + 2 * k, bd + 2 * k, kIdesc, (first && q == 0 && k == 0) ? 0u : 1u);
+        for (int k = 0; k < 4; k++) {  // K = 16 per instruction: +32 bytes in the swizzled row
+            const bool start = first && k == 0 && (q == 0 || q == 1);
+            tc::mma_bf16(d, ad + 2 * k, bd + 2 * k, kIdesc, start ? 0u : 1u);
+        }
     }
 }
 
-__device__ __forceinline__ float bf3(const bf16* h, const bf16* m, const bf16* l, int i) {
-    return __bfloat162float(h[i]) + __bfloat162float(m[i]) + __bfloat162float(l[i]);
+// Drain TMEM buffer `buf` (hh + corrections) into acc[128] (this thread's lane).
+__device__ __forceinline__ void drain(uint32_t tmem, int buf, int quad, float* acc) {
+    const uint32_t base = tmem + ((uint32_t)(quad * 32) << 16) + buf * 256;
+#pragma unroll
+    for (int c16 = 0; c16 < 8; c16++) {
+        float a[16], b[16];
+        tc::tmem_ld16(base + c16 * 16, a);
+        tc::tmem_ld16(base + 128 + c16 * 16, b);
+#pragma unroll
+        for (int j = 0; j < 16; j++) acc[c16 * 16 + j] += a[j] + b[j];
+    }
+}
+
+__device__ __forceinline__ float bf3(const bf16* h, size_t ps, int i) {
+    return __bfloat162float(h[i]) + __bfloat162float(h[ps + i]) + __bfloat162float(h[2 * ps + i]);
 }
 
 // ------------------------------------------------------------ density
+// T = Phi D for one tile, unit = (nu block vb of two slots, mu chunk kc).
 // EPI 0: rho; 1: rho + grad rho; 2: tau contribution of A component acomp.
 template <int EPI>
 __global__ void __launch_bounds__(kThreads, 1) density_tc_kernel(const __grid_constant__ CUtensorMap tm_pf,
@@ -82,37 +134,19 @@ __global__ void __launch_bounds__(kThreads, 1) density_tc_kernel(const __grid_co
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     const int t = blockIdx.x;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int g = threadIdx.x;  // TMEM lane == point row
     const int nkept = md.tile_nkept[t];
     const int* chunks = md.tile_chunks + (size_t)t * md.nchunk;
-
-    if (threadIdx.x == 0) {
-        for (int s = 0; s < kStages; s++) {
-            tc::mbar_init(&sm.full[s], 1);
-            tc::mbar_init(&sm.empty[s], 1);
-        }
-        tc::mbar_init(&sm.done, 1);
-        sm.abort = 0;
-        tc::fence_mbar_init();
-    }
-    if (warp == 0) tc::tmem_alloc(&sm.tmem, 128);
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
+    const int nvb = (nkept + 1) / 2;
+    const int nunits = nvb * nkept;
+    init_cta(sm);
     const uint32_t tmem = sm.tmem;
 
-    const long pt = (long)t * 128 + g;
-    const bool live = pt < Gp;
-    double acc_r = 0, acc_g[3] = {0, 0, 0}, acc_t = 0;
-    const int nvb = (nkept + 1) / 2;
-    uint32_t it = 0;  // pipeline iteration counter (same sequence in producer and MMA threads)
-
-    for (int vb = 0; vb < nvb && nkept > 0; vb++) {
-        if (warp == 0 && lane == 0) {
-            uint32_t i2 = it;
-            for (int kc = 0; kc < nkept; kc++, i2++) {
-                const int s = i2 % kStages;
-                const uint32_t ph = (i2 / kStages) & 1;
+    if (warp == 0) {
+        if (lane == 0) {
+            for (int u = 0; u < nunits; u++) {
+                const int vb = u / nkept, kc = u % nkept;
+                const int s = u % kStages;
+                const uint32_t ph = (u / kStages) & 1;
                 if (sm.abort || !tc::mbar_wait(&sm.empty[s], ph ^ 1)) {
                     flag_timeout(err, &sm);
                     break;
@@ -130,77 +164,94 @@ __global__ void __launch_bounds__(kThreads, 1) density_tc_kernel(const __grid_co
                                         (spin * 3 + p) * md.npad + chunks[vs] * 64, &sm.full[s]);
                     }
             }
-        } else if (warp == 1 && lane == 0) {
-            uint32_t i2 = it;
-            for (int kc = 0; kc < nkept; kc++, i2++) {
-                const int s = i2 % kStages;
-                const uint32_t ph = (i2 / kStages) & 1;
-                if (sm.abort || !tc::mbar_wait(&sm.full[s], ph)) {
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            for (int u = 0; u < nunits; u++) {
+                const int s = u % kStages, b = u & 1;
+                const uint32_t ph = (u / kStages) & 1, bph = (u >> 1) & 1;
+                if (sm.abort || !tc::mbar_wait(&sm.tempty[b], bph ^ 1) || !tc::mbar_wait(&sm.full[s], ph)) {
                     flag_timeout(err, &sm);
+                    tc::mma_commit(&sm.tfull[b]);  // release the epilogue
                     break;
                 }
                 tc::fence_after_sync();
-                mma_stage(tmem, stage_base(smem, s), kc == 0);
+                mma_stage(tmem, b, stage_base(smem, s), true);
                 tc::mma_commit(&sm.empty[s]);
+                tc::mma_commit(&sm.tfull[b]);
             }
-            tc::mma_commit(&sm.done);
         }
-        it += nkept;
-        __syncwarp();
-        // epilogue: this thread's point row, 128 columns (two kept slots)
-        if (!tc::mbar_wait(&sm.done, vb & 1)) flag_timeout(err, &sm);
-        tc::fence_after_sync();
-        float pr = 0, pg0 = 0, pg1 = 0, pg2 = 0, ptau = 0;
-        for (int c16 = 0; c16 < 8; c16++) {
-            float T[16];
-            tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + c16 * 16, T);
-            const int slot = 2 * vb + (c16 >> 2);
-            if (slot >= nkept || !live || sm.abort) continue;
-            const int col = slot * 64 + (c16 & 3) * 16;
-            const bf16* base = md.pf + (size_t)(t * 128 + g) * md.kmax + col;
-            const size_t cstride = (size_t)3 * md.Gt * md.kmax, pstride = (size_t)md.Gt * md.kmax;
-            if (EPI <= 1) {
-                const bf16* b0 = base;
+    } else {
+        // epilogue warps: row g of the tile
+        const int quad = warp & 3;
+        const int g = quad * 32 + lane;
+        const long pt = (long)t * 128 + g;
+        const bool live = pt < Gp;
+        const size_t ps = (size_t)md.Gt * md.kmax, cs = 3 * ps;
+        double acc_r = 0, acc_g0 = 0, acc_g1 = 0, acc_g2 = 0, acc_t = 0;
+        float T[128];
 #pragma unroll
-                for (int j = 0; j < 16; j++) pr = fmaf(T[j], bf3(b0, b0 + pstride, b0 + 2 * pstride, j), pr);
-                if (EPI == 1) {
-                    const bf16* bx = base + cstride;
-                    const bf16* by = base + 2 * cstride;
-                    const bf16* bz = base + 3 * cstride;
+        for (int j = 0; j < 128; j++) T[j] = 0.f;
+        for (int u = 0; u < nunits; u++) {
+            const int vb = u / nkept, kc = u % nkept, b = u & 1;
+            const uint32_t bph = (u >> 1) & 1;
+            if (sm.abort) break;
+            if (!tc::mbar_wait(&sm.tfull[b], bph)) {
+                flag_timeout(err, &sm);
+                break;
+            }
+            tc::fence_after_sync();
+            drain(tmem, b, quad, T);
+            tc::fence_before_sync();
+            mbar_arrive(&sm.tempty[b]);
+            if (kc != nkept - 1) continue;
+            // nu block complete: contract T with this row's AO values
+            if (live && !sm.abort) {
+                float pr = 0, pg0 = 0, pg1 = 0, pg2 = 0, pt_ = 0;
 #pragma unroll
-                    for (int j = 0; j < 16; j++) {
-                        pg0 = fmaf(T[j], bf3(bx, bx + pstride, bx + 2 * pstride, j), pg0);
-                        pg1 = fmaf(T[j], bf3(by, by + pstride, by + 2 * pstride, j), pg1);
-                        pg2 = fmaf(T[j], bf3(bz, bz + pstride, bz + 2 * pstride, j), pg2);
+                for (int h = 0; h < 2; h++) {
+                    const int slot = 2 * vb + h;
+                    if (slot >= nkept) break;
+                    const bf16* base = md.pf + (size_t)(t * 128 + g) * md.kmax + slot * 64;
+#pragma unroll
+                    for (int j = 0; j < 64; j++) {
+                        const float tv = T[h * 64 + j];
+                        if (EPI <= 1) pr = fmaf(tv, bf3(base, ps, j), pr);
+                        if (EPI == 1) {
+                            pg0 = fmaf(tv, bf3(base + cs, ps, j), pg0);
+                            pg1 = fmaf(tv, bf3(base + 2 * cs, ps, j), pg1);
+                            pg2 = fmaf(tv, bf3(base + 3 * cs, ps, j), pg2);
+                        }
+                        if (EPI == 2) pt_ = fmaf(tv, bf3(base + (size_t)acomp * cs, ps, j), pt_);
                     }
                 }
-            } else {
-                const bf16* br = base + (size_t)acomp * cstride;
-#pragma unroll
-                for (int j = 0; j < 16; j++) ptau = fmaf(T[j], bf3(br, br + pstride, br + 2 * pstride, j), ptau);
+                acc_r += pr;
+                acc_g0 += 2.0 * pg0;
+                acc_g1 += 2.0 * pg1;
+                acc_g2 += 2.0 * pg2;
+                acc_t += 0.5 * pt_;
             }
+#pragma unroll
+            for (int j = 0; j < 128; j++) T[j] = 0.f;
         }
-        acc_r += pr;
-        acc_g[0] += 2.0 * pg0;
-        acc_g[1] += 2.0 * pg1;
-        acc_g[2] += 2.0 * pg2;
-        acc_t += 0.5 * ptau;
-        tc::fence_before_sync();
-        __syncthreads();
+        if (live) {
+            if (EPI <= 1) rho[(long)spin * Gp + pt] = acc_r;
+            if (EPI == 1) {
+                rho1[((long)spin * 3 + 0) * Gp + pt] = acc_g0;
+                rho1[((long)spin * 3 + 1) * Gp + pt] = acc_g1;
+                rho1[((long)spin * 3 + 2) * Gp + pt] = acc_g2;
+            }
+            if (EPI == 2) tau[(long)spin * Gp + pt] += acc_t;
+        }
     }
-    if (live) {
-        if (EPI <= 1) rho[(long)spin * Gp + pt] = acc_r;
-        if (EPI == 1)
-            for (int r = 0; r < 3; r++) rho1[((long)spin * 3 + r) * Gp + pt] = acc_g[r];
-        if (EPI == 2) tau[(long)spin * Gp + pt] += acc_t;
-    }
+    tc::fence_before_sync();
     __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(tmem, 128);
+    if (warp == 0) tc::tmem_dealloc(tmem, kTmemCols);
 }
 
 // ------------------------------------------------------------- V_xc
 // One CTA per (128 x 128 block (I, J) of W, split of tiles):
-//   W_IJ += sum_t sum_c L_c,t[I]^T R_c,t[J]   (K = 128 points per tile)
+//   W_IJ = sum_t sum_c L_c,t[I]^T R_c,t[J]   (unit = one point tile, K = 128 points per component)
 __global__ void __launch_bounds__(kThreads, 1) fock_tc_kernel(const __grid_constant__ CUtensorMap tm_fp,
                                                               const __grid_constant__ CUtensorMap tm_r, MixedDev md,
                                                               int ncomp, int r_rows, int nblk, int nsplit,
@@ -213,25 +264,11 @@ __global__ void __launch_bounds__(kThreads, 1) fock_tc_kernel(const __grid_const
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int t0 = (int)((long)md.ntiles * split / nsplit), t1 = (int)((long)md.ntiles * (split + 1) / nsplit);
     const long TK = (long)md.ntiles * md.kmax;
-    const int zero_row = (int)(12 * TK);        // 64 zero rows after the FP planes
-    const int zero_row_r = r_rows;                 // 64 zero rows after the R planes
-
-    if (threadIdx.x == 0) {
-        for (int s = 0; s < kStages; s++) {
-            tc::mbar_init(&sm.full[s], 1);
-            tc::mbar_init(&sm.empty[s], 1);
-        }
-        tc::mbar_init(&sm.done, 1);
-        sm.abort = 0;
-        tc::fence_mbar_init();
-    }
-    if (warp == 0) tc::tmem_alloc(&sm.tmem, 128);
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
+    const int zero_row = (int)(12 * TK);  // 64 zero rows after the FP planes
+    const int zero_row_r = r_rows;        // 64 zero rows after the R planes
+    init_cta(sm);
     const uint32_t tmem = sm.tmem;
 
-    // the tiles that contribute (both an I chunk and a J chunk kept)
     auto slot_of = [&](int t, int chunk) -> int {
         return chunk < md.nchunk ? md.tile_slot[(size_t)t * md.nchunk + chunk] : -1;
     };
@@ -239,69 +276,100 @@ __global__ void __launch_bounds__(kThreads, 1) fock_tc_kernel(const __grid_const
         return (slot_of(t, 2 * I) >= 0 || slot_of(t, 2 * I + 1) >= 0) &&
                (slot_of(t, 2 * J) >= 0 || slot_of(t, 2 * J + 1) >= 0);
     };
-    __shared__ int s_issued;
-    if (warp == 0 && lane == 0) {
-        uint32_t i2 = 0;
-        for (int t = t0; t < t1 && !sm.abort; t++) {
-            if (!wanted(t)) continue;
-            for (int c = 0; c < ncomp; c++)
-                for (int kh = 0; kh < 2; kh++, i2++) {
-                    const int s = i2 % kStages;
-                    const uint32_t ph = (i2 / kStages) & 1;
-                    if (sm.abort || !tc::mbar_wait(&sm.empty[s], ph ^ 1)) {
-                        flag_timeout(err, &sm);
-                        break;
-                    }
-                    uint8_t* st = stage_base(smem, s);
-                    tc::mbar_arrive_expect_tx(&sm.full[s], kStageBytes);
-                    for (int p = 0; p < 3; p++)
-                        for (int h = 0; h < 2; h++) {
-                            const int sa = slot_of(t, 2 * I + h), sb = slot_of(t, 2 * J + h);
-                            const int ra = sa >= 0 ? (int)((c * 3 + p) * TK + (long)t * md.kmax + sa * 64) : zero_row;
-                            const int rb = sb >= 0 ? (int)((c * 3 + p) * TK + (long)t * md.kmax + sb * 64) : zero_row_r;
-                            tc::tma_load_2d(st + p * kPlaneA + h * (kPlaneA / 2), &tm_fp, kh * 64, ra, &sm.full[s]);
-                            tc::tma_load_2d(st + (3 + p) * kPlaneA + h * (kPlaneA / 2), &tm_r, kh * 64, rb,
-                                            &sm.full[s]);
+
+    if (warp == 0) {
+        if (lane == 0) {
+            uint32_t i2 = 0;
+            for (int t = t0; t < t1 && !sm.abort; t++) {
+                if (!wanted(t)) continue;
+                const int sa0 = slot_of(t, 2 * I), sa1 = slot_of(t, 2 * I + 1);
+                const int sb0 = slot_of(t, 2 * J), sb1 = slot_of(t, 2 * J + 1);
+                for (int c = 0; c < ncomp && !sm.abort; c++)
+                    for (int kh = 0; kh < 2; kh++, i2++) {
+                        const int s = i2 % kStages;
+                        const uint32_t ph = (i2 / kStages) & 1;
+                        if (sm.abort || !tc::mbar_wait(&sm.empty[s], ph ^ 1)) {
+                            flag_timeout(err, &sm);
+                            break;
                         }
-                }
-        }
-        s_issued = (int)i2;
-    }
-    if (warp == 1 && lane == 0) {
-        uint32_t i2 = 0;
-        for (int t = t0; t < t1 && !sm.abort; t++) {
-            if (!wanted(t)) continue;
-            for (int c = 0; c < ncomp; c++)
-                for (int kh = 0; kh < 2; kh++, i2++) {
-                    const int s = i2 % kStages;
-                    const uint32_t ph = (i2 / kStages) & 1;
-                    if (sm.abort || !tc::mbar_wait(&sm.full[s], ph)) {
-                        flag_timeout(err, &sm);
-                        break;
+                        uint8_t* st = stage_base(smem, s);
+                        tc::mbar_arrive_expect_tx(&sm.full[s], kStageBytes);
+                        for (int p = 0; p < 3; p++)
+                            for (int h = 0; h < 2; h++) {
+                                const int sa = h ? sa1 : sa0, sb = h ? sb1 : sb0;
+                                const long rbase = (long)(c * 3 + p) * TK + (long)t * md.kmax;
+                                const int ra = sa >= 0 ? (int)(rbase + sa * 64) : zero_row;
+                                const int rb = sb >= 0 ? (int)(rbase + sb * 64) : zero_row_r;
+                                tc::tma_load_2d(st + p * kPlaneA + h * (kPlaneA / 2), &tm_fp, kh * 64, ra, &sm.full[s]);
+                                tc::tma_load_2d(st + (3 + p) * kPlaneA + h * (kPlaneA / 2), &tm_r, kh * 64, rb,
+                                                &sm.full[s]);
+                            }
                     }
-                    tc::fence_after_sync();
-                    mma_stage(tmem, stage_base(smem, s), i2 == 0);
-                    tc::mma_commit(&sm.empty[s]);
-                }
+            }
         }
-        tc::mma_commit(&sm.done);
-    }
-    __syncwarp();
-    __syncthreads();
-    if (!tc::mbar_wait(&sm.done, 0)) flag_timeout(err, &sm);
-    tc::fence_after_sync();
-    const int npadw = nblk * 128;
-    double* out = wpart + (size_t)split * npadw * npadw + (size_t)(I * 128 + threadIdx.x) * npadw + J * 128;
-    const bool any = s_issued > 0 && !sm.abort;
-    for (int c16 = 0; c16 < 8; c16++) {
-        float v[16];
-        tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + c16 * 16, v);
+    } else if (warp == 1) {
+        if (lane == 0) {
+            uint32_t i2 = 0, u = 0;
+            for (int t = t0; t < t1 && !sm.abort; t++) {
+                if (!wanted(t)) continue;
+                const int b = u & 1;
+                const uint32_t bph = (u >> 1) & 1;
+                if (!tc::mbar_wait(&sm.tempty[b], bph ^ 1)) {
+                    flag_timeout(err, &sm);
+                    tc::mma_commit(&sm.tfull[b]);
+                    break;
+                }
+                bool first = true;
+                for (int c = 0; c < ncomp; c++)
+                    for (int kh = 0; kh < 2; kh++, i2++) {
+                        const int s = i2 % kStages;
+                        const uint32_t ph = (i2 / kStages) & 1;
+                        if (sm.abort || !tc::mbar_wait(&sm.full[s], ph)) {
+                            flag_timeout(err, &sm);
+                            break;
+                        }
+                        tc::fence_after_sync();
+                        mma_stage(tmem, b, stage_base(smem, s), first);
+                        first = false;
+                        tc::mma_commit(&sm.empty[s]);
+                    }
+                tc::mma_commit(&sm.tfull[b]);
+                u++;
+            }
+        }
+    } else {
+        const int quad = warp & 3;
+        const int g = quad * 32 + lane;  // row of the W block
+        float W[128];
 #pragma unroll
-        for (int j = 0; j < 16; j++) out[c16 * 16 + j] = any ? (double)v[j] : 0.0;
+        for (int j = 0; j < 128; j++) W[j] = 0.f;
+        uint32_t u = 0;
+        bool any = false;
+        for (int t = t0; t < t1; t++) {
+            if (!wanted(t)) continue;
+            const int b = u & 1;
+            const uint32_t bph = (u >> 1) & 1;
+            if (sm.abort) break;
+            if (!tc::mbar_wait(&sm.tfull[b], bph)) {
+                flag_timeout(err, &sm);
+                break;
+            }
+            if (sm.abort) break;
+            tc::fence_after_sync();
+            drain(tmem, b, quad, W);
+            tc::fence_before_sync();
+            mbar_arrive(&sm.tempty[b]);
+            any = true;
+            u++;
+        }
+        const int npadw = nblk * 128;
+        double* out = wpart + (size_t)split * npadw * npadw + (size_t)(I * 128 + g) * npadw + J * 128;
+#pragma unroll
+        for (int j = 0; j < 128; j++) out[j] = (any && !sm.abort) ? (double)W[j] : 0.0;
     }
     tc::fence_before_sync();
     __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(tmem, 128);
+    if (warp == 0) tc::tmem_dealloc(tmem, kTmemCols);
 }
 
 // V(mu, nu) = sum_s W_s(mu, nu) + W_s(nu, mu), column-major n x n (FP64).
@@ -386,8 +454,9 @@ constexpr int kNcart = (kMaxL + 1) * (kMaxL + 2) / 2;
 __global__ void __launch_bounds__(128) ao_mixed_kernel(MixedDev md, DevShells sh, const int* __restrict__ tile_shells,
                                                        const int* __restrict__ tile_shell_off,
                                                        const double* __restrict__ px, const double* __restrict__ py,
-                                                       const double* __restrict__ pz, long Gp, const double* __restrict__ shtab,
-                                                       bf16* __restrict__ pf, bf16* __restrict__ fp) {
+                                                       const double* __restrict__ pz, long Gp,
+                                                       const double* __restrict__ shtab, bf16* __restrict__ pf,
+                                                       bf16* __restrict__ fp) {
     const int t = blockIdx.x, g = threadIdx.x;
     const long pt = (long)t * 128 + g;
     const long src = pt < Gp ? pt : 0;  // tail points: copies of point 0 (their weight is zero)
