@@ -72,6 +72,7 @@ SIGNATURES = {
     "xc_build": [_P, _P, _P, _I, _I, _P, _P],
     "xc_build_device": [_P, _P, _P, _I, _I, _P, _P],
     "xc_sap_fock": [_P, _P],
+    "xc_functional_energy_static": [_P, _L, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P],
     "xc_grid_profile": [_P, _I],
     "xc_grid_stage_ms": [_P, _P],
 }

@@ -162,6 +162,24 @@ int xc_functional_eval_points(xc_functional* f, long npoints, const double* rho,
                               const double* sigma, const double* tau, double* eps, double* vrho,
                               double* vsigma, double* vtau);
 
+/* Allocation-free functional + E_xc on caller-owned device arrays.  No
+ * counterpart in the reference: it serves callers that may not call
+ * cudaMalloc / cudaFree (device memory owned by another allocator, or code
+ * that must not trigger their device-wide synchronisation).  Inputs rho
+ * (s, n), sigma (ns(ns+1)/2, n), tau (s, n) and weights w (n); outputs eps
+ * (n), vrho, vsigma, vtau (layouts as the inputs) and *d_E = sum_g w_g
+ * rho_g eps_g.  The only scratch (per-CTA energy partials) is a fixed array
+ * inside the library, so npoints <= 2 097 152; larger calls fail with
+ * XC_ERR_ARG.  The first call on a device looks up that array's device
+ * address (with that device current); make that first call before any stream
+ * capture.  Calls share the array, so calls whose kernels overlap on the GPU
+ * race and must be serialised by the caller.  Work is enqueued on `stream`
+ * (cudaStream_t as void*, NULL = legacy default) without synchronising. */
+int xc_functional_energy_static(const xc_functional* f, long npoints, const double* d_w,
+                                const double* d_rho, const double* d_sigma, const double* d_tau,
+                                double* d_eps, double* d_vrho, double* d_vsigma, double* d_vtau,
+                                double* d_E, void* stream);
+
 /* ------------------------------------------------------------ fused build */
 
 /* getDensity + Evaluate("ev") + getEnergy + getFock in one call
