@@ -272,13 +272,13 @@ void Grid::density_device(const double* dD) {
     have_potential = false;
 }
 
-void Grid::evaluate(const Functional& f) {
+void Grid::evaluate(const Functional& f, double float_above) {
     CGB_CHECK(have_density, XC_ERR_STATE, "Evaluate needs a density (getDensity first)");
     CGB_CHECK(f.nspin == nspin, XC_ERR_ARG, "functional and grid disagree on the number of spins");
     CGB_CHECK(f.family <= type, XC_ERR_STATE, "grid type is below the functional family (setType/getAO)");
     mark(1);
     launch_functional_fp64(f.desc, f.family, nspin, Gp, d_w.p, d_rho.p, d_rho1.p, d_tau.p, d_sigma.p, d_eps.p,
-                           d_vrho.p, d_vsigma.p, d_vtau.p, d_fcoef.p, d_partial.p, &n_partial, stream);
+                           d_vrho.p, d_vsigma.p, d_vtau.p, d_fcoef.p, d_partial.p, &n_partial, stream, float_above);
     eval_family = f.family;
     have_potential = true;
 }

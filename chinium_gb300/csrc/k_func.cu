@@ -45,7 +45,7 @@ __global__ void __launch_bounds__(kThreads) functional_kernel(xcf::FuncDesc f, l
                                                               double* __restrict__ sigma, double* __restrict__ eps,
                                                               double* __restrict__ vrho, double* __restrict__ vsigma,
                                                               double* __restrict__ vtau, double* __restrict__ fcoef,
-                                                              double* __restrict__ e_partial) {
+                                                              double* __restrict__ e_partial, double float_above) {
     const long g = (long)blockIdx.x * blockDim.x + threadIdx.x;
     double econtrib = 0;
     if (g < Gp) {
@@ -62,7 +62,14 @@ __global__ void __launch_bounds__(kThreads) functional_kernel(xcf::FuncDesc f, l
             }
             if (FAM >= 2) t = tau[g];
             double e, dv[3] = {0, 0, 0};
-            xcf::eval_unpol<double, FAM>(f, r, s, t, e, dv);
+            if (r >= float_above) {  // mixed path: FP32 functional above the low-density bound
+                float ef, df[3] = {0, 0, 0};
+                xcf::eval_unpol<float, FAM>(f, (float)r, (float)s, (float)t, ef, df);
+                e = ef;
+                for (int i = 0; i < 3; i++) dv[i] = df[i];
+            } else {
+                xcf::eval_unpol<double, FAM>(f, r, s, t, e, dv);
+            }
             eps[g] = e;
             vrho[g] = dv[0];
             if (FAM >= 1) vsigma[g] = dv[1];
@@ -95,7 +102,15 @@ __global__ void __launch_bounds__(kThreads) functional_kernel(xcf::FuncDesc f, l
                 in[6] = tau[Gp + g];
             }
             double e, dv[7] = {0, 0, 0, 0, 0, 0, 0};
-            xcf::eval_pol<double, FAM>(f, in, e, dv);
+            if (in[0] + in[1] >= float_above) {
+                float inf_[7], ef, df[7] = {0, 0, 0, 0, 0, 0, 0};
+                for (int i = 0; i < 7; i++) inf_[i] = (float)in[i];
+                xcf::eval_pol<float, FAM>(f, inf_, ef, df);
+                e = ef;
+                for (int i = 0; i < 7; i++) dv[i] = df[i];
+            } else {
+                xcf::eval_pol<double, FAM>(f, in, e, dv);
+            }
             eps[g] = e;
             vrho[g] = dv[0];
             vrho[Gp + g] = dv[1];
@@ -220,11 +235,12 @@ __global__ void points_kernel(xcf::FuncDesc f, long n, const double* __restrict_
 void launch_functional_fp64(const xcf::FuncDesc& f, int fam, int ns, long Gp, const double* w, const double* rho,
                             const double* rho1, const double* tau, double* sigma, double* eps, double* vrho,
                             double* vsigma, double* vtau, double* fcoef, double* e_partial, int* n_partial,
-                            cudaStream_t s) {
+                            cudaStream_t s, double float_above) {
     const unsigned grid = (unsigned)((Gp + kThreads - 1) / kThreads);
     *n_partial = (int)grid;
-#define CGB_FN(FAM_, NS_) \
-    functional_kernel<FAM_, NS_><<<grid, kThreads, 0, s>>>(f, Gp, w, rho, rho1, tau, sigma, eps, vrho, vsigma, vtau, fcoef, e_partial)
+#define CGB_FN(FAM_, NS_)                                                                                  \
+    functional_kernel<FAM_, NS_><<<grid, kThreads, 0, s>>>(f, Gp, w, rho, rho1, tau, sigma, eps, vrho, vsigma, vtau, \
+                                                           fcoef, e_partial, float_above)
     if (ns == 1) {
         if (fam == 0) CGB_FN(0, 1);
         else if (fam == 1) CGB_FN(1, 1);

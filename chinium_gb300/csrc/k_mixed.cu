@@ -116,10 +116,6 @@ __device__ __forceinline__ void drain(uint32_t tmem, int buf, int quad, float* a
     }
 }
 
-__device__ __forceinline__ float bf3(const bf16* h, size_t ps, int i) {
-    return __bfloat162float(h[i]) + __bfloat162float(h[ps + i]) + __bfloat162float(h[2 * ps + i]);
-}
-
 // ------------------------------------------------------------ density
 // T = Phi D for one tile, unit = (nu block vb of two slots, mu chunk kc).
 // EPI 0: rho; 1: rho + grad rho; 2: tau contribution of A component acomp.
@@ -187,7 +183,7 @@ __global__ void __launch_bounds__(kThreads, 1) density_tc_kernel(const __grid_co
         const int g = quad * 32 + lane;
         const long pt = (long)t * 128 + g;
         const bool live = pt < Gp;
-        const size_t ps = (size_t)md.Gt * md.kmax, cs = 3 * ps;
+        const size_t cs = (size_t)md.ntiles * md.kmax * 128;  // component stride of the FP32 store
         double acc_r = 0, acc_g0 = 0, acc_g1 = 0, acc_g2 = 0, acc_t = 0;
         float T[128];
 #pragma unroll
@@ -205,24 +201,27 @@ __global__ void __launch_bounds__(kThreads, 1) density_tc_kernel(const __grid_co
             tc::fence_before_sync();
             mbar_arrive(&sm.tempty[b]);
             if (kc != nkept - 1) continue;
-            // nu block complete: contract T with this row's AO values
+            // nu block complete: contract T with this row's AO values, read
+            // from the function-major FP32 store (a warp reads 32 consecutive
+            // points of one function: one 128-byte line per load)
             if (live && !sm.abort) {
                 float pr = 0, pg0 = 0, pg1 = 0, pg2 = 0, pt_ = 0;
 #pragma unroll
                 for (int h = 0; h < 2; h++) {
                     const int slot = 2 * vb + h;
                     if (slot >= nkept) break;
-                    const bf16* base = md.pf + (size_t)(t * 128 + g) * md.kmax + slot * 64;
+                    const float* e0 = md.e32 + ((size_t)t * md.kmax + slot * 64) * 128 + g;
 #pragma unroll
                     for (int j = 0; j < 64; j++) {
                         const float tv = T[h * 64 + j];
-                        if (EPI <= 1) pr = fmaf(tv, bf3(base, ps, j), pr);
+                        const size_t o = (size_t)j * 128;
+                        if (EPI <= 1) pr = fmaf(tv, __ldg(e0 + o), pr);
                         if (EPI == 1) {
-                            pg0 = fmaf(tv, bf3(base + cs, ps, j), pg0);
-                            pg1 = fmaf(tv, bf3(base + 2 * cs, ps, j), pg1);
-                            pg2 = fmaf(tv, bf3(base + 3 * cs, ps, j), pg2);
+                            pg0 = fmaf(tv, __ldg(e0 + cs + o), pg0);
+                            pg1 = fmaf(tv, __ldg(e0 + 2 * cs + o), pg1);
+                            pg2 = fmaf(tv, __ldg(e0 + 3 * cs + o), pg2);
                         }
-                        if (EPI == 2) pt_ = fmaf(tv, bf3(base + (size_t)acomp * cs, ps, j), pt_);
+                        if (EPI == 2) pt_ = fmaf(tv, __ldg(e0 + (size_t)acomp * cs + o), pt_);
                     }
                 }
                 acc_r += pr;
@@ -418,28 +417,27 @@ __global__ void prep_r_kernel(MixedDev md, int ncomp, int type, const double* __
             for (int p = 0; p < 3; p++) R[((size_t)(c * 3 + p) * TK + row) * 128 + g] = __float2bfloat16(0.f);
         return;
     }
-    auto fpv = [&](int c) {
-        const bf16* b = md.fp + ((size_t)(c * 3) * TK + row) * 128 + g;
-        const size_t ps = (size_t)TK * 128;
-        return (double)__bfloat162float(b[0]) + (double)__bfloat162float(b[ps]) + (double)__bfloat162float(b[2 * ps]);
-    };
-    const double phi = fpv(0);
-    double a = fcoef[pt] * phi;
-    double d[3] = {0, 0, 0};
+    // FP32 arithmetic: R carries ~2^-24 relative precision in its three planes
+    auto fpv = [&](int c) { return __ldg(md.e32 + ((size_t)c * TK + row) * 128 + g); };
+    const float phi = fpv(0);
+    float a = (float)fcoef[pt] * phi;
+    float d[3] = {0, 0, 0};
     if (type >= 1) {
         for (int r = 0; r < 3; r++) d[r] = fpv(1 + r);
-        a += fcoef[Gp + pt] * d[0] + fcoef[2 * Gp + pt] * d[1] + fcoef[3 * Gp + pt] * d[2];
+        a = fmaf((float)fcoef[Gp + pt], d[0], a);
+        a = fmaf((float)fcoef[2 * Gp + pt], d[1], a);
+        a = fmaf((float)fcoef[3 * Gp + pt], d[2], a);
     }
     bf16 h, m, l;
-    tc::split3(a, h, m, l);
+    tc::split3f(a, h, m, l);
     const size_t ps = (size_t)TK * 128;
     R[row * 128 + g] = h;
     R[ps + row * 128 + g] = m;
     R[2 * ps + row * 128 + g] = l;
     if (ncomp == 4) {
-        const double c2 = fcoef[4 * Gp + pt];
+        const float c2 = (float)fcoef[4 * Gp + pt];
         for (int r = 0; r < 3; r++) {
-            tc::split3(c2 * d[r], h, m, l);
+            tc::split3f(c2 * d[r], h, m, l);
             R[((size_t)((1 + r) * 3 + 0) * TK + row) * 128 + g] = h;
             R[((size_t)((1 + r) * 3 + 1) * TK + row) * 128 + g] = m;
             R[((size_t)((1 + r) * 3 + 2) * TK + row) * 128 + g] = l;
@@ -456,7 +454,7 @@ __global__ void __launch_bounds__(128) ao_mixed_kernel(MixedDev md, DevShells sh
                                                        const double* __restrict__ px, const double* __restrict__ py,
                                                        const double* __restrict__ pz, long Gp,
                                                        const double* __restrict__ shtab, bf16* __restrict__ pf,
-                                                       bf16* __restrict__ fp) {
+                                                       bf16* __restrict__ fp, float* __restrict__ e32) {
     const int t = blockIdx.x, g = threadIdx.x;
     const long pt = (long)t * 128 + g;
     const long src = pt < Gp ? pt : 0;  // tail points: copies of point 0 (their weight is zero)
@@ -509,6 +507,7 @@ __global__ void __launch_bounds__(128) ao_mixed_kernel(MixedDev md, DevShells sh
                     pf[((size_t)(c * 3 + p) * md.Gt + pt) * md.kmax + col] = h[p];
                     fp[((size_t)(c * 3 + p) * TK + (size_t)t * md.kmax + col) * 128 + g] = h[p];
                 }
+                e32[((size_t)c * TK + (size_t)t * md.kmax + col) * 128 + g] = (float)vals[c];
             }
         }
     }
@@ -517,8 +516,9 @@ __global__ void __launch_bounds__(128) ao_mixed_kernel(MixedDev md, DevShells sh
 }  // namespace
 
 void launch_ao_mixed(const MixedDev& md, DevShells sh, const int* tile_shells, const int* tile_shell_off, const double* x,
-                     const double* y, const double* z, long Gp, const double* shtab, bf16* pf, bf16* fp, cudaStream_t s) {
-    ao_mixed_kernel<<<md.ntiles, 128, 0, s>>>(md, sh, tile_shells, tile_shell_off, x, y, z, Gp, shtab, pf, fp);
+                     const double* y, const double* z, long Gp, const double* shtab, bf16* pf, bf16* fp, float* e32,
+                     cudaStream_t s) {
+    ao_mixed_kernel<<<md.ntiles, 128, 0, s>>>(md, sh, tile_shells, tile_shell_off, x, y, z, Gp, shtab, pf, fp, e32);
     CGB_CUDA(cudaGetLastError());
 }
 

@@ -39,11 +39,14 @@ void launch_density_fp64(int nblocks, const BlockDesc* d_blocks, const int* d_ba
                          double* rho1, double* tau, cudaStream_t s);
 
 // Functional on every point: eps, vrho, vsigma, vtau, sigma, the Fock
-// coefficients fcoef (s, 5, G) and per-CTA partial energies.
+// coefficients fcoef (s, 5, G) and per-CTA partial energies.  Points whose
+// total density is >= float_above are evaluated in FP32 (mixed path); the
+// default keeps every point in FP64.
 void launch_functional_fp64(const xcf::FuncDesc& f, int family, int nspin, long Gp, const double* w,
                             const double* rho, const double* rho1, const double* tau, double* sigma,
                             double* eps, double* vrho, double* vsigma, double* vtau, double* fcoef,
-                            double* e_partial, int* n_partial, cudaStream_t s);
+                            double* e_partial, int* n_partial, cudaStream_t s,
+                            double float_above = __builtin_huge_val());
 
 // Deterministic sum of n partials into out[0] (single CTA, fixed order).
 void launch_reduce_sum(const double* partial, int n, double* out, cudaStream_t s);

@@ -116,15 +116,18 @@ void Grid::prepare_mixed(double thr) {
     const long TK = (long)md.ntiles * md.kmax;
     m.d_pf.alloc((size_t)12 * md.Gt * md.kmax);
     m.d_fp.alloc((size_t)(12 * TK + 64) * 128);
+    m.d_e32.alloc((size_t)4 * TK * 128);
     m.d_pf.zero(stream);
     m.d_fp.zero(stream);
+    m.d_e32.zero(stream);
     md.tile_nkept = m.d_nkept.p;
     md.tile_chunks = m.d_chunks.p;
     md.tile_slot = m.d_slot.p;
     md.pf = m.d_pf.p;
     md.fp = m.d_fp.p;
+    md.e32 = m.d_e32.p;
     launch_ao_mixed(md, dev_shells(), m.d_tile_shells.p, m.d_tile_shell_off.p, d_x.p, d_y.p, d_z.p, Gp, m.d_shtab.p,
-                    m.d_pf.p, m.d_fp.p, stream);
+                    m.d_pf.p, m.d_fp.p, m.d_e32.p, stream);
     // per-build operands
     m.r_ncomp = type >= 2 ? 4 : 1;
     m.d_R.alloc((size_t)(m.r_ncomp * 3 * TK + 64) * 128);
@@ -166,7 +169,7 @@ void Grid::build_mixed(const double* dD, const Functional& f, double* dE, double
                 launch_density_tc(m.tm_pf, m.tm_d, md, 2, r, s, d_rho.p, d_rho1.p, d_tau.p, Gp, m.d_err.p, stream);
     }
     have_density = true;
-    evaluate(f);  // marks 1
+    evaluate(f, kMixedFuncFloat);  // marks 1
     energy_device(dE);  // marks 2
     mark(3);
     const size_t npadw = (size_t)m.nblk * 128;

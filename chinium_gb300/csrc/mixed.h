@@ -27,6 +27,7 @@ struct MixedDev {
     const int* tile_slot;    // [ntiles][nchunk] slot of a global chunk, -1 if dropped
     const __nv_bfloat16* pf; // point-major AO planes
     const __nv_bfloat16* fp; // function-major AO planes
+    const float* e32;        // function-major FP32 AO values [c][t][kmax][128] (epilogues)
 };
 
 struct MixedState {
@@ -38,6 +39,7 @@ struct MixedState {
     DevBuf<int> d_nkept, d_chunks, d_slot, d_tile_shells, d_tile_shell_off;
     DevBuf<double> d_shtab;
     DevBuf<__nv_bfloat16> d_pf, d_fp, d_R, d_Dp;
+    DevBuf<float> d_e32;
     DevBuf<double> d_wpart;
     DevBuf<int> d_err;
     int r_ncomp = 0;
@@ -48,7 +50,7 @@ struct MixedState {
 size_t mixed_smem_bytes();
 void launch_ao_mixed(const MixedDev& md, DevShells sh, const int* tile_shells, const int* tile_shell_off,
                      const double* x, const double* y, const double* z, long Gp, const double* shtab,
-                     __nv_bfloat16* pf, __nv_bfloat16* fp, cudaStream_t s);
+                     __nv_bfloat16* pf, __nv_bfloat16* fp, float* e32, cudaStream_t s);
 void launch_split_d(const double* D, int n, int npad, int nspin, __nv_bfloat16* Dp, cudaStream_t s);
 void launch_density_tc(const CUtensorMap& tm_pf, const CUtensorMap& tm_d, const MixedDev& md, int epi, int acomp,
                        int spin, double* rho, double* rho1, double* tau, long Gp, int* err, cudaStream_t s);

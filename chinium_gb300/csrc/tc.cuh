@@ -138,5 +138,14 @@ __device__ __forceinline__ void split3(double x, __nv_bfloat16& h, __nv_bfloat16
     l = __double2bfloat16(r);
 }
 
+// Same for a float (the three parts represent it exactly).
+__device__ __forceinline__ void split3f(float x, __nv_bfloat16& h, __nv_bfloat16& m, __nv_bfloat16& l) {
+    h = __float2bfloat16_rn(x);
+    float r = x - __bfloat162float(h);
+    m = __float2bfloat16_rn(r);
+    r -= __bfloat162float(m);
+    l = __float2bfloat16_rn(r);
+}
+
 }  // namespace tc
 }  // namespace cgb

@@ -16,6 +16,9 @@ void ensure_device();
 
 // Default AO screening threshold of the mixed-precision tiles (|phi|, |grad phi|).
 constexpr double kMixedScreen = 1e-11;
+// Total density at and above which the mixed path evaluates the functional
+// in FP32; below it (the low-density region) the functional stays FP64.
+constexpr double kMixedFuncFloat = 1e-3;
 
 struct Functional {
     std::vector<int> ids;
@@ -66,7 +69,7 @@ struct Grid {
     void get_ao(int derivative);
     void ensure_work();
     void density_device(const double* dD);
-    void evaluate(const Functional& f);
+    void evaluate(const Functional& f, double float_above = __builtin_huge_val());
     void energy_device(double* dE);
     void fock_device(double* dV, int family);
 
