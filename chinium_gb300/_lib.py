@@ -73,6 +73,9 @@ SIGNATURES = {
     "xc_build_device": [_P, _P, _P, _I, _I, _P, _P],
     "xc_sap_fock": [_P, _P],
     "xc_functional_energy_static": [_P, _L, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P],
+    "xc_build_incremental": [_P, _P, _P, _I, _I, _P, _P],
+    "xc_int1e": [_P, _P, _P, _P],
+    "xc_eri": [_P, _P, _D],
     "xc_grid_profile": [_P, _I],
     "xc_grid_stage_ms": [_P, _P],
 }
@@ -81,12 +84,14 @@ _lib = None
 
 
 def header_symbols():
-    """Function names declared in include/chinium_xc.h."""
+    """Function names declared in include/*.h."""
+    import glob
     import re
-    path = os.path.join(os.path.dirname(HERE), "include", "chinium_xc.h")
-    with open(path) as f:
-        txt = f.read()
-    return sorted(set(re.findall(r"^int\s+(xc_\w+)\s*\(", txt, flags=re.M)))
+    names = set()
+    for path in glob.glob(os.path.join(os.path.dirname(HERE), "include", "*.h")):
+        with open(path) as f:
+            names |= set(re.findall(r"^int\s+(xc_\w+)\s*\(", f.read(), flags=re.M))
+    return sorted(names)
 
 
 def lib():

@@ -16,7 +16,7 @@ LIB = os.path.join(OUT, "libchinium_xc.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
-              "-Xcompiler", "-Wall,-Wno-unused-function,-Wno-unknown-pragmas"]
+              "-Xcompiler", "-Wall,-Wno-unused-function,-Wno-unknown-pragmas", "-Xcompiler", "-fopenmp"]
 
 
 def _nvcc():
@@ -52,7 +52,8 @@ def _stale(objs_inputs):
 def build(force=False, verbose=False, extra=()):
     os.makedirs(OUT, exist_ok=True)
     inputs = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [
-        os.path.join(os.path.dirname(HERE), "include", "chinium_xc.h"), os.path.abspath(__file__)]
+        os.path.join(os.path.dirname(HERE), "include", "chinium_xc.h"),
+        os.path.join(os.path.dirname(HERE), "include", "chinium_int.h"), os.path.abspath(__file__)]
     if not force and not _stale(inputs):
         return LIB
     srcs = sources()
@@ -72,7 +73,7 @@ def build(force=False, verbose=False, extra=()):
         for _, err in results:
             if err:
                 sys.stderr.write(err)
-    cmd = [_nvcc()] + ARCH + ["-shared", "-o", LIB] + [o for o, _ in results] + ["-lcudart"]
+    cmd = [_nvcc()] + ARCH + ["-shared", "-o", LIB] + [o for o, _ in results] + ["-lcudart", "-lgomp"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s" % r.stderr)

@@ -736,6 +736,24 @@ int xc_grid_stage_ms(xc_grid* g, double* ms) {
     });
 }
 
+int xc_build_incremental(xc_grid* g, xc_functional* f, const double* D, int nspin, int anchor, double* E,
+                         double* V) {
+    return guard([&] {
+        CGB_CHECK(g && f && D && E && V, XC_ERR_ARG, "null argument");
+        Grid& G = g->g;
+        CGB_CHECK(nspin == G.nspin && f->f.nspin == G.nspin, XC_ERR_ARG, "Wrong number of spin types!");
+        CGB_CHECK(f->f.family <= G.type, XC_ERR_STATE, "grid type is below the functional family (setType/getAO)");
+        G.ensure_work();
+        const size_t nn = (size_t)G.basis.nbasis * G.basis.nbasis * nspin;
+        CGB_CUDA(cudaMemcpyAsync(G.d_D.p, D, nn * sizeof(double), cudaMemcpyHostToDevice, G.stream));
+        G.build_incremental(G.d_D.p, f->f, G.d_scalar.p, G.d_V.p, anchor != 0);
+        CGB_CUDA(cudaMemcpyAsync(E, G.d_scalar.p, sizeof(double), cudaMemcpyDeviceToHost, G.stream));
+        CGB_CUDA(cudaMemcpyAsync(V, G.d_V.p, nn * sizeof(double), cudaMemcpyDeviceToHost, G.stream));
+        CGB_CUDA(cudaStreamSynchronize(G.stream));
+        if (G.mixed_error()) throw Error(XC_ERR_TIMEOUT, "a bounded wait of the tensor-core pipeline gave up");
+    });
+}
+
 int xc_sap_fock(xc_grid* g, double* V) {
     return guard([&] {
         CGB_CHECK(g && V, XC_ERR_ARG, "null argument");

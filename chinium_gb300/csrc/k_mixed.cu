@@ -371,6 +371,13 @@ __global__ void __launch_bounds__(kThreads, 1) fock_tc_kernel(const __grid_const
     if (warp == 0) tc::tmem_dealloc(tmem, kTmemCols);
 }
 
+// out = a * x + b * y (FP64, n elements).
+__global__ void axpby_kernel(long n, double a, const double* __restrict__ x, double b, const double* __restrict__ y,
+                             double* __restrict__ out) {
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = a * x[i] + b * y[i];
+}
+
 // V(mu, nu) = sum_s W_s(mu, nu) + W_s(nu, mu), column-major n x n (FP64).
 __global__ void wsum_kernel(const double* __restrict__ wpart, int nsplit, int npadw, int n, double* __restrict__ V) {
     const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -558,6 +565,12 @@ void launch_fock_tc(const CUtensorMap& tm_fp, const CUtensorMap& tm_r, const Mix
     CGB_CUDA(cudaFuncSetAttribute(fock_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     dim3 grid(nblk * nblk, nsplit);
     fock_tc_kernel<<<grid, kThreads, smem, s>>>(tm_fp, tm_r, md, ncomp, r_rows, nblk, nsplit, wpart, err);
+    CGB_CUDA(cudaGetLastError());
+}
+
+void launch_axpby(long n, double a, const double* x, double b, const double* y, double* out, cudaStream_t s) {
+    if (n <= 0) return;
+    axpby_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, a, x, b, y, out);
     CGB_CUDA(cudaGetLastError());
 }
 

@@ -184,6 +184,82 @@ void Grid::build_mixed(const double* dD, const Functional& f, double* dE, double
     mark(4);
 }
 
+// Incremental build: the density is linear in D and V_xc is linear in the
+// per-point coefficients, so rho(D) = rho_ref + rho(D - D_ref) and
+// V = V_ref + V(c - c_ref), with only the differences on the tensor cores.
+// Their split-BF16 error is relative to the (shrinking, in an SCF) change;
+// the functional and E_xc are evaluated in FP64 on the reconstructed
+// densities.  An anchor (or the first call) is a full FP64 build that resets
+// the references.
+void Grid::build_incremental(const double* dD, const Functional& f, double* dE, double* dV, bool anchor) {
+    MixedState& m = mx;
+    CGB_CHECK(ao_order >= type, XC_ERR_STATE, "getAO must run (for the current type) before a build");
+    ensure_work();
+    const int n = basis.nbasis;
+    const size_t nn = (size_t)n * n * nspin, G1 = (size_t)nspin * Gp;
+    if (anchor || !m.have_ref) {
+        density_device(dD);
+        evaluate(f);
+        energy_device(dE);
+        fock_device(dV, f.family);
+        m.d_Dref.alloc(nn);
+        m.d_rho_ref.alloc(G1);
+        m.d_rho1_ref.alloc(3 * G1);
+        m.d_tau_ref.alloc(G1);
+        m.d_fcoef_ref.alloc(5 * G1);
+        m.d_Vref.alloc(nn);
+        m.d_dD.alloc(nn);
+        m.d_dfcoef.alloc(5 * G1);
+        CGB_CUDA(cudaMemcpyAsync(m.d_Dref.p, dD, nn * 8, cudaMemcpyDeviceToDevice, stream));
+        CGB_CUDA(cudaMemcpyAsync(m.d_rho_ref.p, d_rho.p, G1 * 8, cudaMemcpyDeviceToDevice, stream));
+        CGB_CUDA(cudaMemcpyAsync(m.d_rho1_ref.p, d_rho1.p, 3 * G1 * 8, cudaMemcpyDeviceToDevice, stream));
+        CGB_CUDA(cudaMemcpyAsync(m.d_tau_ref.p, d_tau.p, G1 * 8, cudaMemcpyDeviceToDevice, stream));
+        CGB_CUDA(cudaMemcpyAsync(m.d_fcoef_ref.p, d_fcoef.p, 5 * G1 * 8, cudaMemcpyDeviceToDevice, stream));
+        CGB_CUDA(cudaMemcpyAsync(m.d_Vref.p, dV, nn * 8, cudaMemcpyDeviceToDevice, stream));
+        m.have_ref = true;
+        return;
+    }
+    if (!m.ready || m.r_ncomp != (type >= 2 ? 4 : 1)) prepare_mixed(m.ready ? m.thr : kMixedScreen);
+    const MixedDev& md = m.md;
+    mark(0);
+    launch_axpby((long)nn, 1.0, dD, -1.0, m.d_Dref.p, m.d_dD.p, stream);
+    launch_split_d(m.d_dD.p, n, md.npad, nspin, m.d_Dp.p, stream);
+    if (type >= 2) CGB_CUDA(cudaMemsetAsync(d_tau.p, 0, sizeof(double) * G1, stream));
+    for (int s = 0; s < nspin; s++) {
+        launch_density_tc(m.tm_pf, m.tm_d, md, type >= 1 ? 1 : 0, 0, s, d_rho.p, d_rho1.p, d_tau.p, Gp, m.d_err.p,
+                          stream);
+        if (type >= 2)
+            for (int r = 1; r <= 3; r++)
+                launch_density_tc(m.tm_pf, m.tm_d, md, 2, r, s, d_rho.p, d_rho1.p, d_tau.p, Gp, m.d_err.p, stream);
+    }
+    launch_axpby((long)G1, 1.0, d_rho.p, 1.0, m.d_rho_ref.p, d_rho.p, stream);
+    if (type >= 1) launch_axpby((long)(3 * G1), 1.0, d_rho1.p, 1.0, m.d_rho1_ref.p, d_rho1.p, stream);
+    if (type >= 2) launch_axpby((long)G1, 1.0, d_tau.p, 1.0, m.d_tau_ref.p, d_tau.p, stream);
+    have_density = true;
+    evaluate(f);  // FP64 functional on the reconstructed densities
+    energy_device(dE);
+    mark(3);
+    launch_axpby((long)(5 * G1), 1.0, d_fcoef.p, -1.0, m.d_fcoef_ref.p, m.d_dfcoef.p, stream);
+    const size_t npadw = (size_t)m.nblk * 128;
+    const int ncomp = f.family >= 2 ? 4 : 1;
+    for (int s = 0; s < nspin; s++) {
+        launch_prep_r(md, ncomp, f.family, m.d_dfcoef.p + (size_t)s * 5 * Gp, Gp, m.d_R.p, stream);
+        double* wp = m.d_wpart.p + (size_t)s * m.nsplit * npadw * npadw;
+        const int r_rows = (int)((long)m.r_ncomp * 3 * md.ntiles * md.kmax);
+        launch_fock_tc(m.tm_fp, m.tm_r, md, ncomp, r_rows, m.nblk, m.nsplit, wp, m.d_err.p, stream);
+        launch_wsum(wp, m.nsplit, (int)npadw, n, dV + (size_t)s * n * n, stream);
+    }
+    launch_axpby((long)nn, 1.0, dV, 1.0, m.d_Vref.p, dV, stream);
+    mark(4);
+    // the new references
+    CGB_CUDA(cudaMemcpyAsync(m.d_Dref.p, dD, nn * 8, cudaMemcpyDeviceToDevice, stream));
+    CGB_CUDA(cudaMemcpyAsync(m.d_rho_ref.p, d_rho.p, G1 * 8, cudaMemcpyDeviceToDevice, stream));
+    if (type >= 1) CGB_CUDA(cudaMemcpyAsync(m.d_rho1_ref.p, d_rho1.p, 3 * G1 * 8, cudaMemcpyDeviceToDevice, stream));
+    if (type >= 2) CGB_CUDA(cudaMemcpyAsync(m.d_tau_ref.p, d_tau.p, G1 * 8, cudaMemcpyDeviceToDevice, stream));
+    CGB_CUDA(cudaMemcpyAsync(m.d_fcoef_ref.p, d_fcoef.p, 5 * G1 * 8, cudaMemcpyDeviceToDevice, stream));
+    CGB_CUDA(cudaMemcpyAsync(m.d_Vref.p, dV, nn * 8, cudaMemcpyDeviceToDevice, stream));
+}
+
 int Grid::mixed_error() {
     if (!mx.ready) return 0;
     int e = 0;

@@ -42,6 +42,9 @@ struct MixedState {
     DevBuf<float> d_e32;
     DevBuf<double> d_wpart;
     DevBuf<int> d_err;
+    // incremental builds: references of the previous build and difference scratch
+    bool have_ref = false;
+    DevBuf<double> d_Dref, d_rho_ref, d_rho1_ref, d_tau_ref, d_fcoef_ref, d_Vref, d_dD, d_dfcoef;
     int r_ncomp = 0;
     int nblk = 0, nsplit = 0;
     CUtensorMap tm_pf, tm_d, tm_fp, tm_r;
@@ -60,6 +63,7 @@ void launch_prep_r(const MixedDev& md, int ncomp, int type, const double* fcoef,
 void launch_fock_tc(const CUtensorMap& tm_fp, const CUtensorMap& tm_r, const MixedDev& md, int ncomp, int r_rows,
                     int nblk, int nsplit, double* wpart, int* err, cudaStream_t s);
 void launch_wsum(const double* wpart, int nsplit, int npadw, int n, double* V, cudaStream_t s);
+void launch_axpby(long n, double a, const double* x, double b, const double* y, double* out, cudaStream_t s);
 
 // 2D bf16 tensor map with 128-byte swizzle over a row-major [rows][cols] array.
 void make_tmap_bf16(CUtensorMap* map, const void* base, uint64_t cols, uint64_t rows, uint32_t box_cols,

@@ -77,6 +77,7 @@ struct Grid {
     MixedState mx;
     void prepare_mixed(double thr);
     void build_mixed(const double* dD, const Functional& f, double* dE, double* dV);
+    void build_incremental(const double* dD, const Functional& f, double* dE, double* dV, bool anchor);
     int mixed_error();
 };
 

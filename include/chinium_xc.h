@@ -200,6 +200,18 @@ int xc_build_device(xc_grid* g, xc_functional* f, const double* d_D, int nspin, 
 int xc_grid_profile(xc_grid* g, int enable);
 int xc_grid_stage_ms(xc_grid* g, double* ms);
 
+/* Incremental mixed-precision build for SCF iterations (the per-iteration
+ * sequence at Restricted/SP.cpp:52-55, fused).  Densities are linear in D
+ * and V_xc is linear in the per-point potential coefficients, so this call
+ * forms rho(D) = rho_ref + rho(D - D_ref) and V = V_ref + V(c - c_ref) with
+ * only the differences on the tensor cores (split-BF16, FP32 accumulation);
+ * the functional and E_xc are FP64 on the reconstructed densities.  The
+ * tensor-core error is relative to the change since the previous call, so it
+ * vanishes as an SCF converges.  anchor != 0, or the first call on a grid,
+ * runs a full FP64 build and resets the references.  Host buffers. */
+int xc_build_incremental(xc_grid* g, xc_functional* f, const double* D, int nspin, int anchor,
+                         double* E, double* V);
+
 /* SAP potential matrix (GuessSCF.cpp:17-75): V_mu,nu = sum_g w v_SAP(r_g)
  * phi_mu phi_nu with v_SAP the nearest-radius tabulated atomic potentials. */
 int xc_sap_fock(xc_grid* g, double* V);

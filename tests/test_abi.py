@@ -61,6 +61,33 @@ def test_c18_and_fe4s4_geometry():
     assert sorted(dfs)[:12] == pytest.approx([2.28] * 12, abs=1e-9)
 
 
+def test_integrals_structure():
+    """S, T, V against grid quadrature on the oracle grid; ERI symmetry and
+    positive semidefiniteness of the (mu nu | lambda sigma) supermatrix."""
+    from chinium_gb300.scf import one_electron, repulsion
+    from oracle import oracle as O
+    Z, xyz = M.h2o()
+    b = cg.Basis(Z, xyz, "def2-svp")
+    S, T, V = one_electron(b)
+    assert np.allclose(np.diag(S), 1.0, atol=1e-12)
+    assert np.allclose(S, S.T) and np.allclose(T, T.T) and np.allclose(V, V.T)
+    og = O.OracleGrid(O.Basis(Z, xyz, "def2-svp"), "SG-1", Z, xyz)
+    Sg, Tg, Vg = (np.zeros_like(S) for _ in range(3))
+    for (bx, by, bz, bw), (ao, ao1) in zip(og.blocks, og.ao):
+        Sg += (ao * bw) @ ao.T
+        Tg += 0.5 * sum((ao1[r] * bw) @ ao1[r].T for r in range(3))
+        vn = sum(-z / np.maximum(np.sqrt((bx - xyz[a, 0]) ** 2 + (by - xyz[a, 1]) ** 2 + (bz - xyz[a, 2]) ** 2), 1e-12)
+                 for a, z in enumerate(Z))
+        Vg += (ao * (bw * vn)) @ ao.T
+    assert np.abs(S - Sg).max() < 1e-4
+    assert np.abs(T - Tg).max() < 1e-3
+    assert np.abs(V - Vg).max() < 1e-3
+    eri = repulsion(b)
+    n = b.nbasis
+    assert np.allclose(eri, eri.transpose(1, 0, 2, 3)) and np.allclose(eri, eri.transpose(2, 3, 0, 1))
+    assert np.linalg.eigvalsh(eri.reshape(n * n, n * n)).min() > -1e-12
+
+
 def test_functional_read_fields():
     for name, ids, exx, fam in [("PBE", [321, 322], 0.0, "GGA"), ("B3LYP", [402], 0.2, "GGA"),
                                 ("TPSS", [202, 231], 0.0, "mGGA"), ("R2SCAN", [497, 498], 0.0, "mGGA"),
