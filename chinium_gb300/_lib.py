@@ -74,6 +74,14 @@ SIGNATURES = {
     "xc_sap_fock": [_P, _P],
     "xc_functional_energy_static": [_P, _L, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P],
     "xc_build_incremental": [_P, _P, _P, _I, _I, _P, _P],
+    "xc_mlp_create": [_I, _I, _I, _I, _PP],
+    "xc_mlp_destroy": [_P],
+    "xc_mlp_nparams": [_P, _P],
+    "xc_mlp_set_params": [_P, _P],
+    "xc_mlp_get_params": [_P, _P],
+    "xc_mlp_forward": [_P, _I, _P, _P, _I],
+    "xc_mlp_backward": [_P, _I, _P, _P, _P],
+    "xc_mlp_train_step": [_P, _I, _P, _P, _P, ctypes.c_float, _P],
     "xc_int1e": [_P, _P, _P, _P],
     "xc_eri": [_P, _P, _D],
     "xc_grid_profile": [_P, _I],

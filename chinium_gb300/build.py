@@ -53,7 +53,8 @@ def build(force=False, verbose=False, extra=()):
     os.makedirs(OUT, exist_ok=True)
     inputs = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [
         os.path.join(os.path.dirname(HERE), "include", "chinium_xc.h"),
-        os.path.join(os.path.dirname(HERE), "include", "chinium_int.h"), os.path.abspath(__file__)]
+        os.path.join(os.path.dirname(HERE), "include", "chinium_int.h"),
+        os.path.join(os.path.dirname(HERE), "include", "chinium_guess.h"), os.path.abspath(__file__)]
     if not force and not _stale(inputs):
         return LIB
     srcs = sources()

@@ -1,0 +1,319 @@
+"""Learned starting density: a per-atom-pair MLP over local geometry.
+
+For every atom pair (A, B) -- including A = B -- a local frame is built from
+the pair axis (or, on site, the nearest neighbour) and a reference atom.  The
+network sees rotation-invariant features (element types, the pair distance,
+and the neighbours' coordinates in that frame) and predicts the density
+matrix block D[A, B] expressed in the frame; the block is rotated back to
+the molecular frame with the real-solid-harmonic rotation matrices of each
+shell.  The assembled matrix is made symmetric and purified to an idempotent
+closed-shell density with the right electron count (natural orbitals in the
+overlap metric).  Molecules the model does not cover (other elements, other
+basis) fall back to the SAP guess.
+
+Training data are converged densities from this library's own SCF; the
+network is trained and evaluated by the library's CUDA kernels
+(include/chinium_guess.h).
+"""
+import ctypes
+import math
+import os
+
+import numpy as np
+
+from ._lib import check, lib
+
+ELEMENTS = (1, 8)          # H, O: the water-cluster model
+MAX_FUNC = 14              # def2-SVP: O 14 functions, H 5
+N_NEIGH = 12
+CUTOFF = 12.0              # bohr
+NIN = 7 + 6 * N_NEIGH
+NOUT = MAX_FUNC * MAX_FUNC
+HIDDEN, LAYERS = 256, 3
+
+
+# ----------------------------------------------------------------- rotations
+
+def _binom(n, k):
+    return math.comb(n, k) if 0 <= k <= n else 0
+
+
+def solid_harmonics(l, xyz):
+    """Real solid harmonics S_lm (m = -l..l), Helgaker-Jorgensen-Olsen
+    normalisation (S_l0 = r^l P_l(cos theta)); xyz (K, 3) -> (2l+1, K)."""
+    x, y, z = xyz[:, 0], xyz[:, 1], xyz[:, 2]
+    out = np.zeros((2 * l + 1, len(xyz)))
+    for m in range(-l, l + 1):
+        am = abs(m)
+        vm2 = 1 if m < 0 else 0
+        N = 1.0 / (2 ** am * math.factorial(l)) * math.sqrt(
+            2.0 * math.factorial(l + am) * math.factorial(l - am) / (2.0 if m == 0 else 1.0))
+        vmax2 = 2 * math.floor(am / 2 - vm2 / 2) + vm2
+        acc = np.zeros(len(xyz))
+        for t in range((l - am) // 2 + 1):
+            for u in range(t + 1):
+                for v2 in range(vm2, vmax2 + 1, 2):
+                    sgn = -1.0 if (t + (v2 - vm2) // 2) % 2 else 1.0
+                    C = sgn * 0.25 ** t * _binom(l, t) * _binom(l - t, am + t) * _binom(t, u) * _binom(am, v2)
+                    a, b, c = 2 * t + am - 2 * u - v2, 2 * u + v2, l - 2 * t - am
+                    if a < 0 or b < 0 or c < 0:
+                        continue
+                    acc = acc + C * x ** a * y ** b * z ** c
+        out[m + l] = N * acc
+    return out
+
+
+_RNG_PTS = np.random.default_rng(12345).normal(size=(32, 3))
+
+
+def shell_rotation(shell_type, Q):
+    """U with f_local = U f_global for the functions of one shell, where the
+    local frame has axes Q[:, 0..2] (columns) in global coordinates."""
+    if shell_type == 0:
+        return np.ones((1, 1))
+    if shell_type == 1:  # Cartesian x, y, z
+        return Q.T.copy()
+    l = -shell_type
+    B = solid_harmonics(l, _RNG_PTS)
+    A = solid_harmonics(l, _RNG_PTS @ Q)  # S(Q^T r) for each sample r
+    return A @ np.linalg.pinv(B)
+
+
+def atom_rotation(shell_types, Q):
+    blocks = [shell_rotation(t, Q) for t in shell_types]
+    n = sum(b.shape[0] for b in blocks)
+    U = np.zeros((n, n))
+    o = 0
+    for b in blocks:
+        k = b.shape[0]
+        U[o:o + k, o:o + k] = b
+        o += k
+    return U
+
+
+# -------------------------------------------------------------- geometry
+
+def _frame(ez, ref):
+    ez = ez / np.linalg.norm(ez)
+    v = ref - np.dot(ref, ez) * ez
+    if np.linalg.norm(v) < 1e-6:
+        alt = np.array([1.0, 0.0, 0.0]) if abs(ez[0]) < 0.9 else np.array([0.0, 1.0, 0.0])
+        v = alt - np.dot(alt, ez) * ez
+    ex = v / np.linalg.norm(v)
+    ey = np.cross(ez, ex)
+    return np.stack([ex, ey, ez], axis=1)
+
+
+def _by_distance(d, exclude):
+    """Atom indices by distance; distances equal to 1e-6 bohr (symmetric
+    neighbours, e.g. the two hydrogens of a water) tie-break by index, so the
+    order does not depend on rounding or on the molecule's orientation."""
+    return [i for i in sorted(range(len(d)), key=lambda i: (round(float(d[i]), 6), i)) if i not in exclude]
+
+
+def pair_frame(xyz, a, b):
+    """Local axes (columns) for pair (a, b): z along a->b (on site: toward the
+    nearest neighbour), x toward the nearest other atom."""
+    ra = xyz[a]
+    d = np.linalg.norm(xyz - ra, axis=1)
+    order = _by_distance(d, (a, b))
+    if a == b:
+        if len(order) < 1:
+            return np.eye(3)
+        ez = xyz[order[0]] - ra
+        ref = xyz[order[1]] - ra if len(order) > 1 else np.array([1.0, 0.0, 0.0])
+    else:
+        ez = xyz[b] - ra
+        ref = xyz[order[0]] - ra if order else np.array([1.0, 0.0, 0.0])
+    return _frame(ez, ref)
+
+
+def _cut(r):
+    return np.where(r < CUTOFF, 0.5 * (np.cos(np.pi * r / CUTOFF) + 1.0), 0.0)
+
+
+def pair_features(Z, xyz, a, b, Q):
+    onehot = lambda z: [1.0 if z == e else 0.0 for e in ELEMENTS]
+    dab = np.linalg.norm(xyz[b] - xyz[a])
+    f = onehot(Z[a]) + onehot(Z[b]) + [1.0 if a == b else 0.0, dab, math.exp(-dab)]
+    ra = xyz[a]
+    d = np.linalg.norm(xyz - ra, axis=1)
+    order = _by_distance(d, (a, b))[:N_NEIGH]
+    for i in order:
+        loc = Q.T @ (xyz[i] - ra)
+        w = _cut(d[i])
+        f += list(loc * w) + [w / (1.0 + d[i])] + onehot(Z[i])
+    f += [0.0] * (6 * (N_NEIGH - len(order)))
+    return np.array(f, dtype=np.float32)
+
+
+def atom_functions(basis):
+    sh = basis.shells()
+    natoms = len(basis.Z)
+    types = [[] for _ in range(natoms)]
+    first = [None] * natoms
+    count = [0] * natoms
+    for at, t, f0 in zip(sh["atom"], sh["type"], sh["first"]):
+        types[at].append(int(t))
+        if first[at] is None:
+            first[at] = int(f0)
+        count[at] += 1 if t == 0 else (3 if abs(t) == 1 else 2 * abs(t) + 1)
+    return types, first, count
+
+
+def pairs(xyz):
+    n = len(xyz)
+    out = []
+    for a in range(n):
+        for b in range(a, n):
+            if np.linalg.norm(xyz[a] - xyz[b]) < CUTOFF:
+                out.append((a, b))
+    return out
+
+
+def supported(Z, basis):
+    return all(z in ELEMENTS for z in Z) and basis.name == "def2-svp"
+
+
+def dataset(Z, xyz, basis, D):
+    """Features, local-frame targets and masks for every pair of a molecule
+    with converged total density D."""
+    types, first, count = atom_functions(basis)
+    X, T, Mk = [], [], []
+    for a, b in pairs(xyz):
+        Q = pair_frame(xyz, a, b)
+        Ua, Ub = atom_rotation(types[a], Q), atom_rotation(types[b], Q)
+        blk = D[first[a]:first[a] + count[a], first[b]:first[b] + count[b]]
+        loc = Ua @ blk @ Ub.T
+        t = np.zeros((MAX_FUNC, MAX_FUNC), dtype=np.float32)
+        m = np.zeros_like(t)
+        t[:count[a], :count[b]] = loc
+        m[:count[a], :count[b]] = 1.0
+        X.append(pair_features(Z, xyz, a, b, Q))
+        T.append(t.ravel())
+        Mk.append(m.ravel())
+    return np.array(X), np.array(T), np.array(Mk)
+
+
+# ------------------------------------------------------------------ network
+
+class PairMLP:
+    """Device-resident MLP (include/chinium_guess.h)."""
+
+    def __init__(self, nin=NIN, hidden=HIDDEN, layers=LAYERS, nout=NOUT, seed=0, params=None):
+        self.nin, self.hidden, self.layers, self.nout = nin, hidden, layers, nout
+        h = ctypes.c_void_p()
+        check(lib().xc_mlp_create(nin, hidden, layers, nout, ctypes.byref(h)))
+        self._h = h
+        n = ctypes.c_long()
+        check(lib().xc_mlp_nparams(h, ctypes.byref(n)))
+        self.nparams = n.value
+        self.set_params(params if params is not None else self.init_params(seed))
+
+    def init_params(self, seed):
+        rng = np.random.default_rng(seed)
+        out = []
+        dims = [self.nin] + [self.hidden] * self.layers + [self.nout]
+        for fi, fo in zip(dims[:-1], dims[1:]):
+            out.append((rng.normal(size=(fi, fo)) * math.sqrt(2.0 / fi)).ravel())
+            out.append(np.zeros(fo))
+        p = np.concatenate(out).astype(np.float32)
+        assert len(p) == self.nparams
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        check(lib().xc_mlp_set_params(self._h, p.ctypes.data_as(ctypes.c_void_p)))
+
+    def params(self):
+        p = np.zeros(self.nparams, dtype=np.float32)
+        check(lib().xc_mlp_get_params(self._h, p.ctypes.data_as(ctypes.c_void_p)))
+        return p
+
+    def forward(self, X, bf16=False):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        Y = np.zeros((len(X), self.nout), dtype=np.float32)
+        check(lib().xc_mlp_forward(self._h, len(X), X.ctypes.data_as(ctypes.c_void_p),
+                                   Y.ctypes.data_as(ctypes.c_void_p), int(bf16)))
+        return Y
+
+    def grad(self, X, dY):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        dY = np.ascontiguousarray(dY, dtype=np.float32)
+        g = np.zeros(self.nparams, dtype=np.float32)
+        check(lib().xc_mlp_backward(self._h, len(X), X.ctypes.data_as(ctypes.c_void_p),
+                                    dY.ctypes.data_as(ctypes.c_void_p), g.ctypes.data_as(ctypes.c_void_p)))
+        return g
+
+    def train_step(self, X, T, M, lr):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        T = np.ascontiguousarray(T, dtype=np.float32)
+        M = np.ascontiguousarray(M, dtype=np.float32)
+        loss = ctypes.c_float()
+        check(lib().xc_mlp_train_step(self._h, len(X), X.ctypes.data_as(ctypes.c_void_p),
+                                      T.ctypes.data_as(ctypes.c_void_p), M.ctypes.data_as(ctypes.c_void_p),
+                                      ctypes.c_float(lr), ctypes.byref(loss)))
+        return loss.value
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().xc_mlp_destroy(h)
+            self._h = None
+
+
+def train(model, X, T, M, epochs=200, batch=1024, lr=1e-3, seed=0, log=None):
+    rng = np.random.default_rng(seed)
+    n = len(X)
+    losses = []
+    for ep in range(epochs):
+        perm = rng.permutation(n)
+        tot = 0.0
+        nb = 0
+        lr_ep = lr * 0.5 * (1 + math.cos(math.pi * ep / epochs))
+        for i in range(0, n, batch):
+            idx = perm[i:i + batch]
+            tot += model.train_step(X[idx], T[idx], M[idx], lr_ep)
+            nb += 1
+        losses.append(tot / max(nb, 1))
+        if log and (ep % 20 == 0 or ep == epochs - 1):
+            log("epoch %d loss %.3e" % (ep, losses[-1]))
+    return losses
+
+
+def predict_density(model, Z, xyz, basis, S, nocc, bf16=True):
+    """Learned closed-shell total density (2 C C^T, idempotent in the S metric)."""
+    types, first, count = atom_functions(basis)
+    pr = pairs(xyz)
+    Qs = [pair_frame(xyz, a, b) for a, b in pr]
+    X = np.array([pair_features(Z, xyz, a, b, Q) for (a, b), Q in zip(pr, Qs)])
+    Y = model.forward(X, bf16=bf16).reshape(-1, MAX_FUNC, MAX_FUNC)
+    n = basis.nbasis
+    D = np.zeros((n, n))
+    for (a, b), Q, y in zip(pr, Qs, Y):
+        Ua, Ub = atom_rotation(types[a], Q), atom_rotation(types[b], Q)
+        blk = Ua.T @ y[:count[a], :count[b]].astype(np.float64) @ Ub
+        D[first[a]:first[a] + count[a], first[b]:first[b] + count[b]] = blk
+        if a != b:
+            D[first[b]:first[b] + count[b], first[a]:first[a] + count[a]] = blk.T
+    D = 0.5 * (D + D.T)
+    # purification: occupied natural orbitals in the overlap metric
+    w, V = np.linalg.eigh(S)
+    Xh = V @ np.diag(w ** -0.5) @ V.T
+    Sh = V @ np.diag(w ** 0.5) @ V.T
+    occ, C = np.linalg.eigh(Sh @ D @ Sh)
+    Co = Xh @ C[:, np.argsort(occ)[::-1][:nocc]]
+    return 2.0 * Co @ Co.T
+
+
+def save(model, path):
+    np.savez_compressed(path, params=model.params(), shape=np.array([model.nin, model.hidden, model.layers, model.nout]))
+
+
+def load(path):
+    d = np.load(path)
+    nin, hidden, layers, nout = (int(v) for v in d["shape"])
+    return PairMLP(nin, hidden, layers, nout, params=d["params"])
+
+
+DEFAULT_WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "guess_water_def2svp.npz")
