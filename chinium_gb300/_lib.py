@@ -32,6 +32,20 @@ class GridInfo(ctypes.Structure):
                 ("mixed_tiles", ctypes.c_int), ("mixed_pairs", ctypes.c_long)]
 
 
+class MixedConfig(ctypes.Structure):
+    _fields_ = [("screen", ctypes.c_double), ("fock_tiles", ctypes.c_int), ("spatial", ctypes.c_int)]
+
+
+class TuneCandidate(ctypes.Structure):
+    _fields_ = [("cfg", MixedConfig), ("ms", ctypes.c_double), ("max_de", ctypes.c_double),
+                ("max_dv", ctypes.c_double), ("kept_pairs", ctypes.c_long), ("accepted", ctypes.c_int)]
+
+
+class TuneReport(ctypes.Structure):
+    _fields_ = [("best", MixedConfig), ("ms_best", ctypes.c_double), ("ms_reference", ctypes.c_double),
+                ("ncand", ctypes.c_int), ("cand", TuneCandidate * 32)]
+
+
 _P = ctypes.c_void_p
 _I = ctypes.c_int
 _D = ctypes.c_double
@@ -86,6 +100,11 @@ SIGNATURES = {
     "xc_eri": [_P, _P, _D],
     "xc_grid_profile": [_P, _I],
     "xc_grid_stage_ms": [_P, _P],
+    "xc_grid_create_batch": [_I, _P, _S, _I, _PP],
+    "xc_grid_molecules": [_P, _P, _P, _P, _P],
+    "xc_grid_set_mixed_config": [_P, _P],
+    "xc_grid_get_mixed_config": [_P, _P],
+    "xc_grid_tune": [_P, _P, _P, _I, _D, _D, _I, _P],
 }
 
 _lib = None

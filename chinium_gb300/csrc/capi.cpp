@@ -1,5 +1,6 @@
 // C-ABI implementation: the Grid / ExchangeCorrelation objects and every
 // extern "C" entry point of include/chinium_xc.h.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <fstream>
@@ -203,6 +204,90 @@ void Grid::build(const BasisSet& bs, const std::string& grid_name, int ns, doubl
     CGB_CUDA(cudaStreamSynchronize(stream));
 }
 
+// Batch of molecules: each molecule's grid is generated (and Becke
+// partitioned) on its own; their real points become the molecule sources of
+// the mixed path, and their shells one combined basis in which every
+// molecule's functions start at a multiple of 64.
+void Grid::build_batch(const std::vector<BasisSet>& mols, const std::string& grid_name, int ns) {
+    CGB_CHECK(!mols.empty(), XC_ERR_ARG, "empty batch");
+    nspin = ns;
+    screen_thr = 0;
+    batched = true;
+    BasisSet comb;
+    sources.clear();
+    mol_n.clear();
+    npoints = 0;
+    int f0 = 0;
+    for (const BasisSet& b : mols) {
+        Grid g;
+        g.stream = stream;
+        g.build(b, grid_name, ns, 0.0);
+        std::vector<double> w(g.Gp);
+        CGB_CUDA(cudaMemcpyAsync(w.data(), g.d_w.p, g.Gp * sizeof(double), cudaMemcpyDeviceToHost, stream));
+        CGB_CUDA(cudaStreamSynchronize(stream));
+        MolSource S;
+        S.n = b.nbasis;
+        S.f0 = f0;
+        S.sh0 = (int)comb.shells.size();
+        const int atom0 = comb.natoms(), prim0 = (int)comb.exps.size();
+        comb.Z.insert(comb.Z.end(), b.Z.begin(), b.Z.end());
+        comb.xyz.insert(comb.xyz.end(), b.xyz.begin(), b.xyz.end());
+        comb.exps.insert(comb.exps.end(), b.exps.begin(), b.exps.end());
+        comb.coefs.insert(comb.coefs.end(), b.coefs.begin(), b.coefs.end());
+        for (Shell sh : b.shells) {
+            sh.atom += atom0;
+            sh.first += f0;
+            sh.prim_off += prim0;
+            comb.shells.push_back(sh);
+        }
+        S.sh1 = (int)comb.shells.size();
+        for (const BlockDesc& bd : g.blocks)
+            for (int k = 0; k < bd.nreal; k++) {
+                const long i = bd.pt_off + k;
+                S.x.push_back(g.hx[i]);
+                S.y.push_back(g.hy[i]);
+                S.z.push_back(g.hz[i]);
+                S.w.push_back(w[i]);
+            }
+        npoints += (long)S.x.size();
+        sources.push_back(std::move(S));
+        mol_n.push_back(b.nbasis);
+        f0 += (b.nbasis + 63) / 64 * 64;
+    }
+    comb.nbasis = f0;
+    basis = comb;
+    Gp = 0;
+    blocks.clear();
+    basis_lists.clear();
+    shell_lists.clear();
+    hx.clear();
+    hy.clear();
+    hz.clear();
+    ensure_device();
+    std::vector<int> st, sl, snp, spo, sf;
+    std::vector<double> sxyz;
+    for (auto& sh : basis.shells) {
+        st.push_back(sh.type);
+        sl.push_back(sh.l);
+        snp.push_back(sh.nprim);
+        spo.push_back(sh.prim_off);
+        sf.push_back(sh.first);
+        sxyz.push_back(sh.x);
+        sxyz.push_back(sh.y);
+        sxyz.push_back(sh.z);
+    }
+    d_sh_type.upload(st.data(), st.size(), stream);
+    d_sh_l.upload(sl.data(), sl.size(), stream);
+    d_sh_nprim.upload(snp.data(), snp.size(), stream);
+    d_sh_poff.upload(spo.data(), spo.size(), stream);
+    d_sh_first.upload(sf.data(), sf.size(), stream);
+    d_sh_xyz.upload(sxyz.data(), sxyz.size(), stream);
+    d_exps.upload(basis.exps.data(), basis.exps.size(), stream);
+    d_coefs.upload(basis.coefs.data(), basis.coefs.size(), stream);
+    d_atoms.upload(basis.xyz.data(), basis.xyz.size(), stream);
+    CGB_CUDA(cudaStreamSynchronize(stream));
+}
+
 DevShells Grid::dev_shells() const {
     DevShells s;
     s.nshell = (int)basis.shells.size();
@@ -219,6 +304,7 @@ DevShells Grid::dev_shells() const {
 
 void Grid::get_ao(int derivative) {
     CGB_CHECK(derivative >= 0, XC_ERR_ARG, "negative derivative order");
+    if (batched) return;  // the mixed path evaluates its own FP32 AO store at the first build
     const int order = type + derivative;
     CGB_CHECK(order <= 2, XC_ERR_UNSUPPORTED, "AO derivative order above 2 is not stored by this build");
     ncomp = order >= 1 ? 4 : 1;
@@ -248,9 +334,8 @@ void Grid::ensure_work() {
     d_fcoef.alloc(5 * nspin * Gp);
     d_partial.alloc((Gp + 127) / 128 + 1);
     d_scalar.alloc(2);
-    const size_t nn = (size_t)basis.nbasis * basis.nbasis * nspin;
-    d_D.alloc(nn);
-    d_V.alloc(nn);
+    d_D.alloc(packed_size());
+    d_V.alloc(packed_size());
 }
 
 void Grid::mark(int i) {
@@ -260,9 +345,12 @@ void Grid::mark(int i) {
 Grid::~Grid() {
     for (auto& e : ev)
         if (e) cudaEventDestroy(e);
+    mx.drop_graph();
+    if (capture_stream) cudaStreamDestroy(capture_stream);
 }
 
 void Grid::density_device(const double* dD) {
+    CGB_CHECK(!batched, XC_ERR_UNSUPPORTED, "batch grids run mixed-precision builds only");
     CGB_CHECK(ao_order >= type, XC_ERR_STATE, "getAO must run (for the current type) before getDensity");
     ensure_work();
     mark(0);
@@ -674,16 +762,32 @@ int xc_functional_eval_points(xc_functional* f, long n, const double* rho, const
     });
 }
 
+static void check_build(Grid& G, const xc_functional* f, int nspin, int precision) {
+    CGB_CHECK(nspin == G.nspin, XC_ERR_ARG, "Wrong number of spin types!");
+    CGB_CHECK(precision == XC_PRECISION_FP64 || precision == XC_PRECISION_MIXED, XC_ERR_ARG, "bad precision");
+    CGB_CHECK(f->f.nspin == G.nspin, XC_ERR_ARG, "functional and grid disagree on the number of spins");
+    CGB_CHECK(f->f.family <= G.type, XC_ERR_STATE, "grid type is below the functional family (setType/getAO)");
+    CGB_CHECK(precision == XC_PRECISION_MIXED || !G.batched, XC_ERR_UNSUPPORTED,
+              "batch grids run mixed-precision builds only");
+}
+
+static int num_mols(const Grid& G) { return G.batched ? (int)G.mol_n.size() : 1; }
+
 int xc_build_device(xc_grid* g, xc_functional* f, const double* dD, int nspin, int precision, double* dE, double* dV) {
     return guard([&] {
         CGB_CHECK(g && f && dD && dE && dV, XC_ERR_ARG, "null argument");
         Grid& G = g->g;
-        CGB_CHECK(nspin == G.nspin, XC_ERR_ARG, "Wrong number of spin types!");
-        CGB_CHECK(precision == XC_PRECISION_FP64 || precision == XC_PRECISION_MIXED, XC_ERR_ARG, "bad precision");
-        CGB_CHECK(f->f.nspin == G.nspin, XC_ERR_ARG, "functional and grid disagree on the number of spins");
-        CGB_CHECK(f->f.family <= G.type, XC_ERR_STATE, "grid type is below the functional family (setType/getAO)");
+        check_build(G, f, nspin, precision);
         if (precision == XC_PRECISION_MIXED) {
-            G.build_mixed(dD, f->f, dE, dV);
+            G.ensure_work();
+            const size_t nn = (size_t)G.packed_size();
+            if (dD != G.d_D.p)
+                CGB_CUDA(cudaMemcpyAsync(G.d_D.p, dD, nn * sizeof(double), cudaMemcpyDeviceToDevice, G.stream));
+            G.build_mixed_graph(f->f);
+            CGB_CUDA(cudaMemcpyAsync(dE, G.d_Emol.p, num_mols(G) * sizeof(double), cudaMemcpyDeviceToDevice,
+                                     G.stream));
+            if (dV != G.d_V.p)
+                CGB_CUDA(cudaMemcpyAsync(dV, G.d_V.p, nn * sizeof(double), cudaMemcpyDeviceToDevice, G.stream));
             return;
         }
         G.density_device(dD);
@@ -697,13 +801,20 @@ int xc_build(xc_grid* g, xc_functional* f, const double* D, int nspin, int preci
     return guard([&] {
         CGB_CHECK(g && f && D && E && V, XC_ERR_ARG, "null argument");
         Grid& G = g->g;
-        CGB_CHECK(nspin == G.nspin, XC_ERR_ARG, "Wrong number of spin types!");
+        check_build(G, f, nspin, precision);
         G.ensure_work();
-        const size_t nn = (size_t)G.basis.nbasis * G.basis.nbasis * nspin;
+        const size_t nn = (size_t)G.packed_size();
         CGB_CUDA(cudaMemcpyAsync(G.d_D.p, D, nn * sizeof(double), cudaMemcpyHostToDevice, G.stream));
-        const int st = xc_build_device(g, f, G.d_D.p, nspin, precision, G.d_scalar.p, G.d_V.p);
-        if (st) throw Error(st, g_last_error);
-        CGB_CUDA(cudaMemcpyAsync(E, G.d_scalar.p, sizeof(double), cudaMemcpyDeviceToHost, G.stream));
+        if (precision == XC_PRECISION_MIXED) {
+            G.build_mixed_graph(f->f);
+            CGB_CUDA(cudaMemcpyAsync(E, G.d_Emol.p, num_mols(G) * sizeof(double), cudaMemcpyDeviceToHost, G.stream));
+        } else {
+            G.density_device(G.d_D.p);
+            G.evaluate(f->f);
+            G.energy_device(G.d_scalar.p);
+            G.fock_device(G.d_V.p, f->f.family);
+            CGB_CUDA(cudaMemcpyAsync(E, G.d_scalar.p, sizeof(double), cudaMemcpyDeviceToHost, G.stream));
+        }
         CGB_CUDA(cudaMemcpyAsync(V, G.d_V.p, nn * sizeof(double), cudaMemcpyDeviceToHost, G.stream));
         CGB_CUDA(cudaStreamSynchronize(G.stream));
         if (precision == XC_PRECISION_MIXED && G.mixed_error())
@@ -751,6 +862,197 @@ int xc_build_incremental(xc_grid* g, xc_functional* f, const double* D, int nspi
         CGB_CUDA(cudaMemcpyAsync(V, G.d_V.p, nn * sizeof(double), cudaMemcpyDeviceToHost, G.stream));
         CGB_CUDA(cudaStreamSynchronize(G.stream));
         if (G.mixed_error()) throw Error(XC_ERR_TIMEOUT, "a bounded wait of the tensor-core pipeline gave up");
+    });
+}
+
+int xc_grid_create_batch(int nmol, const xc_basis* const* bases, const char* grid_name, int nspin, xc_grid** out) {
+    return guard([&] {
+        CGB_CHECK(nmol > 0 && bases && grid_name && out, XC_ERR_ARG, "bad batch arguments");
+        CGB_CHECK(nspin == 1 || nspin == 2, XC_ERR_ARG, "nspin must be 1 or 2");
+        std::vector<BasisSet> mols;
+        for (int i = 0; i < nmol; i++) {
+            CGB_CHECK(bases[i], XC_ERR_ARG, "null basis in batch");
+            mols.push_back(bases[i]->b);
+        }
+        auto* g = new xc_grid;
+        try {
+            g->g.build_batch(mols, grid_name, nspin);
+        } catch (...) {
+            delete g;
+            throw;
+        }
+        *out = g;
+    });
+}
+
+int xc_grid_molecules(const xc_grid* g, int* nmol, int* nbasis, long* npoints, long* offset) {
+    return guard([&] {
+        CGB_CHECK(g, XC_ERR_ARG, "null grid");
+        const Grid& G = g->g;
+        const int n = num_mols(G);
+        if (nmol) *nmol = n;
+        long off = 0;
+        for (int i = 0; i < n; i++) {
+            const int nb = G.batched ? G.mol_n[i] : G.basis.nbasis;
+            if (nbasis) nbasis[i] = nb;
+            if (npoints) npoints[i] = G.batched ? (long)G.sources[i].x.size() : G.npoints;
+            if (offset) offset[i] = off;
+            off += (long)G.nspin * nb * nb;
+        }
+    });
+}
+
+int xc_grid_set_mixed_config(xc_grid* g, const xc_mixed_config* cfg) {
+    return guard([&] {
+        CGB_CHECK(g && cfg, XC_ERR_ARG, "null argument");
+        CGB_CHECK(cfg->screen >= 0 && std::isfinite(cfg->screen) && cfg->fock_tiles >= 0 &&
+                      (cfg->spatial == 0 || cfg->spatial == 1),
+                  XC_ERR_ARG, "bad mixed configuration");
+        Grid& G = g->g;
+        MixedConfig c;
+        c.screen = cfg->screen;
+        c.fock_tiles = cfg->fock_tiles;
+        c.spatial = cfg->spatial;
+        G.mx.cfg = c;
+        G.mx.ready = false;
+        G.mx.have_ref = false;
+        G.mx.drop_graph();
+    });
+}
+
+int xc_grid_get_mixed_config(const xc_grid* g, xc_mixed_config* cfg) {
+    return guard([&] {
+        CGB_CHECK(g && cfg, XC_ERR_ARG, "null argument");
+        const MixedConfig& c = g->g.mx.cfg;
+        cfg->screen = c.screen;
+        cfg->fock_tiles = c.fock_tiles;
+        cfg->spatial = c.spatial;
+    });
+}
+
+// Autotuner of the mixed path: screening threshold first (accuracy-gated),
+// then the V work-item length, then the tile formation, each candidate built
+// from scratch (tiles, AO store, work lists) and timed by CUDA events around
+// graph replays.
+int xc_grid_tune(xc_grid* g, xc_functional* f, const double* D, int nspin, double e_tol, double v_tol, int reps,
+                 xc_tune_report* report) {
+    return guard([&] {
+        CGB_CHECK(g && f && D && e_tol > 0 && v_tol > 0, XC_ERR_ARG, "bad tune arguments");
+        Grid& G = g->g;
+        check_build(G, f, nspin, XC_PRECISION_MIXED);
+        CGB_CHECK(G.batched || G.ao_order >= G.type, XC_ERR_STATE, "getAO must run before tuning");
+        reps = std::max(1, std::min(reps, 50));
+        G.ensure_work();
+        const size_t nn = (size_t)G.packed_size();
+        const int nm = num_mols(G);
+        CGB_CUDA(cudaMemcpyAsync(G.d_D.p, D, nn * sizeof(double), cudaMemcpyHostToDevice, G.stream));
+        const bool prof = G.profiling;
+        G.profiling = false;
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        CGB_CUDA(cudaEventCreate(&e0));
+        CGB_CUDA(cudaEventCreate(&e1));
+        struct Run {
+            MixedConfig cfg;
+            double ms;
+            std::vector<double> E, V;
+            long pairs;
+        };
+        auto run = [&](const MixedConfig& c) {
+            Run r;
+            r.cfg = c;
+            G.prepare_mixed(c);
+            G.build_mixed_graph(f->f);  // capture + warm-up
+            CGB_CUDA(cudaStreamSynchronize(G.stream));
+            if (G.mixed_error()) throw Error(XC_ERR_TIMEOUT, "a bounded wait of the tensor-core pipeline gave up");
+            std::vector<double> t;
+            for (int i = 0; i < reps; i++) {
+                CGB_CUDA(cudaEventRecord(e0, G.stream));
+                G.build_mixed_graph(f->f);
+                CGB_CUDA(cudaEventRecord(e1, G.stream));
+                CGB_CUDA(cudaEventSynchronize(e1));
+                float ms = 0;
+                CGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                t.push_back(ms);
+            }
+            std::sort(t.begin(), t.end());
+            r.ms = t[t.size() / 2];
+            r.E.resize(nm);
+            r.V.resize(nn);
+            CGB_CUDA(cudaMemcpyAsync(r.E.data(), G.d_Emol.p, nm * sizeof(double), cudaMemcpyDeviceToHost, G.stream));
+            CGB_CUDA(cudaMemcpyAsync(r.V.data(), G.d_V.p, nn * sizeof(double), cudaMemcpyDeviceToHost, G.stream));
+            CGB_CUDA(cudaStreamSynchronize(G.stream));
+            r.pairs = G.mx.kept_pairs;
+            return r;
+        };
+        MixedConfig rc;
+        rc.screen = 1e-14;
+        rc.spatial = 1;
+        rc.fock_tiles = 0;
+        const Run ref = run(rc);
+        std::vector<xc_tune_candidate> cands;
+        auto judge = [&](const Run& r) {
+            xc_tune_candidate c{};
+            c.cfg.screen = r.cfg.screen;
+            c.cfg.fock_tiles = r.cfg.fock_tiles;
+            c.cfg.spatial = r.cfg.spatial;
+            c.ms = r.ms;
+            for (int i = 0; i < nm; i++) c.max_de = std::max(c.max_de, std::fabs(r.E[i] - ref.E[i]));
+            for (size_t i = 0; i < nn; i++) c.max_dv = std::max(c.max_dv, std::fabs(r.V[i] - ref.V[i]));
+            c.kept_pairs = r.pairs;
+            c.accepted = c.max_de <= e_tol && c.max_dv <= v_tol;
+            cands.push_back(c);
+            return c;
+        };
+        MixedConfig best = rc;
+        double best_ms = ref.ms;
+        auto consider = [&](const MixedConfig& c) {
+            const xc_tune_candidate k = judge(run(c));
+            if (k.accepted && k.ms < best_ms) {
+                best = c;
+                best_ms = k.ms;
+            }
+        };
+        for (double thr : {1e-8, 1e-9, 1e-10, 1e-11, 1e-12}) {
+            MixedConfig c = rc;
+            c.screen = thr;
+            consider(c);
+        }
+        // V work-item length around the SM-count default
+        {
+            long work = 0;
+            int nsm = 148, dev = 0;
+            CGB_CUDA(cudaGetDevice(&dev));
+            CGB_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+            G.prepare_mixed(best);
+            for (auto& R : G.mx.mols) work += (long)(R.t1 - R.t0) * R.nblk * R.nblk;
+            const long L = std::max(1L, (work + 6L * nsm - 1) / (6L * nsm));
+            const MixedConfig base = best;
+            for (long Lc : {L / 4, L / 2, 2 * L, 4 * L}) {
+                if (Lc < 1) continue;
+                MixedConfig c = base;
+                c.fock_tiles = (int)Lc;
+                consider(c);
+            }
+        }
+        {
+            MixedConfig c = best;
+            c.spatial = 0;
+            consider(c);
+        }
+        CGB_CUDA(cudaEventDestroy(e0));
+        CGB_CUDA(cudaEventDestroy(e1));
+        G.prepare_mixed(best);
+        G.profiling = prof;
+        if (report) {
+            std::memset(report, 0, sizeof(*report));
+            report->best.screen = best.screen;
+            report->best.fock_tiles = best.fock_tiles;
+            report->best.spatial = best.spatial;
+            report->ms_best = best_ms;
+            report->ms_reference = ref.ms;
+            report->ncand = (int)std::min<size_t>(cands.size(), 32);
+            for (int i = 0; i < report->ncand; i++) report->cand[i] = cands[i];
+        }
     });
 }
 

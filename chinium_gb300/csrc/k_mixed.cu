@@ -1,28 +1,35 @@
 // Mixed-precision XC contractions on the 5th-generation tensor cores.
 //
-// Points are re-tiled into tiles of 128 consecutive points (generation order,
-// spatially compact); each tile keeps the 64-function chunks of the basis
-// that its screening test marks significant, packed into "slots".  Operands
-// are three-term BF16 splits (x = h + m + l); a product sums the six
-// cross terms of order <= 2 (hh, hm, mh, hl, mm, lh) in FP32 on the tensor
-// core, ~FP32 accuracy.  The leading hh term and the five corrections go to
-// separate TMEM accumulators, and every accumulation unit (one K-chunk of the
-// density product, one point tile of the V_xc product) starts a fresh
-// accumulator that the epilogue warps drain into round-to-nearest FP32
-// registers: tensor-core accumulation chains stay a few instructions long.
-// Cross-unit sums of the final quantities are FP64.
+// Points are grouped into tiles of 128 (spatially compact, one molecule per
+// tile); each tile keeps the 64-function chunks of its molecule that the
+// screening test marks significant, packed into "slots".  The AO values and
+// gradients are stored once, in FP32, function-major (one 512-byte row of
+// 128 points per kept function).  TMA stages FP32 tiles of that store in
+// shared memory; converter warps split them into three-term BF16 planes
+// (x = h + m + l, exact for an FP32 x) written in the 128-byte-swizzled
+// K-major layout that tcgen05.mma reads (transposing on the way for the
+// density product).  A product sums the six cross terms of order <= 2 (hh,
+// hm, mh, hl, mm, lh) in FP32; hh and the five corrections go to separate
+// TMEM accumulators, and every accumulation unit starts fresh and is drained
+// by the epilogue warps into round-to-nearest FP32 registers.  Cross-unit
+// sums of the final quantities are FP64.
 //
-// HBM layouts (bf16, all rows 16-byte aligned, TMA 128-byte swizzle):
-//   PF  (point-major): row (c*3+p)*Gt + t*128 + g, col slot*64 + f      [c: phi, d/dx, d/dy, d/dz]
-//   FP  (function-major): row (c*3+p)*T*K + t*K + slot*64 + f, col g     (+64 zero rows)
-//   R   (function-major, per build): row (c*3+p)*T*K + t*K + slot*64 + f, col g (+64 zero rows)
-//   Dp  (density planes): row (s*3+p)*npad + nu, col mu
+// HBM layouts:
+//   e32 (FP32): component c (phi, d/dx, d/dy, d/dz), row c*rows + tile_row[t] + slot*64 + f, col g (128 points)
+//   Z   (FP32, per build): c0 phi + c1 . grad phi, same rows as e32 component 0
+//   Dp  (BF16 density planes): row (s*3+p)*drows + f0(mol) + nu, col mu
 //
-// CTA roles (192 threads): warp 0 issues TMA loads into a 2-stage ring,
-// warp 1 issues tcgen05.mma into one of two TMEM buffers (256 columns each:
-// hh | corrections), warps 2-5 drain TMEM (lane quadrant = warp % 4) and
-// run the epilogue.  Every wait is bounded (2 s of %globaltimer) and a
-// timeout sets XC_ERR_TIMEOUT in a global flag instead of hanging.
+// Both tensor-core kernels are persistent: one CTA per SM walks a host-made
+// list of work items (tiles, or (I, J, tile range) blocks of V) balanced by
+// cost.  CTA roles (512 threads): warp 0 issues every TMA load and owns
+// TMEM, warp 1 issues tcgen05.mma into one of two TMEM buffers (256 columns
+// each: hh | corrections), warps 4-11 drain TMEM (lane quadrant = warp % 4;
+// warps 4-7 columns 0-63, warps 8-11 columns 64-127) and run the epilogue,
+// warps 2-3 and 12-15 convert operands.  Shared memory
+// (224 KB): density = two operand stages + one raw FP32 tile; V_xc = one
+// operand stage + two raw FP32 stages.  Every wait is bounded (2 s of
+// %globaltimer); a timeout sets XC_ERR_TIMEOUT in a global flag and the CTA
+// unwinds instead of hanging.
 #include <cstdio>
 
 #include "common.h"
@@ -35,10 +42,19 @@ namespace {
 
 using bf16 = __nv_bfloat16;
 
-constexpr int kThreads = 192;
-constexpr int kStages = 2;
+constexpr int kThreads = 512;
+constexpr int kEpiWarp0 = 4;                   // epilogue warps 4-11 (two per TMEM lane quadrant)
+constexpr int kEpiThreads = 256;
+constexpr int kConvWarps = 6;                  // warps 2-3 and 12-15
+constexpr int kConvThreads = kConvWarps * 32;
 constexpr uint32_t kPlaneA = 128 * 64 * 2;     // bytes of one 128x64 bf16 operand plane
 constexpr uint32_t kStageBytes = 6 * kPlaneA;  // A (3 planes) + B (3 planes)
+constexpr uint32_t kRawD = 64 * 128 * 4;       // density raw tile: 64 functions x 128 points FP32
+constexpr uint32_t kRawBox = 64 * 32 * 4;      // V_xc raw box: 64 functions x 32 points FP32
+constexpr uint32_t kRawF = 4 * kRawBox;        // V_xc raw half-stage: L (2 boxes) + R (2 boxes)
+constexpr int kRawSlots = 4;                   // V_xc raw ring
+constexpr uint32_t kSmemBytes = 2 * kStageBytes + kRawD;  // = kStageBytes + kRawSlots * kRawF
+static_assert(2 * kStageBytes + kRawD == kStageBytes + kRawSlots * kRawF, "shared-memory plans differ");
 constexpr uint32_t kIdesc = tc::idesc_bf16(128, 128);
 constexpr uint32_t kTmemCols = 512;            // 2 buffers x (hh 128 | corrections 128)
 // cross terms (i, j) of the three-term splits with i + j <= 2; term 0 is hh
@@ -46,15 +62,20 @@ __constant__ int c_prod_a[6] = {0, 0, 1, 0, 1, 2};
 __constant__ int c_prod_b[6] = {0, 1, 0, 2, 1, 0};
 
 struct Smem {
-    uint64_t full[kStages];
-    uint64_t empty[kStages];
+    uint64_t full[2];
+    uint64_t empty[2];
+    uint64_t rfull[4];
+    uint64_t rempty[4];
     uint64_t tfull[2];
     uint64_t tempty[2];
     uint32_t tmem;
     int abort;
 };
 
-__device__ __forceinline__ uint8_t* stage_base(uint8_t* aligned, int s) { return aligned + (size_t)s * kStageBytes; }
+__device__ __forceinline__ int conv_index() {
+    const int w = threadIdx.x >> 5;
+    return w < kEpiWarp0 ? w - 2 : w - 10;  // warps 2, 3 -> 0, 1; warps 12..15 -> 2..5
+}
 
 __device__ __forceinline__ void flag_timeout(int* err, Smem* sm) {
     atomicExch(err, XC_ERR_TIMEOUT);
@@ -65,15 +86,17 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_u32(bar)) : "memory");
 }
 
-__device__ void init_cta(Smem& sm) {
+__device__ void init_cta(Smem& sm, uint32_t full_count, uint32_t rempty_count) {
     if (threadIdx.x == 0) {
-        for (int s = 0; s < kStages; s++) {
-            tc::mbar_init(&sm.full[s], 1);
+        for (int s = 0; s < 2; s++) {
+            tc::mbar_init(&sm.full[s], full_count);
             tc::mbar_init(&sm.empty[s], 1);
+            tc::mbar_init(&sm.tfull[s], 1);
+            tc::mbar_init(&sm.tempty[s], kEpiThreads);
         }
-        for (int b = 0; b < 2; b++) {
-            tc::mbar_init(&sm.tfull[b], 1);
-            tc::mbar_init(&sm.tempty[b], 128);
+        for (int s = 0; s < 4; s++) {
+            tc::mbar_init(&sm.rfull[s], 1);
+            tc::mbar_init(&sm.rempty[s], rempty_count);
         }
         sm.abort = 0;
         tc::fence_mbar_init();
@@ -82,6 +105,62 @@ __device__ void init_cta(Smem& sm) {
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
+}
+
+// A converter warp waits (lane 0, bounded) for a barrier phase; all lanes
+// learn the outcome.
+__device__ __forceinline__ bool warp_wait(Smem& sm, uint64_t* bar, uint32_t parity, int* err) {
+    int ok = 1;
+    if ((threadIdx.x & 31) == 0) {
+        ok = !sm.abort && tc::mbar_wait(bar, parity);
+        if (!ok) flag_timeout(err, &sm);
+    }
+    return __shfl_sync(0xffffffffu, ok, 0) != 0;
+}
+
+// One arrival per warp once every lane is done.
+__device__ __forceinline__ void warp_arrive(uint64_t* bar) {
+    __syncwarp();
+    if ((threadIdx.x & 31) == 0) mbar_arrive(bar);
+}
+
+// The converted planes of this warp are complete: make them visible to the
+// tensor core (async proxy) and arrive once per warp on the stage.
+__device__ __forceinline__ void conv_publish(uint64_t* full) {
+    tc::fence_proxy_async();
+    warp_arrive(full);
+}
+
+// Three-term split of 8 consecutive K-elements into one 16-byte chunk per plane.
+__device__ __forceinline__ void split8(const float* v, uint4& h, uint4& m, uint4& l) {
+    uint32_t hh[4], mm[4], ll[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const float a = v[2 * k], b = v[2 * k + 1];
+        const __nv_bfloat162 H = __floats2bfloat162_rn(a, b);
+        const float2 Hf = __bfloat1622float2(H);
+        const float ra = a - Hf.x, rb = b - Hf.y;
+        const __nv_bfloat162 Mv = __floats2bfloat162_rn(ra, rb);
+        const float2 Mf = __bfloat1622float2(Mv);
+        const __nv_bfloat162 Lv = __floats2bfloat162_rn(ra - Mf.x, rb - Mf.y);
+        hh[k] = *reinterpret_cast<const uint32_t*>(&H);
+        mm[k] = *reinterpret_cast<const uint32_t*>(&Mv);
+        ll[k] = *reinterpret_cast<const uint32_t*>(&Lv);
+    }
+    h = make_uint4(hh[0], hh[1], hh[2], hh[3]);
+    m = make_uint4(mm[0], mm[1], mm[2], mm[3]);
+    l = make_uint4(ll[0], ll[1], ll[2], ll[3]);
+}
+
+// Store chunk j (8 K-elements) of row r of an operand (three planes from
+// `planes`) in the 128-byte-swizzled K-major layout.
+__device__ __forceinline__ void store_chunk(uint32_t planes, int r, int j, const float* v) {
+    uint4 h, m, l;
+    split8(v, h, m, l);
+    const uint32_t off = (uint32_t)r * 128u + ((uint32_t)(j ^ (r & 7)) << 4);
+    tc::sts128(planes + off, h);
+    tc::sts128(planes + kPlaneA + off, m);
+    tc::sts128(planes + 2 * kPlaneA + off, l);
 }
 
 // The six split products of one stage into TMEM buffer `buf`: term hh into
@@ -103,14 +182,14 @@ __device__ __forceinline__ void mma_stage(uint32_t tmem, int buf, uint8_t* st, b
     }
 }
 
-// Drain TMEM buffer `buf` (hh + corrections) into acc[128] (this thread's lane).
-__device__ __forceinline__ void drain(uint32_t tmem, int buf, int quad, float* acc) {
-    const uint32_t base = tmem + ((uint32_t)(quad * 32) << 16) + buf * 256;
+// Drain columns half*64 .. half*64 + 63 of TMEM buffer `buf` (hh +
+// corrections) into acc[64] (this thread's lane).
+__device__ __forceinline__ void drain(uint32_t tmem, int buf, int quad, int half, float* acc) {
+    const uint32_t base = tmem + ((uint32_t)(quad * 32) << 16) + buf * 256 + half * 64;
 #pragma unroll
-    for (int c16 = 0; c16 < 8; c16++) {
+    for (int c16 = 0; c16 < 4; c16++) {
         float a[16], b[16];
-        tc::tmem_ld16(base + c16 * 16, a);
-        tc::tmem_ld16(base + 128 + c16 * 16, b);
+        tc::tmem_ld16x2_nomem(base + c16 * 16, base + 128 + c16 * 16, a, b);
 #pragma unroll
         for (int j = 0; j < 16; j++) acc[c16 * 16 + j] += a[j] + b[j];
     }
@@ -118,111 +197,161 @@ __device__ __forceinline__ void drain(uint32_t tmem, int buf, int quad, float* a
 
 // ------------------------------------------------------------ density
 // T = Phi D for one tile, unit = (nu block vb of two slots, mu chunk kc).
+// Every unit starts fresh TMEM accumulators (hh | corrections); the
+// epilogue warps drain each unit into round-to-nearest FP32 registers (T,
+// 64 columns per thread) and, at the end of a nu block, contract T with the
+// AO values of their slot.  The two column halves of a row write separate
+// partial outputs (rho / rho_b ...), summed by combine_kernel.
 // EPI 0: rho; 1: rho + grad rho; 2: tau contribution of A component acomp.
+
+// Position in the density unit sequence of one CTA (host-made job list).
+struct DensCursor {
+    int j, end, vb, kc;
+    DensJob job;
+    __device__ void load(const DensJob* jobs) {
+        const int4 r = __ldg(reinterpret_cast<const int4*>(jobs) + j);
+        job.t = r.x;
+        job.nk = r.y;
+        job.trow = r.z;
+        job.c0 = r.w;
+    }
+    __device__ DensCursor(const int* off, const DensJob* jobs) {
+        j = off[blockIdx.x];
+        end = off[blockIdx.x + 1];
+        vb = kc = 0;
+        job = DensJob{0, 1, 0, 0};
+        if (j < end) load(jobs);
+    }
+    __device__ bool valid() const { return j < end; }
+    __device__ int nvb() const { return (job.nk + 1) / 2; }
+    __device__ void advance(const DensJob* jobs) {
+        if (++kc < job.nk) return;
+        kc = 0;
+        if (++vb < nvb()) return;
+        vb = 0;
+        if (++j < end) load(jobs);
+    }
+};
+
+constexpr int kDensItems = (1024 + kConvThreads - 1) / kConvThreads;  // (point, 8-function chunk) items
+constexpr int kMaxChunks = 256;                                       // chunks of one molecule (n <= 16384)
+
+struct DensOut {
+    double *rho, *rho1, *tau;  // column half 0
+    double *rho_b, *rho1_b, *tau_b;  // column half 1
+};
+
 template <int EPI>
-__global__ void __launch_bounds__(kThreads, 1) density_tc_kernel(const __grid_constant__ CUtensorMap tm_pf,
-                                                                 const __grid_constant__ CUtensorMap tm_d,
-                                                                 MixedDev md, int acomp, int spin,
-                                                                 double* __restrict__ rho, double* __restrict__ rho1,
-                                                                 double* __restrict__ tau, long Gp, int* err) {
+__global__ void __launch_bounds__(kThreads, 1) density_tc_kernel(const __grid_constant__ CUtensorMap tm_d,
+                                                                 const __grid_constant__ CUtensorMap tm_raw, MixedDev md,
+                                                                 const int* __restrict__ job_off,
+                                                                 const DensJob* __restrict__ jobs, int acomp, int spin,
+                                                                 DensOut out, int* err) {
     extern __shared__ uint8_t smem_raw[];
     __shared__ Smem sm;
-    uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    const int t = blockIdx.x;
+    __shared__ int s_chunks[kMaxChunks];
+    uint8_t* smem = smem_raw + (((tc::smem_u32(smem_raw) + 1023u) & ~1023u) - tc::smem_u32(smem_raw));
+    const uint32_t ssm = tc::smem_u32(smem);
+    uint8_t* raw = smem + 2 * kStageBytes;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int nkept = md.tile_nkept[t];
-    const int* chunks = md.tile_chunks + (size_t)t * md.nchunk;
-    const int nvb = (nkept + 1) / 2;
-    const int nunits = nvb * nkept;
-    init_cta(sm);
+    init_cta(sm, 1 + kConvWarps, kConvWarps);
     const uint32_t tmem = sm.tmem;
+    const long Gt = md.Gt;
 
     if (warp == 0) {
         if (lane == 0) {
-            for (int u = 0; u < nunits; u++) {
-                const int vb = u / nkept, kc = u % nkept;
-                const int s = u % kStages;
-                const uint32_t ph = (u / kStages) & 1;
-                if (sm.abort || !tc::mbar_wait(&sm.empty[s], ph ^ 1)) {
+            uint32_t uu = 0;
+            for (DensCursor c(job_off, jobs); c.valid(); c.advance(jobs), uu++) {
+                if (c.vb == 0 && c.kc == 0) {  // new tile: its kept chunk ids
+                    const int* src = md.tile_chunks + (size_t)c.job.t * md.nchunk;
+                    for (int k = 0; k < c.job.nk; k++) s_chunks[k] = __ldg(src + k);
+                }
+                // raw Phi tile (one buffer)
+                if (sm.abort || !tc::mbar_wait(&sm.rempty[0], (uu & 1) ^ 1)) {
                     flag_timeout(err, &sm);
                     break;
                 }
-                uint8_t* st = stage_base(smem, s);
-                tc::mbar_arrive_expect_tx(&sm.full[s], kStageBytes);
-                for (int p = 0; p < 3; p++)
-                    tc::tma_load_2d(st + p * kPlaneA, &tm_pf, kc * 64, (int)((acomp * 3 + p) * md.Gt + (long)t * 128),
-                                    &sm.full[s]);
-                const int gmu = chunks[kc];
+                tc::mbar_arrive_expect_tx(&sm.rfull[0], kRawD);
+                tc::tma_load_2d(raw, &tm_raw, 0, (int)((long)acomp * md.rows + c.job.trow + (long)c.kc * 64),
+                                &sm.rfull[0]);
+                // density planes into the stage
+                const int s = uu & 1;
+                if (sm.abort || !tc::mbar_wait(&sm.empty[s], ((uu >> 1) & 1) ^ 1)) {
+                    flag_timeout(err, &sm);
+                    break;
+                }
+                uint8_t* st = smem + (size_t)s * kStageBytes;
+                tc::mbar_arrive_expect_tx(&sm.full[s], 3 * kPlaneA);
+                const int gmu = s_chunks[c.kc];
                 for (int p = 0; p < 3; p++)
                     for (int h = 0; h < 2; h++) {
-                        const int vs = 2 * vb + h < nkept ? 2 * vb + h : nkept - 1;
+                        const int vs = 2 * c.vb + h < c.job.nk ? 2 * c.vb + h : c.job.nk - 1;
                         tc::tma_load_2d(st + (3 + p) * kPlaneA + h * (kPlaneA / 2), &tm_d, gmu * 64,
-                                        (spin * 3 + p) * md.npad + chunks[vs] * 64, &sm.full[s]);
+                                        (int)((spin * 3 + p) * md.drows + (long)(c.job.c0 + s_chunks[vs]) * 64),
+                                        &sm.full[s]);
                     }
             }
         }
     } else if (warp == 1) {
         if (lane == 0) {
-            for (int u = 0; u < nunits; u++) {
-                const int s = u % kStages, b = u & 1;
-                const uint32_t ph = (u / kStages) & 1, bph = (u >> 1) & 1;
-                if (sm.abort || !tc::mbar_wait(&sm.tempty[b], bph ^ 1) || !tc::mbar_wait(&sm.full[s], ph)) {
+            uint32_t uu = 0;
+            for (DensCursor c(job_off, jobs); c.valid(); c.advance(jobs), uu++) {
+                const int s = uu & 1, b = uu & 1;
+                const uint32_t ph = (uu >> 1) & 1;
+                if (sm.abort || !tc::mbar_wait(&sm.tempty[b], ph ^ 1) || !tc::mbar_wait(&sm.full[s], ph)) {
                     flag_timeout(err, &sm);
                     tc::mma_commit(&sm.tfull[b]);  // release the epilogue
                     break;
                 }
                 tc::fence_after_sync();
-                mma_stage(tmem, b, stage_base(smem, s), true);
+                mma_stage(tmem, b, smem + (size_t)s * kStageBytes, true);
                 tc::mma_commit(&sm.empty[s]);
                 tc::mma_commit(&sm.tfull[b]);
             }
         }
-    } else {
-        // epilogue warps: row g of the tile
-        const int quad = warp & 3;
+    } else if (warp >= kEpiWarp0 && warp < kEpiWarp0 + 8) {
+        // epilogue warps: row g of the tile, columns of slot 2 vb + half
+        const int quad = warp & 3, half = (warp - kEpiWarp0) >> 2;
         const int g = quad * 32 + lane;
-        const long pt = (long)t * 128 + g;
-        const bool live = pt < Gp;
-        const size_t cs = (size_t)md.ntiles * md.kmax * 128;  // component stride of the FP32 store
-        double acc_r = 0, acc_g0 = 0, acc_g1 = 0, acc_g2 = 0, acc_t = 0;
-        float T[128];
+        const size_t cs = (size_t)md.rows * 128;  // component stride of the FP32 store
+        double* rho = half ? out.rho_b : out.rho;
+        double* rho1 = half ? out.rho1_b : out.rho1;
+        double* tau = half ? out.tau_b : out.tau;
+        float T[64];
 #pragma unroll
-        for (int j = 0; j < 128; j++) T[j] = 0.f;
-        for (int u = 0; u < nunits; u++) {
-            const int vb = u / nkept, kc = u % nkept, b = u & 1;
-            const uint32_t bph = (u >> 1) & 1;
+        for (int j = 0; j < 64; j++) T[j] = 0.f;
+        double acc_r = 0, acc_g0 = 0, acc_g1 = 0, acc_g2 = 0, acc_t = 0;
+        uint32_t uu = 0;
+        for (DensCursor c(job_off, jobs); c.valid(); c.advance(jobs), uu++) {
+            const int b = uu & 1;
             if (sm.abort) break;
-            if (!tc::mbar_wait(&sm.tfull[b], bph)) {
+            if (!tc::mbar_wait(&sm.tfull[b], (uu >> 1) & 1)) {
                 flag_timeout(err, &sm);
                 break;
             }
             tc::fence_after_sync();
-            drain(tmem, b, quad, T);
+            drain(tmem, b, quad, half, T);
             tc::fence_before_sync();
             mbar_arrive(&sm.tempty[b]);
-            if (kc != nkept - 1) continue;
-            // nu block complete: contract T with this row's AO values, read
-            // from the function-major FP32 store (a warp reads 32 consecutive
-            // points of one function: one 128-byte line per load)
-            if (live && !sm.abort) {
+            if (c.kc != c.job.nk - 1) continue;
+            // nu block complete: contract T with this row's AO values of the
+            // slot (a warp reads 32 consecutive points of one function: one
+            // 128-byte line per load)
+            const int slot = 2 * c.vb + half;
+            if (slot < c.job.nk && !sm.abort) {
                 float pr = 0, pg0 = 0, pg1 = 0, pg2 = 0, pt_ = 0;
+                const float* e0 = md.e32 + ((size_t)c.job.trow + slot * 64) * 128 + g;
 #pragma unroll
-                for (int h = 0; h < 2; h++) {
-                    const int slot = 2 * vb + h;
-                    if (slot >= nkept) break;
-                    const float* e0 = md.e32 + ((size_t)t * md.kmax + slot * 64) * 128 + g;
-#pragma unroll
-                    for (int j = 0; j < 64; j++) {
-                        const float tv = T[h * 64 + j];
-                        const size_t o = (size_t)j * 128;
-                        if (EPI <= 1) pr = fmaf(tv, __ldg(e0 + o), pr);
-                        if (EPI == 1) {
-                            pg0 = fmaf(tv, __ldg(e0 + cs + o), pg0);
-                            pg1 = fmaf(tv, __ldg(e0 + 2 * cs + o), pg1);
-                            pg2 = fmaf(tv, __ldg(e0 + 3 * cs + o), pg2);
-                        }
-                        if (EPI == 2) pt_ = fmaf(tv, __ldg(e0 + (size_t)acomp * cs + o), pt_);
+                for (int j = 0; j < 64; j++) {
+                    const float tv = T[j];
+                    const size_t o = (size_t)j * 128;
+                    if (EPI <= 1) pr = fmaf(tv, __ldg(e0 + o), pr);
+                    if (EPI == 1) {
+                        pg0 = fmaf(tv, __ldg(e0 + cs + o), pg0);
+                        pg1 = fmaf(tv, __ldg(e0 + 2 * cs + o), pg1);
+                        pg2 = fmaf(tv, __ldg(e0 + 3 * cs + o), pg2);
                     }
+                    if (EPI == 2) pt_ = fmaf(tv, __ldg(e0 + (size_t)acomp * cs + o), pt_);
                 }
                 acc_r += pr;
                 acc_g0 += 2.0 * pg0;
@@ -231,16 +360,48 @@ __global__ void __launch_bounds__(kThreads, 1) density_tc_kernel(const __grid_co
                 acc_t += 0.5 * pt_;
             }
 #pragma unroll
-            for (int j = 0; j < 128; j++) T[j] = 0.f;
-        }
-        if (live) {
-            if (EPI <= 1) rho[(long)spin * Gp + pt] = acc_r;
-            if (EPI == 1) {
-                rho1[((long)spin * 3 + 0) * Gp + pt] = acc_g0;
-                rho1[((long)spin * 3 + 1) * Gp + pt] = acc_g1;
-                rho1[((long)spin * 3 + 2) * Gp + pt] = acc_g2;
+            for (int j = 0; j < 64; j++) T[j] = 0.f;
+            if (c.vb == c.nvb() - 1) {  // tile complete
+                const long pt = (long)c.job.t * 128 + g;
+                if (EPI <= 1) rho[(long)spin * Gt + pt] = acc_r;
+                if (EPI == 1) {
+                    rho1[((long)spin * 3 + 0) * Gt + pt] = acc_g0;
+                    rho1[((long)spin * 3 + 1) * Gt + pt] = acc_g1;
+                    rho1[((long)spin * 3 + 2) * Gt + pt] = acc_g2;
+                }
+                if (EPI == 2) tau[(long)spin * Gt + pt] += acc_t;
+                acc_r = acc_g0 = acc_g1 = acc_g2 = acc_t = 0;
             }
-            if (EPI == 2) tau[(long)spin * Gp + pt] += acc_t;
+        }
+    } else if (warp >= 2) {
+        // converter warps: the raw Phi tile [64 functions][128 points] is read
+        // into registers (releasing the buffer for the next TMA load), split
+        // and stored transposed (point-major) as the stage's A planes
+        const int ct = conv_index() * 32 + lane;
+        uint32_t uu = 0;
+        for (DensCursor c(job_off, jobs); c.valid(); c.advance(jobs), uu++) {
+            if (!warp_wait(sm, &sm.rfull[0], uu & 1, err)) break;
+            float v[kDensItems][8];
+            const uint32_t rf = ssm + 2 * kStageBytes;
+#pragma unroll
+            for (int k = 0; k < kDensItems; k++) {
+                const int q = ct + kConvThreads * k;
+                if (q < 1024) {
+                    const int gg = q & 127, jj = q >> 7;
+#pragma unroll
+                    for (int i = 0; i < 8; i++) v[k][i] = tc::lds32f(rf + ((8 * jj + i) * 128 + gg) * 4);
+                }
+            }
+            warp_arrive(&sm.rempty[0]);
+            const int s = uu & 1;
+            if (!warp_wait(sm, &sm.empty[s], ((uu >> 1) & 1) ^ 1, err)) break;
+            const uint32_t st = ssm + s * kStageBytes;
+#pragma unroll
+            for (int k = 0; k < kDensItems; k++) {
+                const int q = ct + kConvThreads * k;
+                if (q < 1024) store_chunk(st, q & 127, q >> 7, v[k]);
+            }
+            conv_publish(&sm.full[s]);
         }
     }
     tc::fence_before_sync();
@@ -249,126 +410,241 @@ __global__ void __launch_bounds__(kThreads, 1) density_tc_kernel(const __grid_co
 }
 
 // ------------------------------------------------------------- V_xc
-// One CTA per (128 x 128 block (I, J) of W, split of tiles):
-//   W_IJ = sum_t sum_c L_c,t[I]^T R_c,t[J]   (unit = one point tile, K = 128 points per component)
-__global__ void __launch_bounds__(kThreads, 1) fock_tc_kernel(const __grid_constant__ CUtensorMap tm_fp,
-                                                              const __grid_constant__ CUtensorMap tm_r, MixedDev md,
-                                                              int ncomp, int r_rows, int nblk, int nsplit,
+// Job (tile t of item I, J):  W_IJ += sum_c L_c,t[I]^T R_c,t[J]
+// with L = Phi component c and R = Z (c = 0) or c2 d_c Phi (c = 1..3).
+// The operand stage is split along K into two halves (32 points each) that
+// act as a two-slot ring: the tensor core runs on one half while the
+// converters fill the other (the swizzled rows keep the halves' 16-byte
+// chunks disjoint).  A half-stage is (component c, point half kh, K-half
+// hk); a tile is one accumulation unit; an item's last tile writes W_IJ.
+// Warps 2-15 convert; warps 4-11 also drain the accumulator of each tile.
+
+// Position in the half-stage sequence of one CTA (host-made job list).
+struct FockCursor {
+    int j, end, c, kh, hk, ncomp;
+    FockJob job;
+    __device__ void load(const FockJob* jobs) {
+        const int4* p = reinterpret_cast<const int4*>(jobs + j);
+        const int4 a = __ldg(p), b = __ldg(p + 1);
+        job.t = a.x;
+        job.trow = a.y;
+        job.sa0 = a.z;
+        job.sa1 = a.w;
+        job.sb0 = b.x;
+        job.sb1 = b.y;
+        job.item = b.z;
+        job.flags = b.w;
+    }
+    __device__ FockCursor(const int* off, const FockJob* jobs, int nc) {
+        j = off[blockIdx.x];
+        end = off[blockIdx.x + 1];
+        ncomp = nc;
+        c = kh = hk = 0;
+        if (j < end) load(jobs);
+    }
+    __device__ bool valid() const { return j < end; }
+    __device__ bool first_of_tile() const { return c == 0 && kh == 0 && hk == 0; }
+    __device__ bool last_of_tile() const { return c == ncomp - 1 && kh == 1 && hk == 1; }
+    __device__ void advance(const FockJob* jobs) {
+        if (++hk < 2) return;
+        hk = 0;
+        if (++kh < 2) return;
+        kh = 0;
+        if (++c < ncomp) return;
+        c = 0;
+        if (++j < end) load(jobs);
+    }
+    __device__ int slot(int box) const {
+        return box == 0 ? job.sa0 : box == 1 ? job.sa1 : box == 2 ? job.sb0 : job.sb1;
+    }
+};
+
+constexpr int kFockConvWarps = 14;                     // warps 2-15
+constexpr int kFockConvThreads = kFockConvWarps * 32;
+constexpr int kFockItems = (1024 + kFockConvThreads - 1) / kFockConvThreads;  // (row, 8-point chunk) items
+
+// The six split products of K-half hk (k-steps 2 hk, 2 hk + 1) of the stage.
+__device__ __forceinline__ void mma_half(uint32_t tmem, int buf, uint8_t* st, int hk, bool first) {
+    const uint32_t a0 = tc::smem_u32(st), b0 = a0 + 3 * kPlaneA;
+    const uint32_t d_hh = tmem + buf * 256, d_corr = tmem + buf * 256 + 128;
+#pragma unroll
+    for (int q = 0; q < 6; q++) {
+        const uint64_t ad = tc::smem_desc_sw128(a0 + c_prod_a[q] * kPlaneA);
+        const uint64_t bd = tc::smem_desc_sw128(b0 + c_prod_b[q] * kPlaneA);
+        const uint32_t d = q == 0 ? d_hh : d_corr;
+#pragma unroll
+        for (int kk = 0; kk < 2; kk++) {
+            const int k = 2 * hk + kk;
+            const bool start = first && kk == 0 && (q == 0 || q == 1);
+            tc::mma_bf16(d, ad + 2 * k, bd + 2 * k, kIdesc, start ? 0u : 1u);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kThreads, 1) fock_tc_kernel(const __grid_constant__ CUtensorMap tm_e32,
+                                                              const __grid_constant__ CUtensorMap tm_z, long rows,
+                                                              const int* __restrict__ job_off,
+                                                              const FockJob* __restrict__ jobs,
+                                                              const float* __restrict__ c2, int ncomp,
                                                               double* __restrict__ wpart, int* err) {
     extern __shared__ uint8_t smem_raw[];
     __shared__ Smem sm;
-    uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    const int I = blockIdx.x / nblk, J = blockIdx.x % nblk;
-    const int split = blockIdx.y;
+    uint8_t* smem = smem_raw + (((tc::smem_u32(smem_raw) + 1023u) & ~1023u) - tc::smem_u32(smem_raw));
+    const uint32_t ssm = tc::smem_u32(smem);
+    uint8_t* raws = smem + kStageBytes;  // kRawSlots raw half-stages of kRawF bytes
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int t0 = (int)((long)md.ntiles * split / nsplit), t1 = (int)((long)md.ntiles * (split + 1) / nsplit);
-    const long TK = (long)md.ntiles * md.kmax;
-    const int zero_row = (int)(12 * TK);  // 64 zero rows after the FP planes
-    const int zero_row_r = r_rows;        // 64 zero rows after the R planes
-    init_cta(sm);
+    init_cta(sm, kFockConvWarps, kFockConvWarps);
     const uint32_t tmem = sm.tmem;
-
-    auto slot_of = [&](int t, int chunk) -> int {
-        return chunk < md.nchunk ? md.tile_slot[(size_t)t * md.nchunk + chunk] : -1;
-    };
-    auto wanted = [&](int t) {
-        return (slot_of(t, 2 * I) >= 0 || slot_of(t, 2 * I + 1) >= 0) &&
-               (slot_of(t, 2 * J) >= 0 || slot_of(t, 2 * J + 1) >= 0);
-    };
 
     if (warp == 0) {
         if (lane == 0) {
-            uint32_t i2 = 0;
-            for (int t = t0; t < t1 && !sm.abort; t++) {
-                if (!wanted(t)) continue;
-                const int sa0 = slot_of(t, 2 * I), sa1 = slot_of(t, 2 * I + 1);
-                const int sb0 = slot_of(t, 2 * J), sb1 = slot_of(t, 2 * J + 1);
-                for (int c = 0; c < ncomp && !sm.abort; c++)
-                    for (int kh = 0; kh < 2; kh++, i2++) {
-                        const int s = i2 % kStages;
-                        const uint32_t ph = (i2 / kStages) & 1;
-                        if (sm.abort || !tc::mbar_wait(&sm.empty[s], ph ^ 1)) {
-                            flag_timeout(err, &sm);
-                            break;
-                        }
-                        uint8_t* st = stage_base(smem, s);
-                        tc::mbar_arrive_expect_tx(&sm.full[s], kStageBytes);
-                        for (int p = 0; p < 3; p++)
-                            for (int h = 0; h < 2; h++) {
-                                const int sa = h ? sa1 : sa0, sb = h ? sb1 : sb0;
-                                const long rbase = (long)(c * 3 + p) * TK + (long)t * md.kmax;
-                                const int ra = sa >= 0 ? (int)(rbase + sa * 64) : zero_row;
-                                const int rb = sb >= 0 ? (int)(rbase + sb * 64) : zero_row_r;
-                                tc::tma_load_2d(st + p * kPlaneA + h * (kPlaneA / 2), &tm_fp, kh * 64, ra, &sm.full[s]);
-                                tc::tma_load_2d(st + (3 + p) * kPlaneA + h * (kPlaneA / 2), &tm_r, kh * 64, rb,
-                                                &sm.full[s]);
-                            }
-                    }
+            uint32_t hs = 0;
+            for (FockCursor c(job_off, jobs, ncomp); c.valid(); c.advance(jobs), hs++) {
+                const int r = hs % kRawSlots;
+                if (sm.abort || !tc::mbar_wait(&sm.rempty[r], ((hs / kRawSlots) & 1) ^ 1)) {
+                    flag_timeout(err, &sm);
+                    break;
+                }
+                uint32_t bytes = 0;
+                for (int k = 0; k < 4; k++) bytes += c.slot(k) >= 0 ? kRawBox : 0;
+                tc::mbar_arrive_expect_tx(&sm.rfull[r], bytes);
+                uint8_t* rb = raws + (size_t)r * kRawF;
+                const int x = c.kh * 64 + c.hk * 32;
+                for (int k = 0; k < 4; k++) {
+                    const int sl = c.slot(k);
+                    if (sl < 0) continue;
+                    const long row = (long)c.job.trow + (long)sl * 64;
+                    if (k >= 2 && c.c == 0)
+                        tc::tma_load_2d(rb + k * kRawBox, &tm_z, x, (int)row, &sm.rfull[r]);
+                    else
+                        tc::tma_load_2d(rb + k * kRawBox, &tm_e32, x, (int)((long)c.c * rows + row), &sm.rfull[r]);
+                }
             }
         }
     } else if (warp == 1) {
         if (lane == 0) {
-            uint32_t i2 = 0, u = 0;
-            for (int t = t0; t < t1 && !sm.abort; t++) {
-                if (!wanted(t)) continue;
-                const int b = u & 1;
-                const uint32_t bph = (u >> 1) & 1;
-                if (!tc::mbar_wait(&sm.tempty[b], bph ^ 1)) {
+            uint32_t hs = 0, ut = 0;
+            for (FockCursor c(job_off, jobs, ncomp); c.valid(); c.advance(jobs), hs++) {
+                const int b = ut & 1, h = c.hk;
+                if (c.first_of_tile() && (sm.abort || !tc::mbar_wait(&sm.tempty[b], ((ut >> 1) & 1) ^ 1))) {
                     flag_timeout(err, &sm);
                     tc::mma_commit(&sm.tfull[b]);
                     break;
                 }
-                bool first = true;
-                for (int c = 0; c < ncomp; c++)
-                    for (int kh = 0; kh < 2; kh++, i2++) {
-                        const int s = i2 % kStages;
-                        const uint32_t ph = (i2 / kStages) & 1;
-                        if (sm.abort || !tc::mbar_wait(&sm.full[s], ph)) {
-                            flag_timeout(err, &sm);
-                            break;
-                        }
-                        tc::fence_after_sync();
-                        mma_stage(tmem, b, stage_base(smem, s), first);
-                        first = false;
-                        tc::mma_commit(&sm.empty[s]);
-                    }
-                tc::mma_commit(&sm.tfull[b]);
-                u++;
+                if (sm.abort || !tc::mbar_wait(&sm.full[h], (hs >> 1) & 1)) {
+                    flag_timeout(err, &sm);
+                    tc::mma_commit(&sm.tfull[b]);
+                    break;
+                }
+                tc::fence_after_sync();
+                mma_half(tmem, b, smem, h, c.first_of_tile());
+                tc::mma_commit(&sm.empty[h]);
+                if (c.last_of_tile()) {
+                    tc::mma_commit(&sm.tfull[b]);
+                    ut++;
+                }
             }
         }
     } else {
-        const int quad = warp & 3;
-        const int g = quad * 32 + lane;  // row of the W block
-        float W[128];
+        // warps 2-15: convert every half-stage (the raw L and R boxes into
+        // the K-half of the operand planes; R = c2 d_c Phi for c > 0);
+        // warps 4-11 drain tile u - 1 after converting tile u
+        const int ct = (warp - 2) * 32 + lane;
+        const bool drainer = warp >= kEpiWarp0 && warp < kEpiWarp0 + 8;
+        const int quad = warp & 3, half = (warp - kEpiWarp0) >> 2;
+        const int g = quad * 32 + lane;
+        float W[64];
 #pragma unroll
-        for (int j = 0; j < 128; j++) W[j] = 0.f;
-        uint32_t u = 0;
-        bool any = false;
-        for (int t = t0; t < t1; t++) {
-            if (!wanted(t)) continue;
-            const int b = u & 1;
-            const uint32_t bph = (u >> 1) & 1;
-            if (sm.abort) break;
-            if (!tc::mbar_wait(&sm.tfull[b], bph)) {
+        for (int jw = 0; jw < 64; jw++) W[jw] = 0.f;
+        uint32_t hs = 0, ut = 0;
+        int prev_flags = 0, prev_item = 0;
+        bool pending = false, ok = true;
+        auto drain_prev = [&]() -> bool {
+            const int b = ut & 1;
+            if (sm.abort || !tc::mbar_wait(&sm.tfull[b], (ut >> 1) & 1)) {
                 flag_timeout(err, &sm);
-                break;
+                return false;
             }
-            if (sm.abort) break;
             tc::fence_after_sync();
-            drain(tmem, b, quad, W);
+            drain(tmem, b, quad, half, W);
             tc::fence_before_sync();
             mbar_arrive(&sm.tempty[b]);
-            any = true;
-            u++;
-        }
-        const int npadw = nblk * 128;
-        double* out = wpart + (size_t)split * npadw * npadw + (size_t)(I * 128 + g) * npadw + J * 128;
+            ut++;
+            if (prev_flags & 2) {
+                double* o = wpart + (size_t)prev_item * 16384 + (size_t)g * 128 + half * 64;
 #pragma unroll
-        for (int j = 0; j < 128; j++) out[j] = (any && !sm.abort) ? (double)W[j] : 0.0;
+                for (int jw = 0; jw < 64; jw += 2) {
+                    *reinterpret_cast<double2*>(o + jw) = make_double2((double)W[jw], (double)W[jw + 1]);
+                    W[jw] = W[jw + 1] = 0.f;
+                }
+            }
+            return true;
+        };
+        for (FockCursor c(job_off, jobs, ncomp); c.valid(); c.advance(jobs), hs++) {
+            const int r = hs % kRawSlots, h = c.hk;
+            if (!warp_wait(sm, &sm.rfull[r], (hs / kRawSlots) & 1, err)) {
+                ok = false;
+                break;
+            }
+            if (!warp_wait(sm, &sm.empty[h], ((hs >> 1) & 1) ^ 1, err)) {
+                ok = false;
+                break;
+            }
+            const uint32_t rb = ssm + kStageBytes + r * kRawF;
+#pragma unroll
+            for (int k = 0; k < kFockItems; k++) {
+                const int q = ct + kFockConvThreads * k;
+                if (q >= 1024) break;
+                const int op = q >> 9, rr = (q >> 2) & 127, jj = q & 3;
+                const int box = op * 2 + (rr >> 6);
+                float v[8];
+                if (c.slot(box) < 0) {
+#pragma unroll
+                    for (int i = 0; i < 8; i++) v[i] = 0.f;
+                } else {
+                    const uint32_t src = rb + box * kRawBox + (rr & 63) * 128 + jj * 32;
+                    const float4 a = tc::lds128f(src), b4 = tc::lds128f(src + 16);
+                    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+                    v[4] = b4.x; v[5] = b4.y; v[6] = b4.z; v[7] = b4.w;
+                    if (op == 1 && c.c > 0) {
+                        const float* cp = c2 + (size_t)c.job.t * 128 + c.kh * 64 + h * 32 + 8 * jj;
+                        const float4 ca = __ldg(reinterpret_cast<const float4*>(cp));
+                        const float4 cb = __ldg(reinterpret_cast<const float4*>(cp + 4));
+                        v[0] *= ca.x; v[1] *= ca.y; v[2] *= ca.z; v[3] *= ca.w;
+                        v[4] *= cb.x; v[5] *= cb.y; v[6] *= cb.z; v[7] *= cb.w;
+                    }
+                }
+                store_chunk(ssm + (op ? 3 * kPlaneA : 0), rr, 4 * h + jj, v);
+            }
+            warp_arrive(&sm.rempty[r]);
+            conv_publish(&sm.full[h]);
+            if (drainer && c.last_of_tile()) {
+                if (pending && !drain_prev()) {
+                    ok = false;
+                    break;
+                }
+                pending = true;
+                prev_flags = c.job.flags;
+                prev_item = c.job.item;
+            }
+        }
+        if (drainer && ok && pending) drain_prev();
     }
     tc::fence_before_sync();
     __syncthreads();
     if (warp == 0) tc::tmem_dealloc(tmem, kTmemCols);
+}
+
+// Sums the two column-half partials of the density outputs (deterministic).
+__global__ void combine_kernel(long n1, long n3, double* __restrict__ rho, const double* __restrict__ rho_b,
+                               double* __restrict__ rho1, const double* __restrict__ rho1_b, double* __restrict__ tau,
+                               const double* __restrict__ tau_b, int type) {
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n1) {
+        rho[i] += rho_b[i];
+        if (type >= 2) tau[i] += tau_b[i];
+    }
+    if (type >= 1 && i < n3) rho1[i] += rho1_b[i];
 }
 
 // out = a * x + b * y (FP64, n elements).
@@ -378,96 +654,124 @@ __global__ void axpby_kernel(long n, double a, const double* __restrict__ x, dou
     if (i < n) out[i] = a * x[i] + b * y[i];
 }
 
-// V(mu, nu) = sum_s W_s(mu, nu) + W_s(nu, mu), column-major n x n (FP64).
-__global__ void wsum_kernel(const double* __restrict__ wpart, int nsplit, int npadw, int n, double* __restrict__ V) {
+// Tile-order copy of FP64-order point arrays (ncomp planes).
+__global__ void gather_kernel(const long* __restrict__ perm, long Gt, long Gp, int ncomp, const double* __restrict__ src,
+                              double* __restrict__ dst, bool zero_pads) {
+    const long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= Gt) return;
+    const long q = perm[p];
+    const bool pad = q < 0;
+    const long i = pad ? -q - 1 : q;
+    for (int c = 0; c < ncomp; c++) dst[(long)c * Gt + p] = (pad && zero_pads) ? 0.0 : src[(long)c * Gp + i];
+}
+
+// V_m(mu, nu) = sum over splits of W(mu, nu) + W(nu, mu); one grid row per molecule.
+__global__ void wsum_kernel(const double* __restrict__ wpart, const int* __restrict__ live,
+                            const MolRange* __restrict__ mols, int spin, double* __restrict__ V) {
+    const MolRange m = mols[blockIdx.y];
     const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (long)n * n) return;
-    const int mu = (int)(idx % n), nu = (int)(idx / n);
+    if (idx >= (long)m.n * m.n) return;
+    const int mu = (int)(idx % m.n), nu = (int)(idx / m.n);
+    const int I = mu >> 7, J = nu >> 7, ri = mu & 127, rj = nu & 127;
     double acc = 0;
-    for (int s = 0; s < nsplit; s++) {
-        const double* w = wpart + (size_t)s * npadw * npadw;
-        acc += w[(size_t)mu * npadw + nu] + w[(size_t)nu * npadw + mu];
+    for (int s = 0; s < m.nsplit; s++) {
+        const long a = m.item0 + ((long)I * m.nblk + J) * m.nsplit + s;
+        const long b = m.item0 + ((long)J * m.nblk + I) * m.nsplit + s;
+        if (live[a]) acc += wpart[(size_t)a * 16384 + (size_t)ri * 128 + rj];
+        if (live[b]) acc += wpart[(size_t)b * 16384 + (size_t)rj * 128 + ri];
     }
-    V[(long)nu * n + mu] = acc;
+    V[m.voff + (long)spin * m.n * m.n + (long)nu * m.n + mu] = acc;
 }
 
-// D (s, n, n) column-major FP64 -> three BF16 planes per spin, row nu, col mu.
-__global__ void split_d_kernel(const double* __restrict__ D, int n, int npad, int nspin, bf16* __restrict__ Dp) {
+// Packed D_m (s, n, n) column-major FP64 -> three BF16 planes per spin of the
+// strip: row f0(m) + nu, col mu (zero outside the molecule's n x n block).
+__global__ void split_d_kernel(const double* __restrict__ D, const MolRange* __restrict__ mols, int nmol, int nspin,
+                               long drows, int dcols, bf16* __restrict__ Dp) {
     const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long total = (long)nspin * npad * npad;
+    const long total = (long)nspin * drows * dcols;
     if (idx >= total) return;
-    const int mu = (int)(idx % npad);
-    const int nu = (int)((idx / npad) % npad);
-    const int s = (int)(idx / ((long)npad * npad));
-    const double v = (mu < n && nu < n) ? D[(long)s * n * n + (long)nu * n + mu] : 0.0;
-    bf16 h, m, l;
-    tc::split3(v, h, m, l);
-    const size_t plane = (size_t)npad * npad;
-    Dp[(size_t)(s * 3 + 0) * plane + (size_t)nu * npad + mu] = h;
-    Dp[(size_t)(s * 3 + 1) * plane + (size_t)nu * npad + mu] = m;
-    Dp[(size_t)(s * 3 + 2) * plane + (size_t)nu * npad + mu] = l;
+    const int mu = (int)(idx % dcols);
+    const long row = (idx / dcols) % drows;
+    const int s = (int)(idx / ((long)dcols * drows));
+    int lo = 0, hi = nmol - 1;  // molecule owning the row (f0 ascending)
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (mols[mid].f0 <= row) lo = mid;
+        else hi = mid - 1;
+    }
+    const MolRange& m = mols[lo];
+    const long nu = row - m.f0;
+    const double v = (mu < m.n && nu < m.n) ? D[m.voff + (long)s * m.n * m.n + nu * m.n + mu] : 0.0;
+    bf16 h, md_, l;
+    tc::split3(v, h, md_, l);
+    const size_t plane = (size_t)drows * dcols;
+    const size_t o = (size_t)row * dcols + mu;
+    Dp[(size_t)(s * 3 + 0) * plane + o] = h;
+    Dp[(size_t)(s * 3 + 1) * plane + o] = md_;
+    Dp[(size_t)(s * 3 + 2) * plane + o] = l;
 }
 
-// R operand: comp 0 = c0 phi + c1 . grad phi, comps 1..3 = c2 d_r phi (meta-GGA).
-__global__ void prep_r_kernel(MixedDev md, int ncomp, int type, const double* __restrict__ fcoef, long Gp,
-                              bf16* __restrict__ R) {
-    const long TK = (long)md.ntiles * md.kmax;
-    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;  // over TK * 128
-    if (idx >= TK * 128) return;
-    const int g = (int)(idx & 127);
-    const long row = idx >> 7;  // t * kmax + slot*64 + f
-    const int t = (int)(row / md.kmax);
-    const int colslot = (int)(row % md.kmax);
+// Z = c0 phi + c1 . grad phi per kept row (FP32); c2 per point (meta-GGA).
+// One CTA per tile, thread = point.
+__global__ void __launch_bounds__(128) prep_z_kernel(MixedDev md, int type, const double* __restrict__ fcoef,
+                                                     float* __restrict__ Z, float* __restrict__ c2) {
+    const int t = blockIdx.x, g = threadIdx.x;
     const long pt = (long)t * 128 + g;
-    if (colslot >= md.tile_nkept[t] * 64 || pt >= Gp) {
-        for (int c = 0; c < ncomp; c++)
-            for (int p = 0; p < 3; p++) R[((size_t)(c * 3 + p) * TK + row) * 128 + g] = __float2bfloat16(0.f);
-        return;
-    }
-    // FP32 arithmetic: R carries ~2^-24 relative precision in its three planes
-    auto fpv = [&](int c) { return __ldg(md.e32 + ((size_t)c * TK + row) * 128 + g); };
-    const float phi = fpv(0);
-    float a = (float)fcoef[pt] * phi;
-    float d[3] = {0, 0, 0};
+    const long Gt = md.Gt;
+    const float a0 = (float)fcoef[pt];
+    float a1 = 0, a2 = 0, a3 = 0;
     if (type >= 1) {
-        for (int r = 0; r < 3; r++) d[r] = fpv(1 + r);
-        a = fmaf((float)fcoef[Gp + pt], d[0], a);
-        a = fmaf((float)fcoef[2 * Gp + pt], d[1], a);
-        a = fmaf((float)fcoef[3 * Gp + pt], d[2], a);
+        a1 = (float)fcoef[Gt + pt];
+        a2 = (float)fcoef[2 * Gt + pt];
+        a3 = (float)fcoef[3 * Gt + pt];
     }
-    bf16 h, m, l;
-    tc::split3f(a, h, m, l);
-    const size_t ps = (size_t)TK * 128;
-    R[row * 128 + g] = h;
-    R[ps + row * 128 + g] = m;
-    R[2 * ps + row * 128 + g] = l;
-    if (ncomp == 4) {
-        const float c2 = (float)fcoef[4 * Gp + pt];
-        for (int r = 0; r < 3; r++) {
-            tc::split3f(c2 * d[r], h, m, l);
-            R[((size_t)((1 + r) * 3 + 0) * TK + row) * 128 + g] = h;
-            R[((size_t)((1 + r) * 3 + 1) * TK + row) * 128 + g] = m;
-            R[((size_t)((1 + r) * 3 + 2) * TK + row) * 128 + g] = l;
+    if (type >= 2) c2[pt] = (float)fcoef[4 * Gt + pt];
+    const long r0 = md.tile_row[t], nr = (long)md.tile_nkept[t] * 64;
+    const size_t cs = (size_t)md.rows * 128;
+    for (long r = 0; r < nr; r++) {
+        const size_t o = (size_t)(r0 + r) * 128 + g;
+        float z = a0 * __ldg(md.e32 + o);
+        if (type >= 1) {
+            z = fmaf(a1, __ldg(md.e32 + cs + o), z);
+            z = fmaf(a2, __ldg(md.e32 + 2 * cs + o), z);
+            z = fmaf(a3, __ldg(md.e32 + 3 * cs + o), z);
         }
+        Z[o] = z;
     }
 }
 
-// AO values and gradients of every mixed tile in both layouts, FP64 then
-// split.  One CTA per tile, thread = point; loops over the tile's shells.
+// E_m = sum of the per-tile partials of molecule m (fixed order).
+__global__ void energy_mols_kernel(const double* __restrict__ partial, const MolRange* __restrict__ mols,
+                                   double* __restrict__ E) {
+    const MolRange m = mols[blockIdx.x];
+    __shared__ double red[256];
+    double v = 0;
+    for (int t = m.t0 + threadIdx.x; t < m.t1; t += blockDim.x) v += partial[t];
+    red[threadIdx.x] = v;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) E[blockIdx.x] = red[0];
+}
+
+// AO values and gradients of every tile into the FP32 store, evaluated in
+// FP64.  One CTA per tile, thread = point; loops over the tile's shells.
 constexpr int kNcart = (kMaxL + 1) * (kMaxL + 2) / 2;
 
 __global__ void __launch_bounds__(128) ao_mixed_kernel(MixedDev md, DevShells sh, const int* __restrict__ tile_shells,
                                                        const int* __restrict__ tile_shell_off,
                                                        const double* __restrict__ px, const double* __restrict__ py,
-                                                       const double* __restrict__ pz, long Gp,
-                                                       const double* __restrict__ shtab, bf16* __restrict__ pf,
-                                                       bf16* __restrict__ fp, float* __restrict__ e32) {
+                                                       const double* __restrict__ pz, const double* __restrict__ shtab,
+                                                       int ao_comp, float* __restrict__ e32) {
     const int t = blockIdx.x, g = threadIdx.x;
     const long pt = (long)t * 128 + g;
-    const long src = pt < Gp ? pt : 0;  // tail points: copies of point 0 (their weight is zero)
-    const double X = px[src], Y = py[src], Z = pz[src];
-    const long TK = (long)md.ntiles * md.kmax;
+    const double X = px[pt], Y = py[pt], Z = pz[pt];
     const int* slots = md.tile_slot + (size_t)t * md.nchunk;
+    const int c0 = md.tile_c0[t];
+    const long trow = md.tile_row[t];
+    const size_t cs = (size_t)md.rows * 128;
     for (int k = tile_shell_off[t]; k < tile_shell_off[t + 1]; k++) {
         const int s = tile_shells[k];
         const int l = sh.l[s], type = sh.type[s], np = sh.nprim[s], po = sh.prim_off[s], first = sh.first[s];
@@ -490,7 +794,7 @@ __global__ void __launch_bounds__(128) ao_mixed_kernel(MixedDev md, DevShells sh
         }
         for (int f = 0; f < 2 * l + 1; f++) {
             const int mu = first + f;
-            const int slot = slots[mu >> 6];
+            const int slot = slots[(mu >> 6) - c0];
             if (slot < 0) continue;
             const int row = (type == 1) ? (f == 0 ? 2 : f - 1) : f;
             double Q = 0, Qx = 0, Qy = 0, Qz = 0;
@@ -505,16 +809,12 @@ __global__ void __launch_bounds__(128) ao_mixed_kernel(MixedDev md, DevShells sh
                     if (b) Qy += c * b * xp[a] * yp[b - 1] * zp[cc];
                     if (cc) Qz += c * cc * xp[a] * yp[b] * zp[cc - 1];
                 }
-            const double vals[4] = {A * Q, Ax * Q + A * Qx, Ay * Q + A * Qy, Az * Q + A * Qz};
-            const int col = slot * 64 + (mu & 63);
-            for (int c = 0; c < 4; c++) {
-                bf16 h[3];
-                tc::split3(vals[c], h[0], h[1], h[2]);
-                for (int p = 0; p < 3; p++) {
-                    pf[((size_t)(c * 3 + p) * md.Gt + pt) * md.kmax + col] = h[p];
-                    fp[((size_t)(c * 3 + p) * TK + (size_t)t * md.kmax + col) * 128 + g] = h[p];
-                }
-                e32[((size_t)c * TK + (size_t)t * md.kmax + col) * 128 + g] = (float)vals[c];
+            const size_t o = (size_t)(trow + slot * 64 + (mu & 63)) * 128 + g;
+            e32[o] = (float)(A * Q);
+            if (ao_comp == 4) {
+                e32[cs + o] = (float)(Ax * Q + A * Qx);
+                e32[2 * cs + o] = (float)(Ay * Q + A * Qy);
+                e32[3 * cs + o] = (float)(Az * Q + A * Qz);
             }
         }
     }
@@ -523,48 +823,65 @@ __global__ void __launch_bounds__(128) ao_mixed_kernel(MixedDev md, DevShells sh
 }  // namespace
 
 void launch_ao_mixed(const MixedDev& md, DevShells sh, const int* tile_shells, const int* tile_shell_off, const double* x,
-                     const double* y, const double* z, long Gp, const double* shtab, bf16* pf, bf16* fp, float* e32,
-                     cudaStream_t s) {
-    ao_mixed_kernel<<<md.ntiles, 128, 0, s>>>(md, sh, tile_shells, tile_shell_off, x, y, z, Gp, shtab, pf, fp, e32);
+                     const double* y, const double* z, const double* shtab, int ao_comp, float* e32, cudaStream_t s) {
+    if (md.ntiles == 0) return;
+    ao_mixed_kernel<<<md.ntiles, 128, 0, s>>>(md, sh, tile_shells, tile_shell_off, x, y, z, shtab, ao_comp, e32);
     CGB_CUDA(cudaGetLastError());
 }
 
-void launch_split_d(const double* D, int n, int npad, int nspin, bf16* Dp, cudaStream_t s) {
-    const long total = (long)nspin * npad * npad;
-    split_d_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(D, n, npad, nspin, Dp);
+void launch_split_d(const double* D, const MolRange* mols, int nmol, int nspin, long drows, int dcols, int /*maxn*/,
+                    bf16* Dp, cudaStream_t s) {
+    const long total = (long)nspin * drows * dcols;
+    split_d_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(D, mols, nmol, nspin, drows, dcols, Dp);
     CGB_CUDA(cudaGetLastError());
 }
 
-size_t mixed_smem_bytes() { return (size_t)kStages * kStageBytes + 1024; }
 
-void launch_density_tc(const CUtensorMap& tm_pf, const CUtensorMap& tm_d, const MixedDev& md, int epi, int acomp,
-                       int spin, double* rho, double* rho1, double* tau, long Gp, int* err, cudaStream_t s) {
+size_t mixed_smem_bytes() { return (size_t)kSmemBytes + 1024; }
+
+void set_mixed_kernel_attributes() {
+    const int smem = (int)mixed_smem_bytes();
+    CGB_CUDA(cudaFuncSetAttribute(density_tc_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    CGB_CUDA(cudaFuncSetAttribute(density_tc_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    CGB_CUDA(cudaFuncSetAttribute(density_tc_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    CGB_CUDA(cudaFuncSetAttribute(fock_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+}
+
+void launch_density_tc(const CUtensorMap& tm_d, const CUtensorMap& tm_raw, const MixedDev& md, int ctas,
+                       const int* job_off, const DensJob* jobs, int epi, int acomp, int spin, double* rho,
+                       double* rho1, double* tau, double* rho_b, double* rho1_b, double* tau_b, int* err,
+                       cudaStream_t s) {
+    if (ctas == 0) return;
+    CGB_CHECK(md.nchunk <= kMaxChunks, XC_ERR_UNSUPPORTED, "more than 16384 basis functions in one molecule");
     const size_t smem = mixed_smem_bytes();
-    if (epi == 0) {
-        CGB_CUDA(cudaFuncSetAttribute(density_tc_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        density_tc_kernel<0><<<md.ntiles, kThreads, smem, s>>>(tm_pf, tm_d, md, acomp, spin, rho, rho1, tau, Gp, err);
-    } else if (epi == 1) {
-        CGB_CUDA(cudaFuncSetAttribute(density_tc_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        density_tc_kernel<1><<<md.ntiles, kThreads, smem, s>>>(tm_pf, tm_d, md, acomp, spin, rho, rho1, tau, Gp, err);
-    } else {
-        CGB_CUDA(cudaFuncSetAttribute(density_tc_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        density_tc_kernel<2><<<md.ntiles, kThreads, smem, s>>>(tm_pf, tm_d, md, acomp, spin, rho, rho1, tau, Gp, err);
-    }
+    DensOut o{rho, rho1, tau, rho_b, rho1_b, tau_b};
+    if (epi == 0)
+        density_tc_kernel<0><<<ctas, kThreads, smem, s>>>(tm_d, tm_raw, md, job_off, jobs, acomp, spin, o, err);
+    else if (epi == 1)
+        density_tc_kernel<1><<<ctas, kThreads, smem, s>>>(tm_d, tm_raw, md, job_off, jobs, acomp, spin, o, err);
+    else
+        density_tc_kernel<2><<<ctas, kThreads, smem, s>>>(tm_d, tm_raw, md, job_off, jobs, acomp, spin, o, err);
     CGB_CUDA(cudaGetLastError());
 }
 
-void launch_prep_r(const MixedDev& md, int ncomp, int type, const double* fcoef, long Gp, bf16* R, cudaStream_t s) {
-    const long total = (long)md.ntiles * md.kmax * 128;
-    prep_r_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(md, ncomp, type, fcoef, Gp, R);
+void launch_combine(long n1, double* rho, const double* rho_b, double* rho1, const double* rho1_b, double* tau,
+                    const double* tau_b, int type, cudaStream_t s) {
+    const long n3 = 3 * n1;
+    combine_kernel<<<(unsigned)((n3 + 255) / 256), 256, 0, s>>>(n1, n3, rho, rho_b, rho1, rho1_b, tau, tau_b, type);
     CGB_CUDA(cudaGetLastError());
 }
 
-void launch_fock_tc(const CUtensorMap& tm_fp, const CUtensorMap& tm_r, const MixedDev& md, int ncomp, int r_rows,
-                    int nblk, int nsplit, double* wpart, int* err, cudaStream_t s) {
-    const size_t smem = mixed_smem_bytes();
-    CGB_CUDA(cudaFuncSetAttribute(fock_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    dim3 grid(nblk * nblk, nsplit);
-    fock_tc_kernel<<<grid, kThreads, smem, s>>>(tm_fp, tm_r, md, ncomp, r_rows, nblk, nsplit, wpart, err);
+void launch_prep_z(const MixedDev& md, int type, const double* fcoef, float* Z, float* c2, cudaStream_t s) {
+    if (md.ntiles == 0) return;
+    prep_z_kernel<<<md.ntiles, 128, 0, s>>>(md, type, fcoef, Z, c2);
+    CGB_CUDA(cudaGetLastError());
+}
+
+void launch_fock_tc(const CUtensorMap& tm_e32, const CUtensorMap& tm_z, long rows, int ctas, const int* job_off,
+                    const FockJob* jobs, const float* c2, int ncomp, double* wpart, int* err, cudaStream_t s) {
+    if (ctas == 0) return;
+    fock_tc_kernel<<<ctas, kThreads, mixed_smem_bytes(), s>>>(tm_e32, tm_z, rows, job_off, jobs, c2, ncomp, wpart,
+                                                             err);
     CGB_CUDA(cudaGetLastError());
 }
 
@@ -574,9 +891,23 @@ void launch_axpby(long n, double a, const double* x, double b, const double* y, 
     CGB_CUDA(cudaGetLastError());
 }
 
-void launch_wsum(const double* wpart, int nsplit, int npadw, int n, double* V, cudaStream_t s) {
-    const long total = (long)n * n;
-    wsum_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(wpart, nsplit, npadw, n, V);
+void launch_wsum(const double* wpart, const int* item_live, const MolRange* mols, int nmol, int maxn, int spin,
+                 int /*nspin*/, double* V, cudaStream_t s) {
+    const long total = (long)maxn * maxn;
+    dim3 grid((unsigned)((total + 255) / 256), (unsigned)nmol);
+    wsum_kernel<<<grid, 256, 0, s>>>(wpart, item_live, mols, spin, V);
+    CGB_CUDA(cudaGetLastError());
+}
+
+void launch_gather(const long* perm, long Gt, long Gp, int ncomp, const double* src, double* dst, bool zero_pads,
+                   cudaStream_t s) {
+    if (Gt <= 0) return;
+    gather_kernel<<<(unsigned)((Gt + 255) / 256), 256, 0, s>>>(perm, Gt, Gp, ncomp, src, dst, zero_pads);
+    CGB_CUDA(cudaGetLastError());
+}
+
+void launch_energy_mols(const double* partial, const MolRange* mols, int nmol, double* E, cudaStream_t s) {
+    energy_mols_kernel<<<nmol, 256, 0, s>>>(partial, mols, E);
     CGB_CUDA(cudaGetLastError());
 }
 

@@ -1,5 +1,6 @@
-// Mixed-precision path: point tiles with chunk screening, split-BF16 operand
-// stores, TMA tensor maps and the launch wrappers of k_mixed.cu.
+// Mixed-precision path: point tiles of one or many molecules, chunk
+// screening, the FP32 AO store, persistent work lists, and the launch
+// wrappers of k_mixed.cu.
 #pragma once
 
 #include <cuda.h>
@@ -16,57 +17,143 @@ constexpr int kChunk = 64;     // functions per chunk (MMA K / N granularity)
 constexpr int kTilePts = 128;  // points per tile (MMA M)
 
 // Device view of the tile structure (passed by value to kernels).
+//   e32 / Z rows: component c, row tile_row[t] + slot*64 + f, 128 points per row.
+//   Dp: plane (s*3 + p), row f0(mol) + nu, column mu (local functions).
 struct MixedDev {
     int ntiles;
-    int nchunk;      // basis chunks of 64 functions
-    int kmax;        // max kept functions per tile (multiple of 64)
-    int npad;        // nchunk * 64
-    long Gt;         // ntiles * 128
+    int nchunk;              // stride of tile_chunks / tile_slot (max chunks of one molecule)
+    long Gt;                 // ntiles * 128 points
+    long rows;               // kept function rows of all tiles (component stride of e32)
+    long drows;              // rows of one density plane (sum of the molecules' padded functions)
     const int* tile_nkept;   // [ntiles]
-    const int* tile_chunks;  // [ntiles][nchunk] kept global chunk ids by slot
-    const int* tile_slot;    // [ntiles][nchunk] slot of a global chunk, -1 if dropped
-    const __nv_bfloat16* pf; // point-major AO planes
-    const __nv_bfloat16* fp; // function-major AO planes
-    const float* e32;        // function-major FP32 AO values [c][t][kmax][128] (epilogues)
+    const int* tile_chunks;  // [ntiles][nchunk] kept local chunk ids by slot
+    const int* tile_slot;    // [ntiles][nchunk] slot of a local chunk, -1 if dropped
+    const long* tile_row;    // [ntiles] first row of the tile
+    const int* tile_c0;      // [ntiles] first chunk of the tile's molecule in the combined numbering
+    const float* e32;        // FP32 AO store [c][rows][128]: phi, d/dx, d/dy, d/dz
+};
+
+// One molecule of a (batched) mixed build.
+struct MolRange {
+    int n = 0;          // basis functions
+    int f0 = 0;         // first function in the combined, 64-aligned numbering
+    int nchunk = 0;     // 64-function chunks
+    int nblk = 0;       // 128-function blocks of V
+    int sh0 = 0, sh1 = 0;  // shells of the combined basis
+    int t0 = 0, t1 = 0;    // tiles
+    long voff = 0;      // offset of the (nspin, n, n) block in packed D / V
+    long item0 = 0;     // first V work item
+    int nsplit = 0;     // tile splits of each (I, J) block
+};
+
+// V work item: W_IJ partial over the wanted tiles of [t0, t1) of one molecule.
+struct FockItem {
+    int I, J, t0, t1;
+};
+
+// One tile of a CTA's density work list.
+struct DensJob {
+    int t, nk, trow, c0;
+};
+
+// One (item, wanted tile) of a CTA's V work list: slots of chunks 2I, 2I+1,
+// 2J, 2J+1 (-1 if dropped); flags 1: first tile of the item, 2: last.
+struct FockJob {
+    int t, trow, sa0, sa1, sb0, sb1, item, flags;
+};
+
+// Tuning knobs of the mixed path (chosen by the autotuner or set directly).
+struct MixedConfig {
+    double screen = 1e-11;   // chunk screening threshold (|phi|, |grad phi| bound)
+    int fock_tiles = 0;      // tiles per V work item (0: from the SM count)
+    int spatial = 1;         // 1: tiles from a k-d split of each molecule's points; 0: generation order
 };
 
 struct MixedState {
     bool ready = false;
-    double thr = 0;
+    MixedConfig cfg;
     MixedDev md{};
+    std::vector<MolRange> mols;
+    int nspin = 1;
+    int dcols = 0;           // columns of a density plane (max padded functions of a molecule)
+    int ao_comp = 1;         // components in e32 (1 or 4)
+    long real_points = 0;
     std::vector<int> h_nkept, h_chunks, h_slot;
-    long kept_pairs = 0;  // sum over tiles of (64 * nkept)^2
-    DevBuf<int> d_nkept, d_chunks, d_slot, d_tile_shells, d_tile_shell_off;
+    std::vector<long> h_row;
+    long kept_pairs = 0;     // sum over tiles of (64 * nkept)^2
+    // work lists (CSR by CTA)
+    int dens_ctas = 0, fock_ctas = 0;
+    long nitems = 0;
+    DevBuf<int> d_nkept, d_chunks, d_slot, d_c0, d_tile_shells, d_tile_shell_off;
+    DevBuf<long> d_row;
+    DevBuf<int> d_dens_off, d_fock_off, d_item_live;
+    DevBuf<DensJob> d_dens_jobs;
+    DevBuf<FockJob> d_fock_jobs;
+    DevBuf<MolRange> d_mols;
     DevBuf<double> d_shtab;
-    DevBuf<__nv_bfloat16> d_pf, d_fp, d_R, d_Dp;
-    DevBuf<float> d_e32;
+    DevBuf<double> d_x, d_y, d_z, d_w;   // tile-ordered points (zero weight on padding)
+    DevBuf<long> d_perm;                 // FP64-array index of each tile point; -(i+1) on padding
+    bool have_perm = false;
+    DevBuf<float> d_e32, d_Z, d_c2;
+    DevBuf<__nv_bfloat16> d_Dp;
     DevBuf<double> d_wpart;
     DevBuf<int> d_err;
+    // per-point work arrays of the mixed build (tile order)
+    DevBuf<double> rho, rho1, tau, sigma, eps, vrho, vsigma, vtau, fcoef, partial;
+    DevBuf<double> rho_b, rho1_b, tau_b;  // column-half-1 partials of the density kernel
+    int n_partial = 0;
     // incremental builds: references of the previous build and difference scratch
     bool have_ref = false;
     DevBuf<double> d_Dref, d_rho_ref, d_rho1_ref, d_tau_ref, d_fcoef_ref, d_Vref, d_dD, d_dfcoef;
-    int r_ncomp = 0;
-    int nblk = 0, nsplit = 0;
-    CUtensorMap tm_pf, tm_d, tm_fp, tm_r;
+    CUtensorMap tm_d;                      // density planes, box 64 x 64
+    CUtensorMap tm_raw_d;                  // e32, box 128 points x 64 rows (density A tiles)
+    CUtensorMap tm_raw_f;                  // e32, box 32 points x 64 rows (V_xc L / R boxes)
+    CUtensorMap tm_z;                      // Z, box 32 points x 64 rows
+    // CUDA graph of one build (replayed while the functional and buffers are unchanged)
+    cudaGraphExec_t graph = nullptr;
+    std::vector<int> graph_ids;  // functional (libxc ids) and grid type the graph was captured for
+    int graph_type = -1;
+    ~MixedState();
+    void drop_graph();
 };
 
 size_t mixed_smem_bytes();
 void launch_ao_mixed(const MixedDev& md, DevShells sh, const int* tile_shells, const int* tile_shell_off,
-                     const double* x, const double* y, const double* z, long Gp, const double* shtab,
-                     __nv_bfloat16* pf, __nv_bfloat16* fp, float* e32, cudaStream_t s);
-void launch_split_d(const double* D, int n, int npad, int nspin, __nv_bfloat16* Dp, cudaStream_t s);
-void launch_density_tc(const CUtensorMap& tm_pf, const CUtensorMap& tm_d, const MixedDev& md, int epi, int acomp,
-                       int spin, double* rho, double* rho1, double* tau, long Gp, int* err, cudaStream_t s);
-void launch_prep_r(const MixedDev& md, int ncomp, int type, const double* fcoef, long Gp, __nv_bfloat16* R,
-                   cudaStream_t s);
-// r_rows: first of the 64 zero rows of the R store (r_ncomp * 3 * ntiles * kmax).
-void launch_fock_tc(const CUtensorMap& tm_fp, const CUtensorMap& tm_r, const MixedDev& md, int ncomp, int r_rows,
-                    int nblk, int nsplit, double* wpart, int* err, cudaStream_t s);
-void launch_wsum(const double* wpart, int nsplit, int npadw, int n, double* V, cudaStream_t s);
+                     const double* x, const double* y, const double* z, const double* shtab, int ao_comp, float* e32,
+                     cudaStream_t s);
+// Packed per-molecule D (s, n, n) -> three BF16 planes per spin of the density strip.
+void launch_split_d(const double* D, const MolRange* mols, int nmol, int nspin, long drows, int dcols, int maxn,
+                    __nv_bfloat16* Dp, cudaStream_t s);
+// Writes the column-half-0 partials to rho / rho1 / tau and the half-1
+// partials to rho_b / rho1_b / tau_b (tau and tau_b accumulate: zero them
+// before the first meta-GGA pass); launch_combine adds them.
+void launch_density_tc(const CUtensorMap& tm_d, const CUtensorMap& tm_raw, const MixedDev& md, int ctas,
+                       const int* job_off, const DensJob* jobs, int epi, int acomp, int spin, double* rho,
+                       double* rho1, double* tau, double* rho_b, double* rho1_b, double* tau_b, int* err,
+                       cudaStream_t s);
+void launch_combine(long n1, double* rho, const double* rho_b, double* rho1, const double* rho1_b, double* tau,
+                    const double* tau_b, int type, cudaStream_t s);
+// Z = c0 phi + c1 . grad phi (FP32, e32 row layout) and c2 per point (meta-GGA).
+void launch_prep_z(const MixedDev& md, int type, const double* fcoef, float* Z, float* c2, cudaStream_t s);
+void launch_fock_tc(const CUtensorMap& tm_e32, const CUtensorMap& tm_z, long rows, int ctas, const int* job_off,
+                    const FockJob* jobs, const float* c2, int ncomp, double* wpart, int* err, cudaStream_t s);
+// V_m(mu, nu) = sum over splits of W(mu, nu) + W(nu, mu), packed per molecule.
+void launch_wsum(const double* wpart, const int* item_live, const MolRange* mols, int nmol, int maxn, int nspin_index,
+                 int nspin, double* V, cudaStream_t s);
+// E_m = sum of the functional's per-tile partials over the molecule's tiles.
+void launch_energy_mols(const double* partial, const MolRange* mols, int nmol, double* E, cudaStream_t s);
 void launch_axpby(long n, double a, const double* x, double b, const double* y, double* out, cudaStream_t s);
+// dst[p] = src[perm[p]] for every tile point (ncomp planes of Gt / Gp);
+// zero_pads: padding points get 0 instead.
+void launch_gather(const long* perm, long Gt, long Gp, int ncomp, const double* src, double* dst, bool zero_pads,
+                   cudaStream_t s);
+void set_mixed_kernel_attributes();
 
 // 2D bf16 tensor map with 128-byte swizzle over a row-major [rows][cols] array.
 void make_tmap_bf16(CUtensorMap* map, const void* base, uint64_t cols, uint64_t rows, uint32_t box_cols,
                     uint32_t box_rows);
+// 2D FP32 tensor map without swizzle over a row-major [rows][cols] array.
+void make_tmap_f32(CUtensorMap* map, const void* base, uint64_t cols, uint64_t rows, uint32_t box_cols,
+                   uint32_t box_rows);
 
 }  // namespace cgb

@@ -29,6 +29,14 @@ struct Functional {
     void init(const std::vector<int>& ids, int nspin);
 };
 
+// One molecule of the mixed path: its real points (generation order) and its
+// place in the combined basis.
+struct MolSource {
+    int n = 0, f0 = 0, sh0 = 0, sh1 = 0;
+    std::vector<double> x, y, z, w;
+    std::vector<long> src;  // index of each point in the grid's FP64 arrays (-1: none)
+};
+
 struct Grid {
     BasisSet basis;
     int nspin = 1;
@@ -75,8 +83,19 @@ struct Grid {
 
     // mixed-precision (tensor-core) path; tiles and stores are prepared on first use
     MixedState mx;
-    void prepare_mixed(double thr);
+    std::vector<MolSource> sources;  // molecules of the mixed path (one unless batched)
+    bool batched = false;            // built by build_batch: mixed precision only
+    std::vector<int> mol_n;          // basis functions of each molecule
+    long packed_size() const;        // doubles of packed per-molecule D / V: sum nspin n^2
+    DevBuf<double> d_Emol;           // per-molecule energies of the last mixed build
+    cudaStream_t capture_stream = nullptr;
+    void build_batch(const std::vector<BasisSet>& mols, const std::string& grid_name, int nspin);
+    void collect_sources();
+    void prepare_mixed(const MixedConfig& cfg);
+    void mixed_ready();
+    void density_passes(const __nv_bfloat16* Dp);
     void build_mixed(const double* dD, const Functional& f, double* dE, double* dV);
+    void build_mixed_graph(const Functional& f);  // d_D -> d_Emol, d_V through a CUDA graph
     void build_incremental(const double* dD, const Functional& f, double* dE, double* dV, bool anchor);
     int mixed_error();
 };

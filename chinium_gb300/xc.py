@@ -17,9 +17,9 @@ import ctypes
 
 import numpy as np
 
-from ._lib import GridInfo, PRECISION_FP64, PRECISION_MIXED, XCError, check, lib
+from ._lib import GridInfo, MixedConfig, PRECISION_FP64, PRECISION_MIXED, TuneReport, XCError, check, lib
 
-__all__ = ["Basis", "Grid", "ExchangeCorrelation", "XCError", "PRECISION_FP64", "PRECISION_MIXED"]
+__all__ = ["Basis", "Grid", "BatchGrid", "ExchangeCorrelation", "XCError", "PRECISION_FP64", "PRECISION_MIXED"]
 
 
 def _p(a):
@@ -128,6 +128,31 @@ class Grid:
     def profile(self, enable=True):
         check(lib().xc_grid_profile(self._h, int(bool(enable))))
 
+    # -- mixed-path knobs and autotuner ------------------------------------------
+    def mixed_config(self):
+        c = MixedConfig()
+        check(lib().xc_grid_get_mixed_config(self._h, ctypes.byref(c)))
+        return dict(screen=c.screen, fock_tiles=c.fock_tiles, spatial=c.spatial)
+
+    def set_mixed_config(self, screen=1e-11, fock_tiles=0, spatial=1):
+        c = MixedConfig(float(screen), int(fock_tiles), int(spatial))
+        check(lib().xc_grid_set_mixed_config(self._h, ctypes.byref(c)))
+
+    def tune(self, xc, D, e_tol=1e-7, v_tol=1e-6, reps=3):
+        """Autotune the mixed path on a representative density; the chosen
+        configuration stays set.  Returns the tuner's report as a dict."""
+        D = self._pack(D)
+        r = TuneReport()
+        check(lib().xc_grid_tune(self._h, xc._h, _p(D), self.nspin, float(e_tol), float(v_tol), int(reps),
+                                 ctypes.byref(r)))
+        cfg = lambda c: dict(screen=c.screen, fock_tiles=c.fock_tiles, spatial=c.spatial)
+        cands = [dict(cfg(c.cfg), ms=c.ms, max_de=c.max_de, max_dv=c.max_dv, kept_pairs=c.kept_pairs,
+                      accepted=bool(c.accepted)) for c in r.cand[:r.ncand]]
+        return dict(best=cfg(r.best), ms_best=r.ms_best, ms_reference=r.ms_reference, candidates=cands)
+
+    def _pack(self, D):
+        return self._stack(D)
+
     def stage_ms(self):
         """[density, functional, energy, fock] device milliseconds of the last build."""
         ms = np.zeros(4)
@@ -195,6 +220,56 @@ class Grid:
             raise XCError(-1, "Wrong number of spin types!")
         # column-major per spin: store D^T row-major
         return np.ascontiguousarray(np.stack([d.T for d in D]))
+
+
+class BatchGrid(Grid):
+    """Many molecules on one GPU: each keeps its own Becke-partitioned grid
+    (as Grid(basis, grid, nspin) with screen threshold 0); the mixed-precision
+    build runs the point tiles of all of them in one persistent launch per
+    stage, replayed from a CUDA graph.  Mixed precision only.
+
+    D and V are lists over molecules of what Grid.build takes and returns
+    (a list of nspin n_m x n_m matrices); E is an array over molecules."""
+
+    def __init__(self, bases, grid="SG-2", nspin=1):
+        self.bases = list(bases)
+        self.basis = None
+        self.nspin = nspin
+        arr = (ctypes.c_void_p * len(self.bases))(*[b._h.value for b in self.bases])
+        h = ctypes.c_void_p()
+        check(lib().xc_grid_create_batch(len(self.bases), arr, grid.encode(), nspin, ctypes.byref(h)))
+        self._h = h
+        self.nmol = len(self.bases)
+        self.nbasis_list = [b.nbasis for b in self.bases]
+        self.npoints = np.zeros(self.nmol, dtype=np.int64)
+        self.offsets = np.zeros(self.nmol, dtype=np.int64)
+        check(lib().xc_grid_molecules(self._h, None, None, _p(self.npoints), _p(self.offsets)))
+        self.packed_size = int(sum(nspin * n * n for n in self.nbasis_list))
+
+    def _pack(self, Ds):
+        if len(Ds) != self.nmol:
+            raise XCError(-1, "one density per molecule")
+        out = np.empty(self.packed_size)
+        for m, D in enumerate(Ds):
+            blk = self._stack(D).ravel()
+            o = int(self.offsets[m])
+            out[o:o + blk.size] = blk
+        return out
+
+    def _unpack(self, V):
+        res = []
+        for m, n in enumerate(self.nbasis_list):
+            o = int(self.offsets[m])
+            blk = V[o:o + self.nspin * n * n].reshape(self.nspin, n, n)
+            res.append([blk[s].T.copy() for s in range(self.nspin)])
+        return res
+
+    def build(self, xc, Ds, precision=PRECISION_MIXED):
+        D = self._pack(Ds)
+        V = np.zeros(self.packed_size)
+        E = np.zeros(self.nmol)
+        check(lib().xc_build(self._h, xc._h, _p(D), self.nspin, int(precision), _p(E), _p(V)))
+        return E, self._unpack(V)
 
 
 class ExchangeCorrelation:

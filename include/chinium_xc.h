@@ -187,8 +187,10 @@ int xc_functional_energy_static(const xc_functional* f, long npoints, const doub
 int xc_build(xc_grid* g, xc_functional* f, const double* D, int nspin, int precision, double* E,
              double* V);
 
-/* Same with caller-owned device pointers (d_D in, d_E scalar and d_V out),
- * issued on the grid's stream; does not synchronise. */
+/* Same with caller-owned device pointers (d_D in, d_E and d_V out, packed
+ * per molecule), issued on the grid's stream; does not synchronise.  Mixed
+ * builds replay a CUDA graph of the whole launch sequence (captured at the
+ * first build for a functional and grid type). */
 int xc_build_device(xc_grid* g, xc_functional* f, const double* d_D, int nspin, int precision,
                     double* d_E, double* d_V);
 
@@ -215,6 +217,60 @@ int xc_build_incremental(xc_grid* g, xc_functional* f, const double* D, int nspi
 /* SAP potential matrix (GuessSCF.cpp:17-75): V_mu,nu = sum_g w v_SAP(r_g)
  * phi_mu phi_nu with v_SAP the nearest-radius tabulated atomic potentials. */
 int xc_sap_fock(xc_grid* g, double* V);
+
+/* ------------------------------------------------------- batched molecules
+ * No reference counterpart: the reference builds one Grid per molecule
+ * (src/Grid/Grid.h:90-116).  A batch grid holds many molecules, each with
+ * its own Becke-partitioned grid (the same generation as xc_grid_create with
+ * screen threshold 0); the mixed-precision build processes the point tiles
+ * of all of them in one persistent launch per stage.  Only
+ * XC_PRECISION_MIXED builds are available on a batch grid.
+ * Packed per-molecule matrices: molecule m's (nspin, n_m, n_m) column-major
+ * block starts at sum_{k<m} nspin n_k^2; E holds one value per molecule.
+ * xc_build / xc_build_device on any grid use this layout (one molecule: the
+ * usual (nspin, n, n) matrix and a scalar E). */
+int xc_grid_create_batch(int nmol, const xc_basis* const* bases, const char* grid_name, int nspin,
+                         xc_grid** out);
+/* Number of molecules; per molecule (arrays of nmol, each may be NULL):
+ * basis functions, real grid points, offset of its block in packed D / V. */
+int xc_grid_molecules(const xc_grid* g, int* nmol, int* nbasis, long* npoints, long* offset);
+
+/* Knobs of the mixed path.  screen: chunk screening threshold on |phi| and
+ * |grad phi| (0 keeps every chunk); fock_tiles: point tiles per V work item
+ * (0 = from the SM count); spatial: 1 forms tiles from k-d cells of each
+ * molecule's points, 0 from 128 consecutive points in generation order.
+ * Setting them discards the prepared tiles (rebuilt at the next build). */
+typedef struct xc_mixed_config {
+    double screen;
+    int fock_tiles;
+    int spatial;
+} xc_mixed_config;
+int xc_grid_set_mixed_config(xc_grid* g, const xc_mixed_config* cfg);
+int xc_grid_get_mixed_config(const xc_grid* g, xc_mixed_config* cfg);
+
+/* Autotuner of the mixed path for one functional and a representative
+ * density (host D, packed).  Reference: a build with screening 0 and
+ * spatial tiles.  Candidates over (screen, spatial, fock_tiles) are built
+ * and timed (median of `reps` graph replays); the fastest candidate whose
+ * energies (every molecule) are within e_tol and whose V is within v_tol
+ * (max abs) of the reference is selected and left set on the grid.
+ * report (may be NULL) receives the choice and the candidates tried. */
+typedef struct xc_tune_candidate {
+    xc_mixed_config cfg;
+    double ms;          /* median build time */
+    double max_de;      /* max over molecules of |E - E_ref| */
+    double max_dv;      /* max |V - V_ref| */
+    long kept_pairs;    /* sum over tiles of (kept functions)^2 */
+    int accepted;
+} xc_tune_candidate;
+typedef struct xc_tune_report {
+    xc_mixed_config best;
+    double ms_best, ms_reference;
+    int ncand;
+    xc_tune_candidate cand[32];
+} xc_tune_report;
+int xc_grid_tune(xc_grid* g, xc_functional* f, const double* D, int nspin, double e_tol, double v_tol,
+                 int reps, xc_tune_report* report);
 
 #ifdef __cplusplus
 }
