@@ -130,3 +130,27 @@ def test_grid_without_gpu_fails_loudly():
     with pytest.raises(cg.XCError) as e:
         cg.Grid(b, "SG-1")
     assert e.value.code == -3
+
+
+def test_batch_and_tuning_argument_errors():
+    """Argument checks of the batch / tuning entry points run before any
+    device work (a missing GPU is not reached)."""
+    L = lib()
+    h = ctypes.c_void_p()
+    assert L.xc_grid_create_batch(0, None, b"SG-1", 1, ctypes.byref(h)) == -1
+    assert L.xc_grid_create_batch(2, None, b"SG-1", 1, ctypes.byref(h)) == -1
+    Z, xyz = M.h2o()
+    b = cg.Basis(Z, xyz, "def2-svp")
+    arr = (ctypes.c_void_p * 2)(b._h.value, None)
+    assert L.xc_grid_create_batch(2, arr, b"SG-1", 1, ctypes.byref(h)) == -1
+    arr = (ctypes.c_void_p * 1)(b._h.value)
+    assert L.xc_grid_create_batch(1, arr, b"SG-1", 3, ctypes.byref(h)) == -1
+    assert L.xc_grid_set_mixed_config(None, None) == -1
+    assert L.xc_grid_tune(None, None, None, 1, 1e-7, 1e-6, 1, None) == -1
+
+
+def test_mixed_config_struct_layout():
+    from chinium_gb300._lib import MixedConfig, TuneCandidate, TuneReport
+    assert ctypes.sizeof(MixedConfig) == 16
+    assert ctypes.sizeof(TuneCandidate) == 16 + 3 * 8 + 8 + 8
+    assert TuneReport.cand.offset == 16 + 8 + 8 + 8

@@ -1,0 +1,133 @@
+"""Batched mixed-precision builds (many molecules, one launch per stage):
+against per-molecule FP64 builds, against single-molecule mixed builds,
+replay determinism of the captured graph, and the autotuner."""
+import numpy as np
+import pytest
+
+import chinium_gb300 as cg
+from chinium_gb300 import molecules as M
+
+pytestmark = pytest.mark.gpu
+
+BATCH_E_TOL = 1e-5  # Eh per molecule, split-BF16 (~FP32) contractions with FP64 accumulation
+BATCH_V_TOL = 1e-5
+
+
+def density(n, nocc, seed):
+    rng = np.random.default_rng(seed)
+    A = rng.normal(size=(n, nocc)) * 0.05
+    A[np.arange(nocc), np.arange(nocc)] += 1.0
+    Q, _ = np.linalg.qr(A)
+    return 2.0 * Q @ Q.T
+
+
+@pytest.fixture(scope="module")
+def small_batch():
+    mols = [M.h2o()] + M.alkane_batch(count=5, seed=3, nmin=1, nmax=4)
+    bases = [cg.Basis(Z, xyz, "def2-svp") for Z, xyz in mols]
+    Ds = [density(b.nbasis, sum(Z) // 2, k) for k, ((Z, _), b) in enumerate(zip(mols, bases))]
+    return mols, bases, Ds
+
+
+@pytest.mark.parametrize("name", ["PBE", "R2SCAN"])
+def test_batch_against_fp64_per_molecule(small_batch, name):
+    mols, bases, Ds = small_batch
+    xc = cg.ExchangeCorrelation().Read(name)
+    bg = cg.BatchGrid(bases, "SG-1")
+    bg.setType(xc.type)
+    E, V = bg.build(xc, [[D] for D in Ds])
+    assert E.shape == (len(mols),)
+    for m, (b, D) in enumerate(zip(bases, Ds)):
+        g = cg.Grid(b, "SG-1")
+        g.setType(xc.type)
+        g.getAO(0)
+        E64, V64 = g.build(xc, [D])
+        dE, dV = abs(E[m] - E64), np.abs(V[m][0] - V64[0]).max()
+        print("%s molecule %d (n=%d): |dE|=%.2e max|dV|=%.2e" % (name, m, b.nbasis, dE, dV))
+        assert dE < BATCH_E_TOL and dV < BATCH_V_TOL
+        assert np.allclose(V[m][0], V[m][0].T, atol=1e-14)
+
+
+def test_batch_matches_single_molecule_mixed(small_batch):
+    """A molecule's tiles, screening and per-tile sums do not depend on the
+    other molecules of the batch: with the same V work-item length (W
+    partials are FP32 sums over an item's tiles) the results are identical."""
+    mols, bases, Ds = small_batch
+    xc = cg.ExchangeCorrelation().Read("PBE")
+    bg = cg.BatchGrid(bases, "SG-1")
+    bg.setType(xc.type)
+    bg.set_mixed_config(fock_tiles=16)
+    E, V = bg.build(xc, [[D] for D in Ds])
+    for m in (0, len(mols) - 1):
+        g = cg.Grid(bases[m], "SG-1")
+        g.setType(xc.type)
+        g.getAO(0)
+        g.set_mixed_config(fock_tiles=16)
+        Em, Vm = g.build(xc, [Ds[m]], precision=cg.PRECISION_MIXED)
+        assert E[m] == Em
+        assert np.array_equal(V[m][0], Vm[0])
+
+
+def test_batch_graph_replay_is_deterministic(small_batch):
+    mols, bases, Ds = small_batch
+    xc = cg.ExchangeCorrelation().Read("R2SCAN")
+    bg = cg.BatchGrid(bases, "SG-1")
+    bg.setType(xc.type)
+    E1, V1 = bg.build(xc, [[D] for D in Ds])
+    E2, V2 = bg.build(xc, [[D] for D in Ds])
+    assert np.array_equal(E1, E2)
+    assert all(np.array_equal(a[0], b[0]) for a, b in zip(V1, V2))
+    # a different density through the same graph
+    E3, _ = bg.build(xc, [[0.9 * D] for D in Ds])
+    assert np.all(E3 != E1)
+
+
+def test_batch_unrestricted():
+    mols = M.alkane_batch(count=3, seed=5, nmin=1, nmax=3)
+    bases = [cg.Basis(Z, xyz, "def2-svp") for Z, xyz in mols]
+    xc = cg.ExchangeCorrelation(spin=2).Read("TPSS")
+    bg = cg.BatchGrid(bases, "SG-1", nspin=2)
+    bg.setType(xc.type)
+    Ds = [[0.5 * density(b.nbasis, 5, k), 0.5 * density(b.nbasis, 4, k + 7)] for k, b in enumerate(bases)]
+    E, V = bg.build(xc, Ds)
+    for m, b in enumerate(bases):
+        g = cg.Grid(b, "SG-1", nspin=2)
+        g.setType(xc.type)
+        g.getAO(0)
+        E64, V64 = g.build(xc, Ds[m])
+        assert abs(E[m] - E64) < BATCH_E_TOL
+        assert max(np.abs(V[m][s] - V64[s]).max() for s in range(2)) < BATCH_V_TOL
+
+
+def test_batch_rejects_fp64():
+    b = cg.Basis(*M.h2o(), "def2-svp")
+    bg = cg.BatchGrid([b, b], "SG-1")
+    xc = cg.ExchangeCorrelation().Read("PBE")
+    bg.setType(xc.type)
+    D = density(b.nbasis, 5, 0)
+    with pytest.raises(cg.XCError) as e:
+        bg.build(xc, [[D], [D]], precision=cg.PRECISION_FP64)
+    assert e.value.code == -6
+
+
+def test_autotuner_picks_an_accurate_configuration(small_batch):
+    mols, bases, Ds = small_batch
+    xc = cg.ExchangeCorrelation().Read("PBE")
+    bg = cg.BatchGrid(bases, "SG-1")
+    bg.setType(xc.type)
+    rep = bg.tune(xc, [[D] for D in Ds], e_tol=1e-7, v_tol=1e-6, reps=2)
+    assert rep["candidates"]
+    best = rep["best"]
+    assert bg.mixed_config() == best
+    chosen = [c for c in rep["candidates"] if c["screen"] == best["screen"] and c["fock_tiles"] == best["fock_tiles"]
+              and c["spatial"] == best["spatial"]]
+    if chosen:
+        assert chosen[0]["accepted"]
+    print("tuner:", best, rep["ms_best"], rep["ms_reference"])
+    E, V = bg.build(xc, [[D] for D in Ds])
+    for m in range(len(mols)):
+        g = cg.Grid(bases[m], "SG-1")
+        g.setType(xc.type)
+        g.getAO(0)
+        E64, _ = g.build(xc, [Ds[m]])
+        assert abs(E[m] - E64) < BATCH_E_TOL
