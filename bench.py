@@ -159,6 +159,27 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def mixed_roofline(info, kms, stage, peaks, passes_density, ncomp_fock):
+    """Tensor-core roofline of the dominant mixed kernel.  Algorithmic FLOPs
+    per build: density 2 * 128 * sum_t (64 nk_t)^2 per pass (T = Phi D of every
+    tile), V_xc 2 * 128 * sum_t (64 nk_t)^2 per component (W = L^T R); the
+    tensor core executes 6x that (three-term split cross products)."""
+    pairs = info["mixed_pairs"]
+    fl_den = 2.0 * 128 * pairs * passes_density
+    fl_fock = 2.0 * 128 * pairs * ncomp_fock
+    ms_den, ms_fock = kms[0], kms[4]
+    dom, dom_ms, fl = ("density_tc", ms_den, fl_den) if ms_den >= ms_fock else ("fock_tc", ms_fock, fl_fock)
+    achieved = fl / (dom_ms / 1e3) / 1e12
+    peak = peaks.get("bf16_tflops", 1900.0)
+    return {"bound": "tensor", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak, "traffic": None,
+            "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst) -- of measured",
+            "executed_tensor_tflops": 6 * achieved, "executed_frac": 6 * achieved / peak,
+            "kernel_ms": {"density_tc(+split,combine)": kms[0], "functional": kms[1], "energy": kms[2],
+                          "prep_z": kms[3], "fock_tc": kms[4], "wsum": kms[5]},
+            "stage_ms": {"density": stage[0], "functional": stage[1], "energy": stage[2], "fock": stage[3]}}
+
+
 def time_builds(torch, grid, xc, dD, dE, dV, precision, steps, stream):
     """Device time of `steps` back-to-back builds on the build stream (s)."""
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -171,6 +192,117 @@ def time_builds(torch, grid, xc, dD, dE, dV, precision, steps, stream):
     return ev0.elapsed_time(ev1) / 1e3
 
 
+ALK_METRIC = "XC grid-pts/s (batched r2SCAN/def2-SVP XC build of 64 alkanes on SG-2)"
+
+
+def run_alkanes(args):
+    """64 linear alkanes C_nH_(2n+2), n ~ U{1..20} (seed 0), restricted
+    r2SCAN/def2-SVP on SG-2: every molecule's tiles in one persistent launch
+    per stage, replayed from a CUDA graph; the autotuner picks the screening
+    threshold, the V work-item length and the tile formation first.  FP64
+    per-molecule builds on the same densities give the accuracy and the plain
+    path's time."""
+    import ctypes
+    import torch
+    import chinium_gb300 as cg
+    from chinium_gb300 import molecules as M
+    from chinium_gb300._lib import check, lib
+    torch.cuda.set_device(0)
+    mols = M.alkane_batch(64, seed=0)
+    bases = [cg.Basis(Z, xyz, "def2-svp") for Z, xyz in mols]
+    xc = cg.ExchangeCorrelation().Read("R2SCAN")
+    PMX, P64 = cg.PRECISION_MIXED, cg.PRECISION_FP64
+    t0 = time.perf_counter()
+    bg = cg.BatchGrid(bases, "SG-2")
+    bg.setType(xc.type)
+    t_grid = time.perf_counter() - t0
+    stream = torch.cuda.Stream()
+    bg.set_stream(stream.cuda_stream)
+    Ds = [[model_density(b.nbasis, sum(Z) // 2, seed=m)] for m, ((Z, _), b) in enumerate(zip(mols, bases))]
+    Dpk = bg._pack(Ds)
+    nm = len(mols)
+    tune = None
+    if not args.no_tune:
+        t0 = time.perf_counter()
+        tune = bg.tune(xc, Ds, e_tol=1e-7, v_tol=1e-5, reps=2)
+        tune["seconds"] = time.perf_counter() - t0
+    dD = torch.from_numpy(Dpk).cuda()
+    dE = torch.zeros(nm, dtype=torch.float64, device="cuda")
+    dV = torch.zeros(bg.packed_size, dtype=torch.float64, device="cuda")
+    t0 = time.perf_counter()
+    bg.build_device(xc, dD, dE, dV, PMX)
+    stream.synchronize()
+    t_first = time.perf_counter() - t0
+    for _ in range(args.warmup):
+        bg.build_device(xc, dD, dE, dV, PMX)
+    stream.synchronize()
+    Emx = dE.cpu().numpy().copy()
+    Vmx = dV.cpu().numpy().copy()
+    info = bg.info()
+    bg.profile(True)
+    bg.build_device(xc, dD, dE, dV, PMX)
+    stage = bg.stage_ms()
+    kms = bg.kernel_ms()
+    bg.profile(False)
+    clk_dir = os.path.join(REPO, "gpurun_out") if os.path.isdir(os.path.join(REPO, "gpurun_out")) else os.path.join(REPO, "_work")
+    os.makedirs(clk_dir, exist_ok=True)
+    clk_path = os.path.join(clk_dir, "clocks_alkanes.csv")
+    cp, cf = clocks_start(clk_path)
+    time.sleep(0.4)
+    t_dev = time_builds(torch, bg, xc, dD, dE, dV, PMX, args.steps, stream)
+    clocks = clocks_stop(cp, cf, clk_path)
+    # end to end through the public host-buffer call
+    Dh = torch.from_numpy(Dpk).pin_memory()
+    Vh = torch.zeros(bg.packed_size, dtype=torch.float64).pin_memory()
+    Eh = torch.zeros(nm, dtype=torch.float64).pin_memory()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        check(lib().xc_build(bg._h, xc._h, ctypes.c_void_p(Dh.data_ptr()), 1, PMX, ctypes.c_void_p(Eh.data_ptr()),
+                             ctypes.c_void_p(Vh.data_ptr())))
+    torch.cuda.synchronize()
+    t_e2e = time.perf_counter() - t0
+    # plain FP64 path, molecule by molecule, same densities
+    nfp = nm if args.fp64_mols <= 0 else min(nm, args.fp64_mols)
+    t64, dEs, dVs = 0.0, [], []
+    for m in range(nfp):
+        g = cg.Grid(bases[m], "SG-2")
+        g.setType(xc.type)
+        g.getAO(0)
+        g.set_stream(stream.cuda_stream)
+        n = bases[m].nbasis
+        d1 = torch.from_numpy(np.ascontiguousarray(Ds[m][0].T)).cuda()
+        e1 = torch.zeros(1, dtype=torch.float64, device="cuda")
+        v1 = torch.zeros((n, n), dtype=torch.float64, device="cuda")
+        g.build_device(xc, d1, e1, v1, P64)
+        t64 += time_builds(torch, g, xc, d1, e1, v1, P64, 1, stream)
+        o = int(bg.offsets[m])
+        dEs.append(abs(float(e1.item()) - Emx[m]))
+        dVs.append(float(np.abs(v1.cpu().numpy().ravel() - Vmx[o:o + n * n]).max()))
+        del g
+    G = int(bg.npoints.sum())
+    Gfp = int(bg.npoints[:nfp].sum())
+    value = G * args.steps / t_dev
+    plain = Gfp / t64
+    peaks = measured_peaks()
+    roof = mixed_roofline(info, kms, stage, peaks, passes_density=4, ncomp_fock=4)
+    line = {"metric": ALK_METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_dev / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16x3 (split) + f64 accumulation", "data": "synthetic",
+            "config": {"workload": "64 alkanes C_nH_(2n+2), n ~ U{1..20} seed 0, RKS r2SCAN/def2-SVP SG-2, batched",
+                       "molecules": nm, "npoints": G, "mixed_tiles": info["mixed_tiles"],
+                       "nbasis_total": int(sum(b.nbasis for b in bases)),
+                       "l2": "inputs larger than L2 (FP32 AO store + Z %.1f GB)" % (info["mixed_store_bytes"] / 1e9),
+                       "grid_setup_s": t_grid, "first_build_s": t_first, "tuner": tune,
+                       "plain_fp64_molecules": nfp, "plain_fp64_pts_per_s": plain,
+                       "speedup_vs_plain_fp64": value / plain,
+                       "max_abs_dE_xc_vs_fp64": max(dEs), "max_abs_dV_xc_vs_fp64": max(dVs)},
+            "e2e": {"value": G * args.steps / t_e2e, "unit": UNIT, "h2d_bytes_per_step": 8 * bg.packed_size,
+                    "d2h_bytes_per_step": 8 * (bg.packed_size + nm)},
+            "gpu_launches": args.steps * info["mixed_launches"], "roofline": roof, "clocks": clocks}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -181,9 +313,14 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--cpu-blocks", type=int, default=96)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="c18", choices=["c18", "alkanes64"])
+    ap.add_argument("--fp64-mols", type=int, default=0, help="alkanes64: molecules checked in FP64 (0 = all)")
+    ap.add_argument("--no-tune", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "alkanes64":
+        return run_alkanes(args)
 
     import ctypes
     import torch
@@ -232,6 +369,7 @@ def main():
     grid.profile(True)
     grid.build_device(xc, dD, dE, dV, precision)
     stage = grid.stage_ms()
+    kms = grid.kernel_ms() if precision == PMX else None
     grid.profile(False)
 
     clk_dir = os.path.join(REPO, "gpurun_out") if os.path.isdir(os.path.join(REPO, "gpurun_out")) else os.path.join(REPO, "_work")
@@ -268,18 +406,8 @@ def main():
     peaks = measured_peaks()
 
     if precision == PMX:
-        # algorithmic FLOPs of one contraction: 2 * 128 * sum_t n_t^2 (screened tile sizes);
-        # the tensor core executes 6x that (three-term split cross products)
-        flops = 2.0 * 128 * info["mixed_pairs"]
-        ms_den, ms_fock = stage[0], stage[3]
-        dom, dom_ms = ("density_tc", ms_den) if ms_den >= ms_fock else ("fock_tc", ms_fock)
-        achieved = flops / (dom_ms / 1e3) / 1e12
-        peak = peaks.get("bf16_tflops", 1900.0)
-        roof = {"bound": "tensor", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak, "traffic": None,
-                "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst) -- of measured",
-                "executed_tensor_tflops": 6 * achieved,
-                "stage_ms": {"density": stage[0], "functional": stage[1], "energy": stage[2], "fock": stage[3]}}
+        roof = mixed_roofline(info, kms, stage, peaks, passes_density=4 if xc.type >= 2 else 1,
+                              ncomp_fock=4 if xc.type >= 2 else 1)
     else:
         flops = 2.0 * info["screened_pairs"] * (G / info["nblocks"])
         ms_den, ms_fock = stage[0], stage[3]
@@ -299,15 +427,15 @@ def main():
             "config": {"workload": wl["name"], "precision": args.precision, "npoints": info["npoints"],
                        "npoints_padded": G, "nblocks": info["nblocks"], "nbasis": n,
                        "mixed_tiles": info["mixed_tiles"],
-                       "l2": "inputs larger than L2 (FP64 AO store %.2f GB; split-BF16 stores larger)"
-                             % (info["ao_elements"] * 4 * 8 / 1e9),
+                       "l2": "inputs larger than L2 (FP64 AO store %.2f GB; FP32 AO store + Z %.2f GB)"
+                             % (info["ao_elements"] * 4 * 8 / 1e9, info["mixed_store_bytes"] / 1e9),
                        "plain_fp64_pts_per_s": plain, "plain_fp64_ms_per_build": t_plain / plain_steps * 1e3,
                        "speedup_vs_plain_fp64": value / world / plain,
                        "E_xc_fp64": E64, "E_xc": Emx if precision == PMX else E64,
                        "abs_dE_xc_vs_fp64": abs(Emx - E64),
                        "max_abs_dV_xc_vs_fp64": float((Vmx - V64).abs().max().item())},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 8 * n * n, "d2h_bytes_per_step": 8 * n * n + 8},
-            "gpu_launches": args.steps * (7 if precision == PMX else 4),
+            "gpu_launches": args.steps * (info["mixed_launches"] if precision == PMX else 4),
             "roofline": roof, "clocks": clocks}
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(wl, D, args.cpu_blocks, os.cpu_count() or 1)

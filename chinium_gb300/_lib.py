@@ -29,7 +29,8 @@ class GridInfo(ctypes.Structure):
     _fields_ = [("npoints", ctypes.c_long), ("npoints_padded", ctypes.c_long), ("nblocks", ctypes.c_int),
                 ("nbasis", ctypes.c_int), ("nspin", ctypes.c_int), ("type", ctypes.c_int),
                 ("ao_elements", ctypes.c_long), ("screened_pairs", ctypes.c_long),
-                ("mixed_tiles", ctypes.c_int), ("mixed_pairs", ctypes.c_long)]
+                ("mixed_tiles", ctypes.c_int), ("mixed_pairs", ctypes.c_long), ("mixed_rows", ctypes.c_long),
+                ("mixed_store_bytes", ctypes.c_long), ("mixed_launches", ctypes.c_int)]
 
 
 class MixedConfig(ctypes.Structure):
@@ -100,6 +101,7 @@ SIGNATURES = {
     "xc_eri": [_P, _P, _D],
     "xc_grid_profile": [_P, _I],
     "xc_grid_stage_ms": [_P, _P],
+    "xc_grid_kernel_ms": [_P, _P],
     "xc_grid_create_batch": [_I, _P, _S, _I, _PP],
     "xc_grid_molecules": [_P, _P, _P, _P, _P],
     "xc_grid_set_mixed_config": [_P, _P],

@@ -606,6 +606,10 @@ int xc_grid_info_get(const xc_grid* g, xc_grid_info* info) {
         info->screened_pairs = G.screened_pairs;
         info->mixed_tiles = G.mx.ready ? G.mx.md.ntiles : 0;
         info->mixed_pairs = G.mx.ready ? G.mx.kept_pairs : 0;
+        info->mixed_rows = G.mx.ready ? G.mx.md.rows : 0;
+        info->mixed_store_bytes = G.mx.ready ? (long)(G.mx.d_e32.n + G.mx.d_Z.n) * 4 : 0;
+        // split_d, density passes, combine, functional, energy, then per spin Z / V partials / reduction
+        info->mixed_launches = 1 + G.nspin * (G.type >= 2 ? 4 : 1) + 3 + 3 * G.nspin;
     });
 }
 
@@ -842,6 +846,21 @@ int xc_grid_stage_ms(xc_grid* g, double* ms) {
         for (int i = 0; i < 4; i++) {
             float t = 0;
             CGB_CUDA(cudaEventElapsedTime(&t, G.ev[i], G.ev[i + 1]));
+            ms[i] = t;
+        }
+    });
+}
+
+int xc_grid_kernel_ms(xc_grid* g, double* ms) {
+    return guard([&] {
+        CGB_CHECK(g && ms, XC_ERR_ARG, "null argument");
+        Grid& G = g->g;
+        CGB_CHECK(G.profiling, XC_ERR_STATE, "profiling is off (xc_grid_profile)");
+        CGB_CUDA(cudaEventSynchronize(G.ev[4]));
+        const int order[7] = {0, 1, 2, 3, 5, 6, 4};
+        for (int i = 0; i < 6; i++) {
+            float t = 0;
+            CGB_CUDA(cudaEventElapsedTime(&t, G.ev[order[i]], G.ev[order[i + 1]]));
             ms[i] = t;
         }
     });

@@ -298,7 +298,7 @@ void Grid::prepare_mixed(const MixedConfig& cfg) {
     std::vector<int> doff, dlist;
     m.dens_ctas = std::min((int)dids.size(), nsm);
     lpt(dcost, dids, m.dens_ctas, doff, dlist);
-    CGB_CHECK(rows < (1L << 31) / kTilePts, XC_ERR_UNSUPPORTED, "FP32 AO store rows exceed the 32-bit job index");
+    CGB_CHECK(4 * rows < (1L << 31), XC_ERR_UNSUPPORTED, "FP32 AO store rows exceed the 32-bit TMA row coordinate");
     std::vector<DensJob> djobs;
     for (int t : dlist) djobs.push_back(DensJob{t, m.h_nkept[t], (int)m.h_row[t], c0s[t]});
 
@@ -481,8 +481,10 @@ void Grid::build_mixed(const double* dD, const Functional& f, double* dE, double
     const int ncomp = f.family >= 2 ? 4 : 1;
     for (int s = 0; s < nspin; s++) {
         launch_prep_z(md, f.family, m.fcoef.p + (size_t)s * 5 * Gt, m.d_Z.p, m.d_c2.p, stream);
+        if (s == 0) mark(5);
         launch_fock_tc(m.tm_raw_f, m.tm_z, md.rows, m.fock_ctas, m.d_fock_off.p, m.d_fock_jobs.p, m.d_c2.p, ncomp,
                        m.d_wpart.p, m.d_err.p, stream);
+        if (s == 0) mark(6);
         launch_wsum(m.d_wpart.p, m.d_item_live.p, m.d_mols.p, nmol, maxn, s, nspin, dV, stream);
     }
     mark(4);

@@ -68,7 +68,7 @@ struct Grid {
 
     // stage timing: events bracket density, functional, energy, fock
     bool profiling = false;
-    cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t ev[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     void mark(int i);
     ~Grid();
 

@@ -162,6 +162,13 @@ class Grid:
     def set_stream(self, stream_ptr):
         check(lib().xc_grid_set_stream(self._h, ctypes.c_void_p(stream_ptr)))
 
+    def kernel_ms(self):
+        """[density, functional, energy, Z operand, V partials, V reduction] (ms)
+        of the last profiled mixed build."""
+        ms = np.zeros(6)
+        check(lib().xc_grid_kernel_ms(self._h, _p(ms)))
+        return ms
+
     def sap_fock(self):
         """SuperpositionAtomicPotential (GuessSCF.cpp:17-75)."""
         n = self.nbasis

@@ -122,6 +122,9 @@ typedef struct xc_grid_info {
     long screened_pairs; /* sum over blocks of n_b^2 */
     int mixed_tiles;     /* 128-point tiles of the mixed-precision path (0 before its first build) */
     long mixed_pairs;    /* sum over tiles of (kept functions)^2 */
+    long mixed_rows;     /* kept function rows of all tiles (FP32 AO store: rows x 128 x components) */
+    long mixed_store_bytes; /* device bytes of the FP32 AO store and the per-build Z operand */
+    int mixed_launches;  /* kernels one mixed build launches (for the current type and spins) */
 } xc_grid_info;
 int xc_grid_info_get(const xc_grid* g, xc_grid_info* info);
 /* Padded points in block order: x, y, z, w (each npoints_padded) and
@@ -201,6 +204,11 @@ int xc_build_device(xc_grid* g, xc_functional* f, const double* d_D, int nspin, 
  * [density, functional, energy, fock] in ms[0..3]. */
 int xc_grid_profile(xc_grid* g, int enable);
 int xc_grid_stage_ms(xc_grid* g, double* ms);
+/* Finer device timing of the last profiled mixed build (one spin, restricted
+ * builds): ms[0..5] = [density planes + tensor-core density, functional,
+ * per-molecule E_xc, Z operand, tensor-core V partials, FP64 V reduction].
+ * No reference counterpart. */
+int xc_grid_kernel_ms(xc_grid* g, double* ms);
 
 /* Incremental mixed-precision build for SCF iterations (the per-iteration
  * sequence at Restricted/SP.cpp:52-55, fused).  Densities are linear in D
