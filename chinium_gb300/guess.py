@@ -175,9 +175,21 @@ def supported(Z, basis):
     return all(z in ELEMENTS for z in Z) and basis.name == "def2-svp"
 
 
+def sap_density(grid, H, S, nocc):
+    """Closed-shell density of the SAP guess (GuessSCF.cpp:17-75): occupied
+    orbitals of H + V_SAP in the overlap metric.  The base the network
+    corrects."""
+    F = H + grid.sap_fock()
+    w, V = np.linalg.eigh(S)
+    X = V[:, w > 1e-8] / np.sqrt(w[w > 1e-8])
+    _, C = np.linalg.eigh(X.T @ F @ X)
+    Co = X @ C[:, :nocc]
+    return 2.0 * Co @ Co.T
+
+
 def dataset(Z, xyz, basis, D):
     """Features, local-frame targets and masks for every pair of a molecule
-    with converged total density D."""
+    with (converged - base) total density D."""
     types, first, count = atom_functions(basis)
     X, T, Mk = [], [], []
     for a, b in pairs(xyz):
@@ -209,6 +221,8 @@ class PairMLP:
         check(lib().xc_mlp_nparams(h, ctypes.byref(n)))
         self.nparams = n.value
         self.set_params(params if params is not None else self.init_params(seed))
+        self.residual = False  # True: targets are (converged - SAP) density blocks
+        self.scale = 1.0       # network outputs are targets / scale
 
     def init_params(self, seed):
         rng = np.random.default_rng(seed)
@@ -281,14 +295,18 @@ def train(model, X, T, M, epochs=200, batch=1024, lr=1e-3, seed=0, log=None):
     return losses
 
 
-def predict_density(model, Z, xyz, basis, S, nocc, bf16=True):
-    """Learned closed-shell total density (2 C C^T, idempotent in the S metric)."""
+def predict_density(model, Z, xyz, basis, S, nocc, bf16=True, D_base=None):
+    """Learned closed-shell total density (2 C C^T, idempotent in the S metric):
+    D_base (the SAP density for a residual model) plus the predicted pair
+    blocks, purified."""
     types, first, count = atom_functions(basis)
     pr = pairs(xyz)
     Qs = [pair_frame(xyz, a, b) for a, b in pr]
     X = np.array([pair_features(Z, xyz, a, b, Q) for (a, b), Q in zip(pr, Qs)])
-    Y = model.forward(X, bf16=bf16).reshape(-1, MAX_FUNC, MAX_FUNC)
+    Y = model.forward(X, bf16=bf16).reshape(-1, MAX_FUNC, MAX_FUNC) * model.scale
     n = basis.nbasis
+    if model.residual and D_base is None:
+        raise ValueError("a residual model needs the base (SAP) density")
     D = np.zeros((n, n))
     for (a, b), Q, y in zip(pr, Qs, Y):
         Ua, Ub = atom_rotation(types[a], Q), atom_rotation(types[b], Q)
@@ -297,6 +315,8 @@ def predict_density(model, Z, xyz, basis, S, nocc, bf16=True):
         if a != b:
             D[first[b]:first[b] + count[b], first[a]:first[a] + count[a]] = blk.T
     D = 0.5 * (D + D.T)
+    if model.residual:
+        D = D + D_base
     # purification: occupied natural orbitals in the overlap metric
     w, V = np.linalg.eigh(S)
     Xh = V @ np.diag(w ** -0.5) @ V.T
@@ -306,14 +326,26 @@ def predict_density(model, Z, xyz, basis, S, nocc, bf16=True):
     return 2.0 * Co @ Co.T
 
 
+def guess_density(model, Z, xyz, ctx, bf16=True):
+    """The learned starting density for a molecule whose SCF context (basis,
+    S, H, grid) exists: the SAP base when the model is residual."""
+    nocc = sum(Z) // 2
+    base = sap_density(ctx["grid"], ctx["H"], ctx["S"], nocc) if model.residual else None
+    return predict_density(model, Z, xyz, ctx["basis"], ctx["S"], nocc, bf16=bf16, D_base=base)
+
+
 def save(model, path):
-    np.savez_compressed(path, params=model.params(), shape=np.array([model.nin, model.hidden, model.layers, model.nout]))
+    np.savez_compressed(path, params=model.params(), shape=np.array([model.nin, model.hidden, model.layers, model.nout]),
+                        residual=np.array(int(model.residual)), scale=np.array(model.scale))
 
 
 def load(path):
     d = np.load(path)
     nin, hidden, layers, nout = (int(v) for v in d["shape"])
-    return PairMLP(nin, hidden, layers, nout, params=d["params"])
+    m = PairMLP(nin, hidden, layers, nout, params=d["params"])
+    m.residual = bool(int(d["residual"])) if "residual" in d else False
+    m.scale = float(d["scale"]) if "scale" in d else 1.0
+    return m
 
 
 DEFAULT_WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "guess_water_def2svp.npz")

@@ -33,6 +33,9 @@ def main():
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--functional", default="PBE")
     ap.add_argument("--out", default=G.DEFAULT_WEIGHTS)
+    ap.add_argument("--residual", type=int, default=1, help="learn (converged - SAP) blocks")
+    ap.add_argument("--test-kmax", type=int, default=0)
+    ap.add_argument("--jk", default="cuda", choices=["cpu", "cuda"])
     args = ap.parse_args()
     log = lambda s: print(s, flush=True)
 
@@ -40,10 +43,12 @@ def main():
     train = M.water_clusters(args.train, seed=0, kmin=args.kmin, kmax=args.kmax)
     X, T, Mk = [], [], []
     for i, (Z, xyz) in enumerate(train):
-        r = run_scf(Z, xyz, functional=args.functional, guess="sap")
+        r = run_scf(Z, xyz, functional=args.functional, guess="sap", jk_device=args.jk)
         if not r.converged:
             continue
-        x, t, m = G.dataset(Z, xyz, r.context["basis"], r.D[0])
+        ctx = r.context
+        base = G.sap_density(ctx["grid"], ctx["H"], ctx["S"], sum(Z) // 2) if args.residual else 0.0
+        x, t, m = G.dataset(Z, xyz, ctx["basis"], r.D[0] - base)
         X.append(x)
         T.append(t)
         Mk.append(m)
@@ -54,27 +59,30 @@ def main():
     log("samples %d, data %.1f s" % (len(X), t_data))
 
     model = G.PairMLP(seed=0)
+    model.residual = bool(args.residual)
+    model.scale = float(np.sqrt((T ** 2 * Mk).sum() / Mk.sum()))
     t1 = time.perf_counter()
-    losses = G.train(model, X, T, Mk, epochs=args.epochs, lr=args.lr, log=log)
+    losses = G.train(model, X, T / model.scale, Mk, epochs=args.epochs, lr=args.lr, log=log)
     t_train = time.perf_counter() - t1
     G.save(model, args.out)
 
-    test = M.water_clusters(args.test, seed=1, kmin=args.kmin, kmax=args.kmax)
+    test = M.water_clusters(args.test, seed=1, kmin=args.kmin, kmax=args.test_kmax or args.kmax)
     rows = []
     for Z, xyz in test:
-        r_sap = run_scf(Z, xyz, functional=args.functional, guess="sap")
+        r_sap = run_scf(Z, xyz, functional=args.functional, guess="sap", jk_device=args.jk)
         ctx = r_sap.context
         tg = time.perf_counter()
-        D0 = G.predict_density(model, Z, xyz, ctx["basis"], ctx["S"], sum(Z) // 2)
+        D0 = G.guess_density(model, Z, xyz, ctx)
         t_guess = time.perf_counter() - tg
-        r_ml = run_scf(Z, xyz, functional=args.functional, guess=D0, context=ctx)
+        r_ml = run_scf(Z, xyz, functional=args.functional, guess=D0, context=ctx, jk_device=args.jk)
         it_time = lambda r: r.wall - r.timings["setup"]
+        log("test (%d atoms): SAP %d iterations, learned %d" % (len(Z), r_sap.iterations, r_ml.iterations))
         rows.append(dict(natoms=len(Z), it_sap=r_sap.iterations, it_ml=r_ml.iterations,
                          t_sap=it_time(r_sap), t_ml=it_time(r_ml) + t_guess,
                          dE=r_ml.energy - r_sap.energy, conv=bool(r_sap.converged and r_ml.converged)))
     summary = {
         "train_clusters": len(train), "samples": int(len(X)), "epochs": args.epochs,
-        "final_loss": losses[-1], "first_loss": losses[0], "data_s": t_data, "train_s": t_train,
+        "final_loss": losses[-1], "first_loss": losses[0], "residual": model.residual, "scale": model.scale, "data_s": t_data, "train_s": t_train,
         "test_clusters": len(rows),
         "mean_iterations_sap": float(np.mean([r["it_sap"] for r in rows])),
         "mean_iterations_learned": float(np.mean([r["it_ml"] for r in rows])),

@@ -62,6 +62,39 @@ class JK:
         return (self.K @ D.ravel()).reshape(self.n, self.n)
 
 
+class JKDevice:
+    """Coulomb and exchange matrices from repulsion integrals resident in HBM
+    (two n^2 x n^2 FP64 layouts; each matrix is one matrix-vector product on
+    the GPU).  Caller-side plumbing for the SCF: torch only moves and
+    multiplies the arrays."""
+
+    def __init__(self, eri):
+        import torch
+        self.torch = torch
+        n = eri.shape[0]
+        self.n = n
+        t = torch.from_numpy(np.ascontiguousarray(eri)).cuda()
+        self.J = t.reshape(n * n, n * n)
+        self.K = t.permute(0, 2, 1, 3).contiguous().reshape(n * n, n * n)
+
+    def _mv(self, A, D):
+        torch = self.torch
+        d = torch.from_numpy(np.ascontiguousarray(D).ravel()).cuda()
+        return (A @ d).reshape(self.n, self.n).cpu().numpy()
+
+    def coulomb(self, D):
+        return self._mv(self.J, D)
+
+    def exchange(self, D):
+        return self._mv(self.K, D)
+
+
+def make_jk(eri, device):
+    if device == "cuda":
+        return JKDevice(eri)
+    return JK(eri)
+
+
 class DIIS:
     def __init__(self, size=20):
         self.size = size
@@ -107,12 +140,13 @@ def occupations(Z, charge, mult):
 
 def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, mult=1, precision="fp64",
             guess="sap", conv_energy=1e-8, conv_grad=1e-6, max_iter=100, diis_size=20, screen=0.0,
-            eri_threshold=1e-12, anchor_every=0, context=None, verbose=False):
+            eri_threshold=1e-12, anchor_every=0, context=None, verbose=False, jk_device="cpu"):
     """Kohn-Sham SCF.  precision: "fp64" (plain XC build every iteration) or
     "mixed" (incremental tensor-core XC builds after an FP64 first build).
     guess: "sap", "core", or a density matrix (total for RKS, [Da, Db] for UKS).
     context: reuse integrals and grid from a previous call on the same
-    molecule ({"basis","S","H","jk","grid","Enuc"})."""
+    molecule ({"basis","S","H","jk","grid","Enuc"}).
+    jk_device: "cpu" (numpy) or "cuda" (repulsion integrals kept in HBM)."""
     t_start = time.perf_counter()
     timings = {"setup": 0.0, "xc": 0.0, "jk": 0.0, "diag": 0.0}
     na, nb = occupations(Z, charge, mult)
@@ -123,7 +157,7 @@ def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, m
     if "basis" not in ctx:
         b = Basis(Z, xyz, basis)
         S, T, Vn = one_electron(b)
-        ctx.update(basis=b, S=S, H=T + Vn, jk=JK(repulsion(b, eri_threshold)),
+        ctx.update(basis=b, S=S, H=T + Vn, jk=make_jk(repulsion(b, eri_threshold), jk_device),
                    Enuc=M.nuclear_repulsion(Z, xyz))
     key = ("grid", nspin, functional, grid, screen)
     xc = ExchangeCorrelation(spin=nspin).Read(functional)

@@ -43,3 +43,13 @@ def test_sap_guess_beats_core_guess():
     assert r_sap.converged and r_core.converged
     assert abs(r_sap.energy - r_core.energy) < 1e-7
     assert r_sap.iterations <= r_core.iterations
+
+
+def test_device_jk_matches_host_jk():
+    """J/K from integrals resident in HBM give the same SCF as the host path."""
+    pytest.importorskip("torch")
+    Z, xyz = M.h2o()
+    r_cpu = run_scf(Z, xyz, functional="B3LYP", jk_device="cpu")
+    r_gpu = run_scf(Z, xyz, functional="B3LYP", jk_device="cuda")
+    assert r_cpu.converged and r_gpu.converged
+    assert abs(r_cpu.energy - r_gpu.energy) < 1e-9

@@ -118,8 +118,7 @@ def test_learned_guess_reduces_scf_iterations():
     for Z, xyz in mols:
         r_sap = run_scf(Z, xyz, functional="PBE", guess="sap")
         ctx = r_sap.context
-        nocc = sum(Z) // 2
-        D0 = G.predict_density(model, Z, xyz, ctx["basis"], ctx["S"], nocc)
+        D0 = G.guess_density(model, Z, xyz, ctx)
         r_ml = run_scf(Z, xyz, functional="PBE", guess=D0, context=ctx)
         assert r_sap.converged and r_ml.converged
         assert abs(r_ml.energy - r_sap.energy) < 1e-7
