@@ -595,7 +595,11 @@ __global__ void __launch_bounds__(kThreads, 1) fock_tc_kernel(const __grid_const
             for (int k = 0; k < kFockItems; k++) {
                 const int q = ct + kFockConvThreads * k;
                 if (q >= 1024) break;
-                const int op = q >> 9, rr = (q >> 2) & 127, jj = q & 3;
+                // a quarter-warp covers rows r and r + 4 (4 chunks each): its 16-byte
+                // stores land in 8 distinct swizzle slots, and lanes of the second row
+                // read the other 16-byte half first, so both reads are conflict-free
+                const int op = q >> 9, jj = q & 3, odd = (q >> 2) & 1;
+                const int rr = ((q & 511) >> 5) * 8 + odd * 4 + ((q >> 3) & 3);
                 const int box = op * 2 + (rr >> 6);
                 float v[8];
                 if (c.slot(box) < 0) {
@@ -603,7 +607,8 @@ __global__ void __launch_bounds__(kThreads, 1) fock_tc_kernel(const __grid_const
                     for (int i = 0; i < 8; i++) v[i] = 0.f;
                 } else {
                     const uint32_t src = rb + box * kRawBox + (rr & 63) * 128 + jj * 32;
-                    const float4 a = tc::lds128f(src), b4 = tc::lds128f(src + 16);
+                    const float4 x0 = tc::lds128f(src + odd * 16), x1 = tc::lds128f(src + (odd ^ 1) * 16);
+                    const float4 a = odd ? x1 : x0, b4 = odd ? x0 : x1;
                     v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
                     v[4] = b4.x; v[5] = b4.y; v[6] = b4.z; v[7] = b4.w;
                     if (op == 1 && c.c > 0) {

@@ -64,31 +64,49 @@ def solid_harmonics(l, xyz):
 
 
 _RNG_PTS = np.random.default_rng(12345).normal(size=(32, 3))
+_BPINV = {}
+
+
+def _sample_pinv(l):
+    if l not in _BPINV:
+        _BPINV[l] = np.linalg.pinv(solid_harmonics(l, _RNG_PTS))
+    return _BPINV[l]
+
+
+def shell_rotations(shell_type, Qs):
+    """U_p with f_local = U_p f_global for the functions of one shell, for
+    frames Qs (P, 3, 3) whose columns are the local axes in global
+    coordinates: S(Q^T r) = U S(r), fitted on 32 sample points."""
+    P = len(Qs)
+    if shell_type == 0:
+        return np.ones((P, 1, 1))
+    if shell_type == 1:  # Cartesian x, y, z
+        return np.ascontiguousarray(np.transpose(Qs, (0, 2, 1)))
+    l = -shell_type
+    pts = np.einsum("kj,pjm->pkm", _RNG_PTS, Qs).reshape(-1, 3)  # rows r^T Q
+    A = solid_harmonics(l, pts).reshape(2 * l + 1, P, len(_RNG_PTS)).transpose(1, 0, 2)
+    return A @ _sample_pinv(l)
+
+
+def atom_rotations(shell_types, Qs):
+    """Block-diagonal rotation of all functions of one atom, (P, n, n)."""
+    blocks = [shell_rotations(t, Qs) for t in shell_types]
+    n = sum(b.shape[1] for b in blocks)
+    U = np.zeros((len(Qs), n, n))
+    o = 0
+    for b in blocks:
+        k = b.shape[1]
+        U[:, o:o + k, o:o + k] = b
+        o += k
+    return U
 
 
 def shell_rotation(shell_type, Q):
-    """U with f_local = U f_global for the functions of one shell, where the
-    local frame has axes Q[:, 0..2] (columns) in global coordinates."""
-    if shell_type == 0:
-        return np.ones((1, 1))
-    if shell_type == 1:  # Cartesian x, y, z
-        return Q.T.copy()
-    l = -shell_type
-    B = solid_harmonics(l, _RNG_PTS)
-    A = solid_harmonics(l, _RNG_PTS @ Q)  # S(Q^T r) for each sample r
-    return A @ np.linalg.pinv(B)
+    return shell_rotations(shell_type, Q[None])[0]
 
 
 def atom_rotation(shell_types, Q):
-    blocks = [shell_rotation(t, Q) for t in shell_types]
-    n = sum(b.shape[0] for b in blocks)
-    U = np.zeros((n, n))
-    o = 0
-    for b in blocks:
-        k = b.shape[0]
-        U[o:o + k, o:o + k] = b
-        o += k
-    return U
+    return atom_rotations(shell_types, Q[None])[0]
 
 
 # -------------------------------------------------------------- geometry
@@ -108,7 +126,8 @@ def _by_distance(d, exclude):
     """Atom indices by distance; distances equal to 1e-6 bohr (symmetric
     neighbours, e.g. the two hydrogens of a water) tie-break by index, so the
     order does not depend on rounding or on the molecule's orientation."""
-    return [i for i in sorted(range(len(d)), key=lambda i: (round(float(d[i]), 6), i)) if i not in exclude]
+    order = np.lexsort((np.arange(len(d)), np.round(d, 6)))
+    return [int(i) for i in order if i not in exclude]
 
 
 def pair_frame(xyz, a, b):
@@ -147,6 +166,52 @@ def pair_features(Z, xyz, a, b, Q):
     return np.array(f, dtype=np.float32)
 
 
+def frames_and_features(Z, xyz, pr):
+    """pair_frame and pair_features for every pair at once: frames (P, 3, 3)
+    and features (P, NIN), identical to the per-pair functions."""
+    xyz = np.asarray(xyz, dtype=np.float64)
+    Z = np.asarray(Z)
+    n = len(xyz)
+    dist = np.linalg.norm(xyz[:, None, :] - xyz[None, :, :], axis=2)
+    orders = [np.lexsort((np.arange(n), np.round(dist[a], 6))) for a in range(n)]
+    P = len(pr)
+    A = np.array([a for a, _ in pr])
+    B = np.array([b for _, b in pr])
+    neigh = -np.ones((P, N_NEIGH + 2), dtype=np.int64)
+    for p, (a, b) in enumerate(pr):
+        o = [int(i) for i in orders[a] if i != a and i != b][:N_NEIGH + 2]
+        neigh[p, :len(o)] = o
+    ra = xyz[A]
+    same = A == B
+    # frame: z along a->b (on site: toward the nearest neighbour), x toward the next reference atom
+    ez = np.where(same[:, None], xyz[np.maximum(neigh[:, 0], 0)] - ra, xyz[B] - ra)
+    ref_idx = np.where(same, neigh[:, 1], neigh[:, 0])
+    ref = np.where((ref_idx >= 0)[:, None], xyz[np.maximum(ref_idx, 0)] - ra, np.array([1.0, 0.0, 0.0]))
+    lone = same & (neigh[:, 0] < 0)
+    ez = ez / np.linalg.norm(np.where(lone[:, None], 1.0, ez), axis=1, keepdims=True)
+    v = ref - np.sum(ref * ez, axis=1, keepdims=True) * ez
+    alt = np.where((np.abs(ez[:, 0]) < 0.9)[:, None], np.array([1.0, 0.0, 0.0]), np.array([0.0, 1.0, 0.0]))
+    valt = alt - np.sum(alt * ez, axis=1, keepdims=True) * ez
+    v = np.where((np.linalg.norm(v, axis=1) < 1e-6)[:, None], valt, v)
+    ex = v / np.linalg.norm(v, axis=1, keepdims=True)
+    ey = np.cross(ez, ex)
+    Qs = np.stack([ex, ey, ez], axis=2)
+    Qs[lone] = np.eye(3)
+    # features
+    oh = lambda zz: np.stack([(zz == e).astype(np.float64) for e in ELEMENTS], axis=1)
+    dab = dist[A, B]
+    cols = [oh(Z[A]), oh(Z[B]), same[:, None].astype(np.float64), dab[:, None], np.exp(-dab)[:, None]]
+    for k in range(N_NEIGH):
+        i = neigh[:, k]
+        ok = (i >= 0)[:, None]
+        ii = np.maximum(i, 0)
+        di = dist[A, ii]
+        w = _cut(di)
+        loc = np.einsum("pji,pj->pi", Qs, xyz[ii] - ra) * w[:, None]
+        cols += [np.where(ok, loc, 0.0), np.where(ok, (w / (1.0 + di))[:, None], 0.0), np.where(ok, oh(Z[ii]), 0.0)]
+    return Qs, np.concatenate(cols, axis=1).astype(np.float32)
+
+
 def atom_functions(basis):
     sh = basis.shells()
     natoms = len(basis.Z)
@@ -162,13 +227,10 @@ def atom_functions(basis):
 
 
 def pairs(xyz):
-    n = len(xyz)
-    out = []
-    for a in range(n):
-        for b in range(a, n):
-            if np.linalg.norm(xyz[a] - xyz[b]) < CUTOFF:
-                out.append((a, b))
-    return out
+    xyz = np.asarray(xyz, dtype=np.float64)
+    d = np.linalg.norm(xyz[:, None, :] - xyz[None, :, :], axis=2)
+    a, b = np.nonzero(np.triu(d < CUTOFF))
+    return [(int(i), int(j)) for i, j in zip(a, b)]
 
 
 def supported(Z, basis):
@@ -191,20 +253,36 @@ def dataset(Z, xyz, basis, D):
     """Features, local-frame targets and masks for every pair of a molecule
     with (converged - base) total density D."""
     types, first, count = atom_functions(basis)
+    pr = pairs(xyz)
+    Qs, Xf = frames_and_features(Z, xyz, pr)
+    Ua, Ub = _pair_rotations(types, pr, Qs)
     X, T, Mk = [], [], []
-    for a, b in pairs(xyz):
-        Q = pair_frame(xyz, a, b)
-        Ua, Ub = atom_rotation(types[a], Q), atom_rotation(types[b], Q)
+    for p, ((a, b), Q) in enumerate(zip(pr, Qs)):
         blk = D[first[a]:first[a] + count[a], first[b]:first[b] + count[b]]
-        loc = Ua @ blk @ Ub.T
+        loc = Ua[p] @ blk @ Ub[p].T
         t = np.zeros((MAX_FUNC, MAX_FUNC), dtype=np.float32)
         m = np.zeros_like(t)
         t[:count[a], :count[b]] = loc
         m[:count[a], :count[b]] = 1.0
-        X.append(pair_features(Z, xyz, a, b, Q))
+        X.append(Xf[p])
         T.append(t.ravel())
         Mk.append(m.ravel())
     return np.array(X), np.array(T), np.array(Mk)
+
+
+def _pair_rotations(types, pr, Qs):
+    """Per pair (a, b): the atom rotations of a and b in the pair's frame,
+    computed in one batch per distinct shell layout."""
+    Ua, Ub = [None] * len(pr), [None] * len(pr)
+    for side, out in ((0, Ua), (1, Ub)):
+        groups = {}
+        for p, ab in enumerate(pr):
+            groups.setdefault(tuple(types[ab[side]]), []).append(p)
+        for layout, idx in groups.items():
+            U = atom_rotations(list(layout), Qs[idx])
+            for k, p in enumerate(idx):
+                out[p] = U[k]
+    return Ua, Ub
 
 
 # ------------------------------------------------------------------ network
@@ -301,15 +379,14 @@ def predict_density(model, Z, xyz, basis, S, nocc, bf16=True, D_base=None):
     blocks, purified."""
     types, first, count = atom_functions(basis)
     pr = pairs(xyz)
-    Qs = [pair_frame(xyz, a, b) for a, b in pr]
-    X = np.array([pair_features(Z, xyz, a, b, Q) for (a, b), Q in zip(pr, Qs)])
+    Qs, X = frames_and_features(Z, xyz, pr)
     Y = model.forward(X, bf16=bf16).reshape(-1, MAX_FUNC, MAX_FUNC) * model.scale
+    Uas, Ubs = _pair_rotations(types, pr, Qs)
     n = basis.nbasis
     if model.residual and D_base is None:
         raise ValueError("a residual model needs the base (SAP) density")
     D = np.zeros((n, n))
-    for (a, b), Q, y in zip(pr, Qs, Y):
-        Ua, Ub = atom_rotation(types[a], Q), atom_rotation(types[b], Q)
+    for (a, b), Ua, Ub, y in zip(pr, Uas, Ubs, Y):
         blk = Ua.T @ y[:count[a], :count[b]].astype(np.float64) @ Ub
         D[first[a]:first[a] + count[a], first[b]:first[b] + count[b]] = blk
         if a != b:

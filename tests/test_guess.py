@@ -126,3 +126,17 @@ def test_learned_guess_reduces_scf_iterations():
         it_ml.append(r_ml.iterations)
     print("iterations SAP", it_sap, "learned", it_ml)
     assert np.mean(it_ml) < np.mean(it_sap)
+
+
+def test_batched_frames_and_features_match_per_pair():
+    Z, xyz = M.water_cluster(5, np.random.default_rng(11))
+    pr = G.pairs(xyz)
+    Qs, X = G.frames_and_features(Z, xyz, pr)
+    for p in range(0, len(pr), 7):
+        a, b = pr[p]
+        Q = G.pair_frame(xyz, a, b)
+        assert np.allclose(Qs[p], Q, atol=1e-12)
+        assert np.allclose(X[p], G.pair_features(Z, xyz, a, b, Q), atol=1e-6)
+    # a lone atom has an identity frame
+    Qs1, X1 = G.frames_and_features([8], np.zeros((1, 3)), [(0, 0)])
+    assert np.allclose(Qs1[0], np.eye(3)) and np.allclose(Qs1[0], G.pair_frame(np.zeros((1, 3)), 0, 0))
