@@ -28,11 +28,16 @@ METRIC = "XC grid-pts/s (one B3LYP/def2-TZVP XC build of C18 on SG-2)"
 UNIT = "grid-points/s"
 
 
-def workload():
+def workload(name="c18"):
     from chinium_gb300 import molecules as M
+    if name == "fe4s4":
+        Z, xyz = M.fe4s4()
+        return dict(name="Fe4S4 UKS TPSS/def2-TZVP SG-3, multiplicity 9", Z=Z, xyz=xyz, basis="def2-tzvp",
+                    grid="SG-3", functional="TPSS", nspin=2, nocc=(88, 80),
+                    metric="XC grid-pts/s (one UKS TPSS/def2-TZVP XC build of Fe4S4 on SG-3)")
     Z, xyz = M.c18()
     return dict(name="C18 RKS B3LYP/def2-TZVP SG-2", Z=Z, xyz=xyz, basis="def2-tzvp", grid="SG-2",
-                functional="B3LYP", ids=[402], nocc=54)
+                functional="B3LYP", ids=[402], nspin=1, nocc=54, metric=METRIC)
 
 
 def model_density(nbasis, nocc, seed=0):
@@ -370,7 +375,7 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--cpu-blocks", type=int, default=96)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="c18", choices=["c18", "alkanes64", "scf-water"])
+    ap.add_argument("--workload", default="c18", choices=["c18", "fe4s4", "alkanes64", "scf-water"])
     ap.add_argument("--scf-mols", type=int, default=4)
     ap.add_argument("--fp64-mols", type=int, default=0, help="alkanes64: molecules checked in FP64 (0 = all)")
     ap.add_argument("--no-tune", action="store_true")
@@ -395,11 +400,12 @@ def main():
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
 
-    wl = workload()
+    wl = workload(args.workload)
+    ns = wl["nspin"]
     basis = cg.Basis(wl["Z"], wl["xyz"], wl["basis"])
     n = basis.nbasis
-    grid = cg.Grid(basis, wl["grid"], nspin=1, screen_threshold=0.0)
-    xc = cg.ExchangeCorrelation().Read(wl["functional"])
+    grid = cg.Grid(basis, wl["grid"], nspin=ns, screen_threshold=0.0)
+    xc = cg.ExchangeCorrelation(spin=ns).Read(wl["functional"])
     grid.setType(xc.type)
     grid.getAO(0)
     stream = torch.cuda.Stream()
@@ -407,10 +413,16 @@ def main():
     P64, PMX = cg.PRECISION_FP64, cg.PRECISION_MIXED
     precision = P64 if args.precision == "fp64" else PMX
 
-    D = model_density(n, wl["nocc"])
-    dD = torch.from_numpy(np.ascontiguousarray(D.T)).cuda()
+    if ns == 1:
+        D = model_density(n, wl["nocc"])
+        Dst = np.ascontiguousarray(D.T)[None]
+    else:  # one-spin densities C_s C_s^T of an open-shell occupation
+        Dsp = [0.5 * model_density(n, no, seed=k) for k, no in enumerate(wl["nocc"])]
+        D = Dsp[0] + Dsp[1]
+        Dst = np.ascontiguousarray(np.stack([d.T for d in Dsp]))
+    dD = torch.from_numpy(Dst).cuda()
     dE = torch.zeros(1, dtype=torch.float64, device="cuda")
-    dV = torch.zeros((n, n), dtype=torch.float64, device="cuda")
+    dV = torch.zeros((ns, n, n), dtype=torch.float64, device="cuda")
 
     # plain FP64 path on the same density: reference numbers and throughput
     grid.build_device(xc, dD, dE, dV, P64)
@@ -448,13 +460,13 @@ def main():
     clocks = clocks_stop(cp, cf, clk_path) if rank == 0 else None
 
     # end to end through the public host-buffer call: pinned D in, E and V out
-    Dh = torch.from_numpy(np.ascontiguousarray(D)).pin_memory()
-    Vh = torch.zeros((n, n), dtype=torch.float64).pin_memory()
+    Dh = torch.from_numpy(Dst).pin_memory()
+    Vh = torch.zeros((ns, n, n), dtype=torch.float64).pin_memory()
     Eh = ctypes.c_double()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        check(lib().xc_build(grid._h, xc._h, ctypes.c_void_p(Dh.data_ptr()), 1, precision, ctypes.byref(Eh),
+        check(lib().xc_build(grid._h, xc._h, ctypes.c_void_p(Dh.data_ptr()), ns, precision, ctypes.byref(Eh),
                              ctypes.c_void_p(Vh.data_ptr())))
     torch.cuda.synchronize()
     t_e2e = time.perf_counter() - t0
@@ -466,7 +478,7 @@ def main():
     peaks = measured_peaks()
 
     if precision == PMX:
-        roof = mixed_roofline(info, kms, stage, peaks, passes_density=4 if xc.type >= 2 else 1,
+        roof = mixed_roofline(info, kms, stage, peaks, passes_density=(4 if xc.type >= 2 else 1) * ns,
                               ncomp_fock=4 if xc.type >= 2 else 1)
     else:
         flops = 2.0 * info["screened_pairs"] * (G / info["nblocks"])
@@ -479,7 +491,7 @@ def main():
                 "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (no FP64 entry in MEASURED_PEAKS.json)",
                 "stage_ms": {"density": stage[0], "functional": stage[1], "energy": stage[2], "fock": stage[3]}}
 
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+    line = {"metric": wl["metric"], "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_dev / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if precision == P64 else "bf16x3 (split) + f64 accumulation",
@@ -494,10 +506,11 @@ def main():
                        "E_xc_fp64": E64, "E_xc": Emx if precision == PMX else E64,
                        "abs_dE_xc_vs_fp64": abs(Emx - E64),
                        "max_abs_dV_xc_vs_fp64": float((Vmx - V64).abs().max().item())},
-            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 8 * n * n, "d2h_bytes_per_step": 8 * n * n + 8},
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 8 * ns * n * n,
+                    "d2h_bytes_per_step": 8 * ns * n * n + 8},
             "gpu_launches": args.steps * (info["mixed_launches"] if precision == PMX else 4),
             "roofline": roof, "clocks": clocks}
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and not args.no_cpu_baseline and ns == 1:
         line["cpu_baseline"] = cpu_baseline(wl, D, args.cpu_blocks, os.cpu_count() or 1)
     if rank == 0:
         print(json.dumps(line), flush=True)
