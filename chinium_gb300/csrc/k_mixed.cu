@@ -418,10 +418,15 @@ __global__ void __launch_bounds__(kThreads, 1) density_tc_kernel(const __grid_co
 // chunks disjoint).  A half-stage is (component c, point half kh, K-half
 // hk); a tile is one accumulation unit; an item's last tile writes W_IJ.
 // Warps 2-15 convert; warps 4-11 also drain the accumulator of each tile.
+//
+// The meta-GGA part sum_r d_r phi^T c2 d_r phi of W is symmetric, so only
+// items with I <= J carry components 1..3, with c2 doubled when I < J
+// (job flags kTauItem, kTauDouble); V = W + W^T then receives it once.
+constexpr int kTauItem = 4, kTauDouble = 8;
 
 // Position in the half-stage sequence of one CTA (host-made job list).
 struct FockCursor {
-    int j, end, c, kh, hk, ncomp;
+    int j, end, c, kh, hk, ncomp, nc_all;
     FockJob job;
     __device__ void load(const FockJob* jobs) {
         const int4* p = reinterpret_cast<const int4*>(jobs + j);
@@ -434,11 +439,13 @@ struct FockCursor {
         job.sb1 = b.y;
         job.item = b.z;
         job.flags = b.w;
+        ncomp = (job.flags & kTauItem) ? nc_all : 1;
     }
     __device__ FockCursor(const int* off, const FockJob* jobs, int nc) {
         j = off[blockIdx.x];
         end = off[blockIdx.x + 1];
-        ncomp = nc;
+        nc_all = nc;
+        ncomp = 1;
         c = kh = hk = 0;
         if (j < end) load(jobs);
     }
@@ -615,8 +622,9 @@ __global__ void __launch_bounds__(kThreads, 1) fock_tc_kernel(const __grid_const
                         const float* cp = c2 + (size_t)c.job.t * 128 + c.kh * 64 + h * 32 + 8 * jj;
                         const float4 ca = __ldg(reinterpret_cast<const float4*>(cp));
                         const float4 cb = __ldg(reinterpret_cast<const float4*>(cp + 4));
-                        v[0] *= ca.x; v[1] *= ca.y; v[2] *= ca.z; v[3] *= ca.w;
-                        v[4] *= cb.x; v[5] *= cb.y; v[6] *= cb.z; v[7] *= cb.w;
+                        const float f = (c.job.flags & kTauDouble) ? 2.f : 1.f;  // exact scaling
+                        v[0] *= f * ca.x; v[1] *= f * ca.y; v[2] *= f * ca.z; v[3] *= f * ca.w;
+                        v[4] *= f * cb.x; v[5] *= f * cb.y; v[6] *= f * cb.z; v[7] *= f * cb.w;
                     }
                 }
                 store_chunk(ssm + (op ? 3 * kPlaneA : 0), rr, 4 * h + jj, v);

@@ -330,7 +330,7 @@ void Grid::prepare_mixed(const MixedConfig& cfg) {
                                   (slot(t, 2 * J) >= 0 || slot(t, 2 * J + 1) >= 0);
                     if (wanted) fids.push_back((int)items.size());
                     live.push_back(wanted > 0);
-                    fcost.push_back(wanted);
+                    fcost.push_back(wanted * (type >= 2 && I <= J ? 4 : 1));
                     items.push_back(it);
                 }
     }
@@ -350,7 +350,8 @@ void Grid::prepare_mixed(const MixedConfig& cfg) {
                 const int sa0 = slot(t, 2 * it.I), sa1 = slot(t, 2 * it.I + 1);
                 const int sb0 = slot(t, 2 * it.J), sb1 = slot(t, 2 * it.J + 1);
                 if ((sa0 < 0 && sa1 < 0) || (sb0 < 0 && sb1 < 0)) continue;
-                fjobs.push_back(FockJob{t, (int)m.h_row[t], sa0, sa1, sb0, sb1, id, 0});
+                const int tau = (it.I <= it.J ? 4 : 0) | (it.I < it.J ? 8 : 0);
+                fjobs.push_back(FockJob{t, (int)m.h_row[t], sa0, sa1, sb0, sb1, id, tau});
             }
             fjobs[first].flags |= 1;
             fjobs.back().flags |= 2;

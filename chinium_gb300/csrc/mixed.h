@@ -57,7 +57,9 @@ struct DensJob {
 };
 
 // One (item, wanted tile) of a CTA's V work list: slots of chunks 2I, 2I+1,
-// 2J, 2J+1 (-1 if dropped); flags 1: first tile of the item, 2: last.
+// 2J, 2J+1 (-1 if dropped); flags 1: first tile of the item, 2: last,
+// 4: the item carries the meta-GGA components (I <= J), 8: with c2 doubled
+// (I < J).
 struct FockJob {
     int t, trow, sa0, sa1, sb0, sb1, item, flags;
 };
