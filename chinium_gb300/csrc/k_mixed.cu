@@ -184,14 +184,14 @@ __device__ __forceinline__ void mma_stage(uint32_t tmem, int buf, uint8_t* st, b
 
 // Drain columns half*64 .. half*64 + 63 of TMEM buffer `buf` (hh +
 // corrections) into acc[64] (this thread's lane).
-__device__ __forceinline__ void drain(uint32_t tmem, int buf, int quad, int half, float* acc) {
+__device__ __forceinline__ void drain(uint32_t tmem, int buf, int quad, int half, float* acc, float w = 1.f) {
     const uint32_t base = tmem + ((uint32_t)(quad * 32) << 16) + buf * 256 + half * 64;
 #pragma unroll
     for (int c16 = 0; c16 < 4; c16++) {
         float a[16], b[16];
         tc::tmem_ld16x2_nomem(base + c16 * 16, base + 128 + c16 * 16, a, b);
 #pragma unroll
-        for (int j = 0; j < 16; j++) acc[c16 * 16 + j] += a[j] + b[j];
+        for (int j = 0; j < 16; j++) acc[c16 * 16 + j] += w * (a[j] + b[j]);
     }
 }
 
@@ -203,10 +203,14 @@ __device__ __forceinline__ void drain(uint32_t tmem, int buf, int quad, int half
 // AO values of their slot.  The two column halves of a row write separate
 // partial outputs (rho / rho_b ...), summed by combine_kernel.
 // EPI 0: rho; 1: rho + grad rho; 2: tau contribution of A component acomp.
+// rho and tau are symmetric in (mu, nu): their nu block vb only takes mu
+// chunks from its own first slot on, and units of later chunks count twice
+// (the mirrored pairs of later nu blocks are skipped).  grad rho is not.
 
 // Position in the density unit sequence of one CTA (host-made job list).
 struct DensCursor {
     int j, end, vb, kc;
+    bool sym;
     DensJob job;
     __device__ void load(const DensJob* jobs) {
         const int4 r = __ldg(reinterpret_cast<const int4*>(jobs) + j);
@@ -215,20 +219,25 @@ struct DensCursor {
         job.trow = r.z;
         job.c0 = r.w;
     }
-    __device__ DensCursor(const int* off, const DensJob* jobs) {
+    __device__ DensCursor(const int* off, const DensJob* jobs, bool symmetric) {
         j = off[blockIdx.x];
         end = off[blockIdx.x + 1];
         vb = kc = 0;
+        sym = symmetric;
         job = DensJob{0, 1, 0, 0};
         if (j < end) load(jobs);
     }
     __device__ bool valid() const { return j < end; }
     __device__ int nvb() const { return (job.nk + 1) / 2; }
+    // weight of the current unit in T (exact in FP32)
+    __device__ float weight() const { return (sym && kc >= 2 * vb + 2) ? 2.f : 1.f; }
     __device__ void advance(const DensJob* jobs) {
         if (++kc < job.nk) return;
-        kc = 0;
-        if (++vb < nvb()) return;
-        vb = 0;
+        if (++vb < nvb()) {
+            kc = sym ? 2 * vb : 0;
+            return;
+        }
+        vb = kc = 0;
         if (++j < end) load(jobs);
     }
 };
@@ -261,7 +270,7 @@ __global__ void __launch_bounds__(kThreads, 1) density_tc_kernel(const __grid_co
     if (warp == 0) {
         if (lane == 0) {
             uint32_t uu = 0;
-            for (DensCursor c(job_off, jobs); c.valid(); c.advance(jobs), uu++) {
+            for (DensCursor c(job_off, jobs, EPI != 1); c.valid(); c.advance(jobs), uu++) {
                 if (c.vb == 0 && c.kc == 0) {  // new tile: its kept chunk ids
                     const int* src = md.tile_chunks + (size_t)c.job.t * md.nchunk;
                     for (int k = 0; k < c.job.nk; k++) s_chunks[k] = __ldg(src + k);
@@ -295,7 +304,7 @@ __global__ void __launch_bounds__(kThreads, 1) density_tc_kernel(const __grid_co
     } else if (warp == 1) {
         if (lane == 0) {
             uint32_t uu = 0;
-            for (DensCursor c(job_off, jobs); c.valid(); c.advance(jobs), uu++) {
+            for (DensCursor c(job_off, jobs, EPI != 1); c.valid(); c.advance(jobs), uu++) {
                 const int s = uu & 1, b = uu & 1;
                 const uint32_t ph = (uu >> 1) & 1;
                 if (sm.abort || !tc::mbar_wait(&sm.tempty[b], ph ^ 1) || !tc::mbar_wait(&sm.full[s], ph)) {
@@ -322,7 +331,7 @@ __global__ void __launch_bounds__(kThreads, 1) density_tc_kernel(const __grid_co
         for (int j = 0; j < 64; j++) T[j] = 0.f;
         double acc_r = 0, acc_g0 = 0, acc_g1 = 0, acc_g2 = 0, acc_t = 0;
         uint32_t uu = 0;
-        for (DensCursor c(job_off, jobs); c.valid(); c.advance(jobs), uu++) {
+        for (DensCursor c(job_off, jobs, EPI != 1); c.valid(); c.advance(jobs), uu++) {
             const int b = uu & 1;
             if (sm.abort) break;
             if (!tc::mbar_wait(&sm.tfull[b], (uu >> 1) & 1)) {
@@ -330,7 +339,7 @@ __global__ void __launch_bounds__(kThreads, 1) density_tc_kernel(const __grid_co
                 break;
             }
             tc::fence_after_sync();
-            drain(tmem, b, quad, half, T);
+            drain(tmem, b, quad, half, T, c.weight());
             tc::fence_before_sync();
             mbar_arrive(&sm.tempty[b]);
             if (c.kc != c.job.nk - 1) continue;
@@ -379,7 +388,7 @@ __global__ void __launch_bounds__(kThreads, 1) density_tc_kernel(const __grid_co
         // and stored transposed (point-major) as the stage's A planes
         const int ct = conv_index() * 32 + lane;
         uint32_t uu = 0;
-        for (DensCursor c(job_off, jobs); c.valid(); c.advance(jobs), uu++) {
+        for (DensCursor c(job_off, jobs, EPI != 1); c.valid(); c.advance(jobs), uu++) {
             if (!warp_wait(sm, &sm.rfull[0], uu & 1, err)) break;
             float v[kDensItems][8];
             const uint32_t rf = ssm + 2 * kStageBytes;
@@ -697,7 +706,8 @@ __global__ void wsum_kernel(const double* __restrict__ wpart, const int* __restr
 }
 
 // Packed D_m (s, n, n) column-major FP64 -> three BF16 planes per spin of the
-// strip: row f0(m) + nu, col mu (zero outside the molecule's n x n block).
+// strip: row f0(m) + nu, col mu, of (D + D^T) / 2 (zero outside the
+// molecule's n x n block).
 __global__ void split_d_kernel(const double* __restrict__ D, const MolRange* __restrict__ mols, int nmol, int nspin,
                                long drows, int dcols, bf16* __restrict__ Dp) {
     const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -714,7 +724,9 @@ __global__ void split_d_kernel(const double* __restrict__ D, const MolRange* __r
     }
     const MolRange& m = mols[lo];
     const long nu = row - m.f0;
-    const double v = (mu < m.n && nu < m.n) ? D[m.voff + (long)s * m.n * m.n + nu * m.n + mu] : 0.0;
+    // symmetric part (the tensor-core density uses one triangle of D for rho and tau)
+    const double* Ds = D + m.voff + (long)s * m.n * m.n;
+    const double v = (mu < m.n && nu < m.n) ? 0.5 * (Ds[nu * m.n + mu] + Ds[(long)mu * m.n + nu]) : 0.0;
     bf16 h, md_, l;
     tc::split3(v, h, md_, l);
     const size_t plane = (size_t)drows * dcols;
