@@ -426,3 +426,12 @@ def load(path):
 
 
 DEFAULT_WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "guess_water_def2svp.npz")
+_DEFAULT = None
+
+
+def default_model():
+    """The packaged network (loaded once per process)."""
+    global _DEFAULT
+    if _DEFAULT is None:
+        _DEFAULT = load(DEFAULT_WEIGHTS)
+    return _DEFAULT

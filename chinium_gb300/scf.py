@@ -143,7 +143,10 @@ def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, m
             eri_threshold=1e-12, anchor_every=0, context=None, verbose=False, jk_device="cpu"):
     """Kohn-Sham SCF.  precision: "fp64" (plain XC build every iteration) or
     "mixed" (incremental tensor-core XC builds after an FP64 first build).
-    guess: "sap", "core", or a density matrix (total for RKS, [Da, Db] for UKS).
+    guess: "sap", "core", "learned" (the per-atom-pair network, with the SAP
+    guess as fallback: for molecules outside the model's elements / basis, for
+    open shells, and when the SCF started from it has not converged within
+    half of max_iter), or a density matrix (total for RKS, [Da, Db] for UKS).
     context: reuse integrals and grid from a previous call on the same
     molecule ({"basis","S","H","jk","grid","Enuc"}).
     jk_device: "cpu" (numpy) or "cuda" (repulsion integrals kept in HBM)."""
@@ -176,6 +179,26 @@ def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, m
     def solve(F):
         e, Cp = np.linalg.eigh(X.T @ F @ X)
         return e, X @ Cp
+
+    if isinstance(guess, str) and guess == "learned":
+        from . import guess as G
+        kw = dict(basis=basis, functional=functional, grid=grid, charge=charge, mult=mult, precision=precision,
+                  conv_energy=conv_energy, conv_grad=conv_grad, diis_size=diis_size, screen=screen,
+                  eri_threshold=eri_threshold, anchor_every=anchor_every, context=ctx, verbose=verbose,
+                  jk_device=jk_device)
+        if unrestricted or charge != 0 or not G.supported(Z, b):
+            r = run_scf(Z, xyz, guess="sap", max_iter=max_iter, **kw)
+            r["guess_used"] = "sap (outside the learned model's scope)"
+            return r
+        D0 = G.guess_density(G.default_model(), Z, xyz, ctx)
+        r = run_scf(Z, xyz, guess=D0, max_iter=max(1, max_iter // 2), **kw)
+        if r.converged:
+            r["guess_used"] = "learned"
+            r["wall"] += timings["setup"]
+            return r
+        r2 = run_scf(Z, xyz, guess="sap", max_iter=max_iter, **kw)
+        r2["guess_used"] = "sap (learned start did not converge in %d iterations)" % r.iterations
+        return r2
 
     # initial guess
     if isinstance(guess, str):
@@ -248,4 +271,5 @@ def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, m
         timings["diag"] += time.perf_counter() - t0
     wall = time.perf_counter() - t_start
     return Result(energy=E, converged=converged, iterations=it, wall=wall, timings=timings, D=Ds,
-                  history=history, Exc=Exc, context=ctx, nbasis=n)
+                  history=history, Exc=Exc, context=ctx, nbasis=n,
+                  guess_used=guess if isinstance(guess, str) else "caller density")

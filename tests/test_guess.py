@@ -140,3 +140,20 @@ def test_batched_frames_and_features_match_per_pair():
     # a lone atom has an identity frame
     Qs1, X1 = G.frames_and_features([8], np.zeros((1, 3)), [(0, 0)])
     assert np.allclose(Qs1[0], np.eye(3)) and np.allclose(Qs1[0], G.pair_frame(np.zeros((1, 3)), 0, 0))
+
+
+@pytest.mark.gpu
+def test_learned_guess_with_sap_fallback_in_scf():
+    """guess="learned" in the SCF driver: the network inside its scope, the
+    SAP guess outside it and when the learned start does not converge."""
+    from chinium_gb300.scf import run_scf
+    Z, xyz = M.water_cluster(3, np.random.default_rng(77))
+    r = run_scf(Z, xyz, functional="PBE", guess="learned")
+    assert r.converged and r.guess_used == "learned"
+    ref = run_scf(Z, xyz, functional="PBE", guess="sap", context=r.context)
+    assert abs(r.energy - ref.energy) < 1e-7
+    Zm, xm = M.alkane(1, np.random.default_rng(0))  # methane: carbon is outside the model
+    rm = run_scf(Zm, xm, functional="PBE", guess="learned")
+    assert rm.converged and rm.guess_used.startswith("sap")
+    rf = run_scf(Z, xyz, functional="PBE", guess="learned", max_iter=4, context=r.context)
+    assert rf.guess_used.startswith("sap (learned start did not converge")
