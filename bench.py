@@ -164,14 +164,23 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def mixed_roofline(info, kms, stage, peaks, passes_density, ncomp_fock):
-    """Tensor-core roofline of the dominant mixed kernel.  Algorithmic FLOPs
-    per build: density 2 * 128 * sum_t (64 nk_t)^2 per pass (T = Phi D of every
-    tile), V_xc 2 * 128 * sum_t (64 nk_t)^2 per component (W = L^T R); the
-    tensor core executes 6x that (three-term split cross products)."""
-    pairs = info["mixed_pairs"]
-    fl_den = 2.0 * 128 * pairs * passes_density
-    fl_fock = 2.0 * 128 * pairs * ncomp_fock
+def mixed_roofline(info, kms, stage, peaks, family, nspin):
+    """Tensor-core roofline of the dominant mixed kernel (algorithmic FLOPs ÷
+    CUDA-event duration).  Algorithmic FLOPs per build, from the grid's unit
+    counts: density 2*128*128*64 per unit — a full pass (rho + grad rho, GGA /
+    meta-GGA) has units_full units, a symmetric pass (rho of LDA, each of the
+    three tau components) units_sym; V_xc 2*128^3 per (item, tile) job and
+    component (components 1-3 only on jobs with I <= J).  The tensor core
+    executes 6x that (three-term split cross products)."""
+    unit = 2.0 * 128 * 128 * 64
+    if family == 0:
+        fl_den = info["mixed_units_sym"] * unit * nspin
+    elif family == 1:
+        fl_den = info["mixed_units_full"] * unit * nspin
+    else:
+        fl_den = (info["mixed_units_full"] + 3 * info["mixed_units_sym"]) * unit * nspin
+    jobs = info["mixed_fock_jobs"] + (3 * info["mixed_fock_tau_jobs"] if family >= 2 else 0)
+    fl_fock = jobs * 2.0 * 128 ** 3  # one spin: fock_tc is timed for spin 0
     ms_den, ms_fock = kms[0], kms[4]
     dom, dom_ms, fl = ("density_tc", ms_den, fl_den) if ms_den >= ms_fock else ("fock_tc", ms_fock, fl_fock)
     achieved = fl / (dom_ms / 1e3) / 1e12
@@ -290,7 +299,7 @@ def run_alkanes(args):
     value = G * args.steps / t_dev
     plain = Gfp / t64
     peaks = measured_peaks()
-    roof = mixed_roofline(info, kms, stage, peaks, passes_density=4, ncomp_fock=4)
+    roof = mixed_roofline(info, kms, stage, peaks, 2, 1)
     line = {"metric": ALK_METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_dev / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "bf16x3 (split) + f64 accumulation", "data": "synthetic",
@@ -298,6 +307,8 @@ def run_alkanes(args):
                        "molecules": nm, "npoints": G, "mixed_tiles": info["mixed_tiles"],
                        "nbasis_total": int(sum(b.nbasis for b in bases)),
                        "l2": "inputs larger than L2 (FP32 AO store + Z %.1f GB)" % (info["mixed_store_bytes"] / 1e9),
+                       "batched_builds_per_s": args.steps / t_dev,
+                       "molecule_builds_per_s": nm * args.steps / t_dev,
                        "grid_setup_s": t_grid, "first_build_s": t_first, "tuner": tune,
                        "plain_fp64_molecules": nfp, "plain_fp64_pts_per_s": plain,
                        "speedup_vs_plain_fp64": value / plain,
@@ -478,8 +489,13 @@ def main():
     peaks = measured_peaks()
 
     if precision == PMX:
-        roof = mixed_roofline(info, kms, stage, peaks, passes_density=(4 if xc.type >= 2 else 1) * ns,
-                              ncomp_fock=4 if xc.type >= 2 else 1)
+        roof = mixed_roofline(info, kms, stage, peaks, xc.type, ns)
+        tf = os.path.join(REPO, "profiles", "traffic_c18_b3lyp_sg2.json")
+        if args.workload == "c18" and os.path.exists(tf):
+            with open(tf) as f:
+                t = json.load(f)
+            roof["traffic"] = t["dram_bytes_per_launch"].get(roof["kernel"])
+            roof["traffic_source"] = "ncu dram__bytes_read.sum + dram__bytes_write.sum, profiles/traffic_c18_b3lyp_sg2.json"
     else:
         flops = 2.0 * info["screened_pairs"] * (G / info["nblocks"])
         ms_den, ms_fock = stage[0], stage[3]
@@ -501,6 +517,7 @@ def main():
                        "mixed_tiles": info["mixed_tiles"],
                        "l2": "inputs larger than L2 (FP64 AO store %.2f GB; FP32 AO store + Z %.2f GB)"
                              % (info["ao_elements"] * 4 * 8 / 1e9, info["mixed_store_bytes"] / 1e9),
+                       "xc_builds_per_s": args.steps / t_dev,
                        "plain_fp64_pts_per_s": plain, "plain_fp64_ms_per_build": t_plain / plain_steps * 1e3,
                        "speedup_vs_plain_fp64": value / world / plain,
                        "E_xc_fp64": E64, "E_xc": Emx if precision == PMX else E64,

@@ -30,7 +30,9 @@ class GridInfo(ctypes.Structure):
                 ("nbasis", ctypes.c_int), ("nspin", ctypes.c_int), ("type", ctypes.c_int),
                 ("ao_elements", ctypes.c_long), ("screened_pairs", ctypes.c_long),
                 ("mixed_tiles", ctypes.c_int), ("mixed_pairs", ctypes.c_long), ("mixed_rows", ctypes.c_long),
-                ("mixed_store_bytes", ctypes.c_long), ("mixed_launches", ctypes.c_int)]
+                ("mixed_store_bytes", ctypes.c_long), ("mixed_launches", ctypes.c_int),
+                ("mixed_units_full", ctypes.c_long), ("mixed_units_sym", ctypes.c_long),
+                ("mixed_fock_jobs", ctypes.c_long), ("mixed_fock_tau_jobs", ctypes.c_long)]
 
 
 class MixedConfig(ctypes.Structure):

@@ -610,6 +610,10 @@ int xc_grid_info_get(const xc_grid* g, xc_grid_info* info) {
         info->mixed_store_bytes = G.mx.ready ? (long)(G.mx.d_e32.n + G.mx.d_Z.n) * 4 : 0;
         // split_d, density passes, combine, functional, energy, then per spin Z / V partials / reduction
         info->mixed_launches = 1 + G.nspin * (G.type >= 2 ? 4 : 1) + 3 + 3 * G.nspin;
+        info->mixed_units_full = G.mx.ready ? G.mx.units_full : 0;
+        info->mixed_units_sym = G.mx.ready ? G.mx.units_sym : 0;
+        info->mixed_fock_jobs = G.mx.ready ? G.mx.fock_jobs : 0;
+        info->mixed_fock_tau_jobs = G.mx.ready ? G.mx.fock_tau_jobs : 0;
     });
 }
 

@@ -290,9 +290,12 @@ void Grid::prepare_mixed(const MixedConfig& cfg) {
     // ---- persistent work lists
     std::vector<long> dcost(ntiles);
     std::vector<int> dids;
+    m.units_full = m.units_sym = 0;
     for (int t = 0; t < ntiles; t++) {
-        const int nk = m.h_nkept[t];
-        dcost[t] = (long)((nk + 1) / 2) * nk;
+        const int nk = m.h_nkept[t], nvb = (nk + 1) / 2;
+        dcost[t] = (long)nvb * nk;
+        m.units_full += (long)nvb * nk;
+        m.units_sym += (long)nvb * nk - (long)nvb * (nvb - 1);
         if (nk > 0) dids.push_back(t);
     }
     std::vector<int> doff, dlist;
@@ -379,6 +382,9 @@ void Grid::prepare_mixed(const MixedConfig& cfg) {
     if (djobs.empty()) djobs.push_back(DensJob{0, 1, 0, 0});
     m.d_dens_jobs.upload(djobs.data(), djobs.size(), s);
     m.d_fock_off.upload(fjoff.data(), fjoff.size(), s);
+    m.fock_jobs = (long)fjobs.size();
+    m.fock_tau_jobs = 0;
+    for (const FockJob& j : fjobs) m.fock_tau_jobs += (j.flags & 4) != 0;
     if (fjobs.empty()) fjobs.push_back(FockJob{0, 0, -1, -1, -1, -1, 0, 0});
     m.d_fock_jobs.upload(fjobs.data(), fjobs.size(), s);
     {

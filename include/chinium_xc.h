@@ -125,6 +125,10 @@ typedef struct xc_grid_info {
     long mixed_rows;     /* kept function rows of all tiles (FP32 AO store: rows x 128 x components) */
     long mixed_store_bytes; /* device bytes of the FP32 AO store and the per-build Z operand */
     int mixed_launches;  /* kernels one mixed build launches (for the current type and spins) */
+    long mixed_units_full; /* density units (128 x 128 x 64 products) of a full pass (rho + grad rho) */
+    long mixed_units_sym;  /* density units of a symmetric pass (rho of LDA, each tau component) */
+    long mixed_fock_jobs;  /* V (item, tile) jobs, each 128 x 128 x 128 per component */
+    long mixed_fock_tau_jobs; /* jobs that also carry the meta-GGA components (I <= J) */
 } xc_grid_info;
 int xc_grid_info_get(const xc_grid* g, xc_grid_info* info);
 /* Padded points in block order: x, y, z, w (each npoints_padded) and
