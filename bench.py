@@ -180,7 +180,7 @@ def mixed_roofline(info, kms, stage, peaks, family, nspin):
     else:
         fl_den = (info["mixed_units_full"] + 3 * info["mixed_units_sym"]) * unit * nspin
     jobs = info["mixed_fock_jobs"] + (3 * info["mixed_fock_tau_jobs"] if family >= 2 else 0)
-    fl_fock = jobs * 2.0 * 128 ** 3  # one spin: fock_tc is timed for spin 0
+    fl_fock = jobs * 2.0 * 128 ** 3 * nspin  # one fock_tc launch per spin; kms[4] sums them
     ms_den, ms_fock = kms[0], kms[4]
     dom, dom_ms, fl = ("density_tc", ms_den, fl_den) if ms_den >= ms_fock else ("fock_tc", ms_fock, fl_fock)
     achieved = fl / (dom_ms / 1e3) / 1e12
@@ -325,10 +325,12 @@ SCF_METRIC = "SCF wall time to 1e-8 Eh, (H2O)_8 RKS PBE/def2-SVP SG-2, mixed + l
 def run_scf_water(args):
     """Held-out water octamers (seeded, disjoint from the guess's training
     seeds): full Kohn-Sham SCFs to 1e-8 Eh with (a) plain FP64 XC builds from
-    the SAP guess and (b) incremental mixed builds from the learned guess, plus
-    the two mixed combinations.  Integrals and the grid are shared setup (ERIs
-    resident in HBM for J/K); the timed SCF includes the guess and every
-    iteration (XC build, J/K, DIIS, diagonalisation)."""
+    the SAP guess and (b) incremental mixed builds from the learned guess (its
+    SAP base on the tensor cores; references from FP64 densities with a
+    tensor-core V), plus the other combinations.  Integrals, the overlap
+    metric and the grid are shared setup (ERIs resident in HBM for J/K); the
+    timed SCF includes the guess and every iteration (XC build, J/K, DIIS,
+    diagonalisation)."""
     import torch
     import chinium_gb300 as cg
     from chinium_gb300 import guess as G
@@ -337,7 +339,11 @@ def run_scf_water(args):
     torch.cuda.set_device(0)
     mols = M.water_clusters(args.scf_mols, seed=424242, kmin=8, kmax=8)
     model = G.load(G.DEFAULT_WEIGHTS)
-    legs = {"fp64_sap": [], "fp64_learned": [], "mixed_sap": [], "mixed_learned": []}
+    # (XC precision, guess, reference build of the incremental mixed SCF)
+    legs_cfg = {"fp64_sap": ("fp64", "sap", "fp64"), "fp64_learned": ("fp64", "learned", "fp64"),
+                "mixed_sap": ("mixed", "sap", "density"), "mixed_learned": ("mixed", "learned", "density"),
+                "mixed_learned_fp64_anchor": ("mixed", "learned", "fp64")}
+    legs = {k: [] for k in legs_cfg}
     dE = []
     t_setup = 0.0
     for Z, xyz in mols:
@@ -351,20 +357,22 @@ def run_scf_water(args):
         t_setup += time.perf_counter() - t0
         nocc = sum(Z) // 2
         res = {}
-        for leg in legs:
-            prec, gs = leg.split("_")
+        for leg, (prec, gs, anchor) in legs_cfg.items():
             t0 = time.perf_counter()
-            guess = "sap" if gs == "sap" else G.guess_density(model, Z, xyz, ctx)
-            r = run_scf(Z, xyz, precision=prec, guess=guess, context=ctx, **kw)
+            guess = "sap" if gs == "sap" else G.guess_density(model, Z, xyz, ctx, precision=prec)
+            r = run_scf(Z, xyz, precision=prec, guess=guess, context=ctx, anchor=anchor, **kw)
             wall = time.perf_counter() - t0
             assert r.converged
             legs[leg].append({"wall": wall, "iters": r.iterations, "E": r.energy, "xc_s": r.timings["xc"],
                               "jk_s": r.timings["jk"], "diag_s": r.timings["diag"]})
             res[leg] = r.energy
         dE.append(abs(res["mixed_learned"] - res["fp64_sap"]))
+        for leg in legs:
+            legs[leg][-1]["dE"] = abs(res[leg] - res["fp64_sap"])
     summ = {k: {"wall_s": float(np.mean([x["wall"] for x in v])), "iterations": float(np.mean([x["iters"] for x in v])),
                 "xc_s": float(np.mean([x["xc_s"] for x in v])), "jk_s": float(np.mean([x["jk_s"] for x in v])),
-                "diag_s": float(np.mean([x["diag_s"] for x in v]))} for k, v in legs.items()}
+                "diag_s": float(np.mean([x["diag_s"] for x in v])),
+                "max_abs_dE_vs_fp64_sap": float(max(x["dE"] for x in v))} for k, v in legs.items()}
     value = summ["mixed_learned"]["wall_s"]
     line = {"metric": SCF_METRIC, "value": value, "unit": "s", "n_gpus": 1, "steps": len(mols), "warmup": 0,
             "ms_per_step": value * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,

@@ -36,7 +36,8 @@ class GridInfo(ctypes.Structure):
 
 
 class MixedConfig(ctypes.Structure):
-    _fields_ = [("screen", ctypes.c_double), ("fock_tiles", ctypes.c_int), ("spatial", ctypes.c_int)]
+    _fields_ = [("screen", ctypes.c_double), ("fock_tiles", ctypes.c_int), ("spatial", ctypes.c_int),
+                ("func_float_above", ctypes.c_double)]
 
 
 class TuneCandidate(ctypes.Structure):
@@ -89,6 +90,7 @@ SIGNATURES = {
     "xc_build": [_P, _P, _P, _I, _I, _P, _P],
     "xc_build_device": [_P, _P, _P, _I, _I, _P, _P],
     "xc_sap_fock": [_P, _P],
+    "xc_sap_fock_tc": [_P, _P],
     "xc_functional_energy_static": [_P, _L, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P],
     "xc_build_incremental": [_P, _P, _P, _I, _I, _P, _P],
     "xc_mlp_create": [_I, _I, _I, _I, _PP],

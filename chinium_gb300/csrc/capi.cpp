@@ -861,11 +861,17 @@ int xc_grid_kernel_ms(xc_grid* g, double* ms) {
         Grid& G = g->g;
         CGB_CHECK(G.profiling, XC_ERR_STATE, "profiling is off (xc_grid_profile)");
         CGB_CUDA(cudaEventSynchronize(G.ev[4]));
-        const int order[7] = {0, 1, 2, 3, 5, 6, 4};
-        for (int i = 0; i < 6; i++) {
+        const auto span = [&](int a, int b) {
             float t = 0;
-            CGB_CUDA(cudaEventElapsedTime(&t, G.ev[order[i]], G.ev[order[i + 1]]));
-            ms[i] = t;
+            CGB_CUDA(cudaEventElapsedTime(&t, G.ev[a], G.ev[b]));
+            return (double)t;
+        };
+        for (int i = 0; i < 3; i++) ms[i] = span(i, i + 1);
+        ms[3] = ms[4] = ms[5] = 0;
+        for (int s = 0; s < G.nspin; s++) {  // summed over the spins
+            ms[3] += span(s == 0 ? 3 : 4 + 3 * s, 5 + 3 * s);
+            ms[4] += span(5 + 3 * s, 6 + 3 * s);
+            ms[5] += span(6 + 3 * s, 7 + 3 * s);
         }
     });
 }
@@ -877,10 +883,11 @@ int xc_build_incremental(xc_grid* g, xc_functional* f, const double* D, int nspi
         Grid& G = g->g;
         CGB_CHECK(nspin == G.nspin && f->f.nspin == G.nspin, XC_ERR_ARG, "Wrong number of spin types!");
         CGB_CHECK(f->f.family <= G.type, XC_ERR_STATE, "grid type is below the functional family (setType/getAO)");
+        CGB_CHECK(anchor >= 0 && anchor <= 2, XC_ERR_ARG, "anchor must be 0, 1 or 2");
         G.ensure_work();
         const size_t nn = (size_t)G.basis.nbasis * G.basis.nbasis * nspin;
         CGB_CUDA(cudaMemcpyAsync(G.d_D.p, D, nn * sizeof(double), cudaMemcpyHostToDevice, G.stream));
-        G.build_incremental(G.d_D.p, f->f, G.d_scalar.p, G.d_V.p, anchor != 0);
+        G.build_incremental(G.d_D.p, f->f, G.d_scalar.p, G.d_V.p, anchor);
         CGB_CUDA(cudaMemcpyAsync(E, G.d_scalar.p, sizeof(double), cudaMemcpyDeviceToHost, G.stream));
         CGB_CUDA(cudaMemcpyAsync(V, G.d_V.p, nn * sizeof(double), cudaMemcpyDeviceToHost, G.stream));
         CGB_CUDA(cudaStreamSynchronize(G.stream));
@@ -929,15 +936,17 @@ int xc_grid_set_mixed_config(xc_grid* g, const xc_mixed_config* cfg) {
     return guard([&] {
         CGB_CHECK(g && cfg, XC_ERR_ARG, "null argument");
         CGB_CHECK(cfg->screen >= 0 && std::isfinite(cfg->screen) && cfg->fock_tiles >= 0 &&
-                      (cfg->spatial == 0 || cfg->spatial == 1),
+                      (cfg->spatial == 0 || cfg->spatial == 1) && cfg->func_float_above > 0 &&
+                      !std::isnan(cfg->func_float_above),
                   XC_ERR_ARG, "bad mixed configuration");
         Grid& G = g->g;
         MixedConfig c;
         c.screen = cfg->screen;
         c.fock_tiles = cfg->fock_tiles;
         c.spatial = cfg->spatial;
+        c.func_float_above = cfg->func_float_above;
+        if (!c.same_tiles(G.mx.cfg)) G.mx.ready = false;
         G.mx.cfg = c;
-        G.mx.ready = false;
         G.mx.have_ref = false;
         G.mx.drop_graph();
     });
@@ -950,6 +959,7 @@ int xc_grid_get_mixed_config(const xc_grid* g, xc_mixed_config* cfg) {
         cfg->screen = c.screen;
         cfg->fock_tiles = c.fock_tiles;
         cfg->spatial = c.spatial;
+        cfg->func_float_above = c.func_float_above;
     });
 }
 
@@ -1011,6 +1021,7 @@ int xc_grid_tune(xc_grid* g, xc_functional* f, const double* D, int nspin, doubl
         rc.screen = 1e-14;
         rc.spatial = 1;
         rc.fock_tiles = 0;
+        rc.func_float_above = G.mx.cfg.func_float_above;
         const Run ref = run(rc);
         std::vector<xc_tune_candidate> cands;
         auto judge = [&](const Run& r) {
@@ -1018,6 +1029,7 @@ int xc_grid_tune(xc_grid* g, xc_functional* f, const double* D, int nspin, doubl
             c.cfg.screen = r.cfg.screen;
             c.cfg.fock_tiles = r.cfg.fock_tiles;
             c.cfg.spatial = r.cfg.spatial;
+            c.cfg.func_float_above = r.cfg.func_float_above;
             c.ms = r.ms;
             for (int i = 0; i < nm; i++) c.max_de = std::max(c.max_de, std::fabs(r.E[i] - ref.E[i]));
             for (size_t i = 0; i < nn; i++) c.max_dv = std::max(c.max_dv, std::fabs(r.V[i] - ref.V[i]));
@@ -1071,6 +1083,7 @@ int xc_grid_tune(xc_grid* g, xc_functional* f, const double* D, int nspin, doubl
             report->best.screen = best.screen;
             report->best.fock_tiles = best.fock_tiles;
             report->best.spatial = best.spatial;
+            report->best.func_float_above = best.func_float_above;
             report->ms_best = best_ms;
             report->ms_reference = ref.ms;
             report->ncand = (int)std::min<size_t>(cands.size(), 32);
@@ -1079,10 +1092,11 @@ int xc_grid_tune(xc_grid* g, xc_functional* f, const double* D, int nspin, doubl
     });
 }
 
-int xc_sap_fock(xc_grid* g, double* V) {
-    return guard([&] {
+static void sap_fock(xc_grid* g, double* V, bool tensor_cores) {
+    {
         CGB_CHECK(g && V, XC_ERR_ARG, "null argument");
         Grid& G = g->g;
+        CGB_CHECK(!G.batched, XC_ERR_UNSUPPORTED, "the SAP guess is per molecule");
         CGB_CHECK(G.ao_order >= 0, XC_ERR_STATE, "getAO must run before the SAP guess");
         G.ensure_work();
         const int natoms = G.basis.natoms();
@@ -1098,14 +1112,37 @@ int xc_sap_fock(xc_grid* g, double* V) {
         // GuessSCF.cpp:19-37: pretend LDA, one spin; V = sum_g w v phi phi
         launch_sap_coef(G.Gp, natoms, G.d_atoms.p, d_table.p, d_radii.p, G.d_x.p, G.d_y.p, G.d_z.p, G.d_w.p,
                         G.d_fcoef.p, G.stream);
-        const size_t nn = (size_t)G.basis.nbasis * G.basis.nbasis;
-        CGB_CUDA(cudaMemsetAsync(G.d_V.p, 0, nn * sizeof(double), G.stream));
-        launch_fock_fp64((int)G.blocks.size(), G.d_blocks.p, G.d_lists.p, G.max_nb, G.basis.nbasis, 1, 0, G.d_ao.p,
-                         G.Gp, G.d_fcoef.p, G.d_V.p, G.stream);
+        const int n = G.basis.nbasis;
+        const size_t nn = (size_t)n * n;
+        if (tensor_cores) {
+            // the same V through the mixed path's tiles: coefficients gathered
+            // into tile order, LDA-type Z operand, tensor-core partials, FP64 sum
+            G.mixed_ready();
+            MixedState& m = G.mx;
+            launch_gather(m.d_perm.p, m.md.Gt, G.Gp, 5, G.d_fcoef.p, m.fcoef.p, true, G.stream);
+            launch_prep_z(m.md, 0, m.fcoef.p, m.d_Z.p, m.d_c2.p, G.stream);
+            launch_fock_tc(m.tm_raw_f, m.tm_z, m.md.rows, m.fock_ctas, m.d_fock_off.p, m.d_fock_jobs.p, m.d_c2.p, 1,
+                           m.d_wpart.p, m.d_err.p, G.stream);
+            launch_wsum(m.d_wpart.p, m.d_item_live.p, m.d_mols.p, 1, n, 0, 1, G.d_V.p, G.stream);
+        } else {
+            CGB_CUDA(cudaMemsetAsync(G.d_V.p, 0, nn * sizeof(double), G.stream));
+            launch_fock_fp64((int)G.blocks.size(), G.d_blocks.p, G.d_lists.p, G.max_nb, n, 1, 0, G.d_ao.p, G.Gp,
+                             G.d_fcoef.p, G.d_V.p, G.stream);
+        }
         CGB_CUDA(cudaMemcpyAsync(V, G.d_V.p, nn * sizeof(double), cudaMemcpyDeviceToHost, G.stream));
         CGB_CUDA(cudaStreamSynchronize(G.stream));
         G.have_potential = false;  // fcoef overwritten
-    });
+        if (tensor_cores && G.mixed_error())
+            throw Error(XC_ERR_TIMEOUT, "a bounded wait of the tensor-core pipeline gave up");
+    }
+}
+
+int xc_sap_fock(xc_grid* g, double* V) {
+    return guard([&] { sap_fock(g, V, false); });
+}
+
+int xc_sap_fock_tc(xc_grid* g, double* V) {
+    return guard([&] { sap_fock(g, V, true); });
 }
 
 }  // extern "C"

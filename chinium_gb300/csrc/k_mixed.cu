@@ -687,22 +687,46 @@ __global__ void gather_kernel(const long* __restrict__ perm, long Gt, long Gp, i
     for (int c = 0; c < ncomp; c++) dst[(long)c * Gt + p] = (pad && zero_pads) ? 0.0 : src[(long)c * Gp + i];
 }
 
-// V_m(mu, nu) = sum over splits of W(mu, nu) + W(nu, mu); one grid row per molecule.
-__global__ void wsum_kernel(const double* __restrict__ wpart, const int* __restrict__ live,
-                            const MolRange* __restrict__ mols, int spin, double* __restrict__ V) {
-    const MolRange m = mols[blockIdx.y];
-    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (long)m.n * m.n) return;
-    const int mu = (int)(idx % m.n), nu = (int)(idx / m.n);
-    const int I = mu >> 7, J = nu >> 7, ri = mu & 127, rj = nu & 127;
-    double acc = 0;
-    for (int s = 0; s < m.nsplit; s++) {
-        const long a = m.item0 + ((long)I * m.nblk + J) * m.nsplit + s;
-        const long b = m.item0 + ((long)J * m.nblk + I) * m.nsplit + s;
-        if (live[a]) acc += wpart[(size_t)a * 16384 + (size_t)ri * 128 + rj];
-        if (live[b]) acc += wpart[(size_t)b * 16384 + (size_t)rj * 128 + ri];
+// V_m(mu, nu) = sum over splits of W(mu, nu) + W(nu, mu).  A block of 32 x 32
+// threads owns a 32 x 32 tile of V (grid z = molecule): the W(nu, mu) partials
+// are read along mu (coalesced, as V is written), the W(mu, nu) partials along
+// nu and turned through shared memory.  Four splits per step keep eight loads
+// in flight per thread.
+__global__ void __launch_bounds__(1024) wsum_kernel(const double* __restrict__ wpart, const int* __restrict__ live,
+                                                    const MolRange* __restrict__ mols, int spin,
+                                                    double* __restrict__ V) {
+    __shared__ double ta[32][33];
+    const MolRange m = mols[blockIdx.z];
+    const int mu0 = blockIdx.x * 32, nu0 = blockIdx.y * 32;
+    if (mu0 >= m.n || nu0 >= m.n) return;  // uniform over the block
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int I = mu0 >> 7, J = nu0 >> 7;
+    const long ia = m.item0 + ((long)I * m.nblk + J) * m.nsplit, ib = m.item0 + ((long)J * m.nblk + I) * m.nsplit;
+    const double* wa = wpart + (size_t)ia * 16384 + (size_t)((mu0 & 127) + ty) * 128 + (nu0 & 127) + tx;
+    const double* wb = wpart + (size_t)ib * 16384 + (size_t)((nu0 & 127) + ty) * 128 + (mu0 & 127) + tx;
+    double acc_a = 0, acc_b = 0;  // (mu0 + ty, nu0 + tx) and (mu0 + tx, nu0 + ty)
+    int s = 0;
+    for (; s + 4 <= m.nsplit; s += 4) {
+        double va[4], vb[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            va[k] = live[ia + s + k] ? wa[(size_t)(s + k) * 16384] : 0.0;
+            vb[k] = live[ib + s + k] ? wb[(size_t)(s + k) * 16384] : 0.0;
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            acc_a += va[k];
+            acc_b += vb[k];
+        }
     }
-    V[m.voff + (long)spin * m.n * m.n + (long)nu * m.n + mu] = acc;
+    for (; s < m.nsplit; s++) {
+        if (live[ia + s]) acc_a += wa[(size_t)s * 16384];
+        if (live[ib + s]) acc_b += wb[(size_t)s * 16384];
+    }
+    ta[ty][tx] = acc_a;
+    __syncthreads();
+    const int mu = mu0 + tx, nu = nu0 + ty;
+    if (mu < m.n && nu < m.n) V[m.voff + (long)spin * m.n * m.n + (long)nu * m.n + mu] = ta[tx][ty] + acc_b;
 }
 
 // Packed D_m (s, n, n) column-major FP64 -> three BF16 planes per spin of the
@@ -918,9 +942,9 @@ void launch_axpby(long n, double a, const double* x, double b, const double* y, 
 
 void launch_wsum(const double* wpart, const int* item_live, const MolRange* mols, int nmol, int maxn, int spin,
                  int /*nspin*/, double* V, cudaStream_t s) {
-    const long total = (long)maxn * maxn;
-    dim3 grid((unsigned)((total + 255) / 256), (unsigned)nmol);
-    wsum_kernel<<<grid, 256, 0, s>>>(wpart, item_live, mols, spin, V);
+    CGB_CHECK(nmol <= 65535, XC_ERR_ARG, "too many molecules in one batch");
+    const unsigned t = (unsigned)((maxn + 31) / 32);
+    wsum_kernel<<<dim3(t, t, (unsigned)nmol), dim3(32, 32), 0, s>>>(wpart, item_live, mols, spin, V);
     CGB_CUDA(cudaGetLastError());
 }
 

@@ -467,7 +467,7 @@ void Grid::density_passes(const __nv_bfloat16*) {
     launch_combine((long)nspin * Gt, m.rho.p, m.rho_b.p, m.rho1.p, m.rho1_b.p, m.tau.p, m.tau_b.p, type, stream);
 }
 
-void Grid::build_mixed(const double* dD, const Functional& f, double* dE, double* dV) {
+void Grid::build_mixed(const double* dD, const Functional& f, double* dE, double* dV, double float_above) {
     mixed_ready();
     MixedState& m = mx;
     const MixedDev& md = m.md;
@@ -481,18 +481,19 @@ void Grid::build_mixed(const double* dD, const Functional& f, double* dE, double
     mark(1);
     launch_functional_fp64(f.desc, f.family, nspin, Gt, m.d_w.p, m.rho.p, m.rho1.p, m.tau.p, m.sigma.p, m.eps.p,
                            m.vrho.p, m.vsigma.p, m.vtau.p, m.fcoef.p, m.partial.p, &m.n_partial, stream,
-                           kMixedFuncFloat);
+                           float_above < 0 ? m.cfg.func_float_above : float_above);
     mark(2);
     launch_energy_mols(m.partial.p, m.d_mols.p, nmol, dE, stream);
     mark(3);
     const int ncomp = f.family >= 2 ? 4 : 1;
     for (int s = 0; s < nspin; s++) {
         launch_prep_z(md, f.family, m.fcoef.p + (size_t)s * 5 * Gt, m.d_Z.p, m.d_c2.p, stream);
-        if (s == 0) mark(5);
+        mark(5 + 3 * s);
         launch_fock_tc(m.tm_raw_f, m.tm_z, md.rows, m.fock_ctas, m.d_fock_off.p, m.d_fock_jobs.p, m.d_c2.p, ncomp,
                        m.d_wpart.p, m.d_err.p, stream);
-        if (s == 0) mark(6);
+        mark(6 + 3 * s);
         launch_wsum(m.d_wpart.p, m.d_item_live.p, m.d_mols.p, nmol, maxn, s, nspin, dV, stream);
+        mark(7 + 3 * s);
     }
     mark(4);
 }
@@ -540,9 +541,10 @@ void Grid::build_mixed_graph(const Functional& f) {
 // V = V_ref + V(c - c_ref), with only the differences on the tensor cores.
 // Their split-BF16 error is relative to the (shrinking, in an SCF) change;
 // the functional and E_xc are evaluated in FP64 on the reconstructed
-// densities.  An anchor (or the first call) is a full FP64 build that resets
-// the references (gathered into tile order).
-void Grid::build_incremental(const double* dD, const Functional& f, double* dE, double* dV, bool anchor) {
+// densities.  An anchor resets the references: a full FP64 build (anchor 1,
+// or the first call; gathered into tile order) or a full tensor-core build
+// with the functional in FP64 everywhere (anchor 2; already in tile order).
+void Grid::build_incremental(const double* dD, const Functional& f, double* dE, double* dV, int anchor) {
     CGB_CHECK(!batched, XC_ERR_UNSUPPORTED, "incremental builds need the FP64 path (one molecule per grid)");
     CGB_CHECK(ao_order >= type, XC_ERR_STATE, "getAO must run (for the current type) before a build");
     ensure_work();
@@ -552,11 +554,7 @@ void Grid::build_incremental(const double* dD, const Functional& f, double* dE, 
     const int n = basis.nbasis;
     const long Gt = md.Gt;
     const size_t nn = (size_t)n * n * nspin, G1 = (size_t)nspin * Gt;
-    if (anchor || !m.have_ref) {
-        density_device(dD);
-        evaluate(f);
-        energy_device(dE);
-        fock_device(dV, f.family);
+    const auto alloc_refs = [&] {
         m.d_Dref.alloc(nn);
         m.d_rho_ref.alloc(G1);
         m.d_rho1_ref.alloc(3 * G1);
@@ -565,6 +563,38 @@ void Grid::build_incremental(const double* dD, const Functional& f, double* dE, 
         m.d_Vref.alloc(nn);
         m.d_dD.alloc(nn);
         m.d_dfcoef.alloc(5 * G1);
+    };
+    if (anchor == 2) {
+        // FP64 densities, functional and E_xc; V from the full coefficients
+        // on the tensor cores
+        density_device(dD);
+        evaluate(f);
+        energy_device(dE);
+        alloc_refs();
+        launch_gather(m.d_perm.p, Gt, Gp, nspin, d_rho.p, m.d_rho_ref.p, false, stream);
+        launch_gather(m.d_perm.p, Gt, Gp, 3 * nspin, d_rho1.p, m.d_rho1_ref.p, false, stream);
+        launch_gather(m.d_perm.p, Gt, Gp, nspin, d_tau.p, m.d_tau_ref.p, false, stream);
+        launch_gather(m.d_perm.p, Gt, Gp, 5 * nspin, d_fcoef.p, m.d_fcoef_ref.p, true, stream);
+        mark(3);
+        const int ncomp = f.family >= 2 ? 4 : 1;
+        for (int s = 0; s < nspin; s++) {
+            launch_prep_z(md, f.family, m.d_fcoef_ref.p + (size_t)s * 5 * Gt, m.d_Z.p, m.d_c2.p, stream);
+            launch_fock_tc(m.tm_raw_f, m.tm_z, md.rows, m.fock_ctas, m.d_fock_off.p, m.d_fock_jobs.p, m.d_c2.p,
+                           ncomp, m.d_wpart.p, m.d_err.p, stream);
+            launch_wsum(m.d_wpart.p, m.d_item_live.p, m.d_mols.p, 1, n, s, nspin, dV, stream);
+        }
+        mark(4);
+        CGB_CUDA(cudaMemcpyAsync(m.d_Dref.p, dD, nn * 8, cudaMemcpyDeviceToDevice, stream));
+        CGB_CUDA(cudaMemcpyAsync(m.d_Vref.p, dV, nn * 8, cudaMemcpyDeviceToDevice, stream));
+        m.have_ref = true;
+        return;
+    }
+    if (anchor == 1 || !m.have_ref) {
+        density_device(dD);
+        evaluate(f);
+        energy_device(dE);
+        fock_device(dV, f.family);
+        alloc_refs();
         CGB_CUDA(cudaMemcpyAsync(m.d_Dref.p, dD, nn * 8, cudaMemcpyDeviceToDevice, stream));
         CGB_CUDA(cudaMemcpyAsync(m.d_Vref.p, dV, nn * 8, cudaMemcpyDeviceToDevice, stream));
         launch_gather(m.d_perm.p, Gt, Gp, nspin, d_rho.p, m.d_rho_ref.p, false, stream);
@@ -599,7 +629,13 @@ void Grid::build_incremental(const double* dD, const Functional& f, double* dE, 
     }
     launch_axpby((long)nn, 1.0, dV, 1.0, m.d_Vref.p, dV, stream);
     mark(4);
-    // the new references
+    save_refs(dD, dV);
+}
+
+// The current D, tile-order densities, coefficients and V become the references.
+void Grid::save_refs(const double* dD, const double* dV) {
+    MixedState& m = mx;
+    const size_t nn = (size_t)basis.nbasis * basis.nbasis * nspin, G1 = (size_t)nspin * m.md.Gt;
     CGB_CUDA(cudaMemcpyAsync(m.d_Dref.p, dD, nn * 8, cudaMemcpyDeviceToDevice, stream));
     CGB_CUDA(cudaMemcpyAsync(m.d_rho_ref.p, m.rho.p, G1 * 8, cudaMemcpyDeviceToDevice, stream));
     if (type >= 1) CGB_CUDA(cudaMemcpyAsync(m.d_rho1_ref.p, m.rho1.p, 3 * G1 * 8, cudaMemcpyDeviceToDevice, stream));

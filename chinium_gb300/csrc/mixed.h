@@ -69,6 +69,10 @@ struct MixedConfig {
     double screen = 1e-11;   // chunk screening threshold (|phi|, |grad phi| bound)
     int fock_tiles = 0;      // tiles per V work item (0: from the SM count)
     int spatial = 1;         // 1: tiles from a k-d split of each molecule's points; 0: generation order
+    double func_float_above = 1e-3;  // FP32 functional at points with total density >= this
+    bool same_tiles(const MixedConfig& o) const {
+        return screen == o.screen && fock_tiles == o.fock_tiles && spatial == o.spatial;
+    }
 };
 
 struct MixedState {

@@ -16,10 +16,6 @@ void ensure_device();
 
 // Default AO screening threshold of the mixed-precision tiles (|phi|, |grad phi|).
 constexpr double kMixedScreen = 1e-11;
-// Total density at and above which the mixed path evaluates the functional
-// in FP32; below it (the low-density region) the functional stays FP64.
-constexpr double kMixedFuncFloat = 1e-3;
-
 struct Functional {
     std::vector<int> ids;
     int nspin = 1;
@@ -68,7 +64,9 @@ struct Grid {
 
     // stage timing: events bracket density, functional, energy, fock
     bool profiling = false;
-    cudaEvent_t ev[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    // 0-4: build stage bounds; 5 + 3 s, 6 + 3 s, 7 + 3 s: after spin s's Z
+    // operand, tensor-core V partials and V reduction (mixed path)
+    cudaEvent_t ev[11] = {};
     void mark(int i);
     ~Grid();
 
@@ -94,9 +92,12 @@ struct Grid {
     void prepare_mixed(const MixedConfig& cfg);
     void mixed_ready();
     void density_passes(const __nv_bfloat16* Dp);
-    void build_mixed(const double* dD, const Functional& f, double* dE, double* dV);
+    // float_above < 0: the configured FP32-functional bound
+    void build_mixed(const double* dD, const Functional& f, double* dE, double* dV, double float_above = -1.0);
     void build_mixed_graph(const Functional& f);  // d_D -> d_Emol, d_V through a CUDA graph
-    void build_incremental(const double* dD, const Functional& f, double* dE, double* dV, bool anchor);
+    // anchor: 0 incremental (FP64 anchor on the first call), 1 FP64 anchor, 2 tensor-core anchor
+    void build_incremental(const double* dD, const Functional& f, double* dE, double* dV, int anchor);
+    void save_refs(const double* dD, const double* dV);
     int mixed_error();
 };
 

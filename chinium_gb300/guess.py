@@ -237,13 +237,15 @@ def supported(Z, basis):
     return all(z in ELEMENTS for z in Z) and basis.name == "def2-svp"
 
 
-def sap_density(grid, H, S, nocc):
+def sap_density(grid, H, S, nocc, metric=None, precision="fp64"):
     """Closed-shell density of the SAP guess (GuessSCF.cpp:17-75): occupied
     orbitals of H + V_SAP in the overlap metric.  The base the network
-    corrects."""
-    F = H + grid.sap_fock()
-    w, V = np.linalg.eigh(S)
-    X = V[:, w > 1e-8] / np.sqrt(w[w > 1e-8])
+    corrects.  metric: overlap_metric(S) when the caller has it; precision
+    "mixed" assembles V_SAP on the tensor cores."""
+    from .scf import overlap_metric
+    from ._lib import PRECISION_FP64, PRECISION_MIXED
+    F = H + grid.sap_fock(PRECISION_MIXED if precision == "mixed" else PRECISION_FP64)
+    X = (metric or overlap_metric(S))[0]
     _, C = np.linalg.eigh(X.T @ F @ X)
     Co = X @ C[:, :nocc]
     return 2.0 * Co @ Co.T
@@ -373,10 +375,34 @@ def train(model, X, T, M, epochs=200, batch=1024, lr=1e-3, seed=0, log=None):
     return losses
 
 
-def predict_density(model, Z, xyz, basis, S, nocc, bf16=True, D_base=None):
+def assemble_blocks(pr, Y, Uas, Ubs, first, count, n):
+    """The molecular-frame matrix from local pair blocks: block (a, b) =
+    Ua^T y Ub and, for a != b, its transpose at (b, a); one batched product
+    per (functions of a, functions of b) layout."""
+    D = np.zeros((n, n))
+    A = np.array([a for a, _ in pr])
+    B = np.array([b for _, b in pr])
+    ca_all = np.array([count[a] for a in A])
+    cb_all = np.array([count[b] for b in B])
+    fa, fb = np.array([first[a] for a in A]), np.array([first[b] for b in B])
+    for ca, cb in sorted(set(zip(ca_all.tolist(), cb_all.tolist()))):
+        idx = np.nonzero((ca_all == ca) & (cb_all == cb))[0]
+        Ua = np.stack([Uas[p] for p in idx])
+        Ub = np.stack([Ubs[p] for p in idx])
+        blk = np.transpose(Ua, (0, 2, 1)) @ Y[idx, :ca, :cb].astype(np.float64) @ Ub
+        rows = fa[idx][:, None] + np.arange(ca)
+        cols = fb[idx][:, None] + np.arange(cb)
+        D[rows[:, :, None], cols[:, None, :]] = blk
+        off = A[idx] != B[idx]
+        D[cols[off][:, :, None], rows[off][:, None, :]] = np.transpose(blk[off], (0, 2, 1))
+    return D
+
+
+def predict_density(model, Z, xyz, basis, S, nocc, bf16=True, D_base=None, metric=None):
     """Learned closed-shell total density (2 C C^T, idempotent in the S metric):
     D_base (the SAP density for a residual model) plus the predicted pair
-    blocks, purified."""
+    blocks, purified.  metric: overlap_metric(S) when the caller has it."""
+    from .scf import overlap_metric
     types, first, count = atom_functions(basis)
     pr = pairs(xyz)
     Qs, X = frames_and_features(Z, xyz, pr)
@@ -385,30 +411,26 @@ def predict_density(model, Z, xyz, basis, S, nocc, bf16=True, D_base=None):
     n = basis.nbasis
     if model.residual and D_base is None:
         raise ValueError("a residual model needs the base (SAP) density")
-    D = np.zeros((n, n))
-    for (a, b), Ua, Ub, y in zip(pr, Uas, Ubs, Y):
-        blk = Ua.T @ y[:count[a], :count[b]].astype(np.float64) @ Ub
-        D[first[a]:first[a] + count[a], first[b]:first[b] + count[b]] = blk
-        if a != b:
-            D[first[b]:first[b] + count[b], first[a]:first[a] + count[a]] = blk.T
+    D = assemble_blocks(pr, Y, Uas, Ubs, first, count, n)
     D = 0.5 * (D + D.T)
     if model.residual:
         D = D + D_base
     # purification: occupied natural orbitals in the overlap metric
-    w, V = np.linalg.eigh(S)
-    Xh = V @ np.diag(w ** -0.5) @ V.T
-    Sh = V @ np.diag(w ** 0.5) @ V.T
+    _, Xh, Sh = metric or overlap_metric(S)
     occ, C = np.linalg.eigh(Sh @ D @ Sh)
     Co = Xh @ C[:, np.argsort(occ)[::-1][:nocc]]
     return 2.0 * Co @ Co.T
 
 
-def guess_density(model, Z, xyz, ctx, bf16=True):
+def guess_density(model, Z, xyz, ctx, bf16=True, precision="fp64"):
     """The learned starting density for a molecule whose SCF context (basis,
-    S, H, grid) exists: the SAP base when the model is residual."""
+    S, H, grid) exists: the SAP base when the model is residual (its V_SAP on
+    the tensor cores for precision "mixed")."""
+    from .scf import overlap_metric
     nocc = sum(Z) // 2
-    base = sap_density(ctx["grid"], ctx["H"], ctx["S"], nocc) if model.residual else None
-    return predict_density(model, Z, xyz, ctx["basis"], ctx["S"], nocc, bf16=bf16, D_base=base)
+    metric = overlap_metric(ctx["S"], ctx)
+    base = sap_density(ctx["grid"], ctx["H"], ctx["S"], nocc, metric, precision) if model.residual else None
+    return predict_density(model, Z, xyz, ctx["basis"], ctx["S"], nocc, bf16=bf16, D_base=base, metric=metric)
 
 
 def save(model, path):

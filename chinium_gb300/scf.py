@@ -24,7 +24,7 @@ import numpy as np
 import scipy.linalg
 
 from . import molecules as M
-from ._lib import check, lib
+from ._lib import PRECISION_FP64, PRECISION_MIXED, check, lib
 from .xc import Basis, ExchangeCorrelation, Grid
 
 
@@ -62,10 +62,30 @@ class JK:
         return (self.K @ D.ravel()).reshape(self.n, self.n)
 
 
+def coulomb_pairs(eri):
+    """Pair form of the Coulomb contraction: the (n(n+1)/2)^2 matrix
+    [(mu nu), (l s)] over mu <= nu, l <= s, the pair indices, and the weights
+    (1 on the diagonal, 2 off it) that fold D_ls + D_sl into one element."""
+    n = eri.shape[0]
+    iu, ju = np.triu_indices(n)
+    pair = iu * n + ju
+    return eri.reshape(n * n, n * n)[np.ix_(pair, pair)], iu, ju, np.where(iu == ju, 1.0, 2.0)
+
+
+def coulomb_from_pairs(Jp, iu, ju, n):
+    J = np.empty((n, n))
+    J[iu, ju] = Jp
+    J[ju, iu] = Jp
+    return J
+
+
 class JKDevice:
-    """Coulomb and exchange matrices from repulsion integrals resident in HBM
-    (two n^2 x n^2 FP64 layouts; each matrix is one matrix-vector product on
-    the GPU).  Caller-side plumbing for the SCF: torch only moves and
+    """Coulomb and exchange matrices from repulsion integrals resident in HBM.
+    J uses the pair symmetry (mu nu|ls) = (nu mu|ls) = (mu nu|sl): one
+    (n(n+1)/2)^2 FP64 matrix times the packed density (off-diagonal elements
+    doubled), a quarter of the full n^4 array.  The exchange layout
+    (mu l|nu s) -> [mu nu, l s] is made on the first exchange() call (hybrid
+    functionals only).  Caller-side plumbing for the SCF: torch only moves and
     multiplies the arrays."""
 
     def __init__(self, eri):
@@ -73,20 +93,40 @@ class JKDevice:
         self.torch = torch
         n = eri.shape[0]
         self.n = n
-        t = torch.from_numpy(np.ascontiguousarray(eri)).cuda()
-        self.J = t.reshape(n * n, n * n)
-        self.K = t.permute(0, 2, 1, 3).contiguous().reshape(n * n, n * n)
-
-    def _mv(self, A, D):
-        torch = self.torch
-        d = torch.from_numpy(np.ascontiguousarray(D).ravel()).cuda()
-        return (A @ d).reshape(self.n, self.n).cpu().numpy()
+        Jpairs, self.iu, self.ju, self.pair_w = coulomb_pairs(eri)
+        self.J = torch.from_numpy(Jpairs).cuda()
+        del Jpairs
+        self._eri = eri
+        self.K = None
 
     def coulomb(self, D):
-        return self._mv(self.J, D)
+        torch = self.torch
+        d = torch.from_numpy(np.ascontiguousarray(D[self.iu, self.ju] * self.pair_w)).cuda()
+        return coulomb_from_pairs((self.J @ d).cpu().numpy(), self.iu, self.ju, self.n)
 
     def exchange(self, D):
-        return self._mv(self.K, D)
+        torch = self.torch
+        n = self.n
+        if self.K is None:
+            t = torch.from_numpy(np.ascontiguousarray(self._eri)).cuda()
+            self.K = t.permute(0, 2, 1, 3).contiguous().reshape(n * n, n * n)
+            del t
+        d = torch.from_numpy(np.ascontiguousarray(D).ravel()).cuda()
+        return (self.K @ d).reshape(n, n).cpu().numpy()
+
+
+def overlap_metric(S, ctx=None):
+    """(X, S^-1/2, S^1/2) of the overlap matrix: X the canonical
+    orthogonaliser (eigenvectors with eigenvalue > 1e-8, scaled), the other
+    two over the full spectrum.  Kept in ctx (one molecule) when given."""
+    if ctx is not None and "S_metric" in ctx:
+        return ctx["S_metric"]
+    w, V = np.linalg.eigh(S)
+    keep = w > 1e-8
+    m = (V[:, keep] / np.sqrt(w[keep]), (V * w ** -0.5) @ V.T, (V * w ** 0.5) @ V.T)
+    if ctx is not None:
+        ctx["S_metric"] = m
+    return m
 
 
 def make_jk(eri, device):
@@ -96,16 +136,28 @@ def make_jk(eri, device):
 
 
 class DIIS:
+    """Pulay's commutator DIIS; the error inner products are kept from one
+    push to the next (each push adds one row)."""
+
     def __init__(self, size=20):
         self.size = size
         self.F, self.E = [], []
+        self.G = np.zeros((0, 0))
 
     def push(self, F, err):
         self.F.append(F)
         self.E.append(err)
+        row = np.array([sum(np.vdot(a, b) for a, b in zip(e, err)) for e in self.E])
+        m = len(self.E)
+        G = np.zeros((m, m))
+        G[:m - 1, :m - 1] = self.G
+        G[m - 1, :] = row
+        G[:, m - 1] = row
+        self.G = G
         if len(self.F) > self.size:
             self.F.pop(0)
             self.E.pop(0)
+            self.G = self.G[1:, 1:]
 
     def extrapolate(self):
         m = len(self.F)
@@ -113,9 +165,7 @@ class DIIS:
             return self.F[-1]
         B = -np.ones((m + 1, m + 1))
         B[m, m] = 0
-        for i in range(m):
-            for j in range(m):
-                B[i, j] = sum(np.vdot(a, b) for a, b in zip(self.E[i], self.E[j]))
+        B[:m, :m] = self.G
         rhs = np.zeros(m + 1)
         rhs[m] = -1
         try:
@@ -140,9 +190,12 @@ def occupations(Z, charge, mult):
 
 def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, mult=1, precision="fp64",
             guess="sap", conv_energy=1e-8, conv_grad=1e-6, max_iter=100, diis_size=20, screen=0.0,
-            eri_threshold=1e-12, anchor_every=0, context=None, verbose=False, jk_device="cpu"):
+            eri_threshold=1e-12, anchor_every=0, context=None, verbose=False, jk_device="cpu", anchor="fp64"):
     """Kohn-Sham SCF.  precision: "fp64" (plain XC build every iteration) or
-    "mixed" (incremental tensor-core XC builds after an FP64 first build).
+    "mixed" (incremental tensor-core XC builds after a first build that sets
+    the references: anchor "fp64", a full FP64 build, or "density", FP64
+    densities, functional and E_xc with V_xc on the tensor cores: V's error
+    moves the converged energy only at second order).
     guess: "sap", "core", "learned" (the per-atom-pair network, with the SAP
     guess as fallback: for molecules outside the model's elements / basis, for
     open shells, and when the SCF started from it has not converged within
@@ -171,9 +224,7 @@ def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, m
         ctx["grid"], ctx["grid_key"] = g, key
     b, S, H, jk, Enuc, g = ctx["basis"], ctx["S"], ctx["H"], ctx["jk"], ctx["Enuc"], ctx["grid"]
     n = b.nbasis
-    s_val, s_vec = np.linalg.eigh(S)
-    keep = s_val > 1e-8
-    X = s_vec[:, keep] / np.sqrt(s_val[keep])
+    X = overlap_metric(S, ctx)[0]
     timings["setup"] = time.perf_counter() - t_start
 
     def solve(F):
@@ -185,12 +236,12 @@ def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, m
         kw = dict(basis=basis, functional=functional, grid=grid, charge=charge, mult=mult, precision=precision,
                   conv_energy=conv_energy, conv_grad=conv_grad, diis_size=diis_size, screen=screen,
                   eri_threshold=eri_threshold, anchor_every=anchor_every, context=ctx, verbose=verbose,
-                  jk_device=jk_device)
+                  jk_device=jk_device, anchor=anchor)
         if unrestricted or charge != 0 or not G.supported(Z, b):
             r = run_scf(Z, xyz, guess="sap", max_iter=max_iter, **kw)
             r["guess_used"] = "sap (outside the learned model's scope)"
             return r
-        D0 = G.guess_density(G.default_model(), Z, xyz, ctx)
+        D0 = G.guess_density(G.default_model(), Z, xyz, ctx, precision=precision)
         r = run_scf(Z, xyz, guess=D0, max_iter=max(1, max_iter // 2), **kw)
         if r.converged:
             r["guess_used"] = "learned"
@@ -203,7 +254,7 @@ def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, m
     # initial guess
     if isinstance(guess, str):
         if guess == "sap":
-            V0 = g.sap_fock()
+            V0 = g.sap_fock(PRECISION_MIXED if precision == "mixed" else PRECISION_FP64)
             F0 = H + V0
         elif guess == "core":
             F0 = H
@@ -217,6 +268,9 @@ def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, m
     else:
         Ds = [np.asarray(d, dtype=np.float64) for d in (guess if unrestricted else [guess])]
 
+    if anchor not in ("fp64", "density"):
+        raise ValueError("anchor must be 'fp64' or 'density'")
+    anchor_code = 1 if anchor == "fp64" else 2
     diis = DIIS(diis_size)
     E_old = None
     history = []
@@ -233,11 +287,12 @@ def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, m
         if precision == "fp64":
             Exc, Vxc = g.build(xc, Ds)
         else:
-            anchor = it == 1 or (anchor_every and (it - 1) % anchor_every == 0)
+            reset = it == 1 or (anchor_every and (it - 1) % anchor_every == 0)
             Dst = np.ascontiguousarray(np.stack([d.T for d in Ds]))
             Vb = np.zeros((nspin, n, n))
             e = ctypes.c_double()
-            check(lib().xc_build_incremental(g._h, xc._h, _p(Dst), nspin, int(anchor), ctypes.byref(e), _p(Vb)))
+            code = anchor_code if reset else 0
+            check(lib().xc_build_incremental(g._h, xc._h, _p(Dst), nspin, code, ctypes.byref(e), _p(Vb)))
             Exc, Vxc = e.value, [Vb[s].T.copy() for s in range(nspin)]
         timings["xc"] += time.perf_counter() - t0
         if unrestricted:
@@ -247,7 +302,10 @@ def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, m
         else:
             Fs = [H + J - 0.5 * exx * Ks[0] + Vxc[0]]
             E = np.sum(Dtot * H) + 0.5 * np.sum(Dtot * J) - 0.25 * exx * np.sum(Dtot * Ks[0]) + Exc + Enuc
-        errs = [X.T @ (F @ D @ S - S @ D @ F) @ X for F, D in zip(Fs, Ds)]
+        errs = []
+        for F, D in zip(Fs, Ds):
+            FDS = F @ D @ S  # S D F = (F D S)^T for symmetric F, D, S
+            errs.append(X.T @ (FDS - FDS.T) @ X)
         gmax = max(np.abs(e).max() for e in errs)
         dE = None if E_old is None else E - E_old
         history.append((E, gmax))

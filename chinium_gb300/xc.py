@@ -132,10 +132,12 @@ class Grid:
     def mixed_config(self):
         c = MixedConfig()
         check(lib().xc_grid_get_mixed_config(self._h, ctypes.byref(c)))
-        return dict(screen=c.screen, fock_tiles=c.fock_tiles, spatial=c.spatial)
+        return dict(screen=c.screen, fock_tiles=c.fock_tiles, spatial=c.spatial, func_float_above=c.func_float_above)
 
-    def set_mixed_config(self, screen=1e-11, fock_tiles=0, spatial=1):
-        c = MixedConfig(float(screen), int(fock_tiles), int(spatial))
+    def set_mixed_config(self, screen=1e-11, fock_tiles=0, spatial=1, func_float_above=1e-3):
+        """func_float_above: total density from which the mixed path's
+        functional runs in FP32 (float("inf"): FP64 everywhere)."""
+        c = MixedConfig(float(screen), int(fock_tiles), int(spatial), float(func_float_above))
         check(lib().xc_grid_set_mixed_config(self._h, ctypes.byref(c)))
 
     def tune(self, xc, D, e_tol=1e-7, v_tol=1e-6, reps=3):
@@ -145,7 +147,8 @@ class Grid:
         r = TuneReport()
         check(lib().xc_grid_tune(self._h, xc._h, _p(D), self.nspin, float(e_tol), float(v_tol), int(reps),
                                  ctypes.byref(r)))
-        cfg = lambda c: dict(screen=c.screen, fock_tiles=c.fock_tiles, spatial=c.spatial)
+        cfg = lambda c: dict(screen=c.screen, fock_tiles=c.fock_tiles, spatial=c.spatial,
+                             func_float_above=c.func_float_above)
         cands = [dict(cfg(c.cfg), ms=c.ms, max_de=c.max_de, max_dv=c.max_dv, kept_pairs=c.kept_pairs,
                       accepted=bool(c.accepted)) for c in r.cand[:r.ncand]]
         return dict(best=cfg(r.best), ms_best=r.ms_best, ms_reference=r.ms_reference, candidates=cands)
@@ -169,11 +172,13 @@ class Grid:
         check(lib().xc_grid_kernel_ms(self._h, _p(ms)))
         return ms
 
-    def sap_fock(self):
-        """SuperpositionAtomicPotential (GuessSCF.cpp:17-75)."""
+    def sap_fock(self, precision=PRECISION_FP64):
+        """SuperpositionAtomicPotential (GuessSCF.cpp:17-75); PRECISION_MIXED
+        assembles it on the tensor cores (FP32-level accuracy)."""
         n = self.nbasis
         V = np.zeros((n, n))
-        check(lib().xc_sap_fock(self._h, _p(V)))
+        fn = lib().xc_sap_fock_tc if precision == PRECISION_MIXED else lib().xc_sap_fock
+        check(fn(self._h, _p(V)))
         return V.T.copy()
 
     # -- inspection -----------------------------------------------------------

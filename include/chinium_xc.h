@@ -208,10 +208,10 @@ int xc_build_device(xc_grid* g, xc_functional* f, const double* d_D, int nspin, 
  * [density, functional, energy, fock] in ms[0..3]. */
 int xc_grid_profile(xc_grid* g, int enable);
 int xc_grid_stage_ms(xc_grid* g, double* ms);
-/* Finer device timing of the last profiled mixed build (one spin, restricted
- * builds): ms[0..5] = [density planes + tensor-core density, functional,
- * per-molecule E_xc, Z operand, tensor-core V partials, FP64 V reduction].
- * No reference counterpart. */
+/* Finer device timing of the last profiled mixed build: ms[0..5] =
+ * [density planes + tensor-core density, functional, per-molecule E_xc,
+ * Z operand, tensor-core V partials, FP64 V reduction], the last three summed
+ * over the spins.  No reference counterpart. */
 int xc_grid_kernel_ms(xc_grid* g, double* ms);
 
 /* Incremental mixed-precision build for SCF iterations (the per-iteration
@@ -221,14 +221,20 @@ int xc_grid_kernel_ms(xc_grid* g, double* ms);
  * only the differences on the tensor cores (split-BF16, FP32 accumulation);
  * the functional and E_xc are FP64 on the reconstructed densities.  The
  * tensor-core error is relative to the change since the previous call, so it
- * vanishes as an SCF converges.  anchor != 0, or the first call on a grid,
- * runs a full FP64 build and resets the references.  Host buffers. */
+ * vanishes as an SCF converges.  anchor resets the references: 1 (or the
+ * first call on a grid with anchor 0) by a full FP64 build; 2 by FP64
+ * densities, functional and E_xc with V on the tensor cores (about half the
+ * cost: an error in V moves a converged SCF energy only at second order,
+ * while E_xc takes the density's error at first order).  Host buffers. */
 int xc_build_incremental(xc_grid* g, xc_functional* f, const double* D, int nspin, int anchor,
                          double* E, double* V);
 
 /* SAP potential matrix (GuessSCF.cpp:17-75): V_mu,nu = sum_g w v_SAP(r_g)
  * phi_mu phi_nu with v_SAP the nearest-radius tabulated atomic potentials. */
 int xc_sap_fock(xc_grid* g, double* V);
+/* The same matrix through the mixed path's tiles (split-BF16 tensor-core
+ * partials, FP64 sum; FP32-level accuracy, which a starting guess can take). */
+int xc_sap_fock_tc(xc_grid* g, double* V);
 
 /* ------------------------------------------------------- batched molecules
  * No reference counterpart: the reference builds one Grid per molecule
@@ -251,11 +257,16 @@ int xc_grid_molecules(const xc_grid* g, int* nmol, int* nbasis, long* npoints, l
  * |grad phi| (0 keeps every chunk); fock_tiles: point tiles per V work item
  * (0 = from the SM count); spatial: 1 forms tiles from k-d cells of each
  * molecule's points, 0 from 128 consecutive points in generation order.
- * Setting them discards the prepared tiles (rebuilt at the next build). */
+ * func_float_above: points whose total density is at least this value
+ * evaluate the functional in FP32, the rest in FP64 (default 1e-3; +inf or
+ * any value above every density keeps the whole functional in FP64).
+ * Changing screen, fock_tiles or spatial discards the prepared tiles
+ * (rebuilt at the next build). */
 typedef struct xc_mixed_config {
     double screen;
     int fock_tiles;
     int spatial;
+    double func_float_above;
 } xc_mixed_config;
 int xc_grid_set_mixed_config(xc_grid* g, const xc_mixed_config* cfg);
 int xc_grid_get_mixed_config(const xc_grid* g, xc_mixed_config* cfg);

@@ -151,6 +151,7 @@ def test_batch_and_tuning_argument_errors():
 
 def test_mixed_config_struct_layout():
     from chinium_gb300._lib import MixedConfig, TuneCandidate, TuneReport
-    assert ctypes.sizeof(MixedConfig) == 16
-    assert ctypes.sizeof(TuneCandidate) == 16 + 3 * 8 + 8 + 8
-    assert TuneReport.cand.offset == 16 + 8 + 8 + 8
+    assert ctypes.sizeof(MixedConfig) == 24
+    assert MixedConfig.func_float_above.offset == 16
+    assert ctypes.sizeof(TuneCandidate) == 24 + 3 * 8 + 8 + 8
+    assert TuneReport.cand.offset == 24 + 8 + 8 + 8

@@ -226,3 +226,15 @@ def test_mixed_precision_against_fp64(h2o, name, type_, nspin):
     # a second call reuses the prepared tiles and gives the same result
     E32b, V32b = g.build(xc, D, precision=cg.PRECISION_MIXED)
     assert E32b == E32
+
+
+def test_sap_fock_tensor_cores(h2o):
+    """The tensor-core SAP matrix against the FP64 one (FP32-level accuracy)."""
+    Z, xyz, b, ob, og = h2o
+    g = make_grid(b, type_=0)
+    V64 = g.sap_fock()
+    Vtc = g.sap_fock(cg.PRECISION_MIXED)
+    scale = np.abs(V64).max()
+    print("SAP tensor-core vs FP64: max|dV| %.2e of max|V| %.2e" % (np.abs(Vtc - V64).max(), scale))
+    assert np.abs(Vtc - V64).max() < 2e-6 * scale
+    assert np.allclose(Vtc, Vtc.T, atol=1e-14)

@@ -20,6 +20,9 @@ def test_rks_h2o_converges_and_mixed_matches_fp64(functional):
                                                               rmx.energy - r64.energy, r64.iterations, rmx.iterations))
     # incremental tensor-core builds: converged energy within 1e-6 Eh of the FP64 path
     assert abs(rmx.energy - r64.energy) < 1e-6
+    # references from FP64 densities with a tensor-core V
+    rd = run_scf(Z, xyz, functional=functional, precision="mixed", anchor="density", context=r64.context)
+    assert rd.converged and abs(rd.energy - r64.energy) < 1e-6
     # physically sensible total energy for water in this basis
     assert -77.0 < r64.energy < -75.5
 
@@ -53,3 +56,28 @@ def test_device_jk_matches_host_jk():
     r_gpu = run_scf(Z, xyz, functional="B3LYP", jk_device="cuda")
     assert r_cpu.converged and r_gpu.converged
     assert abs(r_cpu.energy - r_gpu.energy) < 1e-9
+
+
+def test_device_coulomb_pairs_and_exchange_match_host():
+    pytest.importorskip("torch")
+    from chinium_gb300.scf import JK, JKDevice, repulsion
+    from chinium_gb300.xc import Basis
+    Z, xyz = M.h2o()
+    eri = repulsion(Basis(Z, xyz, "def2-svp"))
+    rng = np.random.default_rng(5)
+    D = rng.normal(size=(24, 24))
+    D = D + D.T
+    host, dev = JK(eri), JKDevice(eri)
+    assert np.abs(dev.coulomb(D) - host.coulomb(D)).max() < 1e-11
+    assert np.abs(dev.exchange(D) - host.exchange(D)).max() < 1e-11
+
+
+def test_mixed_scf_with_learned_guess_uses_tensor_core_sap():
+    """precision="mixed" builds the learned guess's SAP base on the tensor
+    cores; the SCF still converges to the FP64 energy."""
+    Z, xyz = M.water_clusters(1, seed=99, kmin=2, kmax=2)[0]
+    r64 = run_scf(Z, xyz, functional="PBE", precision="fp64", jk_device="cuda")
+    rl = run_scf(Z, xyz, functional="PBE", precision="mixed", guess="learned", anchor="density",
+                 context=r64.context, jk_device="cuda")
+    assert rl.converged and rl.guess_used == "learned"
+    assert abs(rl.energy - r64.energy) < 1e-6

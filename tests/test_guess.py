@@ -157,3 +157,37 @@ def test_learned_guess_with_sap_fallback_in_scf():
     assert rm.converged and rm.guess_used.startswith("sap")
     rf = run_scf(Z, xyz, functional="PBE", guess="learned", max_iter=4, context=r.context)
     assert rf.guess_used.startswith("sap (learned start did not converge")
+
+
+def test_batched_block_assembly_matches_per_pair_loop():
+    """assemble_blocks (one batched product per block layout) against the
+    per-pair rotation and placement it replaces."""
+    rng = np.random.default_rng(11)
+    count = [14, 5, 5, 14, 5]
+    first = list(np.cumsum([0] + count[:-1]))
+    n = sum(count)
+    pr = [(a, b) for a in range(5) for b in range(a, 5)]
+    Y = rng.normal(size=(len(pr), G.MAX_FUNC, G.MAX_FUNC)).astype(np.float32)
+    Uas = [np.linalg.qr(rng.normal(size=(count[a], count[a])))[0] for a, _ in pr]
+    Ubs = [np.linalg.qr(rng.normal(size=(count[b], count[b])))[0] for _, b in pr]
+    want = np.zeros((n, n))
+    for (a, b), Ua, Ub, y in zip(pr, Uas, Ubs, Y):
+        blk = Ua.T @ y[:count[a], :count[b]].astype(np.float64) @ Ub
+        want[first[a]:first[a] + count[a], first[b]:first[b] + count[b]] = blk
+        if a != b:
+            want[first[b]:first[b] + count[b], first[a]:first[a] + count[a]] = blk.T
+    got = G.assemble_blocks(pr, Y, Uas, Ubs, first, count, n)
+    np.testing.assert_allclose(got, want, rtol=1e-13, atol=1e-13)
+
+
+def test_overlap_metric():
+    from chinium_gb300.scf import overlap_metric
+    rng = np.random.default_rng(2)
+    A = rng.normal(size=(9, 9))
+    S = A @ A.T + 9 * np.eye(9)
+    ctx = {}
+    X, Xh, Sh = overlap_metric(S, ctx)
+    np.testing.assert_allclose(X.T @ S @ X, np.eye(9), atol=1e-12)
+    np.testing.assert_allclose(Xh @ S @ Xh, np.eye(9), atol=1e-12)
+    np.testing.assert_allclose(Sh @ Sh, S, atol=1e-11)
+    assert overlap_metric(S, ctx)[0] is X
