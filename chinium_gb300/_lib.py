@@ -37,7 +37,7 @@ class GridInfo(ctypes.Structure):
 
 class MixedConfig(ctypes.Structure):
     _fields_ = [("screen", ctypes.c_double), ("fock_tiles", ctypes.c_int), ("spatial", ctypes.c_int),
-                ("func_float_above", ctypes.c_double)]
+                ("func_float_above", ctypes.c_double), ("v_operands", ctypes.c_int), ("reserved", ctypes.c_int)]
 
 
 class TuneCandidate(ctypes.Structure):

@@ -936,7 +936,8 @@ int xc_grid_set_mixed_config(xc_grid* g, const xc_mixed_config* cfg) {
     return guard([&] {
         CGB_CHECK(g && cfg, XC_ERR_ARG, "null argument");
         CGB_CHECK(cfg->screen >= 0 && std::isfinite(cfg->screen) && cfg->fock_tiles >= 0 &&
-                      (cfg->spatial == 0 || cfg->spatial == 1) && cfg->func_float_above > 0 &&
+                      (cfg->spatial == 0 || cfg->spatial == 1) && cfg->v_operands >= 0 && cfg->v_operands <= 2 &&
+                      cfg->func_float_above > 0 &&
                       !std::isnan(cfg->func_float_above),
                   XC_ERR_ARG, "bad mixed configuration");
         Grid& G = g->g;
@@ -945,6 +946,7 @@ int xc_grid_set_mixed_config(xc_grid* g, const xc_mixed_config* cfg) {
         c.fock_tiles = cfg->fock_tiles;
         c.spatial = cfg->spatial;
         c.func_float_above = cfg->func_float_above;
+        c.v_operands = cfg->v_operands;
         if (!c.same_tiles(G.mx.cfg)) G.mx.ready = false;
         G.mx.cfg = c;
         G.mx.have_ref = false;
@@ -960,6 +962,7 @@ int xc_grid_get_mixed_config(const xc_grid* g, xc_mixed_config* cfg) {
         cfg->fock_tiles = c.fock_tiles;
         cfg->spatial = c.spatial;
         cfg->func_float_above = c.func_float_above;
+        cfg->v_operands = c.v_operands;
     });
 }
 
@@ -1022,6 +1025,7 @@ int xc_grid_tune(xc_grid* g, xc_functional* f, const double* D, int nspin, doubl
         rc.spatial = 1;
         rc.fock_tiles = 0;
         rc.func_float_above = G.mx.cfg.func_float_above;
+        rc.v_operands = G.mx.cfg.v_operands;
         const Run ref = run(rc);
         std::vector<xc_tune_candidate> cands;
         auto judge = [&](const Run& r) {
@@ -1030,6 +1034,7 @@ int xc_grid_tune(xc_grid* g, xc_functional* f, const double* D, int nspin, doubl
             c.cfg.fock_tiles = r.cfg.fock_tiles;
             c.cfg.spatial = r.cfg.spatial;
             c.cfg.func_float_above = r.cfg.func_float_above;
+            c.cfg.v_operands = r.cfg.v_operands;
             c.ms = r.ms;
             for (int i = 0; i < nm; i++) c.max_de = std::max(c.max_de, std::fabs(r.E[i] - ref.E[i]));
             for (size_t i = 0; i < nn; i++) c.max_dv = std::max(c.max_dv, std::fabs(r.V[i] - ref.V[i]));
@@ -1084,6 +1089,7 @@ int xc_grid_tune(xc_grid* g, xc_functional* f, const double* D, int nspin, doubl
             report->best.fock_tiles = best.fock_tiles;
             report->best.spatial = best.spatial;
             report->best.func_float_above = best.func_float_above;
+            report->best.v_operands = best.v_operands;
             report->ms_best = best_ms;
             report->ms_reference = ref.ms;
             report->ncand = (int)std::min<size_t>(cands.size(), 32);
@@ -1120,9 +1126,8 @@ static void sap_fock(xc_grid* g, double* V, bool tensor_cores) {
             G.mixed_ready();
             MixedState& m = G.mx;
             launch_gather(m.d_perm.p, m.md.Gt, G.Gp, 5, G.d_fcoef.p, m.fcoef.p, true, G.stream);
-            launch_prep_z(m.md, 0, m.fcoef.p, m.d_Z.p, m.d_c2.p, G.stream);
-            launch_fock_tc(m.tm_raw_f, m.tm_z, m.md.rows, m.fock_ctas, m.d_fock_off.p, m.d_fock_jobs.p, m.d_c2.p, 1,
-                           m.d_wpart.p, m.d_err.p, G.stream);
+            G.v_prep(m.fcoef.p, 0);
+            G.v_partials(1);
             launch_wsum(m.d_wpart.p, m.d_item_live.p, m.d_mols.p, 1, n, 0, 1, G.d_V.p, G.stream);
         } else {
             CGB_CUDA(cudaMemsetAsync(G.d_V.p, 0, nn * sizeof(double), G.stream));

@@ -166,7 +166,9 @@ __device__ __forceinline__ void store_chunk(uint32_t planes, int r, int j, const
 // The six split products of one stage into TMEM buffer `buf`: term hh into
 // the hh accumulator, the five corrections into the correction accumulator.
 // `first` starts both accumulators (unit boundary).
-__device__ __forceinline__ void mma_stage(uint32_t tmem, int buf, uint8_t* st, bool first) {
+// `halve` (V kernel, items with c2 doubled): the first product into each
+// accumulator halves it (D = A B + D / 2); the drain doubles the unit.
+__device__ __forceinline__ void mma_stage(uint32_t tmem, int buf, uint8_t* st, bool first, bool halve = false) {
     const uint32_t a0 = tc::smem_u32(st), b0 = a0 + 3 * kPlaneA;
     const uint32_t d_hh = tmem + buf * 256, d_corr = tmem + buf * 256 + 128;
 #pragma unroll
@@ -176,8 +178,11 @@ __device__ __forceinline__ void mma_stage(uint32_t tmem, int buf, uint8_t* st, b
         const uint32_t d = q == 0 ? d_hh : d_corr;
 #pragma unroll
         for (int k = 0; k < 4; k++) {  // K = 16 per instruction: +32 bytes in the swizzled row
-            const bool start = first && k == 0 && (q == 0 || q == 1);
-            tc::mma_bf16(d, ad + 2 * k, bd + 2 * k, kIdesc, start ? 0u : 1u);
+            const bool lead = k == 0 && (q == 0 || q == 1);
+            if (halve && lead)
+                tc::mma_bf16_halve_d(d, ad + 2 * k, bd + 2 * k, kIdesc);
+            else
+                tc::mma_bf16(d, ad + 2 * k, bd + 2 * k, kIdesc, (first && lead) ? 0u : 1u);
         }
     }
 }
@@ -657,6 +662,146 @@ __global__ void __launch_bounds__(kThreads, 1) fock_tc_kernel(const __grid_const
     if (warp == 0) tc::tmem_dealloc(tmem, kTmemCols);
 }
 
+// ------------------------------------------------------------ V_xc, pre-split operands
+// The jobs of fock_tc_kernel with both operands read as BF16 planes from HBM
+// (L: the AO store split once per grid; R: Z and c2 d_c phi split once per
+// build), so TMA feeds the tensor core with no conversion in the kernel.  A
+// stage is (component c, 64-point half kh of the tile): three A planes and
+// three B planes (96 KB), two stages in flight.  A dropped 64-function box
+// is loaded from row -64: entirely out of bounds, so TMA fills it with zeros.
+// Items with c2 doubled (I < J) halve the accumulators at their first
+// meta-GGA product and are drained with weight 2 (both exact).
+// CTA roles (384 threads): warp 0 TMA, warp 1 MMA, warps 4-11 drain.
+constexpr int kF16Threads = 384;
+
+struct Fock16Cursor {
+    int j, end, c, kh, ncomp, nc_all;
+    FockJob job;
+    __device__ void load(const FockJob* jobs) {
+        const int4* p = reinterpret_cast<const int4*>(jobs + j);
+        const int4 a = __ldg(p), b = __ldg(p + 1);
+        job = FockJob{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+        ncomp = (job.flags & kTauItem) ? nc_all : 1;
+    }
+    __device__ Fock16Cursor(const int* off, const FockJob* jobs, int nc) {
+        j = off[blockIdx.x];
+        end = off[blockIdx.x + 1];
+        nc_all = nc;
+        ncomp = 1;
+        c = kh = 0;
+        if (j < end) load(jobs);
+    }
+    __device__ bool valid() const { return j < end; }
+    __device__ bool first_of_tile() const { return c == 0 && kh == 0; }
+    __device__ bool last_of_tile() const { return c == ncomp - 1 && kh == 1; }
+    __device__ void advance(const FockJob* jobs) {
+        if (++kh < 2) return;
+        kh = 0;
+        if (++c < ncomp) return;
+        c = 0;
+        if (++j < end) load(jobs);
+    }
+    __device__ int slot(int box) const {
+        return box == 0 ? job.sa0 : box == 1 ? job.sa1 : box == 2 ? job.sb0 : job.sb1;
+    }
+};
+
+__global__ void __launch_bounds__(kF16Threads, 1) fock16_kernel(const __grid_constant__ CUtensorMap tm_l,
+                                                                const __grid_constant__ CUtensorMap tm_r, long rows,
+                                                                const int* __restrict__ job_off,
+                                                                const FockJob* __restrict__ jobs, int ncomp,
+                                                                double* __restrict__ wpart, int* err) {
+    extern __shared__ uint8_t smem_raw[];
+    __shared__ Smem sm;
+    uint8_t* smem = smem_raw + (((tc::smem_u32(smem_raw) + 1023u) & ~1023u) - tc::smem_u32(smem_raw));
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    init_cta(sm, 1, 1);
+    const uint32_t tmem = sm.tmem;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            uint32_t st = 0;
+            for (Fock16Cursor c(job_off, jobs, ncomp); c.valid(); c.advance(jobs), st++) {
+                const int s = st & 1;
+                if (sm.abort || !tc::mbar_wait(&sm.empty[s], ((st >> 1) & 1) ^ 1)) {
+                    flag_timeout(err, &sm);
+                    break;
+                }
+                uint8_t* sb = smem + (size_t)s * kStageBytes;
+                tc::mbar_arrive_expect_tx(&sm.full[s], 12 * (kPlaneA / 2));
+                for (int k = 0; k < 4; k++) {
+                    const int sl = c.slot(k);
+                    const CUtensorMap* map = k < 2 ? &tm_l : &tm_r;
+                    for (int p = 0; p < 3; p++) {
+                        const int y = sl >= 0 ? (int)((long)(c.c * 3 + p) * rows + c.job.trow + (long)sl * 64) : -64;
+                        tc::tma_load_2d(sb + ((k >> 1) * 3 + p) * kPlaneA + (k & 1) * (kPlaneA / 2), map, c.kh * 64,
+                                        y, &sm.full[s]);
+                    }
+                }
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            uint32_t st = 0, ut = 0;
+            for (Fock16Cursor c(job_off, jobs, ncomp); c.valid(); c.advance(jobs), st++) {
+                const int s = st & 1, b = ut & 1;
+                if (c.first_of_tile() && (sm.abort || !tc::mbar_wait(&sm.tempty[b], ((ut >> 1) & 1) ^ 1))) {
+                    flag_timeout(err, &sm);
+                    tc::mma_commit(&sm.tfull[b]);
+                    break;
+                }
+                if (sm.abort || !tc::mbar_wait(&sm.full[s], (st >> 1) & 1)) {
+                    flag_timeout(err, &sm);
+                    tc::mma_commit(&sm.tfull[b]);
+                    break;
+                }
+                tc::fence_after_sync();
+                const bool halve = (c.job.flags & kTauDouble) && c.c == 1 && c.kh == 0;
+                mma_stage(tmem, b, smem + (size_t)s * kStageBytes, c.first_of_tile(), halve);
+                tc::mma_commit(&sm.empty[s]);
+                if (c.last_of_tile()) {
+                    tc::mma_commit(&sm.tfull[b]);
+                    ut++;
+                }
+            }
+        }
+    } else if (warp >= kEpiWarp0 && warp < kEpiWarp0 + 8) {
+        // drain every tile into W (this thread's row g, 64 columns); flush W
+        // at the item's last tile
+        const int quad = warp & 3, half = (warp - kEpiWarp0) >> 2;
+        const int g = quad * 32 + lane;
+        float W[64];
+#pragma unroll
+        for (int jw = 0; jw < 64; jw++) W[jw] = 0.f;
+        uint32_t ut = 0;
+        for (int j = job_off[blockIdx.x]; j < job_off[blockIdx.x + 1]; j++, ut++) {
+            const int4 jb = __ldg(reinterpret_cast<const int4*>(jobs + j) + 1);  // sb0, sb1, item, flags
+            const int item = jb.z, flags = jb.w;
+            const int b = ut & 1;
+            if (sm.abort || !tc::mbar_wait(&sm.tfull[b], (ut >> 1) & 1)) {
+                flag_timeout(err, &sm);
+                break;
+            }
+            tc::fence_after_sync();
+            const bool dbl = (flags & kTauDouble) && ncomp > 1;
+            drain(tmem, b, quad, half, W, dbl ? 2.f : 1.f);
+            tc::fence_before_sync();
+            mbar_arrive(&sm.tempty[b]);
+            if (flags & 2) {
+                double* o = wpart + (size_t)item * 16384 + (size_t)g * 128 + half * 64;
+#pragma unroll
+                for (int jw = 0; jw < 64; jw += 2) {
+                    *reinterpret_cast<double2*>(o + jw) = make_double2((double)W[jw], (double)W[jw + 1]);
+                    W[jw] = W[jw + 1] = 0.f;
+                }
+            }
+        }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, kTmemCols);
+}
+
 // Sums the two column-half partials of the density outputs (deterministic).
 __global__ void combine_kernel(long n1, long n3, double* __restrict__ rho, const double* __restrict__ rho_b,
                                double* __restrict__ rho1, const double* __restrict__ rho1_b, double* __restrict__ tau,
@@ -789,6 +934,86 @@ __global__ void __launch_bounds__(128) prep_z_kernel(MixedDev md, int type, cons
     }
 }
 
+// x = h + m + l in BF16 (the arithmetic of split8, one element).
+__device__ __forceinline__ void split1(float x, bf16& h, bf16& m, bf16& l) {
+    h = __float2bfloat16_rn(x);
+    const float r = x - __bfloat162float(h);
+    m = __float2bfloat16_rn(r);
+    l = __float2bfloat16_rn(r - __bfloat162float(m));
+}
+
+// The FP32 AO store as BF16 planes: e16[(c * 3 + p) * n + i] (n = rows * 128).
+__global__ void split_store_kernel(const float* __restrict__ e32, long n, int ncomp, bf16* __restrict__ e16) {
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n * ncomp) return;
+    const int c = (int)(i / n);
+    const long o = i - (long)c * n;
+    bf16 h, m, l;
+    split1(e32[i], h, m, l);
+    e16[(size_t)(c * 3 + 0) * n + o] = h;
+    e16[(size_t)(c * 3 + 1) * n + o] = m;
+    e16[(size_t)(c * 3 + 2) * n + o] = l;
+}
+
+// R operands of the pre-split V kernel as BF16 planes, per kept row:
+// component 0: Z = c0 phi + c1 . grad phi (the FP32 arithmetic of
+// prep_z_kernel); components 1-3 (meta-GGA): c2 d_c phi.  One CTA per tile,
+// thread = point.
+__device__ __forceinline__ void store3(bf16* __restrict__ R, size_t n, size_t o, float x) {
+    bf16 h, m, l;
+    split1(x, h, m, l);
+    R[o] = h;
+    R[n + o] = m;
+    R[2 * n + o] = l;
+}
+
+__global__ void __launch_bounds__(128) prep16_kernel(MixedDev md, int type, const double* __restrict__ fcoef,
+                                                     bf16* __restrict__ R16) {
+    const int t = blockIdx.x, g = threadIdx.x;
+    const long pt = (long)t * 128 + g;
+    const long Gt = md.Gt;
+    const float a0 = (float)fcoef[pt];
+    float a1 = 0, a2 = 0, a3 = 0, c2 = 0;
+    if (type >= 1) {
+        a1 = (float)fcoef[Gt + pt];
+        a2 = (float)fcoef[2 * Gt + pt];
+        a3 = (float)fcoef[3 * Gt + pt];
+    }
+    if (type >= 2) c2 = (float)fcoef[4 * Gt + pt];
+    const long r0 = md.tile_row[t], nr = (long)md.tile_nkept[t] * 64;  // a multiple of 4
+    const size_t n = (size_t)md.rows * 128;
+    const float* e = md.e32 + (size_t)r0 * 128 + g;
+    bf16* R = R16 + (size_t)r0 * 128 + g;
+    for (long r = 0; r < nr; r += 4) {  // four rows per step: 4 to 16 loads in flight
+        float v[4][4];
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const size_t o = (size_t)(r + i) * 128;
+            v[i][0] = __ldg(e + o);
+            if (type >= 1) {
+                v[i][1] = __ldg(e + n + o);
+                v[i][2] = __ldg(e + 2 * n + o);
+                v[i][3] = __ldg(e + 3 * n + o);
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const size_t o = (size_t)(r + i) * 128;
+            float z = a0 * v[i][0];
+            if (type >= 1) {
+                z = fmaf(a1, v[i][1], z);
+                z = fmaf(a2, v[i][2], z);
+                z = fmaf(a3, v[i][3], z);
+            }
+            store3(R, n, o, z);
+            if (type >= 2) {
+#pragma unroll
+                for (int c = 1; c <= 3; c++) store3(R + 3 * c * n, n, o, v[i][c] * c2);
+            }
+        }
+    }
+}
+
 // E_m = sum of the per-tile partials of molecule m (fixed order).
 __global__ void energy_mols_kernel(const double* __restrict__ partial, const MolRange* __restrict__ mols,
                                    double* __restrict__ E) {
@@ -894,6 +1119,8 @@ void set_mixed_kernel_attributes() {
     CGB_CUDA(cudaFuncSetAttribute(density_tc_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     CGB_CUDA(cudaFuncSetAttribute(density_tc_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     CGB_CUDA(cudaFuncSetAttribute(fock_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    CGB_CUDA(cudaFuncSetAttribute(fock16_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)(2 * kStageBytes + 1024)));
 }
 
 void launch_density_tc(const CUtensorMap& tm_d, const CUtensorMap& tm_raw, const MixedDev& md, int ctas,
@@ -931,6 +1158,27 @@ void launch_fock_tc(const CUtensorMap& tm_e32, const CUtensorMap& tm_z, long row
     if (ctas == 0) return;
     fock_tc_kernel<<<ctas, kThreads, mixed_smem_bytes(), s>>>(tm_e32, tm_z, rows, job_off, jobs, c2, ncomp, wpart,
                                                              err);
+    CGB_CUDA(cudaGetLastError());
+}
+
+void launch_split_store(const float* e32, long n, int ncomp, bf16* e16, cudaStream_t s) {
+    const long total = n * ncomp;
+    if (total == 0) return;
+    split_store_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(e32, n, ncomp, e16);
+    CGB_CUDA(cudaGetLastError());
+}
+
+void launch_prep16(const MixedDev& md, int type, const double* fcoef, bf16* R16, cudaStream_t s) {
+    if (md.ntiles == 0) return;
+    prep16_kernel<<<md.ntiles, 128, 0, s>>>(md, type, fcoef, R16);
+    CGB_CUDA(cudaGetLastError());
+}
+
+void launch_fock16(const CUtensorMap& tm_l, const CUtensorMap& tm_r, long rows, int ctas, const int* job_off,
+                   const FockJob* jobs, int ncomp, double* wpart, int* err, cudaStream_t s) {
+    if (ctas == 0) return;
+    fock16_kernel<<<ctas, kF16Threads, 2 * kStageBytes + 1024, s>>>(tm_l, tm_r, rows, job_off, jobs, ncomp, wpart,
+                                                                     err);
     CGB_CUDA(cudaGetLastError());
 }
 

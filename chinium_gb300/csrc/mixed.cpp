@@ -403,8 +403,34 @@ void Grid::prepare_mixed(const MixedConfig& cfg) {
     md.e32 = m.d_e32.p;
     launch_ao_mixed(md, dev_shells(), m.d_tile_shells.p, m.d_tile_shell_off.p, m.d_x.p, m.d_y.p, m.d_z.p, m.d_shtab.p,
                     m.ao_comp, m.d_e32.p, s);
-    m.d_Z.alloc((size_t)md.rows * kTilePts);
-    m.d_c2.alloc(type >= 2 ? (size_t)md.Gt : 1);
+    // pre-split V operands when they fit: AO planes (3 per component) and R
+    // planes (3 for Z, 9 more for the meta-GGA components), at most half of
+    // the free memory
+    {
+        const int ncv = type >= 2 ? 4 : 1;
+        const size_t n16 = (size_t)md.rows * kTilePts;
+        const size_t need = (size_t)(3 * m.ao_comp + 3 * ncv) * n16 * sizeof(__nv_bfloat16);
+        size_t freeb = 0, totalb = 0;
+        CGB_CUDA(cudaMemGetInfo(&freeb, &totalb));
+        const bool coord_ok = (long)(3 * std::max(m.ao_comp, ncv)) * md.rows < (1L << 31);
+        m.use16 = coord_ok && (cfg.v_operands == 2 || (cfg.v_operands == 0 && need < freeb / 2));
+        CGB_CHECK(cfg.v_operands != 2 || m.use16, XC_ERR_UNSUPPORTED,
+                  "pre-split V operands do not fit (TMA row coordinate)");
+        if (m.use16) {
+            m.d_e16.alloc((size_t)3 * m.ao_comp * n16);
+            m.d_R16.alloc((size_t)3 * ncv * n16);
+            launch_split_store(m.d_e32.p, (long)n16, m.ao_comp, m.d_e16.p, s);
+            make_tmap_bf16(&m.tm_e16, m.d_e16.p, kTilePts, (uint64_t)3 * m.ao_comp * md.rows, 64, 64);
+            make_tmap_bf16(&m.tm_r16, m.d_R16.p, kTilePts, (uint64_t)3 * ncv * md.rows, 64, 64);
+            m.d_Z.alloc(1);
+            m.d_c2.alloc(1);
+        } else {
+            m.d_e16.alloc(1);
+            m.d_R16.alloc(1);
+            m.d_Z.alloc((size_t)md.rows * kTilePts);
+            m.d_c2.alloc(type >= 2 ? (size_t)md.Gt : 1);
+        }
+    }
     m.d_Dp.alloc((size_t)nspin * 3 * drows * dcols);
     m.d_wpart.alloc((size_t)std::max(m.nitems, 1L) * 16384);
     m.d_err.alloc(1);
@@ -412,7 +438,7 @@ void Grid::prepare_mixed(const MixedConfig& cfg) {
     make_tmap_bf16(&m.tm_d, m.d_Dp.p, dcols, (uint64_t)nspin * 3 * drows, 64, 64);
     make_tmap_f32(&m.tm_raw_d, m.d_e32.p, kTilePts, (uint64_t)m.ao_comp * md.rows, 128, 64);
     make_tmap_f32(&m.tm_raw_f, m.d_e32.p, kTilePts, (uint64_t)m.ao_comp * md.rows, 32, 64);
-    make_tmap_f32(&m.tm_z, m.d_Z.p, kTilePts, (uint64_t)md.rows, 32, 64);
+    if (!m.use16) make_tmap_f32(&m.tm_z, m.d_Z.p, kTilePts, (uint64_t)md.rows, 32, 64);
     const long Gt = md.Gt;
     const int nsig = nspin == 1 ? 1 : 3;
     m.rho.alloc(nspin * Gt);
@@ -487,10 +513,9 @@ void Grid::build_mixed(const double* dD, const Functional& f, double* dE, double
     mark(3);
     const int ncomp = f.family >= 2 ? 4 : 1;
     for (int s = 0; s < nspin; s++) {
-        launch_prep_z(md, f.family, m.fcoef.p + (size_t)s * 5 * Gt, m.d_Z.p, m.d_c2.p, stream);
+        v_prep(m.fcoef.p + (size_t)s * 5 * Gt, f.family);
         mark(5 + 3 * s);
-        launch_fock_tc(m.tm_raw_f, m.tm_z, md.rows, m.fock_ctas, m.d_fock_off.p, m.d_fock_jobs.p, m.d_c2.p, ncomp,
-                       m.d_wpart.p, m.d_err.p, stream);
+        v_partials(ncomp);
         mark(6 + 3 * s);
         launch_wsum(m.d_wpart.p, m.d_item_live.p, m.d_mols.p, nmol, maxn, s, nspin, dV, stream);
         mark(7 + 3 * s);
@@ -578,9 +603,8 @@ void Grid::build_incremental(const double* dD, const Functional& f, double* dE, 
         mark(3);
         const int ncomp = f.family >= 2 ? 4 : 1;
         for (int s = 0; s < nspin; s++) {
-            launch_prep_z(md, f.family, m.d_fcoef_ref.p + (size_t)s * 5 * Gt, m.d_Z.p, m.d_c2.p, stream);
-            launch_fock_tc(m.tm_raw_f, m.tm_z, md.rows, m.fock_ctas, m.d_fock_off.p, m.d_fock_jobs.p, m.d_c2.p,
-                           ncomp, m.d_wpart.p, m.d_err.p, stream);
+            v_prep(m.d_fcoef_ref.p + (size_t)s * 5 * Gt, f.family);
+            v_partials(ncomp);
             launch_wsum(m.d_wpart.p, m.d_item_live.p, m.d_mols.p, 1, n, s, nspin, dV, stream);
         }
         mark(4);
@@ -622,9 +646,8 @@ void Grid::build_incremental(const double* dD, const Functional& f, double* dE, 
     launch_axpby((long)(5 * G1), 1.0, m.fcoef.p, -1.0, m.d_fcoef_ref.p, m.d_dfcoef.p, stream);
     const int ncomp = f.family >= 2 ? 4 : 1;
     for (int s = 0; s < nspin; s++) {
-        launch_prep_z(md, f.family, m.d_dfcoef.p + (size_t)s * 5 * Gt, m.d_Z.p, m.d_c2.p, stream);
-        launch_fock_tc(m.tm_raw_f, m.tm_z, md.rows, m.fock_ctas, m.d_fock_off.p, m.d_fock_jobs.p, m.d_c2.p, ncomp,
-                       m.d_wpart.p, m.d_err.p, stream);
+        v_prep(m.d_dfcoef.p + (size_t)s * 5 * Gt, f.family);
+        v_partials(ncomp);
         launch_wsum(m.d_wpart.p, m.d_item_live.p, m.d_mols.p, 1, maxn, s, nspin, dV, stream);
     }
     launch_axpby((long)nn, 1.0, dV, 1.0, m.d_Vref.p, dV, stream);
@@ -642,6 +665,26 @@ void Grid::save_refs(const double* dD, const double* dV) {
     if (type >= 2) CGB_CUDA(cudaMemcpyAsync(m.d_tau_ref.p, m.tau.p, G1 * 8, cudaMemcpyDeviceToDevice, stream));
     CGB_CUDA(cudaMemcpyAsync(m.d_fcoef_ref.p, m.fcoef.p, 5 * G1 * 8, cudaMemcpyDeviceToDevice, stream));
     CGB_CUDA(cudaMemcpyAsync(m.d_Vref.p, dV, nn * 8, cudaMemcpyDeviceToDevice, stream));
+}
+
+// The R operands of V for one spin's coefficients (tile order).
+void Grid::v_prep(const double* fcoef_s, int family) {
+    MixedState& m = mx;
+    if (m.use16)
+        launch_prep16(m.md, family, fcoef_s, m.d_R16.p, stream);
+    else
+        launch_prep_z(m.md, family, fcoef_s, m.d_Z.p, m.d_c2.p, stream);
+}
+
+// W partials of every V work item on the tensor cores (components 0..ncomp-1).
+void Grid::v_partials(int ncomp) {
+    MixedState& m = mx;
+    if (m.use16)
+        launch_fock16(m.tm_e16, m.tm_r16, m.md.rows, m.fock_ctas, m.d_fock_off.p, m.d_fock_jobs.p, ncomp, m.d_wpart.p,
+                      m.d_err.p, stream);
+    else
+        launch_fock_tc(m.tm_raw_f, m.tm_z, m.md.rows, m.fock_ctas, m.d_fock_off.p, m.d_fock_jobs.p, m.d_c2.p, ncomp,
+                       m.d_wpart.p, m.d_err.p, stream);
 }
 
 int Grid::mixed_error() {

@@ -70,8 +70,10 @@ struct MixedConfig {
     int fock_tiles = 0;      // tiles per V work item (0: from the SM count)
     int spatial = 1;         // 1: tiles from a k-d split of each molecule's points; 0: generation order
     double func_float_above = 1e-3;  // FP32 functional at points with total density >= this
+    int v_operands = 0;      // V kernel operands: 0 auto (by free memory), 1 converted in-kernel, 2 pre-split
     bool same_tiles(const MixedConfig& o) const {
-        return screen == o.screen && fock_tiles == o.fock_tiles && spatial == o.spatial;
+        return screen == o.screen && fock_tiles == o.fock_tiles && spatial == o.spatial &&
+               v_operands == o.v_operands;
     }
 };
 
@@ -102,6 +104,8 @@ struct MixedState {
     DevBuf<long> d_perm;                 // FP64-array index of each tile point; -(i+1) on padding
     bool have_perm = false;
     DevBuf<float> d_e32, d_Z, d_c2;
+    bool use16 = false;                  // V kernel on pre-split planes
+    DevBuf<__nv_bfloat16> d_e16, d_R16;  // AO store planes [c][p][rows][128]; R planes [c][p][rows][128]
     DevBuf<__nv_bfloat16> d_Dp;
     DevBuf<double> d_wpart;
     DevBuf<int> d_err;
@@ -116,6 +120,7 @@ struct MixedState {
     CUtensorMap tm_raw_d;                  // e32, box 128 points x 64 rows (density A tiles)
     CUtensorMap tm_raw_f;                  // e32, box 32 points x 64 rows (V_xc L / R boxes)
     CUtensorMap tm_z;                      // Z, box 32 points x 64 rows
+    CUtensorMap tm_e16, tm_r16;            // BF16 planes of e16 / R16, box 64 points x 64 rows
     // CUDA graph of one build (replayed while the functional and buffers are unchanged)
     cudaGraphExec_t graph = nullptr;
     std::vector<int> graph_ids;  // functional (libxc ids) and grid type the graph was captured for
@@ -144,6 +149,12 @@ void launch_combine(long n1, double* rho, const double* rho_b, double* rho1, con
 void launch_prep_z(const MixedDev& md, int type, const double* fcoef, float* Z, float* c2, cudaStream_t s);
 void launch_fock_tc(const CUtensorMap& tm_e32, const CUtensorMap& tm_z, long rows, int ctas, const int* job_off,
                     const FockJob* jobs, const float* c2, int ncomp, double* wpart, int* err, cudaStream_t s);
+// FP32 store (ncomp planes of n) -> BF16 planes e16[(c * 3 + p) * n + i].
+void launch_split_store(const float* e32, long n, int ncomp, __nv_bfloat16* e16, cudaStream_t s);
+// R planes of the pre-split V kernel: Z (component 0) and c2 d_c phi (1-3, meta-GGA).
+void launch_prep16(const MixedDev& md, int type, const double* fcoef, __nv_bfloat16* R16, cudaStream_t s);
+void launch_fock16(const CUtensorMap& tm_l, const CUtensorMap& tm_r, long rows, int ctas, const int* job_off,
+                   const FockJob* jobs, int ncomp, double* wpart, int* err, cudaStream_t s);
 // V_m(mu, nu) = sum over splits of W(mu, nu) + W(nu, mu), packed per molecule.
 void launch_wsum(const double* wpart, const int* item_live, const MolRange* mols, int nmol, int maxn, int nspin_index,
                  int nspin, double* V, cudaStream_t s);

@@ -98,6 +98,8 @@ struct Grid {
     // anchor: 0 incremental (FP64 anchor on the first call), 1 FP64 anchor, 2 tensor-core anchor
     void build_incremental(const double* dD, const Functional& f, double* dE, double* dV, int anchor);
     void save_refs(const double* dD, const double* dV);
+    void v_prep(const double* fcoef_s, int family);
+    void v_partials(int ncomp);
     int mixed_error();
 };
 

@@ -132,12 +132,15 @@ class Grid:
     def mixed_config(self):
         c = MixedConfig()
         check(lib().xc_grid_get_mixed_config(self._h, ctypes.byref(c)))
-        return dict(screen=c.screen, fock_tiles=c.fock_tiles, spatial=c.spatial, func_float_above=c.func_float_above)
+        return dict(screen=c.screen, fock_tiles=c.fock_tiles, spatial=c.spatial, func_float_above=c.func_float_above,
+                    v_operands=c.v_operands)
 
-    def set_mixed_config(self, screen=1e-11, fock_tiles=0, spatial=1, func_float_above=1e-3):
+    def set_mixed_config(self, screen=1e-11, fock_tiles=0, spatial=1, func_float_above=1e-3, v_operands=0):
         """func_float_above: total density from which the mixed path's
-        functional runs in FP32 (float("inf"): FP64 everywhere)."""
-        c = MixedConfig(float(screen), int(fock_tiles), int(spatial), float(func_float_above))
+        functional runs in FP32 (float("inf"): FP64 everywhere).  v_operands:
+        V kernel operands split in-kernel (1), pre-split in HBM (2), or
+        chosen by free memory (0)."""
+        c = MixedConfig(float(screen), int(fock_tiles), int(spatial), float(func_float_above), int(v_operands), 0)
         check(lib().xc_grid_set_mixed_config(self._h, ctypes.byref(c)))
 
     def tune(self, xc, D, e_tol=1e-7, v_tol=1e-6, reps=3):
@@ -148,7 +151,7 @@ class Grid:
         check(lib().xc_grid_tune(self._h, xc._h, _p(D), self.nspin, float(e_tol), float(v_tol), int(reps),
                                  ctypes.byref(r)))
         cfg = lambda c: dict(screen=c.screen, fock_tiles=c.fock_tiles, spatial=c.spatial,
-                             func_float_above=c.func_float_above)
+                             func_float_above=c.func_float_above, v_operands=c.v_operands)
         cands = [dict(cfg(c.cfg), ms=c.ms, max_de=c.max_de, max_dv=c.max_dv, kept_pairs=c.kept_pairs,
                       accepted=bool(c.accepted)) for c in r.cand[:r.ncand]]
         return dict(best=cfg(r.best), ms_best=r.ms_best, ms_reference=r.ms_reference, candidates=cands)

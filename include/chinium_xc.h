@@ -260,13 +260,18 @@ int xc_grid_molecules(const xc_grid* g, int* nmol, int* nbasis, long* npoints, l
  * func_float_above: points whose total density is at least this value
  * evaluate the functional in FP32, the rest in FP64 (default 1e-3; +inf or
  * any value above every density keeps the whole functional in FP64).
- * Changing screen, fock_tiles or spatial discards the prepared tiles
- * (rebuilt at the next build). */
+ * v_operands: operands of the V_xc kernel, 1 split from FP32 inside the
+ * kernel, 2 BF16 planes split beforehand in HBM (1.5x the AO store plus the
+ * per-build R planes), 0 = 2 when that fits in half of the free memory.
+ * Changing screen, fock_tiles, spatial or v_operands discards the prepared
+ * tiles (rebuilt at the next build). */
 typedef struct xc_mixed_config {
     double screen;
     int fock_tiles;
     int spatial;
     double func_float_above;
+    int v_operands;
+    int reserved;
 } xc_mixed_config;
 int xc_grid_set_mixed_config(xc_grid* g, const xc_mixed_config* cfg);
 int xc_grid_get_mixed_config(const xc_grid* g, xc_mixed_config* cfg);

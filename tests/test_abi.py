@@ -151,7 +151,8 @@ def test_batch_and_tuning_argument_errors():
 
 def test_mixed_config_struct_layout():
     from chinium_gb300._lib import MixedConfig, TuneCandidate, TuneReport
-    assert ctypes.sizeof(MixedConfig) == 24
+    assert ctypes.sizeof(MixedConfig) == 32
     assert MixedConfig.func_float_above.offset == 16
-    assert ctypes.sizeof(TuneCandidate) == 24 + 3 * 8 + 8 + 8
-    assert TuneReport.cand.offset == 24 + 8 + 8 + 8
+    assert MixedConfig.v_operands.offset == 24
+    assert ctypes.sizeof(TuneCandidate) == 32 + 3 * 8 + 8 + 8
+    assert TuneReport.cand.offset == 32 + 8 + 8 + 8

@@ -153,3 +153,53 @@ def test_fe4s4_uks_tpss_sg3_mixed_vs_fp64():
     # the FP32 functional (above rho = 1e-3) at iron-core densities gives ~2e-6
     # relative error on the largest V elements (measured 2.1e-6 of max|V| = 9.8)
     assert dE < 5e-5 and dV < 5e-6 * vmax
+
+
+@pytest.mark.parametrize("name,nspin", [("PBE", 1), ("TPSS", 1), ("R2SCAN", 2)])
+def test_presplit_v_operands_match_in_kernel_split(small_batch, name, nspin):
+    """The V kernel on BF16 planes split beforehand in HBM against the kernel
+    that splits FP32 operands itself: the same planes and products (only the
+    order of the correction sums differs), so V agrees to the FP32 rounding
+    of the per-tile sums (~1e-9 relative; a wrong plane, offset or scale
+    would show at 1e-3 or above) and E_xc (density side) is identical."""
+    mols, bases, Ds = small_batch
+    xc = cg.ExchangeCorrelation(spin=nspin).Read(name)
+    bg = cg.BatchGrid(bases, "SG-1", nspin=nspin)
+    bg.setType(xc.type)
+    Dn = [[D] if nspin == 1 else [0.5 * D, 0.45 * D] for D in Ds]
+    out = {}
+    for mode in (1, 2):
+        bg.set_mixed_config(fock_tiles=16, v_operands=mode)
+        out[mode] = bg.build(xc, Dn)
+        assert bg.mixed_config()["v_operands"] == mode
+    (E1, V1), (E2, V2) = out[1], out[2]
+    assert np.array_equal(E1, E2)
+    for a, b in zip(V1, V2):
+        for s in range(nspin):
+            scale = max(np.abs(a[s]).max(), 1.0)
+            assert np.abs(a[s] - b[s]).max() < 1e-7 * scale
+
+
+def test_presplit_v_operands_meta_gga_off_diagonal_items():
+    """Molecules above 128 functions: V items with I < J carry the meta-GGA
+    part with c2 doubled (halved accumulator, weight-2 drain on the
+    pre-split path)."""
+    mols = M.alkane_batch(count=2, seed=11, nmin=9, nmax=12)
+    bases = [cg.Basis(Z, xyz, "def2-svp") for Z, xyz in mols]
+    assert all(b.nbasis > 128 for b in bases)
+    Ds = [[density(b.nbasis, sum(Z) // 2, k)] for k, ((Z, _), b) in enumerate(zip(mols, bases))]
+    xc = cg.ExchangeCorrelation().Read("TPSS")
+    bg = cg.BatchGrid(bases, "SG-1")
+    bg.setType(xc.type)
+    out = {}
+    for mode in (1, 2):
+        bg.set_mixed_config(fock_tiles=16, v_operands=mode)
+        out[mode] = bg.build(xc, Ds)
+    for a, b in zip(out[1][1], out[2][1]):
+        assert np.abs(a[0] - b[0]).max() < 1e-7 * max(np.abs(a[0]).max(), 1.0)
+    g = cg.Grid(bases[0], "SG-1")
+    g.setType(xc.type)
+    g.getAO(0)
+    E64, V64 = g.build(xc, Ds[0])
+    assert abs(out[2][0][0] - E64) < BATCH_E_TOL
+    assert np.abs(out[2][1][0][0] - V64[0]).max() < BATCH_V_TOL
