@@ -43,6 +43,7 @@ namespace {
 using bf16 = __nv_bfloat16;
 
 constexpr int kThreads = 512;
+constexpr int kF16Threads = 384;               // kernels on pre-split operands: no converter warps
 constexpr int kEpiWarp0 = 4;                   // epilogue warps 4-11 (two per TMEM lane quadrant)
 constexpr int kEpiThreads = 256;
 constexpr int kConvWarps = 6;                  // warps 2-3 and 12-15
@@ -168,21 +169,26 @@ __device__ __forceinline__ void store_chunk(uint32_t planes, int r, int j, const
 // `first` starts both accumulators (unit boundary).
 // `halve` (V kernel, items with c2 doubled): the first product into each
 // accumulator halves it (D = A B + D / 2); the drain doubles the unit.
+// A_MN: the A planes are MN-major (two 64-row TMA boxes of a [K][M] array,
+// 8 KB apart), as the pre-split density kernel stages them.
+template <bool A_MN = false>
 __device__ __forceinline__ void mma_stage(uint32_t tmem, int buf, uint8_t* st, bool first, bool halve = false) {
     const uint32_t a0 = tc::smem_u32(st), b0 = a0 + 3 * kPlaneA;
     const uint32_t d_hh = tmem + buf * 256, d_corr = tmem + buf * 256 + 128;
+    constexpr uint32_t idesc = A_MN ? tc::idesc_bf16_amn(128, 128) : kIdesc;
 #pragma unroll
     for (int q = 0; q < 6; q++) {
-        const uint64_t ad = tc::smem_desc_sw128(a0 + c_prod_a[q] * kPlaneA);
+        const uint32_t pa = a0 + c_prod_a[q] * kPlaneA;
         const uint64_t bd = tc::smem_desc_sw128(b0 + c_prod_b[q] * kPlaneA);
         const uint32_t d = q == 0 ? d_hh : d_corr;
 #pragma unroll
-        for (int k = 0; k < 4; k++) {  // K = 16 per instruction: +32 bytes in the swizzled row
+        for (int k = 0; k < 4; k++) {  // K = 16 per instruction: +32 bytes in a K-major row, +2048 MN-major
+            const uint64_t ad = A_MN ? tc::smem_desc_sw128_mn(pa + k * 2048, kPlaneA / 2) : tc::smem_desc_sw128(pa) + 2 * k;
             const bool lead = k == 0 && (q == 0 || q == 1);
             if (halve && lead)
-                tc::mma_bf16_halve_d(d, ad + 2 * k, bd + 2 * k, kIdesc);
+                tc::mma_bf16_halve_d(d, ad, bd + 2 * k, idesc);
             else
-                tc::mma_bf16(d, ad + 2 * k, bd + 2 * k, kIdesc, (first && lead) ? 0u : 1u);
+                tc::mma_bf16(d, ad, bd + 2 * k, idesc, (first && lead) ? 0u : 1u);
         }
     }
 }
@@ -255,6 +261,77 @@ struct DensOut {
     double *rho_b, *rho1_b, *tau_b;  // column half 1
 };
 
+// Epilogue warps 4-11 of both density kernels: row g of the tile, columns
+// of slot 2 vb + half.
+template <int EPI>
+__device__ __forceinline__ void density_epilogue(Smem& sm, uint32_t tmem, const MixedDev& md, const int* job_off,
+                                                 const DensJob* jobs, int acomp, int spin, const DensOut& out, int* err,
+                                                 int warp, int lane) {
+    const long Gt = md.Gt;
+    const int quad = warp & 3, half = (warp - kEpiWarp0) >> 2;
+    const int g = quad * 32 + lane;
+    const size_t cs = (size_t)md.rows * 128;  // component stride of the FP32 store
+    double* rho = half ? out.rho_b : out.rho;
+    double* rho1 = half ? out.rho1_b : out.rho1;
+    double* tau = half ? out.tau_b : out.tau;
+    float T[64];
+#pragma unroll
+    for (int j = 0; j < 64; j++) T[j] = 0.f;
+    double acc_r = 0, acc_g0 = 0, acc_g1 = 0, acc_g2 = 0, acc_t = 0;
+    uint32_t uu = 0;
+    for (DensCursor c(job_off, jobs, EPI != 1); c.valid(); c.advance(jobs), uu++) {
+        const int b = uu & 1;
+        if (sm.abort) break;
+        if (!tc::mbar_wait(&sm.tfull[b], (uu >> 1) & 1)) {
+            flag_timeout(err, &sm);
+            break;
+        }
+        tc::fence_after_sync();
+        drain(tmem, b, quad, half, T, c.weight());
+        tc::fence_before_sync();
+        mbar_arrive(&sm.tempty[b]);
+        if (c.kc != c.job.nk - 1) continue;
+        // nu block complete: contract T with this row's AO values of the
+        // slot (a warp reads 32 consecutive points of one function: one
+        // 128-byte line per load)
+        const int slot = 2 * c.vb + half;
+        if (slot < c.job.nk && !sm.abort) {
+            float pr = 0, pg0 = 0, pg1 = 0, pg2 = 0, pt_ = 0;
+            const float* e0 = md.e32 + ((size_t)c.job.trow + slot * 64) * 128 + g;
+#pragma unroll
+            for (int j = 0; j < 64; j++) {
+                const float tv = T[j];
+                const size_t o = (size_t)j * 128;
+                if (EPI <= 1) pr = fmaf(tv, __ldg(e0 + o), pr);
+                if (EPI == 1) {
+                    pg0 = fmaf(tv, __ldg(e0 + cs + o), pg0);
+                    pg1 = fmaf(tv, __ldg(e0 + 2 * cs + o), pg1);
+                    pg2 = fmaf(tv, __ldg(e0 + 3 * cs + o), pg2);
+                }
+                if (EPI == 2) pt_ = fmaf(tv, __ldg(e0 + (size_t)acomp * cs + o), pt_);
+            }
+            acc_r += pr;
+            acc_g0 += 2.0 * pg0;
+            acc_g1 += 2.0 * pg1;
+            acc_g2 += 2.0 * pg2;
+            acc_t += 0.5 * pt_;
+        }
+#pragma unroll
+        for (int j = 0; j < 64; j++) T[j] = 0.f;
+        if (c.vb == c.nvb() - 1) {  // tile complete
+            const long pt = (long)c.job.t * 128 + g;
+            if (EPI <= 1) rho[(long)spin * Gt + pt] = acc_r;
+            if (EPI == 1) {
+                rho1[((long)spin * 3 + 0) * Gt + pt] = acc_g0;
+                rho1[((long)spin * 3 + 1) * Gt + pt] = acc_g1;
+                rho1[((long)spin * 3 + 2) * Gt + pt] = acc_g2;
+            }
+            if (EPI == 2) tau[(long)spin * Gt + pt] += acc_t;
+            acc_r = acc_g0 = acc_g1 = acc_g2 = acc_t = 0;
+        }
+    }
+}
+
 template <int EPI>
 __global__ void __launch_bounds__(kThreads, 1) density_tc_kernel(const __grid_constant__ CUtensorMap tm_d,
                                                                  const __grid_constant__ CUtensorMap tm_raw, MixedDev md,
@@ -270,7 +347,6 @@ __global__ void __launch_bounds__(kThreads, 1) density_tc_kernel(const __grid_co
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     init_cta(sm, 1 + kConvWarps, kConvWarps);
     const uint32_t tmem = sm.tmem;
-    const long Gt = md.Gt;
 
     if (warp == 0) {
         if (lane == 0) {
@@ -324,69 +400,7 @@ __global__ void __launch_bounds__(kThreads, 1) density_tc_kernel(const __grid_co
             }
         }
     } else if (warp >= kEpiWarp0 && warp < kEpiWarp0 + 8) {
-        // epilogue warps: row g of the tile, columns of slot 2 vb + half
-        const int quad = warp & 3, half = (warp - kEpiWarp0) >> 2;
-        const int g = quad * 32 + lane;
-        const size_t cs = (size_t)md.rows * 128;  // component stride of the FP32 store
-        double* rho = half ? out.rho_b : out.rho;
-        double* rho1 = half ? out.rho1_b : out.rho1;
-        double* tau = half ? out.tau_b : out.tau;
-        float T[64];
-#pragma unroll
-        for (int j = 0; j < 64; j++) T[j] = 0.f;
-        double acc_r = 0, acc_g0 = 0, acc_g1 = 0, acc_g2 = 0, acc_t = 0;
-        uint32_t uu = 0;
-        for (DensCursor c(job_off, jobs, EPI != 1); c.valid(); c.advance(jobs), uu++) {
-            const int b = uu & 1;
-            if (sm.abort) break;
-            if (!tc::mbar_wait(&sm.tfull[b], (uu >> 1) & 1)) {
-                flag_timeout(err, &sm);
-                break;
-            }
-            tc::fence_after_sync();
-            drain(tmem, b, quad, half, T, c.weight());
-            tc::fence_before_sync();
-            mbar_arrive(&sm.tempty[b]);
-            if (c.kc != c.job.nk - 1) continue;
-            // nu block complete: contract T with this row's AO values of the
-            // slot (a warp reads 32 consecutive points of one function: one
-            // 128-byte line per load)
-            const int slot = 2 * c.vb + half;
-            if (slot < c.job.nk && !sm.abort) {
-                float pr = 0, pg0 = 0, pg1 = 0, pg2 = 0, pt_ = 0;
-                const float* e0 = md.e32 + ((size_t)c.job.trow + slot * 64) * 128 + g;
-#pragma unroll
-                for (int j = 0; j < 64; j++) {
-                    const float tv = T[j];
-                    const size_t o = (size_t)j * 128;
-                    if (EPI <= 1) pr = fmaf(tv, __ldg(e0 + o), pr);
-                    if (EPI == 1) {
-                        pg0 = fmaf(tv, __ldg(e0 + cs + o), pg0);
-                        pg1 = fmaf(tv, __ldg(e0 + 2 * cs + o), pg1);
-                        pg2 = fmaf(tv, __ldg(e0 + 3 * cs + o), pg2);
-                    }
-                    if (EPI == 2) pt_ = fmaf(tv, __ldg(e0 + (size_t)acomp * cs + o), pt_);
-                }
-                acc_r += pr;
-                acc_g0 += 2.0 * pg0;
-                acc_g1 += 2.0 * pg1;
-                acc_g2 += 2.0 * pg2;
-                acc_t += 0.5 * pt_;
-            }
-#pragma unroll
-            for (int j = 0; j < 64; j++) T[j] = 0.f;
-            if (c.vb == c.nvb() - 1) {  // tile complete
-                const long pt = (long)c.job.t * 128 + g;
-                if (EPI <= 1) rho[(long)spin * Gt + pt] = acc_r;
-                if (EPI == 1) {
-                    rho1[((long)spin * 3 + 0) * Gt + pt] = acc_g0;
-                    rho1[((long)spin * 3 + 1) * Gt + pt] = acc_g1;
-                    rho1[((long)spin * 3 + 2) * Gt + pt] = acc_g2;
-                }
-                if (EPI == 2) tau[(long)spin * Gt + pt] += acc_t;
-                acc_r = acc_g0 = acc_g1 = acc_g2 = acc_t = 0;
-            }
-        }
+        density_epilogue<EPI>(sm, tmem, md, job_off, jobs, acomp, spin, out, err, warp, lane);
     } else if (warp >= 2) {
         // converter warps: the raw Phi tile [64 functions][128 points] is read
         // into registers (releasing the buffer for the next TMA load), split
@@ -417,6 +431,79 @@ __global__ void __launch_bounds__(kThreads, 1) density_tc_kernel(const __grid_co
             }
             conv_publish(&sm.full[s]);
         }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, kTmemCols);
+}
+
+// The density kernel on the pre-split AO planes: the A operand (Phi of the
+// mu chunk, points x functions) is TMA-loaded MN-major from the BF16 store
+// (two 64-point boxes per plane), so no warp converts; 384 threads (warp 0
+// TMA, warp 1 MMA, warps 4-11 epilogue).
+template <int EPI>
+__global__ void __launch_bounds__(kF16Threads, 1) density16_kernel(const __grid_constant__ CUtensorMap tm_d,
+                                                                   const __grid_constant__ CUtensorMap tm_e16,
+                                                                   MixedDev md, const int* __restrict__ job_off,
+                                                                   const DensJob* __restrict__ jobs, int acomp,
+                                                                   int spin, DensOut out, int* err) {
+    extern __shared__ uint8_t smem_raw[];
+    __shared__ Smem sm;
+    __shared__ int s_chunks[kMaxChunks];
+    uint8_t* smem = smem_raw + (((tc::smem_u32(smem_raw) + 1023u) & ~1023u) - tc::smem_u32(smem_raw));
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    init_cta(sm, 1, 1);
+    const uint32_t tmem = sm.tmem;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            uint32_t uu = 0;
+            for (DensCursor c(job_off, jobs, EPI != 1); c.valid(); c.advance(jobs), uu++) {
+                if (c.vb == 0 && c.kc == 0) {  // new tile: its kept chunk ids
+                    const int* src = md.tile_chunks + (size_t)c.job.t * md.nchunk;
+                    for (int k = 0; k < c.job.nk; k++) s_chunks[k] = __ldg(src + k);
+                }
+                const int s = uu & 1;
+                if (sm.abort || !tc::mbar_wait(&sm.empty[s], ((uu >> 1) & 1) ^ 1)) {
+                    flag_timeout(err, &sm);
+                    break;
+                }
+                uint8_t* st = smem + (size_t)s * kStageBytes;
+                tc::mbar_arrive_expect_tx(&sm.full[s], 6 * kPlaneA);
+                const int gmu = s_chunks[c.kc];
+                const long arow = (long)c.job.trow + (long)c.kc * 64;
+                for (int p = 0; p < 3; p++) {
+                    const int ya = (int)((long)(acomp * 3 + p) * md.rows + arow);
+                    tc::tma_load_2d(st + p * kPlaneA, &tm_e16, 0, ya, &sm.full[s]);
+                    tc::tma_load_2d(st + p * kPlaneA + kPlaneA / 2, &tm_e16, 64, ya, &sm.full[s]);
+                    for (int h = 0; h < 2; h++) {
+                        const int vs = 2 * c.vb + h < c.job.nk ? 2 * c.vb + h : c.job.nk - 1;
+                        tc::tma_load_2d(st + (3 + p) * kPlaneA + h * (kPlaneA / 2), &tm_d, gmu * 64,
+                                        (int)((spin * 3 + p) * md.drows + (long)(c.job.c0 + s_chunks[vs]) * 64),
+                                        &sm.full[s]);
+                    }
+                }
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            uint32_t uu = 0;
+            for (DensCursor c(job_off, jobs, EPI != 1); c.valid(); c.advance(jobs), uu++) {
+                const int s = uu & 1, b = uu & 1;
+                const uint32_t ph = (uu >> 1) & 1;
+                if (sm.abort || !tc::mbar_wait(&sm.tempty[b], ph ^ 1) || !tc::mbar_wait(&sm.full[s], ph)) {
+                    flag_timeout(err, &sm);
+                    tc::mma_commit(&sm.tfull[b]);  // release the epilogue
+                    break;
+                }
+                tc::fence_after_sync();
+                mma_stage<true>(tmem, b, smem + (size_t)s * kStageBytes, true);
+                tc::mma_commit(&sm.empty[s]);
+                tc::mma_commit(&sm.tfull[b]);
+            }
+        }
+    } else if (warp >= kEpiWarp0 && warp < kEpiWarp0 + 8) {
+        density_epilogue<EPI>(sm, tmem, md, job_off, jobs, acomp, spin, out, err, warp, lane);
     }
     tc::fence_before_sync();
     __syncthreads();
@@ -672,7 +759,6 @@ __global__ void __launch_bounds__(kThreads, 1) fock_tc_kernel(const __grid_const
 // Items with c2 doubled (I < J) halve the accumulators at their first
 // meta-GGA product and are drained with weight 2 (both exact).
 // CTA roles (384 threads): warp 0 TMA, warp 1 MMA, warps 4-11 drain.
-constexpr int kF16Threads = 384;
 
 struct Fock16Cursor {
     int j, end, c, kh, ncomp, nc_all;
@@ -1119,8 +1205,11 @@ void set_mixed_kernel_attributes() {
     CGB_CUDA(cudaFuncSetAttribute(density_tc_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     CGB_CUDA(cudaFuncSetAttribute(density_tc_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     CGB_CUDA(cudaFuncSetAttribute(fock_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    CGB_CUDA(cudaFuncSetAttribute(fock16_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)(2 * kStageBytes + 1024)));
+    const int smem16 = (int)(2 * kStageBytes + 1024);
+    CGB_CUDA(cudaFuncSetAttribute(fock16_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem16));
+    CGB_CUDA(cudaFuncSetAttribute(density16_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem16));
+    CGB_CUDA(cudaFuncSetAttribute(density16_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem16));
+    CGB_CUDA(cudaFuncSetAttribute(density16_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem16));
 }
 
 void launch_density_tc(const CUtensorMap& tm_d, const CUtensorMap& tm_raw, const MixedDev& md, int ctas,
@@ -1137,6 +1226,23 @@ void launch_density_tc(const CUtensorMap& tm_d, const CUtensorMap& tm_raw, const
         density_tc_kernel<1><<<ctas, kThreads, smem, s>>>(tm_d, tm_raw, md, job_off, jobs, acomp, spin, o, err);
     else
         density_tc_kernel<2><<<ctas, kThreads, smem, s>>>(tm_d, tm_raw, md, job_off, jobs, acomp, spin, o, err);
+    CGB_CUDA(cudaGetLastError());
+}
+
+void launch_density16(const CUtensorMap& tm_d, const CUtensorMap& tm_e16, const MixedDev& md, int ctas,
+                      const int* job_off, const DensJob* jobs, int epi, int acomp, int spin, double* rho,
+                      double* rho1, double* tau, double* rho_b, double* rho1_b, double* tau_b, int* err,
+                      cudaStream_t s) {
+    if (ctas == 0) return;
+    CGB_CHECK(md.nchunk <= kMaxChunks, XC_ERR_UNSUPPORTED, "more than 16384 basis functions in one molecule");
+    const size_t smem = 2 * kStageBytes + 1024;
+    DensOut o{rho, rho1, tau, rho_b, rho1_b, tau_b};
+    if (epi == 0)
+        density16_kernel<0><<<ctas, kF16Threads, smem, s>>>(tm_d, tm_e16, md, job_off, jobs, acomp, spin, o, err);
+    else if (epi == 1)
+        density16_kernel<1><<<ctas, kF16Threads, smem, s>>>(tm_d, tm_e16, md, job_off, jobs, acomp, spin, o, err);
+    else
+        density16_kernel<2><<<ctas, kF16Threads, smem, s>>>(tm_d, tm_e16, md, job_off, jobs, acomp, spin, o, err);
     CGB_CUDA(cudaGetLastError());
 }
 

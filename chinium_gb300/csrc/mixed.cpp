@@ -482,13 +482,18 @@ void Grid::density_passes(const __nv_bfloat16*) {
         CGB_CUDA(cudaMemsetAsync(m.tau.p, 0, sizeof(double) * nspin * Gt, stream));
         CGB_CUDA(cudaMemsetAsync(m.tau_b.p, 0, sizeof(double) * nspin * Gt, stream));
     }
+    const auto pass = [&](int epi, int acomp, int s) {
+        if (m.use16)
+            launch_density16(m.tm_d, m.tm_e16, md, m.dens_ctas, m.d_dens_off.p, m.d_dens_jobs.p, epi, acomp, s, m.rho.p,
+                             m.rho1.p, m.tau.p, m.rho_b.p, m.rho1_b.p, m.tau_b.p, m.d_err.p, stream);
+        else
+            launch_density_tc(m.tm_d, m.tm_raw_d, md, m.dens_ctas, m.d_dens_off.p, m.d_dens_jobs.p, epi, acomp, s,
+                              m.rho.p, m.rho1.p, m.tau.p, m.rho_b.p, m.rho1_b.p, m.tau_b.p, m.d_err.p, stream);
+    };
     for (int s = 0; s < nspin; s++) {
-        launch_density_tc(m.tm_d, m.tm_raw_d, md, m.dens_ctas, m.d_dens_off.p, m.d_dens_jobs.p, type >= 1 ? 1 : 0, 0, s,
-                          m.rho.p, m.rho1.p, m.tau.p, m.rho_b.p, m.rho1_b.p, m.tau_b.p, m.d_err.p, stream);
+        pass(type >= 1 ? 1 : 0, 0, s);
         if (type >= 2)
-            for (int r = 1; r <= 3; r++)
-                launch_density_tc(m.tm_d, m.tm_raw_d, md, m.dens_ctas, m.d_dens_off.p, m.d_dens_jobs.p, 2, r, s,
-                                  m.rho.p, m.rho1.p, m.tau.p, m.rho_b.p, m.rho1_b.p, m.tau_b.p, m.d_err.p, stream);
+            for (int r = 1; r <= 3; r++) pass(2, r, s);
     }
     launch_combine((long)nspin * Gt, m.rho.p, m.rho_b.p, m.rho1.p, m.rho1_b.p, m.tau.p, m.tau_b.p, type, stream);
 }

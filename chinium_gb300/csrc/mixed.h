@@ -143,6 +143,11 @@ void launch_density_tc(const CUtensorMap& tm_d, const CUtensorMap& tm_raw, const
                        const int* job_off, const DensJob* jobs, int epi, int acomp, int spin, double* rho,
                        double* rho1, double* tau, double* rho_b, double* rho1_b, double* tau_b, int* err,
                        cudaStream_t s);
+// The same on the pre-split AO planes (tm_e16: A operand MN-major, no conversion).
+void launch_density16(const CUtensorMap& tm_d, const CUtensorMap& tm_e16, const MixedDev& md, int ctas,
+                      const int* job_off, const DensJob* jobs, int epi, int acomp, int spin, double* rho,
+                      double* rho1, double* tau, double* rho_b, double* rho1_b, double* tau_b, int* err,
+                      cudaStream_t s);
 void launch_combine(long n1, double* rho, const double* rho_b, double* rho1, const double* rho1_b, double* tau,
                     const double* tau_b, int type, cudaStream_t s);
 // Z = c0 phi + c1 . grad phi (FP32, e32 row layout) and c2 per point (meta-GGA).

@@ -192,6 +192,19 @@ __device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr) {
     return d;
 }
 
+// MN-major operand staged by TMA with 128-byte swizzle from a [K][MN] array:
+// K rows of 128 B (64 bf16 along MN), 8-row groups 1024 B apart (SBO), the
+// next 64 MN elements `lbo` bytes on (LBO); a K step of 16 is +2048 B.
+__device__ __forceinline__ uint64_t smem_desc_sw128_mn(uint32_t saddr, uint32_t lbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;  // leading byte offset: between 64-element MN blocks
+    d |= (uint64_t)(1024 >> 4) << 32;            // stride byte offset: 8 K rows x 128 B
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)2 << 61;
+    return d;
+}
+
 // Instruction descriptor of kind::f16: BF16 A and B (K-major), FP32 D.
 __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
     return (1u << 4)                      // D = F32
@@ -200,6 +213,8 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
            | ((uint32_t)(N >> 3) << 17)   // N / 8
            | ((uint32_t)(M >> 4) << 24);  // M / 16
 }
+// The same with A MN-major (transpose-A bit).
+__host__ __device__ constexpr uint32_t idesc_bf16_amn(int M, int N) { return idesc_bf16(M, N) | (1u << 15); }
 
 // Three-term BF16 split of a double: x ~= h + m + l (relative error ~2^-24).
 __device__ __forceinline__ void split3(double x, __nv_bfloat16& h, __nv_bfloat16& m, __nv_bfloat16& l) {
