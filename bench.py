@@ -165,13 +165,19 @@ def run_reference(args):
 
 
 def mixed_roofline(info, kms, stage, peaks, family, nspin):
-    """Tensor-core roofline of the dominant mixed kernel (algorithmic FLOPs ÷
-    CUDA-event duration).  Algorithmic FLOPs per build, from the grid's unit
+    """Roofline of the dominant mixed kernel against both of its limits.
+    Tensor: algorithmic FLOPs ÷ CUDA-event duration, from the grid's unit
     counts: density 2*128*128*64 per unit — a full pass (rho + grad rho, GGA /
     meta-GGA) has units_full units, a symmetric pass (rho of LDA, each of the
     three tau components) units_sym; V_xc 2*128^3 per (item, tile) job and
     component (components 1-3 only on jobs with I <= J).  The tensor core
-    executes 6x that (three-term split cross products)."""
+    executes 6x that (three-term split cross products).  HBM: algorithmic
+    bytes ÷ duration — per kept (function, point) pair the A operand (6 B of
+    BF16 planes, or 4 B FP32 when split in-kernel) plus the FP32 values the
+    density epilogue contracts (4 B per component), or the V kernel's L and R
+    operands per component; plus the FP64 outputs (densities per point, one
+    128 x 128 W partial per V item).  The reported bound is the resource with
+    the larger fraction (HBM vs the tensor pipe's executed FLOPs)."""
     unit = 2.0 * 128 * 128 * 64
     if family == 0:
         fl_den = info["mixed_units_sym"] * unit * nspin
@@ -182,15 +188,41 @@ def mixed_roofline(info, kms, stage, peaks, family, nspin):
     jobs = info["mixed_fock_jobs"] + (3 * info["mixed_fock_tau_jobs"] if family >= 2 else 0)
     fl_fock = jobs * 2.0 * 128 ** 3 * nspin  # one fock_tc launch per spin; kms[4] sums them
     ms_den, ms_fock = kms[0], kms[4]
-    dom, dom_ms, fl = ("density_tc", ms_den, fl_den) if ms_den >= ms_fock else ("fock_tc", ms_fock, fl_fock)
+    # kernels on pre-split BF16 planes (density16 / fock16) or converting FP32 tiles in-kernel
+    presplit = bool(info.get("mixed_presplit"))
+    kd, kf = ("density16", "fock16") if presplit else ("density_tc", "fock_tc")
+    # algorithmic HBM bytes per build: every operand byte read once, outputs written once
+    rp = info["mixed_rows"] * 128  # kept (function, point) pairs of all tiles
+    G = info["mixed_tiles"] * 128
+    a_op = 6 if presplit else 4    # A operand bytes per element (BF16 planes or FP32)
+    if family == 0:
+        by_den = rp * (a_op + 4) + G * 16
+    elif family == 1:
+        by_den = rp * (a_op + 16) + G * 64
+    else:
+        by_den = rp * (a_op + 16) + G * 64 + 3 * (rp * (a_op + 4) + G * 32)
+    ncv = 4 if family >= 2 else 1
+    by_fock = rp * ncv * (a_op + (6 if presplit else 4)) + info.get("mixed_fock_items", 0) * 16384 * 8
+    by_den, by_fock = by_den * nspin, by_fock * nspin
+    dom, dom_ms, fl, by = (kd, ms_den, fl_den, by_den) if ms_den >= ms_fock else (kf, ms_fock, fl_fock, by_fock)
     achieved = fl / (dom_ms / 1e3) / 1e12
     peak = peaks.get("bf16_tflops", 1900.0)
-    return {"bound": "tensor", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-            "frac": achieved / peak, "traffic": None,
-            "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst) -- of measured",
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    hbm = by / (dom_ms / 1e3) / 1e9
+    tensor = {"achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+              "executed_tflops": 6 * achieved, "executed_frac": 6 * achieved / peak,
+              "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst) -- of measured"}
+    memory = {"achieved": hbm, "peak": hbm_peak, "unit": "GB/s", "frac": hbm / hbm_peak,
+              "algorithmic_bytes_per_build": by, "peak_source": "MEASURED_PEAKS.json hbm_gbs -- of measured"}
+    # the binding resource: the larger of the HBM fraction and the tensor pipe's executed fraction
+    hbm_bound = memory["frac"] >= tensor["executed_frac"]
+    main = memory if hbm_bound else tensor
+    return {"bound": "hbm" if hbm_bound else "tensor", "kernel": dom, "achieved": main["achieved"],
+            "peak": main["peak"], "unit": main["unit"], "frac": main["frac"], "traffic": None,
+            "peak_source": main["peak_source"], "tensor": tensor, "hbm": memory,
             "executed_tensor_tflops": 6 * achieved, "executed_frac": 6 * achieved / peak,
-            "kernel_ms": {"density_tc(+split,combine)": kms[0], "functional": kms[1], "energy": kms[2],
-                          "prep_z": kms[3], "fock_tc": kms[4], "wsum": kms[5]},
+            "kernel_ms": {kd + " (+split_d, combine)": kms[0], "functional": kms[1], "energy": kms[2],
+                          ("prep16" if kd == "density16" else "prep_z"): kms[3], kf: kms[4], "wsum": kms[5]},
             "stage_ms": {"density": stage[0], "functional": stage[1], "energy": stage[2], "fock": stage[3]}}
 
 

@@ -32,7 +32,9 @@ class GridInfo(ctypes.Structure):
                 ("mixed_tiles", ctypes.c_int), ("mixed_pairs", ctypes.c_long), ("mixed_rows", ctypes.c_long),
                 ("mixed_store_bytes", ctypes.c_long), ("mixed_launches", ctypes.c_int),
                 ("mixed_units_full", ctypes.c_long), ("mixed_units_sym", ctypes.c_long),
-                ("mixed_fock_jobs", ctypes.c_long), ("mixed_fock_tau_jobs", ctypes.c_long)]
+                ("mixed_fock_jobs", ctypes.c_long), ("mixed_fock_tau_jobs", ctypes.c_long),
+                ("mixed_presplit", ctypes.c_long), ("mixed_presplit_bytes", ctypes.c_long),
+                ("mixed_fock_items", ctypes.c_long)]
 
 
 class MixedConfig(ctypes.Structure):

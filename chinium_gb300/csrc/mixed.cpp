@@ -287,6 +287,23 @@ void Grid::prepare_mixed(const MixedConfig& cfg) {
     }
     md.rows = std::max(rows, 1L);
 
+    // pre-split operands (BF16 planes of the AO store and of the per-build R
+    // operands) when they fit in half of the memory left after the FP32 store
+    m.ao_comp = type >= 1 ? 4 : 1;
+    {
+        const int ncv = type >= 2 ? 4 : 1;
+        const size_t n16 = (size_t)md.rows * kTilePts;
+        const size_t need = (size_t)(3 * m.ao_comp + 3 * ncv) * n16 * sizeof(__nv_bfloat16);
+        const size_t e32b = (size_t)m.ao_comp * n16 * sizeof(float);
+        size_t freeb = 0, totalb = 0;
+        CGB_CUDA(cudaMemGetInfo(&freeb, &totalb));
+        const size_t room = freeb > e32b ? (freeb - e32b) / 2 : 0;
+        const bool coord_ok = (long)(3 * std::max(m.ao_comp, ncv)) * md.rows < (1L << 31);
+        m.use16 = coord_ok && (cfg.v_operands == 2 || (cfg.v_operands == 0 && need < room));
+        CGB_CHECK(cfg.v_operands != 2 || m.use16, XC_ERR_UNSUPPORTED,
+                  "pre-split V operands do not fit (TMA row coordinate)");
+    }
+
     // ---- persistent work lists
     std::vector<long> dcost(ntiles);
     std::vector<int> dids;
@@ -338,9 +355,41 @@ void Grid::prepare_mixed(const MixedConfig& cfg) {
                 }
     }
     m.nitems = (long)items.size();
+    m.live_items = (long)fids.size();
     std::vector<int> foff, flist;
     m.fock_ctas = std::min((int)fids.size(), nsm);
-    lpt(fcost, fids, m.fock_ctas, foff, flist);
+    {
+        // L2 locality of the pre-split kernel (which streams 96 KB of planes
+        // per stage): items fall into S segments by the position of their
+        // tile range in the molecule (S keeps >= 2 items per CTA in each);
+        // every CTA takes its segment-0 items first, then segment 1, ..., so
+        // concurrently running items read the same stretch of the operand
+        // stores.  Each segment is cost-balanced on its own (LPT).  The
+        // in-kernel-split kernel keeps one LPT over all items (faster there).
+        const int S = !m.use16 ? 1 : std::max(1, std::min(64, (int)(fids.size() / (2 * (size_t)std::max(m.fock_ctas, 1)))));
+        std::vector<std::vector<int>> seg(S);
+        std::vector<int> item_mol(items.size(), 0);
+        for (int i = 0; i < nmol; i++)
+            for (long k = m.mols[i].item0; k < (i + 1 < nmol ? m.mols[i + 1].item0 : (long)items.size()); k++)
+                item_mol[k] = i;
+        for (int id : fids) {
+            const MolRange& R = m.mols[item_mol[id]];
+            const long span = std::max(1, R.t1 - R.t0);
+            seg[std::min(S - 1, (int)((long)(items[id].t0 - R.t0) * S / span))].push_back(id);
+        }
+        std::vector<std::vector<int>> per_cta(m.fock_ctas);
+        for (int k = 0; k < S; k++) {
+            if (seg[k].empty()) continue;
+            std::vector<int> so, sl;
+            lpt(fcost, seg[k], m.fock_ctas, so, sl);
+            for (int b = 0; b < m.fock_ctas; b++) per_cta[b].insert(per_cta[b].end(), sl.begin() + so[b], sl.begin() + so[b + 1]);
+        }
+        foff.assign(1, 0);
+        for (auto& v : per_cta) {
+            flist.insert(flist.end(), v.begin(), v.end());
+            foff.push_back((int)flist.size());
+        }
+    }
     // per CTA: the wanted tiles of its items, in order, with their slots
     std::vector<FockJob> fjobs;
     std::vector<int> fjoff(1, 0);
@@ -397,25 +446,16 @@ void Grid::prepare_mixed(const MixedConfig& cfg) {
     md.tile_slot = m.d_slot.p;
     md.tile_row = m.d_row.p;
     md.tile_c0 = m.d_c0.p;
-    m.ao_comp = type >= 1 ? 4 : 1;
     m.d_e32.alloc((size_t)m.ao_comp * md.rows * kTilePts);
     m.d_e32.zero(s);
     md.e32 = m.d_e32.p;
     launch_ao_mixed(md, dev_shells(), m.d_tile_shells.p, m.d_tile_shell_off.p, m.d_x.p, m.d_y.p, m.d_z.p, m.d_shtab.p,
                     m.ao_comp, m.d_e32.p, s);
-    // pre-split V operands when they fit: AO planes (3 per component) and R
-    // planes (3 for Z, 9 more for the meta-GGA components), at most half of
-    // the free memory
+    // pre-split operands: AO planes (3 per component) and R planes (3 for Z,
+    // 9 more for the meta-GGA components)
     {
         const int ncv = type >= 2 ? 4 : 1;
         const size_t n16 = (size_t)md.rows * kTilePts;
-        const size_t need = (size_t)(3 * m.ao_comp + 3 * ncv) * n16 * sizeof(__nv_bfloat16);
-        size_t freeb = 0, totalb = 0;
-        CGB_CUDA(cudaMemGetInfo(&freeb, &totalb));
-        const bool coord_ok = (long)(3 * std::max(m.ao_comp, ncv)) * md.rows < (1L << 31);
-        m.use16 = coord_ok && (cfg.v_operands == 2 || (cfg.v_operands == 0 && need < freeb / 2));
-        CGB_CHECK(cfg.v_operands != 2 || m.use16, XC_ERR_UNSUPPORTED,
-                  "pre-split V operands do not fit (TMA row coordinate)");
         if (m.use16) {
             m.d_e16.alloc((size_t)3 * m.ao_comp * n16);
             m.d_R16.alloc((size_t)3 * ncv * n16);

@@ -129,6 +129,9 @@ typedef struct xc_grid_info {
     long mixed_units_sym;  /* density units of a symmetric pass (rho of LDA, each tau component) */
     long mixed_fock_jobs;  /* V (item, tile) jobs, each 128 x 128 x 128 per component */
     long mixed_fock_tau_jobs; /* jobs that also carry the meta-GGA components (I <= J) */
+    long mixed_presplit;      /* 1: the tensor-core kernels read pre-split BF16 planes (v_operands) */
+    long mixed_presplit_bytes; /* bytes of those planes (AO store + per-build R planes) */
+    long mixed_fock_items;    /* V work items with at least one job (one W partial written each) */
 } xc_grid_info;
 int xc_grid_info_get(const xc_grid* g, xc_grid_info* info);
 /* Padded points in block order: x, y, z, w (each npoints_padded) and
