@@ -58,6 +58,13 @@ class JK:
     def coulomb(self, D):
         return (self.J @ D.ravel()).reshape(self.n, self.n)
 
+    # the host contraction has nothing to overlap: begin computes, end returns
+    def coulomb_begin(self, D):
+        return self.coulomb(D)
+
+    def coulomb_end(self, h):
+        return h
+
     def exchange(self, D):
         return (self.K @ D.ravel()).reshape(self.n, self.n)
 
@@ -100,9 +107,17 @@ class JKDevice:
         self.K = None
 
     def coulomb(self, D):
+        return self.coulomb_end(self.coulomb_begin(D))
+
+    def coulomb_begin(self, D):
+        """Enqueue J on torch's current stream and return at once (the XC
+        build, on the grid's own stream, can run meanwhile)."""
         torch = self.torch
-        d = torch.from_numpy(np.ascontiguousarray(D[self.iu, self.ju] * self.pair_w)).cuda()
-        return coulomb_from_pairs((self.J @ d).cpu().numpy(), self.iu, self.ju, self.n)
+        d = torch.from_numpy(np.ascontiguousarray(D[self.iu, self.ju] * self.pair_w)).pin_memory()
+        return self.J @ d.cuda(non_blocking=True)
+
+    def coulomb_end(self, h):
+        return coulomb_from_pairs(h.cpu().numpy(), self.iu, self.ju, self.n)
 
     def exchange(self, D):
         torch = self.torch
@@ -221,6 +236,13 @@ def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, m
         g = Grid(ctx["basis"], grid, nspin=nspin, screen_threshold=screen)
         g.setType(xc.type)
         g.getAO(0)
+        if jk_device == "cuda":
+            # the XC build on its own stream, so that the device J of the same
+            # iteration (torch's stream) runs alongside it
+            import torch
+            torch.cuda.synchronize()
+            ctx["grid_stream"] = torch.cuda.Stream()
+            g.set_stream(ctx["grid_stream"].cuda_stream)
         ctx["grid"], ctx["grid_key"] = g, key
     b, S, H, jk, Enuc, g = ctx["basis"], ctx["S"], ctx["H"], ctx["jk"], ctx["Enuc"], ctx["grid"]
     n = b.nbasis
@@ -280,7 +302,7 @@ def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, m
     for it in range(1, max_iter + 1):
         t0 = time.perf_counter()
         Dtot = Ds[0] if not unrestricted else Ds[0] + Ds[1]
-        J = jk.coulomb(Dtot)
+        J_pending = jk.coulomb_begin(Dtot)  # overlaps the XC build below
         Ks = [jk.exchange(d) for d in Ds] if exx > 0 else [np.zeros((n, n))] * nspin
         timings["jk"] += time.perf_counter() - t0
         t0 = time.perf_counter()
@@ -295,6 +317,9 @@ def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, m
             check(lib().xc_build_incremental(g._h, xc._h, _p(Dst), nspin, code, ctypes.byref(e), _p(Vb)))
             Exc, Vxc = e.value, [Vb[s].T.copy() for s in range(nspin)]
         timings["xc"] += time.perf_counter() - t0
+        t0 = time.perf_counter()
+        J = jk.coulomb_end(J_pending)
+        timings["jk"] += time.perf_counter() - t0
         if unrestricted:
             Fs = [H + J - exx * Ks[s] + Vxc[s] for s in range(2)]
             E = (np.sum(Dtot * H) + 0.5 * np.sum(Dtot * J) - 0.5 * exx * (np.sum(Ds[0] * Ks[0]) + np.sum(Ds[1] * Ks[1]))
