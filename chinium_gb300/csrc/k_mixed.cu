@@ -302,13 +302,15 @@ __device__ __forceinline__ void density_epilogue(Smem& sm, uint32_t tmem, const 
             for (int j = 0; j < 64; j++) {
                 const float tv = T[j];
                 const size_t o = (size_t)j * 128;
-                if (EPI <= 1) pr = fmaf(tv, __ldg(e0 + o), pr);
+                // streaming loads (evict-first): each value is read once per build,
+                // and the L2 keeps the operand planes that are re-read
+                if (EPI <= 1) pr = fmaf(tv, __ldcs(e0 + o), pr);
                 if (EPI == 1) {
-                    pg0 = fmaf(tv, __ldg(e0 + cs + o), pg0);
-                    pg1 = fmaf(tv, __ldg(e0 + 2 * cs + o), pg1);
-                    pg2 = fmaf(tv, __ldg(e0 + 3 * cs + o), pg2);
+                    pg0 = fmaf(tv, __ldcs(e0 + cs + o), pg0);
+                    pg1 = fmaf(tv, __ldcs(e0 + 2 * cs + o), pg1);
+                    pg2 = fmaf(tv, __ldcs(e0 + 3 * cs + o), pg2);
                 }
-                if (EPI == 2) pt_ = fmaf(tv, __ldg(e0 + (size_t)acomp * cs + o), pt_);
+                if (EPI == 2) pt_ = fmaf(tv, __ldcs(e0 + (size_t)acomp * cs + o), pt_);
             }
             acc_r += pr;
             acc_g0 += 2.0 * pg0;
