@@ -114,30 +114,44 @@ def fp64_gemm_peak(torch):
     return 2 * n ** 3 / best / 1e12
 
 
-def cpu_baseline(wl, D, sample_blocks, threads):
+class CpuArm:
     """The oracle (CPU restatement of the reference's per-block einsum loops,
-    OpenMP) on the first sample_blocks blocks of the same workload."""
-    from oracle import oracle as O
-    basis = O.Basis(wl["Z"], wl["xyz"], wl["basis"])
-    px, py, pz, w = O.grid_points(wl["Z"], wl["xyz"], wl["grid"])
-    blocks = O.padded_blocks(px, py, pz, w)[:sample_blocks]
+    OpenMP over blocks) on the first sample_blocks blocks of the same
+    workload (0 = every block): grid, blocks and AO values set up once."""
 
-    class G:
-        pass
+    def __init__(self, wl, D, sample_blocks, threads):
+        from oracle import oracle as O
+        basis = O.Basis(wl["Z"], wl["xyz"], wl["basis"])
+        px, py, pz, w = O.grid_points(wl["Z"], wl["xyz"], wl["grid"])
+        allb = O.padded_blocks(px, py, pz, w)
+        self.total = len(allb)
+        blocks = allb[:sample_blocks] if sample_blocks > 0 else allb
+        g = O.OracleGrid.__new__(O.OracleGrid)
+        g.basis = basis
+        g.blocks = blocks
+        g.ao = [basis.ao(b[0], b[1], b[2], 1) for b in blocks]
+        g.npoints = sum(len(b[0]) for b in blocks)
+        self.g, self.D, self.ids, self.threads = g, D, wl["ids"], threads
+        self.npad = g.npoints
+        g.build([D], wl["ids"], 1, nblocks=1, nthreads=threads)  # warm
 
-    g = O.OracleGrid.__new__(O.OracleGrid)
-    g.basis = basis
-    g.blocks = blocks
-    g.ao = [basis.ao(b[0], b[1], b[2], 1) for b in blocks]
-    g.npoints = sum(len(b[0]) for b in blocks)
-    npts = sum(int((b[3] != 0).sum()) for b in blocks)
-    g.build([D], wl["ids"], 1, nblocks=1, nthreads=threads)  # warm
-    t = time.perf_counter()
-    g.build([D], wl["ids"], 1, nthreads=threads)
-    dt = time.perf_counter() - t
-    npad = sum(len(b[0]) for b in blocks)
-    return {"value": npad / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": "%d of 2048 blocks (%d padded points), one build, %.2f s" % (len(blocks), npad, dt)}
+    def step(self):
+        """One timed build of the sample: (grid-points/s, seconds)."""
+        t = time.perf_counter()
+        self.g.build([self.D], self.ids, 1, nthreads=self.threads)
+        dt = time.perf_counter() - t
+        return self.npad / dt, dt
+
+    def describe(self, dt):
+        return {"unit": UNIT, "cores": self.threads, "kind": "port",
+                "sample": "%d of %d blocks (%d padded points), one build, %.2f s" % (
+                    len(self.g.blocks), self.total, self.npad, dt)}
+
+
+def cpu_baseline(wl, D, sample_blocks, threads):
+    arm = CpuArm(wl, D, sample_blocks, threads)
+    v, dt = arm.step()
+    return dict(value=v, **arm.describe(dt))
 
 
 def run_reference(args):
@@ -149,17 +163,19 @@ def run_reference(args):
     nb = cg.Basis(wl["Z"], wl["xyz"], wl["basis"]).nbasis
     D = model_density(nb, wl["nocc"])
     threads = os.cpu_count() or 1
-    vals = []
+    arm = CpuArm(wl, D, args.ref_blocks, threads)
+    vals, times = [], []
     for i in range(args.warmup + args.steps):
-        cb = cpu_baseline(wl, D, args.cpu_blocks, threads)
+        v, dt = arm.step()
         if i >= args.warmup:
-            vals.append(cb["value"])
+            vals.append(v)
+            times.append(dt)
     v = float(np.median(vals))
-    cb["value"] = v
+    cb = dict(value=v, **arm.describe(float(np.median(times))))
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 147456 / v * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": wl["name"], "sample_blocks": args.cpu_blocks},
+            "data": "synthetic", "config": {"workload": wl["name"], "sample_blocks": args.ref_blocks},
             "cpu_baseline": cb, "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -424,7 +440,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--plain-steps", type=int, default=2)
-    ap.add_argument("--cpu-blocks", type=int, default=96)
+    ap.add_argument("--cpu-blocks", type=int, default=0,
+                    help="blocks of the workload in the CPU baseline of this arm (0 = all: one whole build)")
+    ap.add_argument("--ref-blocks", type=int, default=512,
+                    help="blocks per step of the --impl reference arm (a bounded sample of the workload)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="c18", choices=["c18", "fe4s4", "alkanes64", "scf-water"])
     ap.add_argument("--scf-mols", type=int, default=4)
