@@ -34,7 +34,7 @@ class GridInfo(ctypes.Structure):
                 ("mixed_units_full", ctypes.c_long), ("mixed_units_sym", ctypes.c_long),
                 ("mixed_fock_jobs", ctypes.c_long), ("mixed_fock_tau_jobs", ctypes.c_long),
                 ("mixed_presplit", ctypes.c_long), ("mixed_presplit_bytes", ctypes.c_long),
-                ("mixed_fock_items", ctypes.c_long)]
+                ("mixed_fock_items", ctypes.c_long), ("mixed_empty_tiles", ctypes.c_long)]
 
 
 class MixedConfig(ctypes.Structure):

@@ -615,6 +615,7 @@ int xc_grid_info_get(const xc_grid* g, xc_grid_info* info) {
         info->mixed_fock_jobs = G.mx.ready ? G.mx.fock_jobs : 0;
         info->mixed_fock_tau_jobs = G.mx.ready ? G.mx.fock_tau_jobs : 0;
         info->mixed_fock_items = G.mx.ready ? G.mx.live_items : 0;
+        info->mixed_empty_tiles = G.mx.ready ? G.mx.empty_tiles : 0;
         info->mixed_presplit = G.mx.ready && G.mx.use16 ? 1 : 0;
         info->mixed_presplit_bytes =
             info->mixed_presplit ? (long)((G.mx.d_e16.n + G.mx.d_R16.n) * sizeof(__nv_bfloat16)) : 0;

@@ -315,6 +315,7 @@ void Grid::prepare_mixed(const MixedConfig& cfg) {
         m.units_sym += (long)nvb * nk - (long)nvb * (nvb - 1);
         if (nk > 0) dids.push_back(t);
     }
+    m.empty_tiles = ntiles - (long)dids.size();
     std::vector<int> doff, dlist;
     m.dens_ctas = std::min((int)dids.size(), nsm);
     lpt(dcost, dids, m.dens_ctas, doff, dlist);
@@ -494,6 +495,8 @@ void Grid::prepare_mixed(const MixedConfig& cfg) {
     m.rho_b.alloc(nspin * Gt);
     m.rho1_b.alloc(3 * nspin * Gt);
     m.tau_b.alloc(nspin * Gt);
+    m.rho.zero(s);
+    m.rho_b.zero(s);
     m.tau.zero(s);
     m.rho1.zero(s);
     m.tau_b.zero(s);
@@ -521,6 +524,17 @@ void Grid::density_passes(const __nv_bfloat16*) {
     if (type >= 2) {
         CGB_CUDA(cudaMemsetAsync(m.tau.p, 0, sizeof(double) * nspin * Gt, stream));
         CGB_CUDA(cudaMemsetAsync(m.tau_b.p, 0, sizeof(double) * nspin * Gt, stream));
+    }
+    if (m.empty_tiles) {
+        // points of tiles that keep no chunk have zero density; no kernel
+        // writes them, so clear what an earlier build (or an incremental
+        // reconstruction) left there
+        CGB_CUDA(cudaMemsetAsync(m.rho.p, 0, sizeof(double) * nspin * Gt, stream));
+        CGB_CUDA(cudaMemsetAsync(m.rho_b.p, 0, sizeof(double) * nspin * Gt, stream));
+        if (type >= 1) {
+            CGB_CUDA(cudaMemsetAsync(m.rho1.p, 0, sizeof(double) * 3 * nspin * Gt, stream));
+            CGB_CUDA(cudaMemsetAsync(m.rho1_b.p, 0, sizeof(double) * 3 * nspin * Gt, stream));
+        }
     }
     const auto pass = [&](int epi, int acomp, int s) {
         if (m.use16)

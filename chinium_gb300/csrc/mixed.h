@@ -90,6 +90,7 @@ struct MixedState {
     std::vector<long> h_row;
     long kept_pairs = 0;     // sum over tiles of (64 * nkept)^2
     long units_full = 0, units_sym = 0, fock_jobs = 0, fock_tau_jobs = 0, live_items = 0;
+    long empty_tiles = 0;    // tiles that keep no chunk: no density job writes their points
     // work lists (CSR by CTA)
     int dens_ctas = 0, fock_ctas = 0;
     long nitems = 0;

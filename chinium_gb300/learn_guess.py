@@ -2,6 +2,8 @@
 
   python -m chinium_gb300.learn_guess [--train 240] [--test 24] [--kmax 5]
                                       [--epochs 300] [--out weights.npz]
+  python -m chinium_gb300.learn_guess --eval-only [--test 200] [--test-kmax 8]
+                                      [--precision mixed]
 
 1. Seeded clusters (H2O)_k, k ~ U{2..kmax}: rigid monomers, random
    orientations, O-O >= 2.6 A (training seed 0, held-out seed 1).
@@ -36,8 +38,16 @@ def main():
     ap.add_argument("--residual", type=int, default=1, help="learn (converged - SAP) blocks")
     ap.add_argument("--test-kmax", type=int, default=0)
     ap.add_argument("--jk", default="cuda", choices=["cpu", "cuda"])
+    ap.add_argument("--eval-only", action="store_true", help="evaluate the weights at --out on held-out clusters")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
+                    help="XC builds of the held-out SCFs (mixed: incremental tensor-core builds)")
     args = ap.parse_args()
     log = lambda s: print(s, flush=True)
+    if args.eval_only:
+        model = G.load(args.out)
+        rows = evaluate(model, args, log)
+        print(json.dumps(dict(weights=args.out, precision=args.precision, **summarize(rows))), flush=True)
+        return
 
     t0 = time.perf_counter()
     train = M.water_clusters(args.train, seed=0, kmin=args.kmin, kmax=args.kmax)
@@ -66,32 +76,60 @@ def main():
     t_train = time.perf_counter() - t1
     G.save(model, args.out)
 
+    rows = evaluate(model, args, log)
+    summary = {
+        "train_clusters": len(train), "samples": int(len(X)), "epochs": args.epochs,
+        "final_loss": losses[-1], "first_loss": losses[0], "residual": model.residual, "scale": model.scale, "data_s": t_data, "train_s": t_train,
+        **summarize(rows)}
+    print(json.dumps(summary), flush=True)
+
+
+def evaluate(model, args, log):
+    """Held-out clusters (seed 1): SCF from the SAP guess and from the
+    learned density (timed including the guess); the setup (integrals, grid)
+    is shared and not timed."""
     test = M.water_clusters(args.test, seed=1, kmin=args.kmin, kmax=args.test_kmax or args.kmax)
+    kw = dict(functional=args.functional, jk_device=args.jk, precision=args.precision)
+    if args.precision == "mixed":
+        kw["anchor"] = "density"
     rows = []
     for Z, xyz in test:
-        r_sap = run_scf(Z, xyz, functional=args.functional, guess="sap", jk_device=args.jk)
-        ctx = r_sap.context
+        warm = run_scf(Z, xyz, functional=args.functional, guess="core", max_iter=1, jk_device=args.jk)
+        ctx = warm.context
+        if args.precision == "mixed":  # tiles and AO planes of the mixed path are setup too
+            from ._lib import PRECISION_MIXED
+            from .xc import ExchangeCorrelation
+            ctx["grid"].build(ExchangeCorrelation().Read(args.functional), [warm.D[0]], precision=PRECISION_MIXED)
+        r_sap = run_scf(Z, xyz, guess="sap", context=ctx, **kw)
         tg = time.perf_counter()
-        D0 = G.guess_density(model, Z, xyz, ctx)
+        D0 = G.guess_density(model, Z, xyz, ctx, precision=args.precision)
         t_guess = time.perf_counter() - tg
-        r_ml = run_scf(Z, xyz, functional=args.functional, guess=D0, context=ctx, jk_device=args.jk)
+        r_ml = run_scf(Z, xyz, guess=D0, context=ctx, **kw)
         it_time = lambda r: r.wall - r.timings["setup"]
         log("test (%d atoms): SAP %d iterations, learned %d" % (len(Z), r_sap.iterations, r_ml.iterations))
         rows.append(dict(natoms=len(Z), it_sap=r_sap.iterations, it_ml=r_ml.iterations,
                          t_sap=it_time(r_sap), t_ml=it_time(r_ml) + t_guess,
                          dE=r_ml.energy - r_sap.energy, conv=bool(r_sap.converged and r_ml.converged)))
-    summary = {
-        "train_clusters": len(train), "samples": int(len(X)), "epochs": args.epochs,
-        "final_loss": losses[-1], "first_loss": losses[0], "residual": model.residual, "scale": model.scale, "data_s": t_data, "train_s": t_train,
+    return rows
+
+
+def summarize(rows):
+    it_sap = np.array([r["it_sap"] for r in rows], dtype=float)
+    it_ml = np.array([r["it_ml"] for r in rows], dtype=float)
+    return {
         "test_clusters": len(rows),
-        "mean_iterations_sap": float(np.mean([r["it_sap"] for r in rows])),
-        "mean_iterations_learned": float(np.mean([r["it_ml"] for r in rows])),
+        "mean_iterations_sap": float(it_sap.mean()),
+        "mean_iterations_learned": float(it_ml.mean()),
+        "fewer_iterations_fraction": float((it_ml < it_sap).mean()),
+        "more_iterations_fraction": float((it_ml > it_sap).mean()),
         "mean_scf_s_sap": float(np.mean([r["t_sap"] for r in rows])),
         "mean_scf_s_learned": float(np.mean([r["t_ml"] for r in rows])),
+        "by_waters": {str(k): [float(it_sap[[r["natoms"] == 3 * k for r in rows]].mean()),
+                               float(it_ml[[r["natoms"] == 3 * k for r in rows]].mean())]
+                      for k in sorted({r["natoms"] // 3 for r in rows})},
         "max_abs_dE": float(np.max(np.abs([r["dE"] for r in rows]))),
         "all_converged": all(r["conv"] for r in rows),
     }
-    print(json.dumps(summary), flush=True)
 
 
 if __name__ == "__main__":

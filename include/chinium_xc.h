@@ -132,6 +132,7 @@ typedef struct xc_grid_info {
     long mixed_presplit;      /* 1: the tensor-core kernels read pre-split BF16 planes (v_operands) */
     long mixed_presplit_bytes; /* bytes of those planes (AO store + per-build R planes) */
     long mixed_fock_items;    /* V work items with at least one job (one W partial written each) */
+    long mixed_empty_tiles;   /* tiles whose points no kept chunk reaches (zero density there) */
 } xc_grid_info;
 int xc_grid_info_get(const xc_grid* g, xc_grid_info* info);
 /* Padded points in block order: x, y, z, w (each npoints_padded) and

@@ -81,3 +81,29 @@ def test_mixed_scf_with_learned_guess_uses_tensor_core_sap():
                  context=r64.context, jk_device="cuda")
     assert rl.converged and rl.guess_used == "learned"
     assert abs(rl.energy - r64.energy) < 1e-6
+
+
+def test_incremental_builds_are_stationary_with_empty_tiles():
+    """A water trimer on SG-1 whose grid has a tile that keeps no basis chunk.
+    Forty incremental builds at an unchanged density must return the
+    anchor's energy every time: no density kernel writes that tile's points,
+    and nothing may accumulate there from one call to the next (it once
+    doubled per call, which stalled longer SCFs)."""
+    import ctypes
+    import chinium_gb300 as cg
+    from chinium_gb300._lib import check, lib
+    Z2, xyz2 = M.water_clusters(24, seed=1, kmin=2, kmax=8)[5]
+    r = run_scf(Z2, xyz2, functional="PBE", precision="fp64", max_iter=3)
+    g = r.context["grid"]
+    xc = cg.ExchangeCorrelation().Read("PBE")
+    n = r.nbasis
+    D = np.ascontiguousarray(r.D[0].T)[None]
+    V = np.zeros((1, n, n))
+    e = ctypes.c_double()
+    Es = []
+    for it in range(40):
+        check(lib().xc_build_incremental(g._h, xc._h, ctypes.c_void_p(D.ctypes.data), 1, 2 if it == 0 else 0,
+                                         ctypes.byref(e), ctypes.c_void_p(V.ctypes.data)))
+        Es.append(e.value)
+    assert g.info()["mixed_empty_tiles"] > 0
+    assert max(abs(x - Es[0]) for x in Es) < 1e-10
