@@ -1043,60 +1043,71 @@ __global__ void split_store_kernel(const float* __restrict__ e32, long n, int nc
     e16[(size_t)(c * 3 + 2) * n + o] = l;
 }
 
+// Two consecutive points of one row into the three planes (one 4-byte
+// store per plane).
+__device__ __forceinline__ void store3x2(bf16* __restrict__ R, size_t n, size_t o, float x0, float x1) {
+    bf16 h0, m0, l0, h1, m1, l1;
+    split1(x0, h0, m0, l0);
+    split1(x1, h1, m1, l1);
+    *reinterpret_cast<__nv_bfloat162*>(R + o) = __halves2bfloat162(h0, h1);
+    *reinterpret_cast<__nv_bfloat162*>(R + n + o) = __halves2bfloat162(m0, m1);
+    *reinterpret_cast<__nv_bfloat162*>(R + 2 * n + o) = __halves2bfloat162(l0, l1);
+}
+
 // R operands of the pre-split V kernel as BF16 planes, per kept row:
 // component 0: Z = c0 phi + c1 . grad phi (the FP32 arithmetic of
 // prep_z_kernel); components 1-3 (meta-GGA): c2 d_c phi.  One CTA per tile,
-// thread = point.
-__device__ __forceinline__ void store3(bf16* __restrict__ R, size_t n, size_t o, float x) {
-    bf16 h, m, l;
-    split1(x, h, m, l);
-    R[o] = h;
-    R[n + o] = m;
-    R[2 * n + o] = l;
-}
-
-__global__ void __launch_bounds__(128) prep16_kernel(MixedDev md, int type, const double* __restrict__ fcoef,
+// 256 threads: thread = (point pair, row phase); rows phase + 4k, two at a
+// time (8 to 32 loads in flight).
+__global__ void __launch_bounds__(256) prep16_kernel(MixedDev md, int type, const double* __restrict__ fcoef,
                                                      bf16* __restrict__ R16) {
-    const int t = blockIdx.x, g = threadIdx.x;
-    const long pt = (long)t * 128 + g;
+    const int t = blockIdx.x, pp = threadIdx.x & 63, ph = threadIdx.x >> 6;
+    const long pt = (long)t * 128 + 2 * pp;
     const long Gt = md.Gt;
-    const float a0 = (float)fcoef[pt];
-    float a1 = 0, a2 = 0, a3 = 0, c2 = 0;
-    if (type >= 1) {
-        a1 = (float)fcoef[Gt + pt];
-        a2 = (float)fcoef[2 * Gt + pt];
-        a3 = (float)fcoef[3 * Gt + pt];
-    }
-    if (type >= 2) c2 = (float)fcoef[4 * Gt + pt];
-    const long r0 = md.tile_row[t], nr = (long)md.tile_nkept[t] * 64;  // a multiple of 4
-    const size_t n = (size_t)md.rows * 128;
-    const float* e = md.e32 + (size_t)r0 * 128 + g;
-    bf16* R = R16 + (size_t)r0 * 128 + g;
-    for (long r = 0; r < nr; r += 4) {  // four rows per step: 4 to 16 loads in flight
-        float v[4][4];
+    float a0[2], a1[2] = {0, 0}, a2[2] = {0, 0}, a3[2] = {0, 0}, c2[2] = {0, 0};
 #pragma unroll
-        for (int i = 0; i < 4; i++) {
-            const size_t o = (size_t)(r + i) * 128;
-            v[i][0] = __ldg(e + o);
+    for (int q = 0; q < 2; q++) {
+        a0[q] = (float)fcoef[pt + q];
+        if (type >= 1) {
+            a1[q] = (float)fcoef[Gt + pt + q];
+            a2[q] = (float)fcoef[2 * Gt + pt + q];
+            a3[q] = (float)fcoef[3 * Gt + pt + q];
+        }
+        if (type >= 2) c2[q] = (float)fcoef[4 * Gt + pt + q];
+    }
+    const long r0 = md.tile_row[t], nr = (long)md.tile_nkept[t] * 64;  // a multiple of 8
+    const size_t n = (size_t)md.rows * 128;
+    const float* e = md.e32 + (size_t)r0 * 128 + 2 * pp;
+    bf16* R = R16 + (size_t)r0 * 128 + 2 * pp;
+    for (long r = ph; r < nr; r += 8) {
+        float2 v[2][4];
+#pragma unroll
+        for (int i = 0; i < 2; i++) {
+            const size_t o = (size_t)(r + 4 * i) * 128;
+            v[i][0] = __ldg(reinterpret_cast<const float2*>(e + o));
             if (type >= 1) {
-                v[i][1] = __ldg(e + n + o);
-                v[i][2] = __ldg(e + 2 * n + o);
-                v[i][3] = __ldg(e + 3 * n + o);
+                v[i][1] = __ldg(reinterpret_cast<const float2*>(e + n + o));
+                v[i][2] = __ldg(reinterpret_cast<const float2*>(e + 2 * n + o));
+                v[i][3] = __ldg(reinterpret_cast<const float2*>(e + 3 * n + o));
             }
         }
 #pragma unroll
-        for (int i = 0; i < 4; i++) {
-            const size_t o = (size_t)(r + i) * 128;
-            float z = a0 * v[i][0];
+        for (int i = 0; i < 2; i++) {
+            const size_t o = (size_t)(r + 4 * i) * 128;
+            float z0 = a0[0] * v[i][0].x, z1 = a0[1] * v[i][0].y;
             if (type >= 1) {
-                z = fmaf(a1, v[i][1], z);
-                z = fmaf(a2, v[i][2], z);
-                z = fmaf(a3, v[i][3], z);
+                z0 = fmaf(a1[0], v[i][1].x, z0);
+                z1 = fmaf(a1[1], v[i][1].y, z1);
+                z0 = fmaf(a2[0], v[i][2].x, z0);
+                z1 = fmaf(a2[1], v[i][2].y, z1);
+                z0 = fmaf(a3[0], v[i][3].x, z0);
+                z1 = fmaf(a3[1], v[i][3].y, z1);
             }
-            store3(R, n, o, z);
+            store3x2(R, n, o, z0, z1);
             if (type >= 2) {
-#pragma unroll
-                for (int c = 1; c <= 3; c++) store3(R + 3 * c * n, n, o, v[i][c] * c2);
+                store3x2(R + 3 * n, n, o, v[i][1].x * c2[0], v[i][1].y * c2[1]);
+                store3x2(R + 6 * n, n, o, v[i][2].x * c2[0], v[i][2].y * c2[1]);
+                store3x2(R + 9 * n, n, o, v[i][3].x * c2[0], v[i][3].y * c2[1]);
             }
         }
     }
@@ -1278,7 +1289,7 @@ void launch_split_store(const float* e32, long n, int ncomp, bf16* e16, cudaStre
 
 void launch_prep16(const MixedDev& md, int type, const double* fcoef, bf16* R16, cudaStream_t s) {
     if (md.ntiles == 0) return;
-    prep16_kernel<<<md.ntiles, 128, 0, s>>>(md, type, fcoef, R16);
+    prep16_kernel<<<md.ntiles, 256, 0, s>>>(md, type, fcoef, R16);
     CGB_CUDA(cudaGetLastError());
 }
 
