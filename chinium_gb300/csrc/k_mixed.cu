@@ -1057,8 +1057,9 @@ __device__ __forceinline__ void store3x2(bf16* __restrict__ R, size_t n, size_t 
 // R operands of the pre-split V kernel as BF16 planes, per kept row:
 // component 0: Z = c0 phi + c1 . grad phi (the FP32 arithmetic of
 // prep_z_kernel); components 1-3 (meta-GGA): c2 d_c phi.  One CTA per tile,
-// 256 threads: thread = (point pair, row phase); rows phase + 4k, two at a
-// time (8 to 32 loads in flight).
+// 256 threads: thread = (point pair, row phase); rows phase + 4k, U at a
+// time (U = 4 for LDA / GGA, 2 for meta-GGA with its twelve output planes).
+template <int U>
 __global__ void __launch_bounds__(256) prep16_kernel(MixedDev md, int type, const double* __restrict__ fcoef,
                                                      bf16* __restrict__ R16) {
     const int t = blockIdx.x, pp = threadIdx.x & 63, ph = threadIdx.x >> 6;
@@ -1075,14 +1076,14 @@ __global__ void __launch_bounds__(256) prep16_kernel(MixedDev md, int type, cons
         }
         if (type >= 2) c2[q] = (float)fcoef[4 * Gt + pt + q];
     }
-    const long r0 = md.tile_row[t], nr = (long)md.tile_nkept[t] * 64;  // a multiple of 8
+    const long r0 = md.tile_row[t], nr = (long)md.tile_nkept[t] * 64;  // a multiple of 4 U
     const size_t n = (size_t)md.rows * 128;
     const float* e = md.e32 + (size_t)r0 * 128 + 2 * pp;
     bf16* R = R16 + (size_t)r0 * 128 + 2 * pp;
-    for (long r = ph; r < nr; r += 8) {
-        float2 v[2][4];
+    for (long r = ph; r < nr; r += 4 * U) {
+        float2 v[U][4];
 #pragma unroll
-        for (int i = 0; i < 2; i++) {
+        for (int i = 0; i < U; i++) {
             const size_t o = (size_t)(r + 4 * i) * 128;
             v[i][0] = __ldg(reinterpret_cast<const float2*>(e + o));
             if (type >= 1) {
@@ -1092,7 +1093,7 @@ __global__ void __launch_bounds__(256) prep16_kernel(MixedDev md, int type, cons
             }
         }
 #pragma unroll
-        for (int i = 0; i < 2; i++) {
+        for (int i = 0; i < U; i++) {
             const size_t o = (size_t)(r + 4 * i) * 128;
             float z0 = a0[0] * v[i][0].x, z1 = a0[1] * v[i][0].y;
             if (type >= 1) {
@@ -1289,7 +1290,10 @@ void launch_split_store(const float* e32, long n, int ncomp, bf16* e16, cudaStre
 
 void launch_prep16(const MixedDev& md, int type, const double* fcoef, bf16* R16, cudaStream_t s) {
     if (md.ntiles == 0) return;
-    prep16_kernel<<<md.ntiles, 256, 0, s>>>(md, type, fcoef, R16);
+    if (type >= 2)
+        prep16_kernel<2><<<md.ntiles, 256, 0, s>>>(md, type, fcoef, R16);
+    else
+        prep16_kernel<4><<<md.ntiles, 256, 0, s>>>(md, type, fcoef, R16);
     CGB_CUDA(cudaGetLastError());
 }
 
