@@ -1084,6 +1084,18 @@ int xc_grid_tune(xc_grid* g, xc_functional* f, const double* D, int nspin, doubl
             c.spatial = 0;
             consider(c);
         }
+        {
+            // both operand forms of the tensor-core kernels (pre-split planes /
+            // in-kernel split) when the automatic choice finds that the planes fit
+            MixedConfig probe = best;
+            probe.v_operands = 0;
+            G.prepare_mixed(probe);
+            if (G.mx.use16) {
+                MixedConfig c = best;
+                c.v_operands = best.v_operands == 1 ? 2 : 1;
+                consider(c);
+            }
+        }
         CGB_CUDA(cudaEventDestroy(e0));
         CGB_CUDA(cudaEventDestroy(e1));
         G.prepare_mixed(best);

@@ -281,8 +281,9 @@ int xc_grid_set_mixed_config(xc_grid* g, const xc_mixed_config* cfg);
 int xc_grid_get_mixed_config(const xc_grid* g, xc_mixed_config* cfg);
 
 /* Autotuner of the mixed path for one functional and a representative
- * density (host D, packed).  Reference: a build with screening 0 and
- * spatial tiles.  Candidates over (screen, spatial, fock_tiles) are built
+ * density (host D, packed).  Reference: a build with screening 1e-14 and
+ * spatial tiles.  Candidates over (screen, spatial, fock_tiles, and the
+ * operand form when pre-split planes fit) are built
  * and timed (median of `reps` graph replays); the fastest candidate whose
  * energies (every molecule) are within e_tol and whose V is within v_tol
  * (max abs) of the reference is selected and left set on the grid.
