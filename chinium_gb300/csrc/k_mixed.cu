@@ -4,32 +4,42 @@
 // tile); each tile keeps the 64-function chunks of its molecule that the
 // screening test marks significant, packed into "slots".  The AO values and
 // gradients are stored once, in FP32, function-major (one 512-byte row of
-// 128 points per kept function).  TMA stages FP32 tiles of that store in
-// shared memory; converter warps split them into three-term BF16 planes
-// (x = h + m + l, exact for an FP32 x) written in the 128-byte-swizzled
-// K-major layout that tcgen05.mma reads (transposing on the way for the
-// density product).  A product sums the six cross terms of order <= 2 (hh,
-// hm, mh, hl, mm, lh) in FP32; hh and the five corrections go to separate
-// TMEM accumulators, and every accumulation unit starts fresh and is drained
-// by the epilogue warps into round-to-nearest FP32 registers.  Cross-unit
-// sums of the final quantities are FP64.
+// 128 points per kept function).  Operands reach tcgen05.mma as three-term
+// BF16 planes (x = h + m + l, exact for an FP32 x) in the 128-byte-swizzled
+// layout, in one of two forms:
+//   pre-split (density16_kernel, fock16_kernel): the planes are split once in
+//     HBM (split_store_kernel for the AO store, prep16_kernel per build for
+//     the V kernel's R operand) and TMA loads them straight into the stages;
+//   in-kernel split (density_tc_kernel, fock_tc_kernel): TMA stages FP32
+//     tiles in shared memory and converter warps split them (transposing on
+//     the way for the density product) — 1.5x less HBM, used when the planes
+//     do not fit.
+// A product sums the six cross terms of order <= 2 (hh, hm, mh, hl, mm, lh)
+// in FP32; hh and the five corrections go to separate TMEM accumulators, and
+// every accumulation unit starts fresh and is drained by the epilogue warps
+// into round-to-nearest FP32 registers.  Cross-unit sums of the final
+// quantities are FP64.
 //
 // HBM layouts:
 //   e32 (FP32): component c (phi, d/dx, d/dy, d/dz), row c*rows + tile_row[t] + slot*64 + f, col g (128 points)
-//   Z   (FP32, per build): c0 phi + c1 . grad phi, same rows as e32 component 0
+//   e16 (BF16): row (c*3 + p)*rows + (the e32 row within component c), p = h, m, l
+//   R16 (BF16, per build): row (c*3 + p)*rows + ..., c = 0: Z, c = 1..3: c2 d_c phi (meta-GGA)
+//   Z   (FP32, per build, in-kernel split): c0 phi + c1 . grad phi, same rows as e32 component 0
 //   Dp  (BF16 density planes): row (s*3+p)*drows + f0(mol) + nu, col mu
 //
-// Both tensor-core kernels are persistent: one CTA per SM walks a host-made
+// The tensor-core kernels are persistent: one CTA per SM walks a host-made
 // list of work items (tiles, or (I, J, tile range) blocks of V) balanced by
-// cost.  CTA roles (512 threads): warp 0 issues every TMA load and owns
-// TMEM, warp 1 issues tcgen05.mma into one of two TMEM buffers (256 columns
-// each: hh | corrections), warps 4-11 drain TMEM (lane quadrant = warp % 4;
-// warps 4-7 columns 0-63, warps 8-11 columns 64-127) and run the epilogue,
-// warps 2-3 and 12-15 convert operands.  Shared memory
-// (224 KB): density = two operand stages + one raw FP32 tile; V_xc = one
-// operand stage + two raw FP32 stages.  Every wait is bounded (2 s of
-// %globaltimer); a timeout sets XC_ERR_TIMEOUT in a global flag and the CTA
-// unwinds instead of hanging.
+// cost.  Roles: warp 0 issues every TMA load and owns TMEM, warp 1 issues
+// tcgen05.mma into one of two TMEM buffers (256 columns each: hh |
+// corrections), warps 4-11 drain TMEM (lane quadrant = warp % 4; warps 4-7
+// columns 0-63, warps 8-11 columns 64-127) and run the epilogue; the
+// in-kernel-split kernels (512 threads) add converter warps (2-3 and 12-15,
+// and for V also 4-11), the pre-split ones run 384 threads.  Shared memory:
+// pre-split = two 96 KB operand stages; in-kernel split (224 KB): density =
+// two operand stages + one raw FP32 tile, V_xc = one operand stage + a ring
+// of raw FP32 half-stages.  Every wait is bounded (2 s of %globaltimer); a
+// timeout sets XC_ERR_TIMEOUT in a global flag and the CTA unwinds instead
+// of hanging.
 #include <cstdio>
 
 #include "common.h"
