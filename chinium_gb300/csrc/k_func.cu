@@ -37,7 +37,12 @@ __device__ double cta_sum(double v) {
     return r;
 }
 
-template <int FAM, int NS>
+// MODE 1: only the points whose total density is >= float_above, in FP32;
+// MODE 2: only the others, in FP64 (float_above = +inf: every point).  The
+// mixed path runs both launches (separate kernels: each gets the registers
+// and occupancy of its own precision); accumulate adds the CTA's energy
+// partial to the first launch's.
+template <int FAM, int NS, int MODE>
 __global__ void __launch_bounds__(kThreads) functional_kernel(xcf::FuncDesc f, long Gp, const double* __restrict__ w,
                                                               const double* __restrict__ rho,
                                                               const double* __restrict__ rho1,
@@ -45,10 +50,16 @@ __global__ void __launch_bounds__(kThreads) functional_kernel(xcf::FuncDesc f, l
                                                               double* __restrict__ sigma, double* __restrict__ eps,
                                                               double* __restrict__ vrho, double* __restrict__ vsigma,
                                                               double* __restrict__ vtau, double* __restrict__ fcoef,
-                                                              double* __restrict__ e_partial, double float_above) {
+                                                              double* __restrict__ e_partial, double float_above,
+                                                              bool accumulate) {
     const long g = (long)blockIdx.x * blockDim.x + threadIdx.x;
     double econtrib = 0;
-    if (g < Gp) {
+    bool mine = g < Gp;
+    if (mine) {
+        const double tot_rho = NS == 1 ? rho[g] : rho[g] + rho[Gp + g];
+        mine = (tot_rho >= float_above) == (MODE == 1);
+    }
+    if (mine) {
         const double wg = w[g];
         if (NS == 1) {
             const double r = rho[g];
@@ -62,7 +73,7 @@ __global__ void __launch_bounds__(kThreads) functional_kernel(xcf::FuncDesc f, l
             }
             if (FAM >= 2) t = tau[g];
             double e, dv[3] = {0, 0, 0};
-            if (r >= float_above) {  // mixed path: FP32 functional above the low-density bound
+            if (MODE == 1) {  // mixed path: FP32 functional above the low-density bound
                 float ef, df[3] = {0, 0, 0};
                 xcf::eval_unpol<float, FAM>(f, (float)r, (float)s, (float)t, ef, df);
                 e = ef;
@@ -102,7 +113,7 @@ __global__ void __launch_bounds__(kThreads) functional_kernel(xcf::FuncDesc f, l
                 in[6] = tau[Gp + g];
             }
             double e, dv[7] = {0, 0, 0, 0, 0, 0, 0};
-            if (in[0] + in[1] >= float_above) {
+            if (MODE == 1) {
                 float inf_[7], ef, df[7] = {0, 0, 0, 0, 0, 0, 0};
                 for (int i = 0; i < 7; i++) inf_[i] = (float)in[i];
                 xcf::eval_pol<float, FAM>(f, inf_, ef, df);
@@ -138,7 +149,7 @@ __global__ void __launch_bounds__(kThreads) functional_kernel(xcf::FuncDesc f, l
         }
     }
     const double tot = cta_sum(econtrib);
-    if (threadIdx.x == 0) e_partial[blockIdx.x] = tot;
+    if (threadIdx.x == 0) e_partial[blockIdx.x] = accumulate ? e_partial[blockIdx.x] + tot : tot;
 }
 
 __global__ void reduce_kernel(const double* __restrict__ partial, int n, double* __restrict__ out) {
@@ -238,18 +249,26 @@ void launch_functional_fp64(const xcf::FuncDesc& f, int fam, int ns, long Gp, co
                             cudaStream_t s, double float_above) {
     const unsigned grid = (unsigned)((Gp + kThreads - 1) / kThreads);
     *n_partial = (int)grid;
-#define CGB_FN(FAM_, NS_)                                                                                  \
-    functional_kernel<FAM_, NS_><<<grid, kThreads, 0, s>>>(f, Gp, w, rho, rho1, tau, sigma, eps, vrho, vsigma, vtau, \
-                                                           fcoef, e_partial, float_above)
+    // FP32 points first (mixed path only), then the FP64 ones adding to the same CTA partials
+    const bool split = float_above < __builtin_huge_val();
+#define CGB_FN(FAM_, NS_, MODE_, ACC_)                                                                          \
+    functional_kernel<FAM_, NS_, MODE_><<<grid, kThreads, 0, s>>>(f, Gp, w, rho, rho1, tau, sigma, eps, vrho, vsigma, \
+                                                                  vtau, fcoef, e_partial, float_above, ACC_)
+#define CGB_FN2(FAM_, NS_)                       \
+    do {                                         \
+        if (split) CGB_FN(FAM_, NS_, 1, false);  \
+        CGB_FN(FAM_, NS_, 2, split);             \
+    } while (0)
     if (ns == 1) {
-        if (fam == 0) CGB_FN(0, 1);
-        else if (fam == 1) CGB_FN(1, 1);
-        else CGB_FN(2, 1);
+        if (fam == 0) CGB_FN2(0, 1);
+        else if (fam == 1) CGB_FN2(1, 1);
+        else CGB_FN2(2, 1);
     } else {
-        if (fam == 0) CGB_FN(0, 2);
-        else if (fam == 1) CGB_FN(1, 2);
-        else CGB_FN(2, 2);
+        if (fam == 0) CGB_FN2(0, 2);
+        else if (fam == 1) CGB_FN2(1, 2);
+        else CGB_FN2(2, 2);
     }
+#undef CGB_FN2
 #undef CGB_FN
     CGB_CUDA(cudaGetLastError());
 }

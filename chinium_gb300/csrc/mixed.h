@@ -69,7 +69,7 @@ struct MixedConfig {
     double screen = 1e-11;   // chunk screening threshold (|phi|, |grad phi| bound)
     int fock_tiles = 0;      // tiles per V work item (0: from the SM count)
     int spatial = 1;         // 1: tiles from a k-d split of each molecule's points; 0: generation order
-    double func_float_above = 1e-3;  // FP32 functional at points with total density >= this
+    double func_float_above = 1e-5;  // FP32 functional at points with total density >= this
     int v_operands = 0;      // V kernel operands: 0 auto (by free memory), 1 converted in-kernel, 2 pre-split
     bool same_tiles(const MixedConfig& o) const {
         return screen == o.screen && fock_tiles == o.fock_tiles && spatial == o.spatial &&

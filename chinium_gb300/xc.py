@@ -135,7 +135,7 @@ class Grid:
         return dict(screen=c.screen, fock_tiles=c.fock_tiles, spatial=c.spatial, func_float_above=c.func_float_above,
                     v_operands=c.v_operands)
 
-    def set_mixed_config(self, screen=1e-11, fock_tiles=0, spatial=1, func_float_above=1e-3, v_operands=0):
+    def set_mixed_config(self, screen=1e-11, fock_tiles=0, spatial=1, func_float_above=1e-5, v_operands=0):
         """func_float_above: total density from which the mixed path's
         functional runs in FP32 (float("inf"): FP64 everywhere).  v_operands:
         V kernel operands split in-kernel (1), pre-split in HBM (2), or

@@ -262,7 +262,7 @@ int xc_grid_molecules(const xc_grid* g, int* nmol, int* nbasis, long* npoints, l
  * (0 = from the SM count); spatial: 1 forms tiles from k-d cells of each
  * molecule's points, 0 from 128 consecutive points in generation order.
  * func_float_above: points whose total density is at least this value
- * evaluate the functional in FP32, the rest in FP64 (default 1e-3; +inf or
+ * evaluate the functional in FP32, the rest in FP64 (default 1e-5; +inf or
  * any value above every density keeps the whole functional in FP64).
  * v_operands: operands of the V_xc kernel, 1 split from FP32 inside the
  * kernel, 2 BF16 planes split beforehand in HBM (1.5x the AO store plus the

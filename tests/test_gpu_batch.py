@@ -150,7 +150,7 @@ def test_fe4s4_uks_tpss_sg3_mixed_vs_fp64():
     dV = max(np.abs(V32[s] - V64[s]).max() for s in range(2))
     vmax = max(np.abs(V64[s]).max() for s in range(2))
     print("Fe4S4 UKS TPSS SG-3: E64 %.10f |dE|=%.2e max|dV|=%.2e (max|V| %.3e)" % (E64, dE, dV, vmax))
-    # the FP32 functional (above rho = 1e-3) at iron-core densities gives ~2e-6
+    # the FP32 functional (above rho = 1e-5) at iron-core densities gives ~2e-6
     # relative error on the largest V elements (measured 2.1e-6 of max|V| = 9.8)
     assert dE < 5e-5 and dV < 5e-6 * vmax
 
