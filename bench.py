@@ -192,8 +192,8 @@ def mixed_roofline(info, kms, stage, peaks, family, nspin):
     BF16 planes, or 4 B FP32 when split in-kernel) plus the FP32 values the
     density epilogue contracts (4 B per component), or the V kernel's L and R
     operands per component; plus the FP64 outputs (densities per point, one
-    128 x 128 W partial per V item).  The reported bound is the resource with
-    the larger fraction (HBM vs the tensor pipe's executed FLOPs)."""
+    128 x 128 W partial per V item).  The reported bound is the roof with the
+    larger algorithmic fraction; both sub-objects are in the line."""
     unit = 2.0 * 128 * 128 * 64
     if family == 0:
         fl_den = info["mixed_units_sym"] * unit * nspin
@@ -230,8 +230,9 @@ def mixed_roofline(info, kms, stage, peaks, family, nspin):
               "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst) -- of measured"}
     memory = {"achieved": hbm, "peak": hbm_peak, "unit": "GB/s", "frac": hbm / hbm_peak,
               "algorithmic_bytes_per_build": by, "peak_source": "MEASURED_PEAKS.json hbm_gbs -- of measured"}
-    # the binding resource: the larger of the HBM fraction and the tensor pipe's executed fraction
-    hbm_bound = memory["frac"] >= tensor["executed_frac"]
+    # the binding roof: the one whose algorithmic fraction is larger (the kernel is closest to it);
+    # the tensor pipe's executed fraction (6 split products) is reported beside it
+    hbm_bound = memory["frac"] >= tensor["frac"]
     main = memory if hbm_bound else tensor
     return {"bound": "hbm" if hbm_bound else "tensor", "kernel": dom, "achieved": main["achieved"],
             "peak": main["peak"], "unit": main["unit"], "frac": main["frac"], "traffic": None,
