@@ -519,6 +519,20 @@ def main():
     E64s = float(dE.item())
     t_plain_s = time_builds(torch, gs, xc, dD, dE, dV, P64, plain_steps, stream)
     del gs
+    # the FP64 XC nuclear gradient (grid fixed; LDA / GGA only), on a grid with AO Hessians
+    t_grad = None
+    if xc.type <= 1:
+        gg = cg.Grid(basis, wl["grid"], nspin=ns, screen_threshold=0.0)
+        gg.setType(xc.type)
+        gg.getAO(1)
+        Dl = [D] if ns == 1 else Dsp
+        gg.getEnergyGrad(xc, Dl)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(3):
+            gg.getEnergyGrad(xc, Dl)
+        t_grad = (time.perf_counter() - t0) / 3 * 1e3
+        del gg
 
     for _ in range(args.warmup):
         grid.build_device(xc, dD, dE, dV, precision)
@@ -601,6 +615,7 @@ def main():
                        "plain_fp64_screened_ms_per_build": t_plain_s / plain_steps * 1e3,
                        "speedup_vs_screened_fp64": (t_plain_s / plain_steps) / (t_dev / args.steps),
                        "abs_dE_xc_screened_vs_unscreened_fp64": abs(E64s - E64),
+                       "xc_gradient_fp64_ms": t_grad,
                        "E_xc_fp64": E64, "E_xc": Emx if precision == PMX else E64,
                        "abs_dE_xc_vs_fp64": abs(Emx - E64),
                        "max_abs_dV_xc_vs_fp64": float((Vmx - V64).abs().max().item())},

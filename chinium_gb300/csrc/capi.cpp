@@ -307,7 +307,8 @@ void Grid::get_ao(int derivative) {
     if (batched) return;  // the mixed path evaluates its own FP32 AO store at the first build
     const int order = type + derivative;
     CGB_CHECK(order <= 2, XC_ERR_UNSUPPORTED, "AO derivative order above 2 is not stored by this build");
-    ncomp = order >= 1 ? 4 : 1;
+    // Hessians (AO2) only when a derivative beyond the functional's own order is asked for (gradients)
+    ncomp = (derivative >= 1 && order >= 2) ? 10 : (order >= 1 ? 4 : 1);
     long long off = 0;
     for (auto& bd : blocks) {
         bd.ao_off = off;
@@ -807,6 +808,46 @@ int xc_build_device(xc_grid* g, xc_functional* f, const double* dD, int nspin, i
         G.evaluate(f->f);
         G.energy_device(dE);
         G.fock_device(dV, f->f.family);
+    });
+}
+
+int xc_grid_energy_grad(xc_grid* g, xc_functional* f, const double* D, int nspin, double* grad) {
+    return guard([&] {
+        CGB_CHECK(g && f && D && grad, XC_ERR_ARG, "null argument");
+        Grid& G = g->g;
+        CGB_CHECK(!G.batched, XC_ERR_UNSUPPORTED, "gradients are per molecule");
+        CGB_CHECK(nspin == G.nspin && f->f.nspin == G.nspin, XC_ERR_ARG, "Wrong number of spin types!");
+        CGB_CHECK(f->f.family <= 1, XC_ERR_UNSUPPORTED,
+                  "XC gradients cover LDA and GGA functionals (as the reference's getEnergyGrad)");
+        CGB_CHECK(f->f.family <= G.type, XC_ERR_STATE, "grid type is below the functional family (setType/getAO)");
+        CGB_CHECK(G.ncomp >= (f->f.family >= 1 ? 10 : 4), XC_ERR_STATE,
+                  "the gradient needs AO derivatives one order above the functional's (getAO(1))");
+        G.ensure_work();
+        const int n = G.basis.nbasis;
+        const size_t nn = (size_t)n * n * nspin;
+        CGB_CUDA(cudaMemcpyAsync(G.d_D.p, D, nn * sizeof(double), cudaMemcpyHostToDevice, G.stream));
+        G.density_device(G.d_D.p);
+        G.evaluate(f->f);
+        const long nlist = (long)G.basis_lists.size();
+        DevBuf<double> part;
+        part.alloc((size_t)nspin * nlist * 3);
+        launch_xc_grad((int)G.blocks.size(), G.d_blocks.p, G.d_lists.p, nlist, n, nspin, f->f.family, G.d_D.p,
+                       G.d_ao.p, G.Gp, G.d_fcoef.p, part.p, G.stream);
+        std::vector<double> h((size_t)nspin * nlist * 3);
+        CGB_CUDA(cudaMemcpyAsync(h.data(), part.p, h.size() * sizeof(double), cudaMemcpyDeviceToHost, G.stream));
+        CGB_CUDA(cudaStreamSynchronize(G.stream));
+        // atom of every basis function, then a fixed-order sum over spins, blocks and functions
+        std::vector<int> atom_of(n, 0);
+        for (const Shell& sh : G.basis.shells)
+            for (int k = 0; k < shell_size(sh.type); k++) atom_of[sh.first + k] = sh.atom;
+        const int na = G.basis.natoms();
+        std::fill(grad, grad + 3 * na, 0.0);
+        for (int sp = 0; sp < nspin; sp++)
+            for (long e = 0; e < nlist; e++) {
+                const int a = atom_of[G.basis_lists[e]];
+                for (int t = 0; t < 3; t++) grad[3 * a + t] += h[((size_t)sp * nlist + e) * 3 + t];
+            }
+        G.have_potential = false;  // the functional ran on this D
     });
 }
 

@@ -107,14 +107,18 @@ __global__ void __launch_bounds__(kMaxBlockPts) ao_kernel(const BlockDesc* __res
         const int l = sh.l[s], type = sh.type[s], np = sh.nprim[s], po = sh.prim_off[s];
         const double x = X - sh.xyz[3 * s], y = Y - sh.xyz[3 * s + 1], z = Z - sh.xyz[3 * s + 2];
         const double r2 = x * x + y * y + z * z;
-        double t0 = 0, t1 = 0;
+        double t0 = 0, t1 = 0, t2 = 0;
         for (int p = 0; p < np; p++) {  // GridAO.cpp:113-124
             const double e = sh.exps[po + p];
             const double t = sh.coefs[po + p] * exp(-e * r2);
             t0 += t;
             t1 += t * e;
+            t2 += t * e * e;
         }
         const double A = t0, Ax = -2 * x * t1, Ay = -2 * y * t1, Az = -2 * z * t1;
+        // second derivatives of the radial part: d_t d_r R = 4 x_t x_r t2 - 2 delta_tr t1
+        const double Axx = 4 * x * x * t2 - 2 * t1, Ayy = 4 * y * y * t2 - 2 * t1, Azz = 4 * z * z * t2 - 2 * t1;
+        const double Axy = 4 * x * y * t2, Axz = 4 * x * z * t2, Ayz = 4 * y * z * t2;
         double xp[kMaxL + 1], yp[kMaxL + 1], zp[kMaxL + 1];
         xp[0] = yp[0] = zp[0] = 1;
         for (int i = 1; i <= l; i++) {
@@ -127,6 +131,7 @@ __global__ void __launch_bounds__(kMaxBlockPts) ao_kernel(const BlockDesc* __res
             // Cartesian P shells (type 1) are x, y, z = table rows m = +1, -1, 0.
             const int row = (type == 1) ? (f == 0 ? 2 : f - 1) : f;
             double Q = 0, Qx = 0, Qy = 0, Qz = 0;
+            double Qxx = 0, Qxy = 0, Qxz = 0, Qyy = 0, Qyz = 0, Qzz = 0;
             int k = 0;
             for (int a = l; a >= 0; a--)
                 for (int b = l - a; b >= 0; b--, k++) {
@@ -139,6 +144,14 @@ __global__ void __launch_bounds__(kMaxBlockPts) ao_kernel(const BlockDesc* __res
                         if (b) Qy += c * b * xp[a] * yp[b - 1] * zp[cc];
                         if (cc) Qz += c * cc * xp[a] * yp[b] * zp[cc - 1];
                     }
+                    if (ncomp > 4) {  // Hessian of the angular polynomial
+                        if (a > 1) Qxx += c * a * (a - 1) * xp[a - 2] * yp[b] * zp[cc];
+                        if (b > 1) Qyy += c * b * (b - 1) * xp[a] * yp[b - 2] * zp[cc];
+                        if (cc > 1) Qzz += c * cc * (cc - 1) * xp[a] * yp[b] * zp[cc - 2];
+                        if (a && b) Qxy += c * a * b * xp[a - 1] * yp[b - 1] * zp[cc];
+                        if (a && cc) Qxz += c * a * cc * xp[a - 1] * yp[b] * zp[cc - 1];
+                        if (b && cc) Qyz += c * b * cc * xp[a] * yp[b - 1] * zp[cc - 1];
+                    }
                 }
             const long o = (long)(mu + f) * bd.ng + g;
             out[o] = A * Q;  // GridAO.cpp:180-184 (product rule)
@@ -146,6 +159,14 @@ __global__ void __launch_bounds__(kMaxBlockPts) ao_kernel(const BlockDesc* __res
                 out[comp_stride + o] = Ax * Q + A * Qx;
                 out[2 * comp_stride + o] = Ay * Q + A * Qy;
                 out[3 * comp_stride + o] = Az * Q + A * Qz;
+            }
+            if (ncomp > 4) {  // xx, xy, xz, yy, yz, zz: d_t d_r (R Q)
+                out[4 * comp_stride + o] = Axx * Q + 2 * Ax * Qx + A * Qxx;
+                out[5 * comp_stride + o] = Axy * Q + Ax * Qy + Ay * Qx + A * Qxy;
+                out[6 * comp_stride + o] = Axz * Q + Ax * Qz + Az * Qx + A * Qxz;
+                out[7 * comp_stride + o] = Ayy * Q + 2 * Ay * Qy + A * Qyy;
+                out[8 * comp_stride + o] = Ayz * Q + Ay * Qz + Az * Qy + A * Qyz;
+                out[9 * comp_stride + o] = Azz * Q + 2 * Az * Qz + A * Qzz;
             }
         }
         mu += nf;

@@ -38,6 +38,13 @@ void launch_density_fp64(int nblocks, const BlockDesc* d_blocks, const int* d_ba
                          int nspin, int type, const double* D, const double* ao, long Gp, double* rho,
                          double* rho1, double* tau, cudaStream_t s);
 
+// XC nuclear-gradient partials with the grid fixed (LDA / GGA): part[s][list entry][t]
+// = -2 sum_g [d_t phi U + sum_r d_t d_r phi f_r T] for the block function at that list entry
+// (AO store with Hessians for GGA: 10 components).
+void launch_xc_grad(int nblocks, const BlockDesc* d_blocks, const int* d_lists, long nlist, int nbasis, int nspin,
+                    int family, const double* D, const double* ao, long Gp, const double* fcoef, double* part,
+                    cudaStream_t s);
+
 // Functional on every point: eps, vrho, vsigma, vtau, sigma, the Fock
 // coefficients fcoef (s, 5, G) and per-CTA partial energies.  Points whose
 // total density is >= float_above are evaluated in FP32 (mixed path); the

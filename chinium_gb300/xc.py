@@ -175,6 +175,15 @@ class Grid:
         check(lib().xc_grid_kernel_ms(self._h, _p(ms)))
         return ms
 
+    def getEnergyGrad(self, xc, D):
+        """Nuclear gradient of E_xc with the grid fixed (SubGrid::getDensitySkeleton
+        + getEnergyGrad); (natoms, 3).  Needs getAO(1) (AO derivatives one
+        order above the functional's)."""
+        Dst = self._stack(D)
+        g = np.zeros(3 * len(self.basis.Z))
+        check(lib().xc_grid_energy_grad(self._h, xc._h, _p(Dst), self.nspin, _p(g)))
+        return g.reshape(-1, 3)
+
     def sap_fock(self, precision=PRECISION_FP64):
         """SuperpositionAtomicPotential (GuessSCF.cpp:17-75); PRECISION_MIXED
         assembles it on the tensor cores (FP32-level accuracy)."""

@@ -218,6 +218,15 @@ int xc_grid_stage_ms(xc_grid* g, double* ms);
  * over the spins.  No reference counterpart. */
 int xc_grid_kernel_ms(xc_grid* g, double* ms);
 
+/* Nuclear gradient of E_xc with the grid held fixed (SubGrid::getDensitySkeleton
+ * + SubGrid::getEnergyGrad, GridDensity.cpp:79-130, GridEnergy.cpp:15-30,
+ * summed over blocks as Grid::getEnergyGrad): grad[3 * atom + t] = dE_xc/dR
+ * from the derivatives of the basis functions centred on each atom, FP64.
+ * LDA and GGA functionals (the reference's gradient has no meta-GGA terms);
+ * needs the AO derivatives one order above the functional's: getAO(1) after
+ * setType.  D as for xc_build (column-major, spins concatenated). */
+int xc_grid_energy_grad(xc_grid* g, xc_functional* f, const double* D, int nspin, double* grad);
+
 /* Incremental mixed-precision build for SCF iterations (the per-iteration
  * sequence at Restricted/SP.cpp:52-55, fused).  Densities are linear in D
  * and V_xc is linear in the per-point potential coefficients, so this call

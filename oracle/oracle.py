@@ -359,3 +359,37 @@ class OracleGrid:
         if st:
             raise ValueError("oracle build failed")
         return E.value, F.transpose(0, 2, 1).copy()
+
+
+def skeleton_grad_fd(og, Z, xyz_bohr, basis_name, D, ids, nspin, h=1e-4):
+    """Nuclear gradient of E_xc with the grid held fixed by central finite
+    differences: the basis functions of one atom are displaced by +-h along
+    one axis and E_xc is rebuilt on the unchanged grid points at fixed D --
+    the quantity SubGrid::getDensitySkeleton + SubGrid::getEnergyGrad give
+    analytically (GridDensity.cpp:79-130, GridEnergy.cpp:15-30).  Richardson
+    extrapolation of the steps h and h/2 leaves an O(h^4) error (~1e-10 Eh/bohr
+    for H2O).  Test infrastructure; (natoms, 3)."""
+    g1 = _central_fd(og, Z, xyz_bohr, basis_name, D, ids, nspin, h)
+    g2 = _central_fd(og, Z, xyz_bohr, basis_name, D, ids, nspin, 0.5 * h)
+    return (4.0 * g2 - g1) / 3.0
+
+
+def _central_fd(og, Z, xyz_bohr, basis_name, D, ids, nspin, h):
+    xyz = np.asarray(xyz_bohr, dtype=np.float64).reshape(-1, 3)
+    saved = og.ao, og.basis
+    out = np.zeros((len(Z), 3))
+    try:
+        for a in range(len(Z)):
+            for t in range(3):
+                es = []
+                for sgn in (1.0, -1.0):
+                    moved = xyz.copy()
+                    moved[a, t] += sgn * h
+                    bm = Basis(Z, moved, basis_name)
+                    og.basis = bm
+                    og.ao = [bm.ao(bx, by, bz, og.deriv) for bx, by, bz, bw in og.blocks]
+                    es.append(og.build(D, ids, nspin)[0])
+                out[a, t] = (es[0] - es[1]) / (2 * h)
+    finally:
+        og.ao, og.basis = saved
+    return out

@@ -238,3 +238,35 @@ def test_sap_fock_tensor_cores(h2o):
     print("SAP tensor-core vs FP64: max|dV| %.2e of max|V| %.2e" % (np.abs(Vtc - V64).max(), scale))
     assert np.abs(Vtc - V64).max() < 2e-6 * scale
     assert np.allclose(Vtc, Vtc.T, atol=1e-14)
+
+
+@pytest.mark.parametrize("name,type_,nspin", [("SVWN5", 0, 1), ("PBE", 1, 1), ("PBE", 1, 2), ("B3LYP", 1, 1)])
+def test_xc_gradient_against_oracle_finite_differences(h2o, name, type_, nspin):
+    """dE_xc/dR with the grid fixed (getDensitySkeleton + getEnergyGrad): the
+    CUDA FP64 gradient against central finite differences of the oracle's
+    E_xc with one atom's basis functions displaced (Richardson-extrapolated
+    steps of 1e-4 and 5e-5 bohr, accurate to ~1e-9)."""
+    Z, xyz, b, ob, og = h2o
+    xc = cg.ExchangeCorrelation(spin=nspin).Read(name)
+    g = cg.Grid(b, "SG-1", nspin=nspin)
+    g.setType(type_)
+    g.getAO(1)
+    D = [model_density(og, 5)] if nspin == 1 else model_density(og, (5, 4), nspin=2, seed=2)
+    G = g.getEnergyGrad(xc, D)
+    ref = O.skeleton_grad_fd(og, Z, xyz, "def2-svp", np.stack(D), O.FUNCTIONAL_FILES[name], nspin)
+    print(name, nspin, "max |dG| %.2e, max |G| %.2e" % (np.abs(G - ref).max(), np.abs(ref).max()))
+    assert np.abs(G - ref).max() < 1e-8
+    # the gradient needs the AO derivatives one order above the functional's
+    g0 = make_grid(b, nspin=nspin, type_=type_)
+    with pytest.raises(cg.XCError):
+        g0.getEnergyGrad(xc, D)
+
+
+def test_xc_gradient_rejects_meta_gga(h2o):
+    """The reference's skeleton gradient has no tau terms; neither has this one."""
+    Z, xyz, b, ob, og = h2o
+    xc = cg.ExchangeCorrelation().Read("TPSS")
+    g = make_grid(b, type_=2)
+    with pytest.raises(cg.XCError) as e:
+        g.getEnergyGrad(xc, [model_density(og, 5)])
+    assert e.value.code == -6
