@@ -14,6 +14,7 @@ build (the path does not need a collective: replicas only).
 """
 import argparse
 import json
+import tempfile
 import os
 import subprocess
 import sys
@@ -307,7 +308,7 @@ def run_alkanes(args):
     stage = bg.stage_ms()
     kms = bg.kernel_ms()
     bg.profile(False)
-    clk_dir = os.path.join(REPO, "gpurun_out") if os.path.isdir(os.path.join(REPO, "gpurun_out")) else os.path.join(REPO, "_work")
+    clk_dir = os.environ.get("XC_BENCH_OUT") or tempfile.gettempdir()
     os.makedirs(clk_dir, exist_ok=True)
     clk_path = os.path.join(clk_dir, "clocks_alkanes.csv")
     cp, cf = clocks_start(clk_path)
@@ -547,7 +548,7 @@ def main():
     kms = grid.kernel_ms() if precision == PMX else None
     grid.profile(False)
 
-    clk_dir = os.path.join(REPO, "gpurun_out") if os.path.isdir(os.path.join(REPO, "gpurun_out")) else os.path.join(REPO, "_work")
+    clk_dir = os.environ.get("XC_BENCH_OUT") or tempfile.gettempdir()
     os.makedirs(clk_dir, exist_ok=True)
     clk_path = os.path.join(clk_dir, "clocks_bench.csv")
     cp, cf = clocks_start(clk_path) if rank == 0 else (None, None)

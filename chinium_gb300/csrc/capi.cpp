@@ -1074,7 +1074,7 @@ int xc_grid_tune(xc_grid* g, xc_functional* f, const double* D, int nspin, doubl
         rc.v_operands = G.mx.cfg.v_operands;
         const Run ref = run(rc);
         std::vector<xc_tune_candidate> cands;
-        auto judge = [&](const Run& r) {
+        auto assess = [&](const Run& r) {
             xc_tune_candidate c{};
             c.cfg.screen = r.cfg.screen;
             c.cfg.fock_tiles = r.cfg.fock_tiles;
@@ -1092,7 +1092,7 @@ int xc_grid_tune(xc_grid* g, xc_functional* f, const double* D, int nspin, doubl
         MixedConfig best = rc;
         double best_ms = ref.ms;
         auto consider = [&](const MixedConfig& c) {
-            const xc_tune_candidate k = judge(run(c));
+            const xc_tune_candidate k = assess(run(c));
             if (k.accepted && k.ms < best_ms) {
                 best = c;
                 best_ms = k.ms;

@@ -1,6 +1,6 @@
 """GPU parity: the CUDA path through the C ABI against the oracle on the same
 inputs.  Tolerances: FP64 path 1e-10 Eh in E_xc and 1e-10 max-abs in V_xc
-(the spec bar); pointwise stages (weights, AO, densities,
+(the parity bar for the plain path); pointwise stages (weights, AO, densities,
 functional) at 1e-12 relative or tighter where FP64 rounding allows."""
 import numpy as np
 import pytest
