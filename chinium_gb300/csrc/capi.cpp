@@ -359,6 +359,54 @@ void Grid::density_device(const double* dD) {
                         d_rho.p, d_rho1.p, d_tau.p, stream);
     have_density = true;
     have_potential = false;
+    have_fxc = false;
+}
+
+void Grid::evaluate_fxc(const Functional& f) {
+    CGB_CHECK(have_density, XC_ERR_STATE, "Evaluate needs a density (getDensity first)");
+    CGB_CHECK(f.nspin == nspin, XC_ERR_ARG, "functional and grid disagree on the number of spins");
+    CGB_CHECK(f.family <= 1, XC_ERR_UNSUPPORTED,
+              "second derivatives cover LDA and GGA functionals (as the reference's Evaluate(\"f\"))");
+    CGB_CHECK(f.family <= type, XC_ERR_STATE, "grid type is below the functional family (setType/getAO)");
+    d_f2.alloc((size_t)(nspin == 1 ? 3 : 15) * Gp);
+    launch_fxc(f.desc, f.family, nspin, Gp, d_rho.p, d_rho1.p, d_f2.p, stream);
+    fxc_family = f.family;
+    have_fxc = true;
+}
+
+void Grid::density_u_device(const double* dDU, int nmat) {
+    CGB_CHECK(!batched, XC_ERR_UNSUPPORTED, "response densities are per molecule");
+    CGB_CHECK(ao_order >= type, XC_ERR_STATE, "getAO must run (for the current type) before getDensityU");
+    CGB_CHECK(nmat >= 1, XC_ERR_ARG, "at least one response matrix");
+    const int n = basis.nbasis;
+    const long q = (long)nspin * nmat;
+    CGB_CHECK(q <= 65535, XC_ERR_ARG, "at most 65535 (spin, matrix) pairs per call");
+    d_DU.alloc((size_t)q * n * n);
+    d_rhoU.alloc((size_t)q * Gp);
+    d_rho1U.alloc((size_t)q * 3 * Gp);
+    // the plain density kernel forms 2 sum D(mu, nu) phi_mu grad phi_nu; the transpose gives the
+    // reference's 2 sum D(mu, nu) grad phi_mu phi_nu (GridDensity.cpp:67-68) for any D_U
+    launch_transpose_batch(n, q, dDU, d_DU.p, stream);
+    // (spin, matrix) pairs run as the kernel's spin index; gradients only up to GGA
+    launch_density_fp64((int)blocks.size(), d_blocks.p, d_lists.p, n, (int)q, type >= 1 ? 1 : 0, d_DU.p, d_ao.p,
+                        Gp, d_rhoU.p, d_rho1U.p, nullptr, stream);
+    nmat_u = nmat;
+    have_density_u = true;
+}
+
+void Grid::fock_u_device(double* dFU) {
+    CGB_CHECK(have_fxc, XC_ERR_STATE, "getFockU needs Evaluate(\"f\") on the current density");
+    CGB_CHECK(have_density_u, XC_ERR_STATE, "getFockU needs getDensityU first");
+    CGB_CHECK(fxc_family == 0 || (have_potential && eval_family >= 1), XC_ERR_STATE,
+              "getFockU of a GGA needs vsigma: Evaluate(\"v\" or \"ev\") on the current density");
+    const int n = basis.nbasis;
+    const long q = (long)nspin * nmat_u;
+    d_fcoefU.alloc((size_t)q * 5 * Gp);
+    launch_response_coef(fxc_family, nspin, Gp, nmat_u, d_w.p, d_rho1.p, d_vsigma.p, d_f2.p, d_rhoU.p, d_rho1U.p,
+                         d_fcoefU.p, stream);
+    CGB_CUDA(cudaMemsetAsync(dFU, 0, (size_t)q * n * n * sizeof(double), stream));
+    launch_fock_fp64((int)blocks.size(), d_blocks.p, d_lists.p, max_nb, n, (int)q, fxc_family, d_ao.p, Gp,
+                     d_fcoefU.p, dFU, stream);
 }
 
 void Grid::evaluate(const Functional& f, double float_above) {
@@ -743,9 +791,106 @@ int xc_evaluate(xc_functional* f, xc_grid* g, const char* order) {
     return guard([&] {
         CGB_CHECK(f && g && order, XC_ERR_ARG, "null argument");
         const std::string o = order;
-        CGB_CHECK(o == "e" || o == "v" || o == "ev", XC_ERR_UNSUPPORTED, "order must be e, v or ev");
-        g->g.evaluate(f->f);
+        CGB_CHECK(o == "e" || o == "v" || o == "ev" || o == "f", XC_ERR_UNSUPPORTED, "order must be e, v, ev or f");
+        if (o == "f") g->g.evaluate_fxc(f->f);
+        else g->g.evaluate(f->f);
         CGB_CUDA(cudaStreamSynchronize(g->g.stream));
+    });
+}
+
+int xc_functional_fxc_points(xc_functional* f, long n, const double* rho, const double* sigma, double* v2rho2,
+                             double* v2rhosigma, double* v2sigma2) {
+    return guard([&] {
+        CGB_CHECK(f && rho && v2rho2 && n > 0, XC_ERR_ARG, "bad arguments");
+        ensure_device();
+        const Functional& F = f->f;
+        CGB_CHECK(F.family <= 1, XC_ERR_UNSUPPORTED,
+                  "second derivatives cover LDA and GGA functionals (as the reference's Evaluate(\"f\"))");
+        CGB_CHECK(F.family < 1 || (sigma && v2rhosigma && v2sigma2), XC_ERR_ARG, "sigma arrays required for GGA");
+        const int ns = F.nspin, nsig = ns == 1 ? 1 : 3, nrr = ns == 1 ? 1 : 3, nrs = ns == 1 ? 1 : 6;
+        DevBuf<double> dr, ds, d1, d2, d3;
+        dr.upload(rho, ns * n);
+        ds.alloc(nsig * n);
+        if (F.family >= 1) ds.upload(sigma, nsig * n);
+        d1.alloc(nrr * n);
+        d2.alloc(nrs * n);
+        d3.alloc(nrs * n);
+        launch_fxc_points(F.desc, F.family, ns, n, dr.p, ds.p, d1.p, d2.p, d3.p, 0);
+        CGB_CUDA(cudaMemcpy(v2rho2, d1.p, nrr * n * sizeof(double), cudaMemcpyDeviceToHost));
+        if (F.family >= 1) {
+            CGB_CUDA(cudaMemcpy(v2rhosigma, d2.p, nrs * n * sizeof(double), cudaMemcpyDeviceToHost));
+            CGB_CUDA(cudaMemcpy(v2sigma2, d3.p, nrs * n * sizeof(double), cudaMemcpyDeviceToHost));
+        }
+    });
+}
+
+int xc_grid_get_density_u(xc_grid* g, const double* DU, int nspin, int nmat) {
+    return guard([&] {
+        CGB_CHECK(g && DU, XC_ERR_ARG, "null argument");
+        Grid& G = g->g;
+        CGB_CHECK(nspin == G.nspin, XC_ERR_ARG, "Wrong number of spin types!");
+        CGB_CHECK(nmat >= 1, XC_ERR_ARG, "at least one response matrix");
+        const size_t cnt = (size_t)nspin * nmat * G.basis.nbasis * G.basis.nbasis;
+        DevBuf<double> dU;
+        dU.upload(DU, cnt);
+        G.density_u_device(dU.p, nmat);
+        CGB_CUDA(cudaStreamSynchronize(G.stream));
+    });
+}
+
+int xc_grid_get_fock_u(xc_grid* g, double* FU) {
+    return guard([&] {
+        CGB_CHECK(g && FU, XC_ERR_ARG, "null argument");
+        Grid& G = g->g;
+        const size_t cnt = (size_t)G.nspin * G.nmat_u * G.basis.nbasis * G.basis.nbasis;
+        DevBuf<double> dF;
+        dF.alloc(cnt);
+        G.fock_u_device(dF.p);
+        CGB_CUDA(cudaMemcpyAsync(FU, dF.p, cnt * sizeof(double), cudaMemcpyDeviceToHost, G.stream));
+        CGB_CUDA(cudaStreamSynchronize(G.stream));
+    });
+}
+
+int xc_build_response(xc_grid* g, xc_functional* f, const double* D, int nspin, int nmat, const double* DU,
+                      double* FU) {
+    return guard([&] {
+        CGB_CHECK(g && f && D && DU && FU, XC_ERR_ARG, "null argument");
+        Grid& G = g->g;
+        CGB_CHECK(!G.batched, XC_ERR_UNSUPPORTED, "response builds are per molecule");
+        CGB_CHECK(nspin == G.nspin && f->f.nspin == G.nspin, XC_ERR_ARG, "Wrong number of spin types!");
+        CGB_CHECK(nmat >= 1, XC_ERR_ARG, "at least one response matrix");
+        CGB_CHECK(f->f.family <= 1, XC_ERR_UNSUPPORTED,
+                  "response V_xc covers LDA and GGA functionals (as the reference's Evaluate(\"f\"))");
+        G.ensure_work();
+        const int n = G.basis.nbasis;
+        const size_t nn = (size_t)n * n;
+        CGB_CUDA(cudaMemcpyAsync(G.d_D.p, D, nn * nspin * sizeof(double), cudaMemcpyHostToDevice, G.stream));
+        G.density_device(G.d_D.p);
+        G.evaluate(f->f);
+        G.evaluate_fxc(f->f);
+        // matrices in chunks whose per-point scratch (rho_U, grad rho_U, 5 coefficients) stays near 2 GB
+        const long per_mat = 9L * nspin * G.Gp * (long)sizeof(double);
+        const int chunk = (int)std::max(1L, std::min<long>(nmat, (2L << 30) / std::max(per_mat, 1L)));
+        DevBuf<double> dU, dF;
+        dU.alloc((size_t)nspin * chunk * nn);
+        dF.alloc((size_t)nspin * chunk * nn);
+        std::vector<double> hU((size_t)nspin * chunk * nn), hF((size_t)nspin * chunk * nn);
+        for (int m0 = 0; m0 < nmat; m0 += chunk) {
+            const int mc = std::min(chunk, nmat - m0);
+            for (int s = 0; s < nspin; s++)  // D_U[s][m0 .. m0 + mc) -> [s][0 .. mc)
+                std::memcpy(hU.data() + (size_t)s * mc * nn, DU + ((size_t)s * nmat + m0) * nn,
+                            (size_t)mc * nn * sizeof(double));
+            CGB_CUDA(cudaMemcpyAsync(dU.p, hU.data(), (size_t)nspin * mc * nn * sizeof(double),
+                                     cudaMemcpyHostToDevice, G.stream));
+            G.density_u_device(dU.p, mc);
+            G.fock_u_device(dF.p);
+            CGB_CUDA(cudaMemcpyAsync(hF.data(), dF.p, (size_t)nspin * mc * nn * sizeof(double),
+                                     cudaMemcpyDeviceToHost, G.stream));
+            CGB_CUDA(cudaStreamSynchronize(G.stream));
+            for (int s = 0; s < nspin; s++)
+                std::memcpy(FU + ((size_t)s * nmat + m0) * nn, hF.data() + (size_t)s * mc * nn,
+                            (size_t)mc * nn * sizeof(double));
+        }
     });
 }
 

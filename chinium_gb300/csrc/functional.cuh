@@ -525,14 +525,12 @@ CGB_HDN T e_r2scan_c(const XIn<T>& v) {
 }
 
 // ------------------------------------------------------------- registry
-// Energy density of one libxc id; unknown ids contribute nothing (ids are
-// validated on the host before any launch).
+// Energy density of one LDA or GGA libxc id (the ids that also have second
+// derivatives, order "f"); zero for any other id.
 template <class T, class R>
-CGB_HDN T e_id(int id, const XIn<T>& v) {
+CGB_HD T e_id_gga(int id, const XIn<T>& v) {
     auto pbe_x = [](const T& n, const T& s, const T&) { return fx_pbe<T, R>(n, s, R(0.8040), R(0.2195149727645171)); };
     auto pbe_xg = [](const T& n, const T& s, const T&) { return fx_pbe<T, R>(n, s, R(0.804), R(0.2195164512208958)); };
-    auto tpss_x = [](const T& n, const T& s, const T& t) { return fx_tpss<T, R>(n, s, t); };
-    auto r2_x = [](const T& n, const T& s, const T& t) { return fx_r2scan<T, R>(n, s, t); };
     switch (id) {
         case 1: return e_lda_x<T, R>(v);
         case 7: return e_vwn<T, R>(v, false);
@@ -548,13 +546,24 @@ CGB_HDN T e_id(int id, const XIn<T>& v) {
                    R(0.81) * e_lyp<T, R>(v);
         case 406: return R(0.75) * spin_exchange<T, R>(v, pbe_x) + e_pbe_c<T, R>(v, R(0.06672455060314922));
         case 436: return R(0.5) * e_b88<T, R>(v) + e_lyp<T, R>(v);
+    }
+    return T(R(0));
+}
+
+// Energy density of one libxc id; unknown ids contribute nothing (ids are
+// validated on the host before any launch).
+template <class T, class R>
+CGB_HDN T e_id(int id, const XIn<T>& v) {
+    auto tpss_x = [](const T& n, const T& s, const T& t) { return fx_tpss<T, R>(n, s, t); };
+    auto r2_x = [](const T& n, const T& s, const T& t) { return fx_r2scan<T, R>(n, s, t); };
+    switch (id) {
         case 202: return spin_exchange<T, R>(v, tpss_x);
         case 231: return e_tpss_c<T, R>(v);
         case 457: return R(0.9) * spin_exchange<T, R>(v, tpss_x) + e_tpss_c<T, R>(v);
         case 497: return spin_exchange<T, R>(v, r2_x);
         case 498: return e_r2scan_c<T, R>(v);
     }
-    return T(R(0));
+    return e_id_gga<T, R>(id, v);
 }
 
 // Family of an id (0 LDA, 1 GGA, 2 mGGA), -1 if unknown; EXX fraction.
@@ -647,6 +656,233 @@ CGB_HDN bool eval_pol(const FuncDesc& f, const R* in, R& eps, R* dv) {
     const T e = e_sum<T, R>(f, v);
     eps = e.v / rt;
     for (int i = 0; i < N; i++) dv[i] = e.d[i];
+    return true;
+}
+
+// ------------------------------------------------ second derivatives ("f")
+// Jet2<R, N>: value, gradient and the upper triangle of the Hessian in N
+// seeded inputs, propagated by the chain and product rules (second-order
+// forward mode), so the kernel f_xc of ExchangeCorrelation::Evaluate("f")
+// (ExchangeCorrelation.cpp:101-104, 126-133) is the exact Hessian of the
+// same expression that gives eps and v_xc.  Entry (i, j), i <= j, is
+// h[i N - i (i - 1) / 2 + j - i].
+template <class R, int N>
+struct Jet2 {
+    static constexpr int NH = N * (N + 1) / 2;
+    R v;
+    R d[N];
+    R h[NH];
+    CGB_HD Jet2() {}
+    CGB_HD Jet2(R x) : v(x) {
+#pragma unroll
+        for (int i = 0; i < N; i++) d[i] = R(0);
+#pragma unroll
+        for (int k = 0; k < NH; k++) h[k] = R(0);
+    }
+};
+
+// f(a) with f' = f1 and f'' = f2 at a.v
+template <class R, int N>
+CGB_HD Jet2<R, N> chain2(const Jet2<R, N>& a, R f, R f1, R f2) {
+    Jet2<R, N> r;
+    r.v = f;
+#pragma unroll
+    for (int i = 0; i < N; i++) r.d[i] = f1 * a.d[i];
+    int k = 0;
+#pragma unroll
+    for (int i = 0; i < N; i++)
+#pragma unroll
+        for (int j = i; j < N; j++, k++) r.h[k] = f1 * a.h[k] + f2 * a.d[i] * a.d[j];
+    return r;
+}
+
+template <class R, int N>
+CGB_HD Jet2<R, N> operator+(const Jet2<R, N>& a, const Jet2<R, N>& b) {
+    Jet2<R, N> r;
+    r.v = a.v + b.v;
+#pragma unroll
+    for (int i = 0; i < N; i++) r.d[i] = a.d[i] + b.d[i];
+#pragma unroll
+    for (int k = 0; k < Jet2<R, N>::NH; k++) r.h[k] = a.h[k] + b.h[k];
+    return r;
+}
+template <class R, int N>
+CGB_HD Jet2<R, N> operator-(const Jet2<R, N>& a) {
+    Jet2<R, N> r;
+    r.v = -a.v;
+#pragma unroll
+    for (int i = 0; i < N; i++) r.d[i] = -a.d[i];
+#pragma unroll
+    for (int k = 0; k < Jet2<R, N>::NH; k++) r.h[k] = -a.h[k];
+    return r;
+}
+template <class R, int N>
+CGB_HD Jet2<R, N> operator-(const Jet2<R, N>& a, const Jet2<R, N>& b) { return a + (-b); }
+template <class R, int N>
+CGB_HD Jet2<R, N> operator*(const Jet2<R, N>& a, const Jet2<R, N>& b) {
+    Jet2<R, N> r;
+    r.v = a.v * b.v;
+#pragma unroll
+    for (int i = 0; i < N; i++) r.d[i] = a.d[i] * b.v + a.v * b.d[i];
+    int k = 0;
+#pragma unroll
+    for (int i = 0; i < N; i++)
+#pragma unroll
+        for (int j = i; j < N; j++, k++)
+            r.h[k] = a.h[k] * b.v + a.v * b.h[k] + a.d[i] * b.d[j] + a.d[j] * b.d[i];
+    return r;
+}
+// q = a / b from a = q b: q' = (a' - q b') / b, q'' = (a'' - q b'' - q'_i b'_j - q'_j b'_i) / b
+template <class R, int N>
+CGB_HD Jet2<R, N> operator/(const Jet2<R, N>& a, const Jet2<R, N>& b) {
+    Jet2<R, N> r;
+    const R ib = R(1) / b.v;
+    r.v = a.v * ib;
+#pragma unroll
+    for (int i = 0; i < N; i++) r.d[i] = (a.d[i] - r.v * b.d[i]) * ib;
+    int k = 0;
+#pragma unroll
+    for (int i = 0; i < N; i++)
+#pragma unroll
+        for (int j = i; j < N; j++, k++)
+            r.h[k] = (a.h[k] - r.v * b.h[k] - r.d[i] * b.d[j] - r.d[j] * b.d[i]) * ib;
+    return r;
+}
+template <class R, int N>
+CGB_HD Jet2<R, N> operator+(const Jet2<R, N>& a, R b) {
+    Jet2<R, N> r = a;
+    r.v += b;
+    return r;
+}
+template <class R, int N>
+CGB_HD Jet2<R, N> operator+(R b, const Jet2<R, N>& a) { return a + b; }
+template <class R, int N>
+CGB_HD Jet2<R, N> operator-(const Jet2<R, N>& a, R b) { return a + (-b); }
+template <class R, int N>
+CGB_HD Jet2<R, N> operator-(R b, const Jet2<R, N>& a) { return (-a) + b; }
+template <class R, int N>
+CGB_HD Jet2<R, N> operator*(const Jet2<R, N>& a, R b) {
+    Jet2<R, N> r;
+    r.v = a.v * b;
+#pragma unroll
+    for (int i = 0; i < N; i++) r.d[i] = a.d[i] * b;
+#pragma unroll
+    for (int k = 0; k < Jet2<R, N>::NH; k++) r.h[k] = a.h[k] * b;
+    return r;
+}
+template <class R, int N>
+CGB_HD Jet2<R, N> operator*(R b, const Jet2<R, N>& a) { return a * b; }
+template <class R, int N>
+CGB_HD Jet2<R, N> operator/(const Jet2<R, N>& a, R b) { return a * (R(1) / b); }
+template <class R, int N>
+CGB_HD Jet2<R, N> operator/(R a, const Jet2<R, N>& b) {
+    const R q = a / b.v;
+    return chain2(b, q, -q / b.v, R(2) * q / (b.v * b.v));
+}
+
+template <class R, int N>
+CGB_HD Jet2<R, N> exp(const Jet2<R, N>& a) {
+    const R e = Scal<R>::exp_(a.v);
+    return chain2(a, e, e, e);
+}
+template <class R, int N>
+CGB_HD Jet2<R, N> log(const Jet2<R, N>& a) {
+    const R i = R(1) / a.v;
+    return chain2(a, Scal<R>::log_(a.v), i, -i * i);
+}
+template <class R, int N>
+CGB_HD Jet2<R, N> sqrt(const Jet2<R, N>& a) {
+    const R s = Scal<R>::sqrt_(a.v);
+    return chain2(a, s, R(0.5) / s, R(-0.25) / (s * a.v));
+}
+template <class R, int N>
+CGB_HD Jet2<R, N> pow(const Jet2<R, N>& a, R p) {
+    const R f = Scal<R>::pow_(a.v, p);
+    const R i = R(1) / a.v;
+    return chain2(a, f, p * f * i, p * (p - R(1)) * f * i * i);
+}
+template <class R, int N>
+CGB_HD Jet2<R, N> atan(const Jet2<R, N>& a) {
+    const R q = R(1) / (R(1) + a.v * a.v);
+    return chain2(a, Scal<R>::atan_(a.v), q, R(-2) * a.v * q * q);
+}
+template <class R, int N>
+CGB_HD Jet2<R, N> asinh(const Jet2<R, N>& a) {
+    const R q = R(1) / Scal<R>::sqrt_(R(1) + a.v * a.v);
+    return chain2(a, Scal<R>::asinh_(a.v), q, -a.v * q * q * q);
+}
+template <class R, int N>
+CGB_HD R val(const Jet2<R, N>& a) { return a.v; }
+
+template <class T, class R>
+CGB_HD T e_sum_gga(const FuncDesc& f, const XIn<T>& v) {
+    T e(R(0));
+    for (int i = 0; i < f.nids; i++) e = e + e_id_gga<T, R>(f.ids[i], v);
+    return e;
+}
+
+// Restricted point, LDA (FAM 0) or GGA (FAM 1): eps, dv = (vrho, vsigma)
+// and d2 = (v2rho2, v2rhosigma, v2sigma2), derivatives in the total rho and
+// sigma as libxc's unpolarized kernels.  Zeros below the density threshold.
+template <class R, int FAM>
+CGB_HDN bool eval_unpol2(const FuncDesc& f, R rho, R sigma, R& eps, R* dv, R* d2) {
+    constexpr int N = FAM == 0 ? 1 : 2;
+    using T = Jet2<R, N>;
+    for (int i = 0; i < 2; i++) dv[i] = R(0);
+    for (int i = 0; i < 3; i++) d2[i] = R(0);
+    eps = R(0);
+    if (!(rho >= R(kDensThr))) return false;
+    T r(rho), s(sigma);
+    r.d[0] = R(1);
+    if (N > 1) s.d[N - 1] = R(1);
+    s = tmax(s, T(R(1.0000000000000011e-40)));  // kDensThr^(8/3)
+    XIn<T> v{r * R(0.5), r * R(0.5), s * R(0.25), s * R(0.25), s * R(0.25), T(R(0)), T(R(0))};
+    const T e = e_sum_gga<T, R>(f, v);
+    eps = e.v / rho;
+    for (int i = 0; i < N; i++) dv[i] = e.d[i];
+    for (int k = 0; k < T::NH; k++) d2[k] = e.h[k];
+    return true;
+}
+
+// Unrestricted point: in = (ra, rb, saa, sab, sbb); dv in the same order;
+// d2 = v2rho2 (aa, ab, bb), v2rhosigma (a-aa, a-ab, a-bb, b-aa, b-ab, b-bb),
+// v2sigma2 (aa-aa, aa-ab, aa-bb, ab-ab, ab-bb, bb-bb): libxc's polarized layouts.
+template <class R, int FAM>
+CGB_HDN bool eval_pol2(const FuncDesc& f, const R* in, R& eps, R* dv, R* d2) {
+    constexpr int N = FAM == 0 ? 2 : 5;
+    using T = Jet2<R, N>;
+    for (int i = 0; i < 5; i++) dv[i] = R(0);
+    for (int i = 0; i < 15; i++) d2[i] = R(0);
+    eps = R(0);
+    const R rt = in[0] + in[1];
+    if (!(rt >= R(kDensThr))) return false;
+    T x[5];
+    for (int i = 0; i < 5; i++) {
+        x[i] = T(in[i]);
+        if (i < N) x[i].d[i] = R(1);
+    }
+    XIn<T> v{x[0], x[1], x[2], x[3], x[4], T(R(0)), T(R(0))};
+    v.ra = tmax(v.ra, T(R(kDensThr)));
+    v.rb = tmax(v.rb, T(R(kDensThr)));
+    v.saa = tmax(v.saa, T(R(1.0000000000000011e-40)));
+    v.sbb = tmax(v.sbb, T(R(1.0000000000000011e-40)));
+    const T half = (v.saa + v.sbb) * R(0.5);
+    v.sab = tmax(tmin(v.sab, half), -half);
+    const T e = e_sum_gga<T, R>(f, v);
+    eps = e.v / rt;
+    for (int i = 0; i < N; i++) dv[i] = e.d[i];
+    // Hessian (i <= j) of inputs 0..N-1 into the three libxc blocks
+    auto H = [&](int i, int j) { return e.h[i * N - i * (i - 1) / 2 + j - i]; };
+    d2[0] = H(0, 0);
+    d2[1] = H(0, 1);
+    d2[2] = H(1, 1);
+    if (FAM >= 1) {
+        for (int a = 0; a < 2; a++)
+            for (int x2 = 0; x2 < 3; x2++) d2[3 + 3 * a + x2] = H(a, 2 + x2);
+        int k = 9;
+        for (int p = 2; p < 5; p++)
+            for (int q = p; q < 5; q++) d2[k++] = H(p, q);
+    }
     return true;
 }
 

@@ -72,6 +72,21 @@ void launch_sap_coef(long Gp, int natoms, const double* d_atoms, const double* d
                      const double* d_radii, const double* x, const double* y, const double* z,
                      const double* w, double* fcoef, cudaStream_t s);
 
+// Second derivatives of an LDA / GGA functional at the grid's density (rho, rho1):
+// f2 (3 or 15, Gp), rows v2rho2, v2rhosigma, v2sigma2 in libxc's layouts.
+void launch_fxc(const xcf::FuncDesc& f, int family, int nspin, long Gp, const double* rho, const double* rho1,
+                double* f2, cudaStream_t s);
+// The same on caller arrays (parity tests).
+void launch_fxc_points(const xcf::FuncDesc& f, int family, int nspin, long n, const double* rho, const double* sigma,
+                       double* v2rho2, double* v2rhosigma, double* v2sigma2, cudaStream_t s);
+// out[q] = in[q]^T for nmat n x n matrices.
+void launch_transpose_batch(int n, long nmat, const double* in, double* out, cudaStream_t s);
+// Response V coefficients (layout of fcoef, one 5-row set per (spin, matrix) pair q = s nmat + m)
+// from the ground-state gradients and vsigma, f2 and the response densities rhoU (q, Gp), rho1U (q, 3, Gp).
+void launch_response_coef(int family, int nspin, long Gp, int nmat, const double* w, const double* rho1,
+                          const double* vsigma, const double* f2, const double* rhoU, const double* rho1U,
+                          double* fcoefU, cudaStream_t s);
+
 // Pointwise functional on caller arrays (parity tests).
 void launch_functional_points(const xcf::FuncDesc& f, int family, int nspin, long n, const double* rho,
                               const double* sigma, const double* tau, double* eps, double* vrho,

@@ -79,6 +79,15 @@ struct Grid {
     void energy_device(double* dE);
     void fock_device(double* dV, int family);
 
+    // response (coupled-perturbed) V_xc, FP64, LDA / GGA: Evaluate("f"), getDensityU, getFockU<u_t>
+    bool have_fxc = false, have_density_u = false;
+    int fxc_family = 0;
+    int nmat_u = 0;
+    DevBuf<double> d_f2, d_DU, d_rhoU, d_rho1U, d_fcoefU;
+    void evaluate_fxc(const Functional& f);
+    void density_u_device(const double* dDU, int nmat);  // D_U (s, nmat, n, n) on the device
+    void fock_u_device(double* dFU);                      // V_U (s, nmat, n, n)
+
     // mixed-precision (tensor-core) path; tiles and stores are prepared on first use
     MixedState mx;
     std::vector<MolSource> sources;  // molecules of the mixed path (one unless batched)

@@ -76,6 +76,7 @@ class Grid:
         check(lib().xc_grid_create(basis._h, grid.encode(), nspin, float(screen_threshold), ctypes.byref(h)))
         self._h = h
         self.nbasis = basis.nbasis
+        self._nmat_u = 0
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -183,6 +184,43 @@ class Grid:
         g = np.zeros(3 * len(self.basis.Z))
         check(lib().xc_grid_energy_grad(self._h, xc._h, _p(Dst), self.nspin, _p(g)))
         return g.reshape(-1, 3)
+
+    # -- response (coupled-perturbed) V_xc ---------------------------------
+    def _stack_u(self, DU):
+        """DU[spin][mat] (or, for one spin, a list of matrices) -> column-major (s, nmat, n, n)."""
+        if self.nspin == 1 and len(DU) and np.asarray(DU[0]).ndim == 2:
+            DU = [DU]
+        if len(DU) != self.nspin:
+            raise XCError(-1, "Wrong number of spin types!")
+        nmat = len(DU[0])
+        out = np.stack([np.stack([np.asarray(d, dtype=np.float64).T for d in DU[s]]) for s in range(self.nspin)])
+        return np.ascontiguousarray(out), nmat
+
+    def _unstack_u(self, F, nmat):
+        return [[F[s, m].T.copy() for m in range(nmat)] for s in range(self.nspin)]
+
+    def getDensityU(self, DU):
+        """Grid::getDensityU: DU[spin][mat] (restricted: a list of matrices)."""
+        Du, nmat = self._stack_u(DU)
+        check(lib().xc_grid_get_density_u(self._h, _p(Du), self.nspin, nmat))
+        self._nmat_u = nmat
+
+    def getFockU(self):
+        """Grid::getFockU<u_t>: V_U[spin][mat] of the last getDensityU."""
+        n, nmat = self.nbasis, self._nmat_u
+        F = np.zeros((self.nspin, nmat, n, n))
+        check(lib().xc_grid_get_fock_u(self._h, _p(F)))
+        return self._unstack_u(F, nmat)
+
+    def build_response(self, xc, D, DU):
+        """getDensity(D) + Evaluate("ev") + Evaluate("f") + getDensityU(DU) +
+        getFockU<u_t> in one call; returns V_U[spin][mat]."""
+        Dst = self._stack(D)
+        Du, nmat = self._stack_u(DU)
+        n = self.nbasis
+        F = np.zeros((self.nspin, nmat, n, n))
+        check(lib().xc_build_response(self._h, xc._h, _p(Dst), self.nspin, nmat, _p(Du), _p(F)))
+        return self._unstack_u(F, nmat)
 
     def sap_fock(self, precision=PRECISION_FP64):
         """SuperpositionAtomicPotential (GuessSCF.cpp:17-75); PRECISION_MIXED
@@ -352,6 +390,19 @@ class ExchangeCorrelation:
         check(lib().xc_functional_eval_points(self._h, n, _p(rho), _p(sigma), _p(tau), _p(eps), _p(vrho),
                                               _p(vsigma), _p(vtau)))
         return eps, vrho, vsigma, vtau
+
+    def fxc_points(self, rho, sigma=None):
+        """Second derivatives (order "f") on host arrays: v2rho2, v2rhosigma,
+        v2sigma2 in libxc's layouts, (1 or 3, n), (1 or 6, n), (1 or 6, n)."""
+        s = self.Spin
+        rho = np.ascontiguousarray(rho, dtype=np.float64).reshape(s, -1)
+        n = rho.shape[1]
+        nsig, nrr, nrs = (1, 1, 1) if s == 1 else (3, 3, 6)
+        sigma = np.zeros((nsig, n)) if sigma is None else np.ascontiguousarray(sigma, dtype=np.float64).reshape(nsig, n)
+        v2rho2, v2rhosigma, v2sigma2 = np.zeros((nrr, n)), np.zeros((nrs, n)), np.zeros((nrs, n))
+        check(lib().xc_functional_fxc_points(self._h, n, _p(rho), _p(sigma), _p(v2rho2), _p(v2rhosigma),
+                                             _p(v2sigma2)))
+        return v2rho2, v2rhosigma, v2sigma2
 
     def __bool__(self):
         return self._h is not None

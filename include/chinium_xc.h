@@ -164,7 +164,11 @@ int xc_functional_exx(const xc_functional* f, double* exx);
 int xc_functional_family(const xc_functional* f, int* family);
 
 /* ExchangeCorrelation::Evaluate(order, grid) (ExchangeCorrelation.cpp:165-248):
- * order "e", "v" or "ev" on the grid's current density. */
+ * order "e", "v" or "ev" on the grid's current density; "f" stores the
+ * second derivatives (v2rho2, v2rhosigma, v2sigma2; :101-133, :192-199,
+ * :241-244) for xc_grid_get_fock_u, LDA and GGA functionals only (the
+ * reference's meta-GGA branch has no "f"; here it fails with
+ * XC_ERR_UNSUPPORTED). */
 int xc_evaluate(xc_functional* f, xc_grid* g, const char* order);
 
 /* Pointwise evaluation on caller data (host arrays, layout as
@@ -226,6 +230,43 @@ int xc_grid_kernel_ms(xc_grid* g, double* ms);
  * needs the AO derivatives one order above the functional's: getAO(1) after
  * setType.  D as for xc_build (column-major, spins concatenated). */
 int xc_grid_energy_grad(xc_grid* g, xc_functional* f, const double* D, int nspin, double* grad);
+
+/* --------------------------------------------- response (coupled-perturbed)
+ * FP64, LDA and GGA.  D_U and V_U hold nspin x nmat column-major n x n
+ * matrices, spin-major: matrix m of spin s starts at (s * nmat + m) n^2, as
+ * the reference's std::vector<std::vector<EigenMatrix>> D[spin][mat]. */
+
+/* Second derivatives on caller points (host arrays): rho (s, n), sigma
+ * (1 or 3, n) -> v2rho2 (1 or 3, n), v2rhosigma (1 or 6, n), v2sigma2 (1 or 6,
+ * n) in libxc's layouts (rho_a rho_a, rho_a rho_b, rho_b rho_b; rho_a sigma_aa,
+ * rho_a sigma_ab, rho_a sigma_bb, rho_b sigma_aa, ...; the upper triangle of
+ * sigma_aa, sigma_ab, sigma_bb).  For parity tests. */
+int xc_functional_fxc_points(xc_functional* f, long npoints, const double* rho, const double* sigma,
+                             double* v2rho2, double* v2rhosigma, double* v2sigma2);
+
+/* Grid::getDensityU (Grid.cpp:63-77, GridDensity.cpp:47-77): response
+ * densities rho_U = sum D_U phi phi and grad rho_U = 2 sum D_U(mu, nu)
+ * grad phi_mu phi_nu of every matrix, kept on the grid. */
+int xc_grid_get_density_u(xc_grid* g, const double* DU, int nspin, int nmat);
+
+/* Grid::getFockU<u_t> (Grid.cpp:194-218, GridFock.cpp:97-160): V_U of every
+ * matrix of the last xc_grid_get_density_u, from the second derivatives of
+ * Evaluate("f") and, for GGAs, vsigma and grad rho of the ground-state
+ * density (getDensity + Evaluate("v"/"ev") + Evaluate("f") first).  V_U is the
+ * derivative of V_xc along D_U.  Restricted grids reproduce the reference's
+ * expression; unrestricted grids use the libxc layout of v2rhosigma and the
+ * spin-diagonal factor 2 on the output sigma pair, where the reference copies
+ * v2rhosigma into a (g, 2, 3) tensor in the other index order
+ * (ExchangeCorrelation.cpp:243) and scales the contracted pair
+ * (GridFock.cpp:136-138, 145). */
+int xc_grid_get_fock_u(xc_grid* g, double* FU);
+
+/* getDensity(D) + Evaluate("ev") + Evaluate("f") + getDensityU(D_U) +
+ * getFockU<u_t>, the sequence of CoupledPerturbed.cpp:131-134 and
+ * Universal.h:92-118, in one call (matrices processed in chunks that bound
+ * the device scratch).  Host buffers. */
+int xc_build_response(xc_grid* g, xc_functional* f, const double* D, int nspin, int nmat, const double* DU,
+                      double* FU);
 
 /* Incremental mixed-precision build for SCF iterations (the per-iteration
  * sequence at Restricted/SP.cpp:52-55, fused).  Densities are linear in D

@@ -296,6 +296,22 @@ def functional(ids, nspin, rho, sigma=None, tau=None):
     return eps, vrho, vsigma, vtau
 
 
+def functional_fxc(ids, nspin, rho, sigma=None):
+    """v2rho2, v2rhosigma, v2sigma2 on points (libxc layouts, component-major);
+    LDA and GGA only."""
+    ids = np.asarray(ids, dtype=np.int32)
+    rho = np.ascontiguousarray(rho, dtype=np.float64).reshape(nspin, -1)
+    ng = rho.shape[1]
+    nsig, nrr, nrs = (1, 1, 1) if nspin == 1 else (3, 3, 6)
+    sigma = np.zeros((nsig, ng)) if sigma is None else np.ascontiguousarray(sigma, dtype=np.float64).reshape(nsig, ng)
+    v2rho2, v2rhosigma, v2sigma2 = np.zeros((nrr, ng)), np.zeros((nrs, ng)), np.zeros((nrs, ng))
+    st = lib().oracle_functional_fxc(ctypes.c_int(len(ids)), _p(ids), ctypes.c_int(nspin), ctypes.c_int(ng),
+                                     _p(rho), _p(sigma), _p(v2rho2), _p(v2rhosigma), _p(v2sigma2))
+    if st:
+        raise ValueError("second derivatives need LDA / GGA ids, got %s" % list(ids))
+    return v2rho2, v2rhosigma, v2sigma2
+
+
 def functional_point(ids, nspin, inputs):
     ids = np.asarray(ids, dtype=np.int32)
     x = np.ascontiguousarray(inputs, dtype=np.float64)
@@ -359,6 +375,43 @@ class OracleGrid:
         if st:
             raise ValueError("oracle build failed")
         return E.value, F.transpose(0, 2, 1).copy()
+
+
+    def response(self, D, DU, ids, nspin):
+        """getDensity(D) + Evaluate("v", "f") + getDensityU(DU) + getFockU<u_t>
+        block by block with the C oracle (GridDensity.cpp:47-77,
+        GridFock.cpp:97-160).  D (nspin, n, n); DU (nspin, nmat, n, n).
+        Returns V_U (nspin, nmat, n, n)."""
+        fam = family(ids)
+        nb = self.basis.nbasis
+        D = np.asarray(D, dtype=np.float64).reshape(nspin, nb, nb)
+        DU = np.asarray(DU, dtype=np.float64).reshape(nspin, -1, nb, nb)
+        nmat = DU.shape[1]
+        Dc = np.ascontiguousarray(D.transpose(0, 2, 1))       # column-major per spin
+        DUc = np.ascontiguousarray(DU.transpose(0, 1, 3, 2))  # (mu, nu, mat, s) column-major
+        F = np.zeros((nspin, nmat, nb, nb))
+        blist = np.arange(nb, dtype=np.int32)
+        nsig = 1 if nspin == 1 else 3
+        L = lib()
+        for b, blk in enumerate(self.blocks):
+            ng = len(blk[0])
+            w = np.ascontiguousarray(blk[3], dtype=np.float64)
+            ao = np.ascontiguousarray(self.ao[b][0], dtype=np.float64)
+            ao1 = np.ascontiguousarray(self.ao[b][1], dtype=np.float64) if fam >= 1 else np.zeros(1)
+            rho, rho1 = np.zeros(nspin * ng), np.zeros(nspin * 3 * ng)
+            sigma, tau = np.zeros(nsig * ng), np.zeros(nspin * ng)
+            L.oracle_density(ctypes.c_int(ng), ctypes.c_int(nb), ctypes.c_int(nspin), ctypes.c_int(fam), _p(Dc),
+                             _p(ao), _p(ao1), _p(rho), _p(rho1), _p(sigma), _p(tau))
+            vsigma = functional(ids, nspin, rho, sigma)[2] if fam >= 1 else np.zeros((nsig, ng))
+            v2rho2, v2rhosigma, v2sigma2 = functional_fxc(ids, nspin, rho, sigma)
+            rhoU, rho1U, sigmaU = np.zeros(nspin * nmat * ng), np.zeros(nspin * nmat * 3 * ng), np.zeros(nsig * nmat * ng)
+            L.oracle_density_u(ctypes.c_int(ng), ctypes.c_int(nb), ctypes.c_int(nspin), ctypes.c_int(nmat),
+                               ctypes.c_int(fam), _p(DUc), _p(ao), _p(ao1), _p(rho1), _p(rhoU), _p(rho1U), _p(sigmaU))
+            vsigma = np.ascontiguousarray(vsigma)
+            L.oracle_fock_u(ctypes.c_int(ng), ctypes.c_int(nb), ctypes.c_int(nb), _p(blist), ctypes.c_int(nspin),
+                            ctypes.c_int(nmat), ctypes.c_int(fam), _p(w), _p(ao), _p(ao1), _p(rho1), _p(vsigma),
+                            _p(v2rho2), _p(v2rhosigma), _p(v2sigma2), _p(rhoU), _p(rho1U), _p(sigmaU), _p(F))
+        return F.transpose(0, 1, 3, 2).copy()
 
 
 def skeleton_grad_fd(og, Z, xyz_bohr, basis_name, D, ids, nspin, h=1e-4):

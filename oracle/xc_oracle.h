@@ -76,6 +76,32 @@ int oracle_build(int nblocks, const int* blk_ng, const long* blk_pt_off, const l
                  int type, const double* D, int nids, const int* ids, int nthreads,
                  double* E_out, double* F_out);
 
+/* Second derivatives of an LDA / GGA functional (order "f",
+ * ExchangeCorrelation.cpp:101-133) on ng points: v2rho2 (1 or 3, ng),
+ * v2rhosigma (1 or 6, ng), v2sigma2 (1 or 6, ng) in libxc's layouts
+ * (rho_a rho_a, rho_a rho_b, rho_b rho_b; rho_w sigma_x at 3 w + x; upper
+ * triangle of sigma_aa, sigma_ab, sigma_bb).  Returns -1 for a meta-GGA or an
+ * unknown id. */
+int oracle_functional_fxc(int nids, const int* ids, int nspin, int ng, const double* rho,
+                          const double* sigma, double* v2rho2, double* v2rhosigma, double* v2sigma2);
+
+/* Response densities of one block (GridDensity.cpp:47-77): D_U (n,n,nmat,s)
+ * -> RhoU (g,mat,s), Rho1U (g,r,mat,s), SigmaU (g,mat,uv); rho1 is the
+ * ground-state Rho1 (g,r,s). */
+void oracle_density_u(int ng, int nbasis, int nspin, int nmat, int type, const double* DU,
+                      const double* ao, const double* ao1, const double* rho1, double* rhoU,
+                      double* rho1U, double* sigmaU);
+
+/* Response V_xc of one block accumulated into F (ntot,ntot,nmat,s) through
+ * basis_list (GridFock.cpp:97-160, getFockU<u_t>), from the ground-state Rho1
+ * and vsigma, the second derivatives (layouts of oracle_functional_fxc) and
+ * the response densities of oracle_density_u. */
+void oracle_fock_u(int ng, int nbasis_block, int nbasis_total, const int* basis_list, int nspin,
+                   int nmat, int type, const double* w, const double* ao, const double* ao1,
+                   const double* rho1, const double* vsigma, const double* v2rho2,
+                   const double* v2rhosigma, const double* v2sigma2, const double* rhoU,
+                   const double* rho1U, const double* sigmaU, double* F);
+
 #ifdef __cplusplus
 }
 #endif

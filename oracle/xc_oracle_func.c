@@ -542,3 +542,128 @@ double oracle_functional_point(int nids, const int* ids, int ns, const double* i
     v = condition_pol(v, fam >= 2);
     return creal(e_sum(nids, ids, &v, &bad));
 }
+
+/* Second derivatives (order "f", ExchangeCorrelation.cpp:101-133): the
+ * complex-step first derivative g_i = Im e(x + i h e_i) / h, differentiated
+ * in x_j by differences combined by Richardson extrapolation; f_ij and f_ji
+ * are averaged.  Central steps d, d/2 (d = 1e-3 |x_j|, error O(d^4)), except
+ * for a sigma input of a polarized point whose step could cross the clamp
+ * |sigma_ab| <= (sigma_aa + sigma_bb) / 2 (gradients of the two spins nearly
+ * parallel and equal, as near a nucleus): there one-sided steps s, s/2, s/4
+ * away from the clamp (s = 1e-4 |x_j|, error O(s^3)).  Outputs in libxc's
+ * layouts, component-major [k][g] (see xc_oracle.h). */
+static void grad_cs(int nids, const int* ids, int ns, const double* x, int nin, double* gout, int* bad) {
+    for (int k = 0; k < nin; k++) {
+        cplx xc[7];
+        for (int j = 0; j < 7; j++) xc[j] = x[j];
+        const double h = step(x[k]);
+        xc[k] += I * h;
+        xin v;
+        if (ns == 1) v = from_unpol(xc[0], xc[1], xc[2], 0);
+        else {
+            xin v0 = {xc[0], xc[1], xc[2], xc[3], xc[4], xc[5], xc[6]};
+            v = condition_pol(v0, 0);
+        }
+        gout[k] = cimag(e_sum(nids, ids, &v, bad)) / h;
+    }
+}
+
+/* column j of the Hessian: d g / d x_j; dir 0 central, +-1 one-sided */
+static void hess_col(int nids, const int* ids, int ns, const double* x, int nin, int j, int dir, double* col,
+                     int* bad) {
+    double xs[7], a[5], b[5], c[5], e[5];
+    if (dir == 0) {
+        const double d = fabs(x[j]) > 0 ? 1e-3 * fabs(x[j]) : 1e-30;
+        const double st[4] = {d, -d, 0.5 * d, -0.5 * d};
+        double* out[4] = {a, b, c, e};
+        for (int k = 0; k < 4; k++) {
+            memcpy(xs, x, sizeof(xs));
+            xs[j] += st[k];
+            grad_cs(nids, ids, ns, xs, nin, out[k], bad);
+        }
+        for (int i = 0; i < nin; i++) {
+            const double c1 = (a[i] - b[i]) / (2 * d), c2 = (c[i] - e[i]) / d;
+            col[i] = (4 * c2 - c1) / 3;
+        }
+        return;
+    }
+    const double s = dir * (fabs(x[j]) > 0 ? 1e-4 * fabs(x[j]) : 1e-30);
+    const double st[3] = {s, 0.5 * s, 0.25 * s};
+    double* out[3] = {a, b, c};
+    grad_cs(nids, ids, ns, x, nin, e, bad);
+    for (int k = 0; k < 3; k++) {
+        memcpy(xs, x, sizeof(xs));
+        xs[j] += st[k];
+        grad_cs(nids, ids, ns, xs, nin, out[k], bad);
+    }
+    for (int i = 0; i < nin; i++) {
+        const double D1 = (a[i] - e[i]) / s, D2 = (b[i] - e[i]) / (0.5 * s), D4 = (c[i] - e[i]) / (0.25 * s);
+        const double R1 = 2 * D2 - D1, R2 = 2 * D4 - D2;
+        col[i] = (4 * R2 - R1) / 3;
+    }
+}
+
+int oracle_functional_fxc(int nids, const int* ids, int ns, int ng, const double* rho, const double* sigma,
+                          double* v2rho2, double* v2rhosigma, double* v2sigma2) {
+    const int fam = family_of(nids, ids);
+    if (fam < 0 || fam > 1) return -1;
+    const int nrr = ns == 1 ? 1 : 3, nrs = ns == 1 ? 1 : 6;
+    for (long i = 0; i < (long)nrr * ng; i++) v2rho2[i] = 0;
+    if (fam >= 1)
+        for (long i = 0; i < (long)nrs * ng; i++) v2rhosigma[i] = v2sigma2[i] = 0;
+    int bad = 0;
+    for (int g = 0; g < ng; g++) {
+        double x[7] = {0, 0, 0, 0, 0, 0, 0};
+        int nin;
+        if (ns == 1) {
+            x[0] = rho[g];
+            x[1] = fam >= 1 ? sigma[g] : 0;
+            nin = fam >= 1 ? 2 : 1;
+            if (x[0] < DENS_THR) continue;
+        } else {
+            x[0] = rho[g];
+            x[1] = rho[ng + g];
+            if (fam >= 1) {
+                x[2] = sigma[g];
+                x[3] = sigma[ng + g];
+                x[4] = sigma[2 * ng + g];
+            }
+            nin = fam >= 1 ? 5 : 2;
+            if (x[0] + x[1] < DENS_THR) continue;
+        }
+        double H[5][5];
+        const double gap = 0.5 * (x[2] + x[4]) - fabs(x[3]);
+        for (int j = 0; j < nin; j++) {
+            int dir = 0;
+            if (ns == 2 && j >= 2 && gap < 2e-3 * (fabs(x[j]) + fabs(x[3]))) {
+                if (j == 3) dir = x[3] >= 0 ? -1 : 1;  /* shrink |sigma_ab| */
+                else dir = 1;                           /* grow sigma_aa / sigma_bb */
+            }
+            double col[5];
+            hess_col(nids, ids, ns, x, nin, j, dir, col, &bad);
+            for (int i = 0; i < nin; i++) H[i][j] = col[i];
+        }
+        double S[5][5];
+        for (int i = 0; i < nin; i++)
+            for (int j = 0; j < nin; j++) S[i][j] = 0.5 * (H[i][j] + H[j][i]);
+        if (ns == 1) {
+            v2rho2[g] = S[0][0];
+            if (fam >= 1) {
+                v2rhosigma[g] = S[0][1];
+                v2sigma2[g] = S[1][1];
+            }
+        } else {
+            v2rho2[g] = S[0][0];
+            v2rho2[ng + g] = S[0][1];
+            v2rho2[2 * ng + g] = S[1][1];
+            if (fam >= 1) {
+                for (int a = 0; a < 2; a++)
+                    for (int xx = 0; xx < 3; xx++) v2rhosigma[(long)(3 * a + xx) * ng + g] = S[a][2 + xx];
+                int k = 0;
+                for (int p = 2; p < 5; p++)
+                    for (int q = p; q < 5; q++) v2sigma2[(long)(k++) * ng + g] = S[p][q];
+            }
+        }
+    }
+    return bad ? -1 : 0;
+}
