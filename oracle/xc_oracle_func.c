@@ -545,8 +545,11 @@ double oracle_functional_point(int nids, const int* ids, int ns, const double* i
 
 /* Second derivatives (order "f", ExchangeCorrelation.cpp:101-133): the
  * complex-step first derivative g_i = Im e(x + i h e_i) / h, differentiated
- * in x_j by differences combined by Richardson extrapolation; f_ij and f_ji
- * are averaged.  Central steps d, d/2 (d = 1e-3 |x_j|, error O(d^4)), except
+ * in x_j by differences combined by Richardson extrapolation.  A mixed entry
+ * comes from the better-conditioned of d g_i / d x_j and d g_j / d x_i: the
+ * step along the input with the larger |x g| (a step of 1e-3 sigma at a tiny
+ * sigma moves v_rho by less than its rounding, while the step along rho moves
+ * v_sigma well).  Central steps d, d/2, d/4 (d = 1e-2 |x_j|, error O(d^6)), except
  * for a sigma input of a polarized point whose step could cross the clamp
  * |sigma_ab| <= (sigma_aa + sigma_bb) / 2 (gradients of the two spins nearly
  * parallel and equal, as near a nucleus): there one-sided steps s, s/2, s/4
@@ -572,22 +575,31 @@ static void grad_cs(int nids, const int* ids, int ns, const double* x, int nin, 
 static void hess_col(int nids, const int* ids, int ns, const double* x, int nin, int j, int dir, double* col,
                      int* bad) {
     double xs[7], a[5], b[5], c[5], e[5];
+    /* sigma_ab enters through sigma_aa + 2 sigma_ab + sigma_bb and is smooth
+     * through zero: its step follows the larger of |sigma_ab| and a tenth of
+     * (sigma_aa + sigma_bb) / 2 */
+    const double scale = (ns == 2 && j == 3) ? fmax(fabs(x[3]), 0.05 * (x[2] + x[4])) : fabs(x[j]);
     if (dir == 0) {
-        const double d = fabs(x[j]) > 0 ? 1e-3 * fabs(x[j]) : 1e-30;
-        const double st[4] = {d, -d, 0.5 * d, -0.5 * d};
-        double* out[4] = {a, b, c, e};
-        for (int k = 0; k < 4; k++) {
+        /* central differences with steps d, d/2, d/4 and two Richardson levels (error O(d^6)) */
+        const double d = scale > 0 ? 1e-2 * scale : 1e-30;
+        double cd[3][5];
+        for (int l = 0; l < 3; l++) {
+            const double h = d / (double)(1 << l);
             memcpy(xs, x, sizeof(xs));
-            xs[j] += st[k];
-            grad_cs(nids, ids, ns, xs, nin, out[k], bad);
+            xs[j] += h;
+            grad_cs(nids, ids, ns, xs, nin, a, bad);
+            memcpy(xs, x, sizeof(xs));
+            xs[j] -= h;
+            grad_cs(nids, ids, ns, xs, nin, b, bad);
+            for (int i = 0; i < nin; i++) cd[l][i] = (a[i] - b[i]) / (2 * h);
         }
         for (int i = 0; i < nin; i++) {
-            const double c1 = (a[i] - b[i]) / (2 * d), c2 = (c[i] - e[i]) / d;
-            col[i] = (4 * c2 - c1) / 3;
+            const double r1 = (4 * cd[1][i] - cd[0][i]) / 3, r2 = (4 * cd[2][i] - cd[1][i]) / 3;
+            col[i] = (16 * r2 - r1) / 15;
         }
         return;
     }
-    const double s = dir * (fabs(x[j]) > 0 ? 1e-4 * fabs(x[j]) : 1e-30);
+    const double s = dir * (scale > 0 ? 1e-4 * scale : 1e-30);
     const double st[3] = {s, 0.5 * s, 0.25 * s};
     double* out[3] = {a, b, c};
     grad_cs(nids, ids, ns, x, nin, e, bad);
@@ -635,7 +647,8 @@ int oracle_functional_fxc(int nids, const int* ids, int ns, int ng, const double
         const double gap = 0.5 * (x[2] + x[4]) - fabs(x[3]);
         for (int j = 0; j < nin; j++) {
             int dir = 0;
-            if (ns == 2 && j >= 2 && gap < 2e-3 * (fabs(x[j]) + fabs(x[3]))) {
+            const double sc = j == 3 ? fmax(fabs(x[3]), 0.05 * (x[2] + x[4])) : fabs(x[j]);
+            if (ns == 2 && j >= 2 && gap < 2e-2 * (sc + fabs(x[3]))) {
                 if (j == 3) dir = x[3] >= 0 ? -1 : 1;  /* shrink |sigma_ab| */
                 else dir = 1;                           /* grow sigma_aa / sigma_bb */
             }
@@ -643,9 +656,11 @@ int oracle_functional_fxc(int nids, const int* ids, int ns, int ng, const double
             hess_col(nids, ids, ns, x, nin, j, dir, col, &bad);
             for (int i = 0; i < nin; i++) H[i][j] = col[i];
         }
-        double S[5][5];
+        double g0[5], S[5][5];
+        grad_cs(nids, ids, ns, x, nin, g0, &bad);
         for (int i = 0; i < nin; i++)
-            for (int j = 0; j < nin; j++) S[i][j] = 0.5 * (H[i][j] + H[j][i]);
+            for (int j = 0; j < nin; j++)
+                S[i][j] = fabs(x[j] * g0[j]) >= fabs(x[i] * g0[i]) ? H[i][j] : H[j][i];
         if (ns == 1) {
             v2rho2[g] = S[0][0];
             if (fam >= 1) {
