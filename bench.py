@@ -534,6 +534,34 @@ def main():
             gg.getEnergyGrad(xc, Dl)
         t_grad = (time.perf_counter() - t0) / 3 * 1e3
         del gg
+    # the FP64 response V_U (Evaluate("f") + getDensityU + getFockU<u_t>) for the
+    # 3 N_atoms perturbations a CPSCF / Hessian step carries, on the screened grid
+    resp = None
+    if xc.type <= 1:
+        gr = cg.Grid(basis, wl["grid"], nspin=ns, screen_threshold=1e-11)
+        gr.setType(xc.type)
+        gr.getAO(0)
+        nmat = 3 * len(wl["Z"])
+        rng = np.random.default_rng(11)
+        Dl = [D] if ns == 1 else Dsp
+        U = []
+        for _ in range(ns):
+            A = rng.normal(size=(nmat, n, n)) * 0.01
+            U.append(list(A + A.transpose(0, 2, 1)))
+        resp = {"nmat": nmat, "grid": "shells screened at 1e-11", "host_buffers": True,
+                "ground_state": "fp64 (density, functional, second derivatives)"}
+        out = {}
+        for prec, key in ((P64, "fp64"), (PMX, "mixed")):
+            gr.build_response(xc, Dl, [u[:2] for u in U], precision=prec)  # scratch allocation, first launches
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            out[key] = np.array(gr.build_response(xc, Dl, U, precision=prec))
+            t_resp = (time.perf_counter() - t0) * 1e3
+            resp[key] = {"ms": t_resp, "ms_per_matrix": t_resp / nmat}
+        resp["speedup_mixed_vs_fp64"] = resp["fp64"]["ms"] / resp["mixed"]["ms"]
+        resp["max_abs_dV_U_mixed_vs_fp64"] = float(np.abs(out["mixed"] - out["fp64"]).max())
+        resp["max_abs_V_U"] = float(np.abs(out["fp64"]).max())
+        del gr, U, out
 
     for _ in range(args.warmup):
         grid.build_device(xc, dD, dE, dV, precision)
@@ -617,6 +645,7 @@ def main():
                        "speedup_vs_screened_fp64": (t_plain_s / plain_steps) / (t_dev / args.steps),
                        "abs_dE_xc_screened_vs_unscreened_fp64": abs(E64s - E64),
                        "xc_gradient_fp64_ms": t_grad,
+                       "xc_response_fp64": resp,
                        "E_xc_fp64": E64, "E_xc": Emx if precision == PMX else E64,
                        "abs_dE_xc_vs_fp64": abs(Emx - E64),
                        "max_abs_dV_xc_vs_fp64": float((Vmx - V64).abs().max().item())},

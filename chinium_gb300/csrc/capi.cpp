@@ -851,25 +851,29 @@ int xc_grid_get_fock_u(xc_grid* g, double* FU) {
     });
 }
 
-int xc_build_response(xc_grid* g, xc_functional* f, const double* D, int nspin, int nmat, const double* DU,
-                      double* FU) {
+int xc_build_response(xc_grid* g, xc_functional* f, const double* D, int nspin, int precision, int nmat,
+                      const double* DU, double* FU) {
     return guard([&] {
         CGB_CHECK(g && f && D && DU && FU, XC_ERR_ARG, "null argument");
         Grid& G = g->g;
         CGB_CHECK(!G.batched, XC_ERR_UNSUPPORTED, "response builds are per molecule");
         CGB_CHECK(nspin == G.nspin && f->f.nspin == G.nspin, XC_ERR_ARG, "Wrong number of spin types!");
+        CGB_CHECK(precision == XC_PRECISION_FP64 || precision == XC_PRECISION_MIXED, XC_ERR_ARG, "bad precision");
         CGB_CHECK(nmat >= 1, XC_ERR_ARG, "at least one response matrix");
         CGB_CHECK(f->f.family <= 1, XC_ERR_UNSUPPORTED,
                   "response V_xc covers LDA and GGA functionals (as the reference's Evaluate(\"f\"))");
         G.ensure_work();
+        const bool mixed = precision == XC_PRECISION_MIXED;
         const int n = G.basis.nbasis;
         const size_t nn = (size_t)n * n;
         CGB_CUDA(cudaMemcpyAsync(G.d_D.p, D, nn * nspin * sizeof(double), cudaMemcpyHostToDevice, G.stream));
         G.density_device(G.d_D.p);
         G.evaluate(f->f);
         G.evaluate_fxc(f->f);
-        // matrices in chunks whose per-point scratch (rho_U, grad rho_U, 5 coefficients) stays near 2 GB
-        const long per_mat = 9L * nspin * G.Gp * (long)sizeof(double);
+        if (mixed) G.response_tiles_prepare();
+        // matrices in chunks that keep the device scratch near 2 GB: per matrix the FP64 path
+        // holds rho_U, grad rho_U and 5 coefficient rows per point, both paths D_U and V_U
+        const long per_mat = (long)sizeof(double) * nspin * ((mixed ? 0L : 9L * G.Gp) + 2L * (long)nn);
         const int chunk = (int)std::max(1L, std::min<long>(nmat, (2L << 30) / std::max(per_mat, 1L)));
         DevBuf<double> dU, dF;
         dU.alloc((size_t)nspin * chunk * nn);
@@ -882,8 +886,12 @@ int xc_build_response(xc_grid* g, xc_functional* f, const double* D, int nspin, 
                             (size_t)mc * nn * sizeof(double));
             CGB_CUDA(cudaMemcpyAsync(dU.p, hU.data(), (size_t)nspin * mc * nn * sizeof(double),
                                      cudaMemcpyHostToDevice, G.stream));
-            G.density_u_device(dU.p, mc);
-            G.fock_u_device(dF.p);
+            if (mixed) {
+                G.response_mixed(dU.p, mc, dF.p);
+            } else {
+                G.density_u_device(dU.p, mc);
+                G.fock_u_device(dF.p);
+            }
             CGB_CUDA(cudaMemcpyAsync(hF.data(), dF.p, (size_t)nspin * mc * nn * sizeof(double),
                                      cudaMemcpyDeviceToHost, G.stream));
             CGB_CUDA(cudaStreamSynchronize(G.stream));
@@ -891,6 +899,8 @@ int xc_build_response(xc_grid* g, xc_functional* f, const double* D, int nspin, 
                 std::memcpy(FU + ((size_t)s * nmat + m0) * nn, hF.data() + (size_t)s * mc * nn,
                             (size_t)mc * nn * sizeof(double));
         }
+        if (mixed && G.mixed_error())
+            throw Error(XC_ERR_TIMEOUT, "a bounded wait of the tensor-core pipeline gave up");
     });
 }
 

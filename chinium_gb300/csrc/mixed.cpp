@@ -756,3 +756,59 @@ int Grid::mixed_error() {
 }
 
 }  // namespace cgb
+
+namespace cgb {
+
+// Ground-state grad rho, vsigma and the second derivatives of the last
+// Evaluate("ev") / Evaluate("f") (FP64 grid) in tile order, for response_mixed.
+void Grid::response_tiles_prepare() {
+    CGB_CHECK(!batched, XC_ERR_UNSUPPORTED, "response builds are per molecule");
+    CGB_CHECK(have_fxc && (fxc_family == 0 || (have_potential && eval_family >= 1)), XC_ERR_STATE,
+              "the response needs Evaluate(\"ev\") and Evaluate(\"f\") on the current density");
+    mixed_ready();
+    MixedState& m = mx;
+    const long Gt = m.md.Gt;
+    const int nsig = nspin == 1 ? 1 : 3, nf2 = nspin == 1 ? 3 : 15;
+    const size_t nn = (size_t)basis.nbasis * basis.nbasis;
+    d_rt_rho1.alloc((size_t)3 * nspin * Gt);
+    d_rt_vsig.alloc((size_t)nsig * Gt);
+    d_rt_f2.alloc((size_t)nf2 * Gt);
+    d_rt_fcU.alloc((size_t)5 * nspin * Gt);
+    d_rt_D.alloc(nspin * nn);
+    d_rt_V.alloc(nspin * nn);
+    if (fxc_family >= 1) {
+        launch_gather(m.d_perm.p, Gt, Gp, 3 * nspin, d_rho1.p, d_rt_rho1.p, true, stream);
+        launch_gather(m.d_perm.p, Gt, Gp, nsig, d_vsigma.p, d_rt_vsig.p, true, stream);
+    }
+    launch_gather(m.d_perm.p, Gt, Gp, nf2, d_f2.p, d_rt_f2.p, true, stream);
+}
+
+// V_U of nmat matrices D_U (s, nmat, n, n) on the tensor cores: per matrix the
+// split-BF16 density of its symmetric part (rho_U, grad rho_U in tile order),
+// the response coefficients (FP64) and V_U through the V kernels, FP64 sums.
+void Grid::response_mixed(const double* dDU, int nmat, double* dFU) {
+    MixedState& m = mx;
+    const MixedDev& md = m.md;
+    const long Gt = md.Gt;
+    const int n = basis.nbasis;
+    const size_t nn = (size_t)n * n;
+    for (int k = 0; k < nmat; k++) {
+        for (int s = 0; s < nspin; s++)
+            CGB_CUDA(cudaMemcpyAsync(d_rt_D.p + s * nn, dDU + ((size_t)s * nmat + k) * nn, nn * sizeof(double),
+                                     cudaMemcpyDeviceToDevice, stream));
+        launch_split_d(d_rt_D.p, m.d_mols.p, 1, nspin, md.drows, m.dcols, n, m.d_Dp.p, stream);
+        density_passes(m.d_Dp.p);
+        launch_response_coef(fxc_family, nspin, Gt, 1, m.d_w.p, d_rt_rho1.p, d_rt_vsig.p, d_rt_f2.p, m.rho.p,
+                             m.rho1.p, d_rt_fcU.p, stream);
+        for (int s = 0; s < nspin; s++) {
+            v_prep(d_rt_fcU.p + (size_t)s * 5 * Gt, fxc_family);
+            v_partials(1);
+            launch_wsum(m.d_wpart.p, m.d_item_live.p, m.d_mols.p, 1, n, s, nspin, d_rt_V.p, stream);
+        }
+        for (int s = 0; s < nspin; s++)
+            CGB_CUDA(cudaMemcpyAsync(dFU + ((size_t)s * nmat + k) * nn, d_rt_V.p + s * nn, nn * sizeof(double),
+                                     cudaMemcpyDeviceToDevice, stream));
+    }
+}
+
+}  // namespace cgb

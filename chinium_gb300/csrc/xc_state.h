@@ -87,6 +87,11 @@ struct Grid {
     void evaluate_fxc(const Functional& f);
     void density_u_device(const double* dDU, int nmat);  // D_U (s, nmat, n, n) on the device
     void fock_u_device(double* dFU);                      // V_U (s, nmat, n, n)
+    // the same on the tensor cores (symmetric part of each D_U): ground-state grad rho,
+    // vsigma and f_xc gathered into tile order once, then density and V_U per matrix
+    DevBuf<double> d_rt_rho1, d_rt_vsig, d_rt_f2, d_rt_fcU, d_rt_D, d_rt_V;
+    void response_tiles_prepare();
+    void response_mixed(const double* dDU, int nmat, double* dFU);
 
     // mixed-precision (tensor-core) path; tiles and stores are prepared on first use
     MixedState mx;

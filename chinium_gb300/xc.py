@@ -212,14 +212,16 @@ class Grid:
         check(lib().xc_grid_get_fock_u(self._h, _p(F)))
         return self._unstack_u(F, nmat)
 
-    def build_response(self, xc, D, DU):
+    def build_response(self, xc, D, DU, precision=PRECISION_FP64):
         """getDensity(D) + Evaluate("ev") + Evaluate("f") + getDensityU(DU) +
-        getFockU<u_t> in one call; returns V_U[spin][mat]."""
+        getFockU<u_t> in one call; returns V_U[spin][mat].  PRECISION_MIXED
+        forms the response densities and V_U on the tensor cores (symmetric
+        part of each D_U)."""
         Dst = self._stack(D)
         Du, nmat = self._stack_u(DU)
         n = self.nbasis
         F = np.zeros((self.nspin, nmat, n, n))
-        check(lib().xc_build_response(self._h, xc._h, _p(Dst), self.nspin, nmat, _p(Du), _p(F)))
+        check(lib().xc_build_response(self._h, xc._h, _p(Dst), self.nspin, int(precision), nmat, _p(Du), _p(F)))
         return self._unstack_u(F, nmat)
 
     def sap_fock(self, precision=PRECISION_FP64):

@@ -264,9 +264,15 @@ int xc_grid_get_fock_u(xc_grid* g, double* FU);
 /* getDensity(D) + Evaluate("ev") + Evaluate("f") + getDensityU(D_U) +
  * getFockU<u_t>, the sequence of CoupledPerturbed.cpp:131-134 and
  * Universal.h:92-118, in one call (matrices processed in chunks that bound
- * the device scratch).  Host buffers. */
-int xc_build_response(xc_grid* g, xc_functional* f, const double* D, int nspin, int nmat, const double* DU,
-                      double* FU);
+ * the device scratch).  Host buffers.  precision XC_PRECISION_FP64 is the
+ * plain path (as xc_grid_get_fock_u); XC_PRECISION_MIXED keeps the ground
+ * state (densities, vsigma, second derivatives) in FP64 and forms each
+ * matrix's response density and V_U on the tensor cores (split-BF16 products,
+ * FP32 accumulation per unit, FP64 sums; ~1e-6 relative), from the symmetric
+ * part of D_U -- the response matrices of the reference's callers are
+ * symmetric (CoupledPerturbed.cpp:113). */
+int xc_build_response(xc_grid* g, xc_functional* f, const double* D, int nspin, int precision, int nmat,
+                      const double* DU, double* FU);
 
 /* Incremental mixed-precision build for SCF iterations (the per-iteration
  * sequence at Restricted/SP.cpp:52-55, fused).  Densities are linear in D

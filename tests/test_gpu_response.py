@@ -168,7 +168,7 @@ def bench_density(nbasis, nocc, seed=0):
 def test_response_is_derivative_of_gpu_fock(case):
     """Size-independent property at a production size: V_U(D_U) equals the
     Richardson-extrapolated central difference of the CUDA FP64 V_xc along
-    D_U (C18 B3LYP/def2-TZVP SG-2 RKS; Fe4S4 PBE/def2-SVP SG-1 UKS), on
+    D_U (C18 B3LYP/def2-TZVP SG-2 RKS; Fe4S4 PBE/def2-SVP SG-2 UKS), on
     screened grids (the response uses the same blocks as V_xc)."""
     if case == "c18":
         Z, xyz = M.c18()
@@ -178,7 +178,7 @@ def test_response_is_derivative_of_gpu_fock(case):
     else:
         Z, xyz = M.fe4s4()
         b = cg.Basis(Z, xyz, "def2-svp")
-        name, nspin, grid = "PBE", 2, "SG-1"
+        name, nspin, grid = "PBE", 2, "SG-2"
         ne = sum(Z)
         D = [0.5 * bench_density(b.nbasis, (ne + 8) // 2, 1), 0.5 * bench_density(b.nbasis, (ne - 8) // 2, 2)]
     n = b.nbasis
@@ -202,3 +202,53 @@ def test_response_is_derivative_of_gpu_fock(case):
     err = np.abs(FU - ref).max()
     print(case, "max |dV_U| %.2e, max |V_U| %.2e" % (err, np.abs(ref).max()))
     assert err < 1e-8 * max(1.0, np.abs(ref).max())
+
+
+MIXED_RTOL = 5e-6  # of max |V_U|: split-BF16 products with FP32 accumulation per unit, FP64 sums
+
+
+@pytest.mark.parametrize("name,nspin", [("SVWN5", 1), ("PBE", 1), ("B3LYP", 1), ("PBE", 2)])
+def test_response_mixed_matches_fp64(h2o, name, nspin):
+    """Tensor-core response densities and V_U (FP64 ground state) against the
+    FP64 response on symmetric D_U; a non-symmetric D_U gives exactly the
+    result of its symmetric part."""
+    Z, xyz, b, ob, og = h2o
+    n = b.nbasis
+    fam = O.family(O.FUNCTIONAL_FILES[name])
+    D, U = response_case(og, n, nspin)
+    g = cg.Grid(b, "SG-1", nspin=nspin)
+    g.setType(fam)
+    g.getAO(0)
+    xc = cg.ExchangeCorrelation(spin=nspin).Read(name)
+    Us = [list(U[s, :2]) for s in range(nspin)]
+    ref = np.array(g.build_response(xc, D, Us))
+    got = np.array(g.build_response(xc, D, Us, precision=cg.PRECISION_MIXED))
+    err = np.abs(got - ref).max()
+    print(name, nspin, "mixed max |dV_U| %.2e, max |V_U| %.2e" % (err, np.abs(ref).max()))
+    assert err < MIXED_RTOL * np.abs(ref).max()
+    A = U[:, 2]
+    sym = 0.5 * (A + A.transpose(0, 2, 1))
+    ga = np.array(g.build_response(xc, D, [[A[s]] for s in range(nspin)], precision=cg.PRECISION_MIXED))
+    gs = np.array(g.build_response(xc, D, [[sym[s]] for s in range(nspin)], precision=cg.PRECISION_MIXED))
+    assert np.array_equal(ga, gs)
+
+
+def test_response_mixed_c18_b3lyp():
+    """C18 B3LYP/def2-TZVP SG-2: the tensor-core response of three symmetric
+    perturbations against the FP64 response (screened grid)."""
+    Z, xyz = M.c18()
+    b = cg.Basis(Z, xyz, "def2-tzvp")
+    n = b.nbasis
+    g = cg.Grid(b, "SG-2", screen_threshold=1e-11)
+    g.setType(1)
+    g.getAO(0)
+    xc = cg.ExchangeCorrelation().Read("B3LYP")
+    D = [bench_density(n, 54)]
+    rng = np.random.default_rng(5)
+    A = rng.normal(size=(3, n, n)) * 0.01
+    U = [list(A + A.transpose(0, 2, 1))]
+    ref = np.array(g.build_response(xc, D, U))
+    got = np.array(g.build_response(xc, D, U, precision=cg.PRECISION_MIXED))
+    err = np.abs(got - ref).max()
+    print("c18 mixed max |dV_U| %.2e, max |V_U| %.2e" % (err, np.abs(ref).max()))
+    assert err < MIXED_RTOL * np.abs(ref).max()
