@@ -441,6 +441,73 @@ def run_scf_water(args):
     print(json.dumps(line), flush=True)
 
 
+def run_response(args):
+    """C18 RKS B3LYP/def2-TZVP SG-2 (shells screened at 1e-11): one step is one
+    response build (getDensity + Evaluate("ev", "f") + getDensityU + getFockU<u_t>,
+    fused) for the 3 N_atoms = 54 symmetric perturbations of a CPSCF / Hessian
+    step, through the C ABI with host buffers (uploads, FP64 ground state,
+    response densities and V_U, downloads inside the timed region).  The FP64
+    path runs once on the same input for the speed-up and the accuracy."""
+    import ctypes
+    import torch
+    import chinium_gb300 as cg
+    from chinium_gb300._lib import check, lib
+
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    wl = workload("c18")
+    basis = cg.Basis(wl["Z"], wl["xyz"], wl["basis"])
+    n = basis.nbasis
+    g = cg.Grid(basis, wl["grid"], screen_threshold=1e-11)
+    xc = cg.ExchangeCorrelation().Read(wl["functional"])
+    g.setType(xc.type)
+    g.getAO(0)
+    P64, PMX = cg.PRECISION_FP64, cg.PRECISION_MIXED
+    prec = P64 if args.precision == "fp64" else PMX
+    nmat = 3 * len(wl["Z"])
+    D = model_density(n, wl["nocc"])
+    rng = np.random.default_rng(11)
+    A = rng.normal(size=(nmat, n, n)) * 0.01
+    Dst = g._stack([D])
+    Du = np.ascontiguousarray((A + A.transpose(0, 2, 1))[None])  # symmetric: column-major = row-major
+    ptr = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+
+    def call(p, F):
+        check(lib().xc_build_response(g._h, xc._h, ptr(Dst), 1, p, nmat, ptr(Du), ptr(F)))
+
+    F = np.zeros_like(Du)
+    for _ in range(max(args.warmup, 1)):
+        call(prec, F)
+    cp, cf = clocks_start(os.path.join(os.environ.get("XC_BENCH_OUT") or tempfile.gettempdir(), "clocks_resp.csv"))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        call(prec, F)
+    t = (time.perf_counter() - t0) / args.steps
+    clocks = clocks_stop(cp, cf, os.path.join(os.environ.get("XC_BENCH_OUT") or tempfile.gettempdir(),
+                                              "clocks_resp.csv"))
+    cfg = {"workload": "C18 RKS B3LYP/def2-TZVP SG-2, 54 symmetric perturbations",
+           "precision": args.precision, "nbasis": n, "nmat": nmat, "grid": "shells screened at 1e-11",
+           "ground_state": "fp64 (density, functional, second derivatives) in every step",
+           "l2": "inputs larger than L2 (D_U of the step 134 MB; FP64 AO store)"}
+    if not args.no_fp64 and prec == PMX:
+        F64 = np.zeros_like(Du)
+        t1 = time.perf_counter()
+        call(P64, F64)
+        t64 = time.perf_counter() - t1
+        cfg.update({"fp64_ms_per_step": t64 * 1e3, "speedup_vs_fp64": t64 / t,
+                    "max_abs_dV_U_vs_fp64": float(np.abs(F - F64).max()), "max_abs_V_U": float(np.abs(F64).max())})
+    line = {"metric": "XC response V_U matrices/s (C18 B3LYP/def2-TZVP SG-2, 54 perturbations per step)",
+            "value": nmat / t, "unit": "matrices/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16x3 (split) + f64 accumulation" if prec == PMX else "f64", "data": "synthetic",
+            "config": cfg,
+            "e2e": {"value": nmat / t, "unit": "matrices/s", "h2d_bytes_per_step": int(Du.nbytes + Dst.nbytes),
+                    "d2h_bytes_per_step": int(F.nbytes)},
+            "clocks": clocks}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -454,7 +521,8 @@ def main():
     ap.add_argument("--ref-blocks", type=int, default=512,
                     help="blocks per step of the --impl reference arm (a bounded sample of the workload)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="c18", choices=["c18", "fe4s4", "alkanes64", "scf-water"])
+    ap.add_argument("--workload", default="c18", choices=["c18", "fe4s4", "alkanes64", "scf-water", "c18-response"])
+    ap.add_argument("--no-fp64", action="store_true", help="c18-response: skip the FP64 comparison")
     ap.add_argument("--scf-mols", type=int, default=4)
     ap.add_argument("--fp64-mols", type=int, default=0, help="alkanes64: molecules checked in FP64 (0 = all)")
     ap.add_argument("--no-tune", action="store_true")
@@ -465,6 +533,8 @@ def main():
         return run_alkanes(args)
     if args.workload == "scf-water":
         return run_scf_water(args)
+    if args.workload == "c18-response":
+        return run_response(args)
 
     import ctypes
     import torch
@@ -548,15 +618,26 @@ def main():
         for _ in range(ns):
             A = rng.normal(size=(nmat, n, n)) * 0.01
             U.append(list(A + A.transpose(0, 2, 1)))
-        resp = {"nmat": nmat, "grid": "shells screened at 1e-11", "host_buffers": True,
+        resp = {"nmat": nmat, "grid": "shells screened at 1e-11", "host_buffers": "C-ABI call, column-major host arrays",
                 "ground_state": "fp64 (density, functional, second derivatives)"}
+        # column-major host buffers prepared once: the timed region is the C-ABI call
+        # (upload of D and D_U, FP64 ground state, response, download of V_U)
+        from chinium_gb300._lib import lib as _xl, check as _xchk
+        import ctypes
+        Dst_r = gr._stack(Dl)
+        Du, _ = gr._stack_u(U)
+        Du2, _ = gr._stack_u([u[:2] for u in U])
+        _ptr = lambda a: a.ctypes.data_as(ctypes.c_void_p)
         out = {}
         for prec, key in ((P64, "fp64"), (PMX, "mixed")):
-            gr.build_response(xc, Dl, [u[:2] for u in U], precision=prec)  # scratch allocation, first launches
+            F2 = np.zeros_like(Du2)
+            _xchk(_xl().xc_build_response(gr._h, xc._h, _ptr(Dst_r), ns, prec, 2, _ptr(Du2), _ptr(F2)))  # warm-up
+            F = np.zeros_like(Du)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            out[key] = np.array(gr.build_response(xc, Dl, U, precision=prec))
+            _xchk(_xl().xc_build_response(gr._h, xc._h, _ptr(Dst_r), ns, prec, nmat, _ptr(Du), _ptr(F)))
             t_resp = (time.perf_counter() - t0) * 1e3
+            out[key] = F
             resp[key] = {"ms": t_resp, "ms_per_matrix": t_resp / nmat}
         resp["speedup_mixed_vs_fp64"] = resp["fp64"]["ms"] / resp["mixed"]["ms"]
         resp["max_abs_dV_U_mixed_vs_fp64"] = float(np.abs(out["mixed"] - out["fp64"]).max())
@@ -645,7 +726,7 @@ def main():
                        "speedup_vs_screened_fp64": (t_plain_s / plain_steps) / (t_dev / args.steps),
                        "abs_dE_xc_screened_vs_unscreened_fp64": abs(E64s - E64),
                        "xc_gradient_fp64_ms": t_grad,
-                       "xc_response_fp64": resp,
+                       "xc_response": resp,
                        "E_xc_fp64": E64, "E_xc": Emx if precision == PMX else E64,
                        "abs_dE_xc_vs_fp64": abs(Emx - E64),
                        "max_abs_dV_xc_vs_fp64": float((Vmx - V64).abs().max().item())},

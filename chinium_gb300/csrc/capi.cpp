@@ -878,26 +878,22 @@ int xc_build_response(xc_grid* g, xc_functional* f, const double* D, int nspin, 
         DevBuf<double> dU, dF;
         dU.alloc((size_t)nspin * chunk * nn);
         dF.alloc((size_t)nspin * chunk * nn);
-        std::vector<double> hU((size_t)nspin * chunk * nn), hF((size_t)nspin * chunk * nn);
         for (int m0 = 0; m0 < nmat; m0 += chunk) {
             const int mc = std::min(chunk, nmat - m0);
-            for (int s = 0; s < nspin; s++)  // D_U[s][m0 .. m0 + mc) -> [s][0 .. mc)
-                std::memcpy(hU.data() + (size_t)s * mc * nn, DU + ((size_t)s * nmat + m0) * nn,
-                            (size_t)mc * nn * sizeof(double));
-            CGB_CUDA(cudaMemcpyAsync(dU.p, hU.data(), (size_t)nspin * mc * nn * sizeof(double),
-                                     cudaMemcpyHostToDevice, G.stream));
+            // D_U[s][m0 .. m0 + mc) -> device [s][0 .. mc): one contiguous copy per spin
+            for (int s = 0; s < nspin; s++)
+                CGB_CUDA(cudaMemcpyAsync(dU.p + (size_t)s * mc * nn, DU + ((size_t)s * nmat + m0) * nn,
+                                         (size_t)mc * nn * sizeof(double), cudaMemcpyHostToDevice, G.stream));
             if (mixed) {
                 G.response_mixed(dU.p, mc, dF.p);
             } else {
                 G.density_u_device(dU.p, mc);
                 G.fock_u_device(dF.p);
             }
-            CGB_CUDA(cudaMemcpyAsync(hF.data(), dF.p, (size_t)nspin * mc * nn * sizeof(double),
-                                     cudaMemcpyDeviceToHost, G.stream));
-            CGB_CUDA(cudaStreamSynchronize(G.stream));
             for (int s = 0; s < nspin; s++)
-                std::memcpy(FU + ((size_t)s * nmat + m0) * nn, hF.data() + (size_t)s * mc * nn,
-                            (size_t)mc * nn * sizeof(double));
+                CGB_CUDA(cudaMemcpyAsync(FU + ((size_t)s * nmat + m0) * nn, dF.p + (size_t)s * mc * nn,
+                                         (size_t)mc * nn * sizeof(double), cudaMemcpyDeviceToHost, G.stream));
+            CGB_CUDA(cudaStreamSynchronize(G.stream));
         }
         if (mixed && G.mixed_error())
             throw Error(XC_ERR_TIMEOUT, "a bounded wait of the tensor-core pipeline gave up");
