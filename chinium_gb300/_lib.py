@@ -97,6 +97,7 @@ SIGNATURES = {
     "xc_functional_fxc_points": [_P, _L, _P, _P, _P, _P, _P],
     "xc_grid_get_density_u": [_P, _P, _I, _I],
     "xc_grid_get_fock_u": [_P, _P],
+    "xc_grid_set_response_precision": [_P, _I],
     "xc_build_response": [_P, _P, _P, _I, _I, _I, _P, _P],
     "xc_functional_energy_static": [_P, _L, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P],
     "xc_build_incremental": [_P, _P, _P, _I, _I, _P, _P],

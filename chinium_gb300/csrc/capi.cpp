@@ -360,6 +360,7 @@ void Grid::density_device(const double* dD) {
     have_density = true;
     have_potential = false;
     have_fxc = false;
+    rt_ready = false;
 }
 
 void Grid::evaluate_fxc(const Functional& f) {
@@ -372,6 +373,7 @@ void Grid::evaluate_fxc(const Functional& f) {
     launch_fxc(f.desc, f.family, nspin, Gp, d_rho.p, d_rho1.p, d_f2.p, stream);
     fxc_family = f.family;
     have_fxc = true;
+    rt_ready = false;
 }
 
 void Grid::density_u_device(const double* dDU, int nmat) {
@@ -382,6 +384,14 @@ void Grid::density_u_device(const double* dDU, int nmat) {
     const long q = (long)nspin * nmat;
     CGB_CHECK(q <= 65535, XC_ERR_ARG, "at most 65535 (spin, matrix) pairs per call");
     d_DU.alloc((size_t)q * n * n);
+    if (resp_precision == XC_PRECISION_MIXED) {
+        // the tensor-core path forms each matrix's response density inside getFockU
+        // (from the symmetric part of D_U); keep the matrices
+        CGB_CUDA(cudaMemcpyAsync(d_DU.p, dDU, (size_t)q * n * n * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+        nmat_u = nmat;
+        have_density_u = true;
+        return;
+    }
     d_rhoU.alloc((size_t)q * Gp);
     d_rho1U.alloc((size_t)q * 3 * Gp);
     // the plain density kernel forms 2 sum D(mu, nu) phi_mu grad phi_nu; the transpose gives the
@@ -401,6 +411,14 @@ void Grid::fock_u_device(double* dFU) {
               "getFockU of a GGA needs vsigma: Evaluate(\"v\" or \"ev\") on the current density");
     const int n = basis.nbasis;
     const long q = (long)nspin * nmat_u;
+    if (resp_precision == XC_PRECISION_MIXED) {
+        if (!rt_ready) {
+            response_tiles_prepare();
+            rt_ready = true;
+        }
+        response_mixed(d_DU.p, nmat_u, dFU);
+        return;
+    }
     d_fcoefU.alloc((size_t)q * 5 * Gp);
     launch_response_coef(fxc_family, nspin, Gp, nmat_u, d_w.p, d_rho1.p, d_vsigma.p, d_f2.p, d_rhoU.p, d_rho1U.p,
                          d_fcoefU.p, stream);
@@ -848,6 +866,18 @@ int xc_grid_get_fock_u(xc_grid* g, double* FU) {
         G.fock_u_device(dF.p);
         CGB_CUDA(cudaMemcpyAsync(FU, dF.p, cnt * sizeof(double), cudaMemcpyDeviceToHost, G.stream));
         CGB_CUDA(cudaStreamSynchronize(G.stream));
+        if (G.resp_precision == XC_PRECISION_MIXED && G.mixed_error())
+            throw Error(XC_ERR_TIMEOUT, "a bounded wait of the tensor-core pipeline gave up");
+    });
+}
+
+int xc_grid_set_response_precision(xc_grid* g, int precision) {
+    return guard([&] {
+        CGB_CHECK(g, XC_ERR_ARG, "null grid");
+        CGB_CHECK(precision == XC_PRECISION_FP64 || precision == XC_PRECISION_MIXED, XC_ERR_ARG, "bad precision");
+        CGB_CHECK(!g->g.batched, XC_ERR_UNSUPPORTED, "response builds are per molecule");
+        if (g->g.resp_precision != precision) g->g.have_density_u = false;
+        g->g.resp_precision = precision;
     });
 }
 
@@ -870,7 +900,13 @@ int xc_build_response(xc_grid* g, xc_functional* f, const double* D, int nspin, 
         G.density_device(G.d_D.p);
         G.evaluate(f->f);
         G.evaluate_fxc(f->f);
-        if (mixed) G.response_tiles_prepare();
+        const int saved = G.resp_precision;
+        G.resp_precision = precision;
+        struct Restore {
+            Grid& g;
+            int p;
+            ~Restore() { g.resp_precision = p; }
+        } restore{G, saved};
         // matrices in chunks that keep the device scratch near 2 GB: per matrix the FP64 path
         // holds rho_U, grad rho_U and 5 coefficient rows per point, both paths D_U and V_U
         const long per_mat = (long)sizeof(double) * nspin * ((mixed ? 0L : 9L * G.Gp) + 2L * (long)nn);
@@ -884,12 +920,8 @@ int xc_build_response(xc_grid* g, xc_functional* f, const double* D, int nspin, 
             for (int s = 0; s < nspin; s++)
                 CGB_CUDA(cudaMemcpyAsync(dU.p + (size_t)s * mc * nn, DU + ((size_t)s * nmat + m0) * nn,
                                          (size_t)mc * nn * sizeof(double), cudaMemcpyHostToDevice, G.stream));
-            if (mixed) {
-                G.response_mixed(dU.p, mc, dF.p);
-            } else {
-                G.density_u_device(dU.p, mc);
-                G.fock_u_device(dF.p);
-            }
+            G.density_u_device(dU.p, mc);
+            G.fock_u_device(dF.p);
             for (int s = 0; s < nspin; s++)
                 CGB_CUDA(cudaMemcpyAsync(FU + ((size_t)s * nmat + m0) * nn, dF.p + (size_t)s * mc * nn,
                                          (size_t)mc * nn * sizeof(double), cudaMemcpyDeviceToHost, G.stream));

@@ -90,6 +90,8 @@ struct Grid {
     // the same on the tensor cores (symmetric part of each D_U): ground-state grad rho,
     // vsigma and f_xc gathered into tile order once, then density and V_U per matrix
     DevBuf<double> d_rt_rho1, d_rt_vsig, d_rt_f2, d_rt_fcU, d_rt_D, d_rt_V;
+    int resp_precision = 0;  // xc_precision of getDensityU / getFockU
+    bool rt_ready = false;   // tile-order ground state matches the current Evaluate("f")
     void response_tiles_prepare();
     void response_mixed(const double* dDU, int nmat, double* dFU);
 

@@ -199,6 +199,12 @@ class Grid:
     def _unstack_u(self, F, nmat):
         return [[F[s, m].T.copy() for m in range(nmat)] for s in range(self.nspin)]
 
+    def setResponsePrecision(self, precision):
+        """Precision of getDensityU / getFockU (PRECISION_FP64 default;
+        PRECISION_MIXED: tensor-core response densities and V_U on the FP64
+        ground state of Evaluate("ev") / Evaluate("f"))."""
+        check(lib().xc_grid_set_response_precision(self._h, int(precision)))
+
     def getDensityU(self, DU):
         """Grid::getDensityU: DU[spin][mat] (restricted: a list of matrices)."""
         Du, nmat = self._stack_u(DU)

@@ -261,6 +261,14 @@ int xc_grid_get_density_u(xc_grid* g, const double* DU, int nspin, int nmat);
  * (GridFock.cpp:136-138, 145). */
 int xc_grid_get_fock_u(xc_grid* g, double* FU);
 
+/* Precision of xc_grid_get_density_u / xc_grid_get_fock_u (no reference
+ * counterpart; default XC_PRECISION_FP64).  XC_PRECISION_MIXED keeps the
+ * FP64 ground state of Evaluate("ev") / Evaluate("f"), gathered once into the
+ * tensor-core tiles, and forms each matrix's response density (symmetric part
+ * of D_U) and V_U on the tensor cores inside xc_grid_get_fock_u: the
+ * per-iteration work of a CPSCF loop (CoupledPerturbed.cpp:131-134). */
+int xc_grid_set_response_precision(xc_grid* g, int precision);
+
 /* getDensity(D) + Evaluate("ev") + Evaluate("f") + getDensityU(D_U) +
  * getFockU<u_t>, the sequence of CoupledPerturbed.cpp:131-134 and
  * Universal.h:92-118, in one call (matrices processed in chunks that bound

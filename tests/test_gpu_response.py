@@ -252,3 +252,29 @@ def test_response_mixed_c18_b3lyp():
     err = np.abs(got - ref).max()
     print("c18 mixed max |dV_U| %.2e, max |V_U| %.2e" % (err, np.abs(ref).max()))
     assert err < MIXED_RTOL * np.abs(ref).max()
+
+
+def test_response_mixed_split_calls_equal_fused(h2o):
+    """setResponsePrecision(MIXED) + getDensityU + getFockU on the ground state
+    of getDensity + Evaluate("ev", "f") give the fused mixed call's matrices;
+    a second iteration reuses the tile-order ground state."""
+    Z, xyz, b, ob, og = h2o
+    D, U = response_case(og, b.nbasis, 1)
+    xc = cg.ExchangeCorrelation().Read("PBE")
+    g = cg.Grid(b, "SG-1")
+    g.setType(1)
+    g.getAO(0)
+    Us = list(U[0, :2])
+    fused = np.array(g.build_response(xc, D, Us, precision=cg.PRECISION_MIXED))
+    g.getDensity(D)
+    xc.Evaluate("ev", g)
+    xc.Evaluate("f", g)
+    g.setResponsePrecision(cg.PRECISION_MIXED)
+    for _ in range(2):
+        g.getDensityU(Us)
+        split = np.array(g.getFockU())
+        assert np.array_equal(split, fused)
+    g.setResponsePrecision(cg.PRECISION_FP64)
+    g.getDensityU(Us)
+    f64 = np.array(g.getFockU())
+    assert np.abs(f64 - split).max() < MIXED_RTOL * np.abs(f64).max()
