@@ -441,6 +441,69 @@ def run_scf_water(args):
     print(json.dumps(line), flush=True)
 
 
+def run_gradient(args):
+    """C18 RKS B3LYP/def2-TZVP SG-2: the XC nuclear gradient with the grid fixed
+    (getDensitySkeleton + getEnergyGrad, FP64) through the C ABI, host buffers;
+    one step is one gradient (upload of D, FP64 density and functional, the
+    gradient kernel, reduction by atom).  Unscreened blocks (the reference's
+    BasisList) and shells screened at 1e-11 (the same gradient to 1e-12).
+    Roofline of the gradient kernel: FP64 FLOPs of its two products per block
+    (T = phi D and U = Z D: 2 * 2 g n_b^2), the Z operand (8 g n_b) and the
+    contraction with the AO gradients and Hessians (27 g n_b), over the
+    kernel's CUDA-event time, against the cuBLAS DGEMM rate measured here."""
+    import torch
+    import chinium_gb300 as cg
+
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    wl = workload("c18")
+    basis = cg.Basis(wl["Z"], wl["xyz"], wl["basis"])
+    n = basis.nbasis
+    xc = cg.ExchangeCorrelation().Read(wl["functional"])
+    D = model_density(n, wl["nocc"])
+    out = {}
+    for key, thr in (("unscreened", 0.0), ("screened_1e-11", 1e-11)):
+        g = cg.Grid(basis, wl["grid"], screen_threshold=thr)
+        g.setType(xc.type)
+        g.getAO(1)
+        for _ in range(max(args.warmup, 1)):
+            G = g.getEnergyGrad(xc, [D])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            G = g.getEnergyGrad(xc, [D])
+        t = (time.perf_counter() - t0) / args.steps
+        g.profile(True)
+        g.getEnergyGrad(xc, [D])
+        ms = g.stage_ms()
+        g.profile(False)
+        pts = g.points()
+        nb = np.asarray(pts["nb"], dtype=np.float64)
+        ng = np.asarray(pts["ng"], dtype=np.float64)
+        flops = float(np.sum(4 * ng * nb * nb + 35 * ng * nb))
+        out[key] = {"ms_per_gradient": t * 1e3, "kernel_ms": ms[2], "density_ms": ms[0], "functional_ms": ms[1],
+                    "kernel_fp64_tflops": flops / (ms[2] * 1e-3) / 1e12, "grad": G}
+        del g
+    peak = fp64_gemm_peak(torch)
+    sc = out["screened_1e-11"]
+    diff = float(np.abs(out["unscreened"]["grad"] - sc["grad"]).max())
+    for v in out.values():
+        v.pop("grad")
+    line = {"metric": "XC nuclear gradients/s (C18 B3LYP/def2-TZVP SG-2, grid fixed, FP64)",
+            "value": 1e3 / sc["ms_per_gradient"], "unit": "gradients/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": sc["ms_per_gradient"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "C18 RKS B3LYP/def2-TZVP SG-2, XC gradient (getDensitySkeleton + getEnergyGrad)",
+                       "legs": out, "max_abs_dgrad_screened_vs_unscreened": diff,
+                       "l2": "inputs larger than L2 (AO store with Hessians, 10 components)"},
+            "e2e": {"value": 1e3 / sc["ms_per_gradient"], "unit": "gradients/s", "h2d_bytes_per_step": 8 * n * n,
+                    "d2h_bytes_per_step": 0},
+            "roofline": {"bound": "fp64", "kernel": "grad_fp64_kernel", "achieved": sc["kernel_fp64_tflops"],
+                         "peak": peak, "unit": "TFLOP/s", "frac": sc["kernel_fp64_tflops"] / peak,
+                         "traffic": None, "peak_source": "cuBLAS DGEMM 4096^3 measured in this run"}}
+    print(json.dumps(line), flush=True)
+
+
 def run_response(args):
     """C18 RKS B3LYP/def2-TZVP SG-2 (shells screened at 1e-11), the response
     work of one CPSCF iteration for the 3 N_atoms = 54 symmetric perturbations
@@ -538,7 +601,8 @@ def main():
     ap.add_argument("--ref-blocks", type=int, default=512,
                     help="blocks per step of the --impl reference arm (a bounded sample of the workload)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="c18", choices=["c18", "fe4s4", "alkanes64", "scf-water", "c18-response"])
+    ap.add_argument("--workload", default="c18", choices=["c18", "fe4s4", "alkanes64", "scf-water", "c18-response",
+                                                         "c18-gradient"])
     ap.add_argument("--no-fp64", action="store_true", help="c18-response: skip the FP64 comparison")
     ap.add_argument("--scf-mols", type=int, default=4)
     ap.add_argument("--fp64-mols", type=int, default=0, help="alkanes64: molecules checked in FP64 (0 = all)")
@@ -552,6 +616,8 @@ def main():
         return run_scf_water(args)
     if args.workload == "c18-response":
         return run_response(args)
+    if args.workload == "c18-gradient":
+        return run_gradient(args)
 
     import ctypes
     import torch

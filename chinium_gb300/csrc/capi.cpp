@@ -1014,8 +1014,11 @@ int xc_grid_energy_grad(xc_grid* g, xc_functional* f, const double* D, int nspin
         const long nlist = (long)G.basis_lists.size();
         DevBuf<double> part;
         part.alloc((size_t)nspin * nlist * 3);
+        G.mark(2);  // stage timers: ms[2] = the gradient kernel, ms[3] = 0
         launch_xc_grad((int)G.blocks.size(), G.d_blocks.p, G.d_lists.p, nlist, n, nspin, f->f.family, G.d_D.p,
                        G.d_ao.p, G.Gp, G.d_fcoef.p, part.p, G.stream);
+        G.mark(3);
+        G.mark(4);
         std::vector<double> h((size_t)nspin * nlist * 3);
         CGB_CUDA(cudaMemcpyAsync(h.data(), part.p, h.size() * sizeof(double), cudaMemcpyDeviceToHost, G.stream));
         CGB_CUDA(cudaStreamSynchronize(G.stream));

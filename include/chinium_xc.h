@@ -228,7 +228,9 @@ int xc_grid_kernel_ms(xc_grid* g, double* ms);
  * from the derivatives of the basis functions centred on each atom, FP64.
  * LDA and GGA functionals (the reference's gradient has no meta-GGA terms);
  * needs the AO derivatives one order above the functional's: getAO(1) after
- * setType.  D as for xc_build (column-major, spins concatenated). */
+ * setType.  D as for xc_build (column-major, spins concatenated).  With
+ * xc_grid_profile on, xc_grid_stage_ms then returns [density, functional,
+ * gradient kernel, 0]. */
 int xc_grid_energy_grad(xc_grid* g, xc_functional* f, const double* D, int nspin, double* grad);
 
 /* --------------------------------------------- response (coupled-perturbed)
