@@ -110,6 +110,7 @@ SIGNATURES = {
     "xc_mlp_backward": [_P, _I, _P, _P, _P],
     "xc_mlp_train_step": [_P, _I, _P, _P, _P, ctypes.c_float, _P],
     "xc_int1e": [_P, _P, _P, _P],
+    "xc_dipole": [_P, _P, _P],
     "xc_eri": [_P, _P, _D],
     "xc_grid_profile": [_P, _I],
     "xc_grid_stage_ms": [_P, _P],

@@ -225,6 +225,37 @@ void one_e_pair(const CShell& a, const CShell& b, const BasisSet& bs, double* S,
         }
 }
 
+// Dipole blocks <a| r_k - C_k |b> (k = x, y, z) of a shell pair, Cartesian:
+// per direction M1(i, j) = sqrt(pi / p) (E_1^{ij} + (P_k - C_k) E_0^{ij}).
+void dipole_pair(const CShell& a, const CShell& b, const double* C, double* M /* 3 x na x nb */) {
+    const int na = a.ncart, nb = b.ncart;
+    std::fill(M, M + 3 * na * nb, 0.0);
+    Herm1 h[3];
+    for (size_t pa = 0; pa < a.exps.size(); pa++)
+        for (size_t pb = 0; pb < b.exps.size(); pb++) {
+            const double ea = a.exps[pa], eb = b.exps[pb], p = ea + eb;
+            const double cab = a.coefs[pa] * b.coefs[pb];
+            for (int k = 0; k < 3; k++) hermite_e(a.l, b.l, ea, eb, a.A[k], b.A[k], h[k]);
+            const double sp = std::sqrt(M_PI / p);
+            double PC[3];
+            for (int k = 0; k < 3; k++) PC[k] = (ea * a.A[k] + eb * b.A[k]) / p - C[k];
+            for (int ka = 0; ka < na; ka++)
+                for (int kb = 0; kb < nb; kb++) {
+                    const int ix[3] = {a.ca[ka], a.cb[ka], a.cc[ka]}, jx[3] = {b.ca[kb], b.cb[kb], b.cc[kb]};
+                    double s0[3], m1[3];
+                    for (int k = 0; k < 3; k++) {
+                        const double e0 = h[k].E[ix[k]][jx[k]][0];
+                        const double e1 = ix[k] + jx[k] >= 1 ? h[k].E[ix[k]][jx[k]][1] : 0.0;
+                        s0[k] = e0 * sp;
+                        m1[k] = (e1 + PC[k] * e0) * sp;
+                    }
+                    M[(0 * na + ka) * nb + kb] += cab * m1[0] * s0[1] * s0[2];
+                    M[(1 * na + ka) * nb + kb] += cab * s0[0] * m1[1] * s0[2];
+                    M[(2 * na + ka) * nb + kb] += cab * s0[0] * s0[1] * m1[2];
+                }
+        }
+}
+
 // Primitive-pair Hermite data for the ERI.
 struct PairData {
     double p, P[3], K;  // K = c_a c_b (E00 factors folded in E)
@@ -393,6 +424,35 @@ extern "C" int xc_int1e(const xc_basis* bh, double* S, double* T, double* V) {
                     T[mu * n + nu] = T[nu * n + mu] = pt[k];
                     V[mu * n + nu] = V[nu * n + mu] = pv[k];
                 }
+        }
+    });
+}
+
+extern "C" int xc_dipole(const xc_basis* bh, const double* origin, double* M) {
+    return guard([&] {
+        CGB_CHECK(bh && origin && M, XC_ERR_ARG, "null argument");
+        const BasisSet& b = bh->b;
+        for (const Shell& s : b.shells) CGB_CHECK(s.l <= kMaxLInt, XC_ERR_UNSUPPORTED, "integrals support l <= 4");
+        auto sh = make_shells(b);
+        const int n = b.nbasis, ns = (int)sh.size();
+        const size_t nn = (size_t)n * n;
+#pragma omp parallel for schedule(dynamic)
+        for (int ij = 0; ij < ns * ns; ij++) {
+            const int i = ij / ns, j = ij % ns;
+            if (j > i) continue;
+            const CShell &a = sh[i], &c = sh[j];
+            const size_t blk = (size_t)a.ncart * c.ncart;
+            std::vector<double> cm(3 * blk), pm((size_t)a.nfunc * c.nfunc);
+            dipole_pair(a, c, origin, cm.data());
+            for (int k = 0; k < 3; k++) {
+                to_pure2(a, c, cm.data() + k * blk, pm.data());
+                for (int fa = 0; fa < a.nfunc; fa++)
+                    for (int fc = 0; fc < c.nfunc; fc++) {
+                        const size_t mu = a.first + fa, nu = c.first + fc;
+                        const double v = pm[fa * c.nfunc + fc];
+                        M[k * nn + mu * n + nu] = M[k * nn + nu * n + mu] = v;
+                    }
+            }
         }
     });
 }

@@ -21,6 +21,14 @@ extern "C" {
  * the layout is the same in row and column order). */
 int xc_int1e(const xc_basis* b, double* S, double* T, double* V);
 
+/* Dipole integrals <mu| r_k - C_k |nu> for k = x, y, z about the origin C
+ * (3 doubles, bohr): M holds three symmetric n x n matrices, x first (the
+ * position operator itself; the electronic dipole is minus its trace with
+ * D).  The reference's counterpart is the dipole part of its libint2
+ * multipole call (Int2C1E.cpp:313-324, DipoleX/Y/Z); here they serve the
+ * coupled-perturbed electric-field response. */
+int xc_dipole(const xc_basis* b, const double* origin, double* M);
+
 /* All electron-repulsion integrals (mu nu | lambda sigma) as an n^4 array,
  * element ((mu*n + nu)*n + lambda)*n + sigma.  Shell quartets whose Schwarz
  * bound is below schwarz_threshold are left zero. */

@@ -156,3 +156,33 @@ def test_mixed_config_struct_layout():
     assert MixedConfig.v_operands.offset == 24
     assert ctypes.sizeof(TuneCandidate) == 32 + 3 * 8 + 8 + 8
     assert TuneReport.cand.offset == 32 + 8 + 8 + 8
+
+
+def test_dipole_integrals_shift_symmetry_and_quadrature():
+    """xc_dipole: <mu| r - C |nu> = <mu| r |nu> - C S exactly, symmetric, and
+    equal to the SG-3 quadrature of (r - C) phi phi within that quadrature's
+    own error on S."""
+    from chinium_gb300 import molecules as M
+    from chinium_gb300.cpscf import dipole_integrals
+    from chinium_gb300.scf import one_electron
+    from oracle import oracle as O
+    Z, xyz = M.h2o()
+    b = cg.Basis(Z, xyz, "def2-svp")
+    S = one_electron(b)[0]
+    C = np.array([0.1, -0.2, 0.3])
+    M0, MC = dipole_integrals(b), dipole_integrals(b, C)
+    assert np.abs(MC - (M0 - C[:, None, None] * S)).max() < 1e-14
+    assert np.array_equal(M0, M0.transpose(0, 2, 1))
+    ob = O.Basis(Z, xyz, "def2-svp")
+    px, py, pz, w = O.grid_points(Z, xyz, "SG-3")
+    n = b.nbasis
+    qS, qM = np.zeros((n, n)), np.zeros((3, n, n))
+    for i0 in range(0, len(px), 20000):
+        sl = slice(i0, i0 + 20000)
+        ao = ob.ao(px[sl], py[sl], pz[sl], 0)[0]
+        qS += (ao * w[sl]) @ ao.T
+        for k, q in enumerate((px[sl], py[sl], pz[sl])):
+            qM[k] += (ao * (w[sl] * q)) @ ao.T
+    errS = np.abs(S - qS).max()
+    assert errS < 5e-5
+    assert np.abs(M0 - qM).max() < 5 * errS
