@@ -820,11 +820,11 @@ int xc_functional_fxc_points(xc_functional* f, long n, const double* rho, const 
                              double* v2rhosigma, double* v2sigma2) {
     return guard([&] {
         CGB_CHECK(f && rho && v2rho2 && n > 0, XC_ERR_ARG, "bad arguments");
-        ensure_device();
         const Functional& F = f->f;
         CGB_CHECK(F.family <= 1, XC_ERR_UNSUPPORTED,
                   "second derivatives cover LDA and GGA functionals (as the reference's Evaluate(\"f\"))");
         CGB_CHECK(F.family < 1 || (sigma && v2rhosigma && v2sigma2), XC_ERR_ARG, "sigma arrays required for GGA");
+        ensure_device();
         const int ns = F.nspin, nsig = ns == 1 ? 1 : 3, nrr = ns == 1 ? 1 : 3, nrs = ns == 1 ? 1 : 6;
         DevBuf<double> dr, ds, d1, d2, d3;
         dr.upload(rho, ns * n);

@@ -186,3 +186,27 @@ def test_dipole_integrals_shift_symmetry_and_quadrature():
     errS = np.abs(S - qS).max()
     assert errS < 5e-5
     assert np.abs(M0 - qM).max() < 5 * errS
+
+
+def test_response_entry_points_validate_arguments_on_the_host():
+    """The response entry points reject null handles and buffers, and meta-GGA
+    second derivatives, before touching a device."""
+    import ctypes
+    from chinium_gb300._lib import lib
+    L = lib()
+    nul = ctypes.c_void_p()
+    one = np.zeros(4)
+    p = one.ctypes.data_as(ctypes.c_void_p)
+    assert L.xc_grid_get_density_u(nul, p, 1, 1) == -1
+    assert L.xc_grid_get_fock_u(nul, p) == -1
+    assert L.xc_grid_set_response_precision(nul, 0) == -1
+    assert L.xc_build_response(nul, nul, p, 1, 0, 1, p, p) == -1
+    assert L.xc_functional_fxc_points(nul, 1, p, p, p, p, p) == -1
+    assert L.xc_dipole(nul, p, p) == -1
+    f = ctypes.c_void_p()
+    ids = (ctypes.c_int * 2)(202, 231)
+    assert L.xc_functional_create(ids, 2, 1, ctypes.byref(f)) == 0
+    try:
+        assert L.xc_functional_fxc_points(f, 1, p, p, p, p, p) == -6  # TPSS: no "f" (as the reference)
+    finally:
+        L.xc_functional_destroy(f)
