@@ -8,18 +8,10 @@
 //   dE/dR_{A,t} += -2 sum_{nu on A} sum_g [d_t phi(g, nu) U(g, nu) + sum_r d_t d_r phi(g, nu) f_r(g) T(g, nu)]
 // which is dE = sum_g w (v_rho d rho + v_sigma d sigma) with d rho and d grad rho
 // the derivatives of the functions centred on A.  T and U are tiled like the
-// FP64 density kernel (128 points x 32 functions x 16 inner); the
+// FP64 density kernel (128 points x 32 functions x 16 inner); each warp owns
+// four functions of the tile and reduces its point sums with shuffles; the
 // per-(block, function) partials are summed by atom on the host in a fixed
 // order.
-//
-// The two products run on the FP64 tensor path: mma.sync m8n8k4 (A 8 x 4
-// row-major, B 4 x 8 column-major, one element of each per lane; C 8 x 8, two
-// per lane: row lane / 4, columns 2 (lane % 4) + {0, 1}).  Warp w owns the
-// 8-function column tile w % 4 of the 32-function tile and the 64 points of
-// half w / 4: eight 8-point row tiles, for T and U.  The contraction with the
-// AO gradients and Hessians then sums its points in registers, across the
-// lanes of a column group by shuffles, and across the two point halves in
-// shared memory.
 #include "common.h"
 #include "kernels.h"
 
@@ -27,16 +19,8 @@ namespace cgb {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kNV = 32;                // nu tile
-constexpr int kKC = 16;                // inner (mu) chunk
-constexpr int kPS = kMaxBlockPts + 4;  // padded point stride of the staged chunk (bank spread)
-
-// d += a b, FP64 8 x 8 x 4 (fragments as above)
-__device__ __forceinline__ void dmma(double (&d)[2], double a, double b) {
-    asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0, %1}, {%2}, {%3}, {%0, %1};\n"
-                 : "+d"(d[0]), "+d"(d[1])
-                 : "d"(a), "d"(b));
-}
+constexpr int kNV = 32;  // nu tile
+constexpr int kKC = 16;  // inner (mu) chunk
 
 template <int FAM>
 __global__ void __launch_bounds__(kThreads) grad_fp64_kernel(const BlockDesc* __restrict__ blocks,
@@ -45,10 +29,9 @@ __global__ void __launch_bounds__(kThreads) grad_fp64_kernel(const BlockDesc* __
                                                              const double* __restrict__ ao, long Gp,
                                                              const double* __restrict__ fcoef, long nlist,
                                                              double* __restrict__ part) {
-    __shared__ double Ps[2][kKC][kPS];      // phi and the Z-like combination of the mu chunk
-    __shared__ double Ds[kKC][kNV + 1];
-    __shared__ double fs[4][kMaxBlockPts];  // 2 fcoef0, f_x, f_y, f_z of the block's points
-    __shared__ double red[2][kNV][3];       // per point half: the column tile's sums
+    __shared__ double Ps[2][kKC][kMaxBlockPts];  // phi and the Z-like combination of the mu chunk
+    __shared__ double Ds[kKC][kNV];
+    __shared__ double fs[4][kMaxBlockPts];       // 2 fcoef0, f_x, f_y, f_z of the block's points
 
     const BlockDesc bd = blocks[blockIdx.x];
     const int spin = blockIdx.y;
@@ -59,9 +42,7 @@ __global__ void __launch_bounds__(kThreads) grad_fp64_kernel(const BlockDesc* __
     const double* Dsp = D + (long)spin * n * n;
     const double* fc = fcoef + (long)spin * 5 * Gp + bd.pt_off;
     const int tid = threadIdx.x;
-    const int warp = tid >> 5, lane = tid & 31;
-    const int nt = warp & 3, ph = warp >> 2;  // column tile, point half
-    const int gr = lane >> 2, kq = lane & 3;  // fragment row / column group, k index / column pair
+    const int tg = tid & 31, tv = tid >> 5;
     for (int g = tid; g < kMaxBlockPts; g += kThreads) {
         const bool in = g < ng;
         fs[0][g] = in ? 2.0 * fc[g] : 0.0;
@@ -72,9 +53,11 @@ __global__ void __launch_bounds__(kThreads) grad_fp64_kernel(const BlockDesc* __
     __syncthreads();
 
     for (int nu0 = 0; nu0 < nb; nu0 += kNV) {
-        double accT[8][2], accU[8][2];
+        double accT[4][4], accU[4][4];
 #pragma unroll
-        for (int i = 0; i < 8; i++) accT[i][0] = accT[i][1] = accU[i][0] = accU[i][1] = 0.0;
+        for (int i = 0; i < 4; i++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) accT[i][j] = accU[i][j] = 0;
         for (int mu0 = 0; mu0 < nb; mu0 += kKC) {
             for (int idx = tid; idx < kKC * kMaxBlockPts; idx += kThreads) {
                 const int k = idx / kMaxBlockPts, g = idx % kMaxBlockPts;
@@ -95,70 +78,61 @@ __global__ void __launch_bounds__(kThreads) grad_fp64_kernel(const BlockDesc* __
                 Ds[k][j] = (mu < nb && nu < nb) ? Dsp[(long)list[nu] * n + list[mu]] : 0.0;
             }
             __syncthreads();
+#pragma unroll 4
+            for (int k = 0; k < kKC; k++) {
+                double dv[4];
 #pragma unroll
-            for (int ks = 0; ks < kKC / 4; ks++) {
-                const int k = 4 * ks + kq;
-                const double b = Ds[k][8 * nt + gr];  // B(mu = k, nu = 8 nt + gr)
+                for (int j = 0; j < 4; j++) dv[j] = Ds[k][tv * 4 + j];
 #pragma unroll
-                for (int mt = 0; mt < 8; mt++) {
-                    const int g = 64 * ph + 8 * mt + gr;  // A(point g, mu = k)
-                    dmma(accT[mt], Ps[0][k][g], b);
-                    dmma(accU[mt], Ps[1][k][g], b);
+                for (int i = 0; i < 4; i++) {
+                    const double pv = Ps[0][k][tg + 32 * i], zv = Ps[1][k][tg + 32 * i];
+#pragma unroll
+                    for (int j = 0; j < 4; j++) {
+                        accT[i][j] = fma(pv, dv[j], accT[i][j]);
+                        accU[i][j] = fma(zv, dv[j], accU[i][j]);
+                    }
                 }
             }
             __syncthreads();
         }
-        // contraction: this lane holds points 64 ph + 8 mt + gr and functions nu0 + 8 nt + 2 kq + i
-        double sx[2] = {0, 0}, sy[2] = {0, 0}, sz[2] = {0, 0};
+        // per function of the tile: sum over this thread's points, then over the warp
 #pragma unroll
-        for (int i = 0; i < 2; i++) {
-            const int nu = nu0 + 8 * nt + 2 * kq + i;
-            if (nu >= nb) continue;
+        for (int j = 0; j < 4; j++) {
+            const int nu = nu0 + tv * 4 + j;
+            double gx = 0, gy = 0, gz = 0;
+            if (nu < nb) {
 #pragma unroll
-            for (int mt = 0; mt < 8; mt++) {
-                const int g = 64 * ph + 8 * mt + gr;
-                if (g >= ng) continue;
-                const long o = (long)nu * ng + g;
-                const double U = accU[mt][i], T = accT[mt][i];
-                double gx = A0[cs + o] * U, gy = A0[2 * cs + o] * U, gz = A0[3 * cs + o] * U;
-                if (FAM >= 1) {
-                    const double fx = fs[1][g] * T, fy = fs[2][g] * T, fz = fs[3][g] * T;
-                    const double hxx = A0[4 * cs + o], hxy = A0[5 * cs + o], hxz = A0[6 * cs + o];
-                    const double hyy = A0[7 * cs + o], hyz = A0[8 * cs + o], hzz = A0[9 * cs + o];
-                    gx += hxx * fx + hxy * fy + hxz * fz;
-                    gy += hxy * fx + hyy * fy + hyz * fz;
-                    gz += hxz * fx + hyz * fy + hzz * fz;
+                for (int i = 0; i < 4; i++) {
+                    const int g = tg + 32 * i;
+                    if (g >= ng) continue;
+                    const long o = (long)nu * ng + g;
+                    const double U = accU[i][j], T = accT[i][j];
+                    gx = fma(A0[cs + o], U, gx);
+                    gy = fma(A0[2 * cs + o], U, gy);
+                    gz = fma(A0[3 * cs + o], U, gz);
+                    if (FAM >= 1) {
+                        const double fx = fs[1][g] * T, fy = fs[2][g] * T, fz = fs[3][g] * T;
+                        const double hxx = A0[4 * cs + o], hxy = A0[5 * cs + o], hxz = A0[6 * cs + o];
+                        const double hyy = A0[7 * cs + o], hyz = A0[8 * cs + o], hzz = A0[9 * cs + o];
+                        gx += hxx * fx + hxy * fy + hxz * fz;
+                        gy += hxy * fx + hyy * fy + hyz * fz;
+                        gz += hxz * fx + hyz * fy + hzz * fz;
+                    }
                 }
-                sx[i] += gx;
-                sy[i] += gy;
-                sz[i] += gz;
+            }
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                gx += __shfl_xor_sync(0xffffffffu, gx, off);
+                gy += __shfl_xor_sync(0xffffffffu, gy, off);
+                gz += __shfl_xor_sync(0xffffffffu, gz, off);
+            }
+            if (tg == 0 && nu < nb) {  // part[spin][list entry][t]
+                double* o = part + ((long)spin * nlist + bd.bas_off + nu) * 3;
+                o[0] = -2.0 * gx;
+                o[1] = -2.0 * gy;
+                o[2] = -2.0 * gz;
             }
         }
-        // sum over the eight row groups (the lanes with equal kq)
-#pragma unroll
-        for (int i = 0; i < 2; i++)
-#pragma unroll
-            for (int off = 4; off < 32; off <<= 1) {
-                sx[i] += __shfl_xor_sync(0xffffffffu, sx[i], off);
-                sy[i] += __shfl_xor_sync(0xffffffffu, sy[i], off);
-                sz[i] += __shfl_xor_sync(0xffffffffu, sz[i], off);
-            }
-        if (gr == 0) {
-#pragma unroll
-            for (int i = 0; i < 2; i++) {
-                const int j = 8 * nt + 2 * kq + i;
-                red[ph][j][0] = sx[i];
-                red[ph][j][1] = sy[i];
-                red[ph][j][2] = sz[i];
-            }
-        }
-        __syncthreads();
-        if (tid < kNV * 3) {  // part[spin][list entry][t] for the tile's functions
-            const int j = tid / 3, t = tid % 3;
-            const int nu = nu0 + j;
-            if (nu < nb) part[((long)spin * nlist + bd.bas_off + nu) * 3 + t] = -2.0 * (red[0][j][t] + red[1][j][t]);
-        }
-        __syncthreads();
     }
 }
 
