@@ -558,6 +558,26 @@ def run_response(args):
         step(prec, F)
     t = (time.perf_counter() - t0) / args.steps
     clocks = clocks_stop(cp, cf, clk)
+    roof = None
+    if prec == PMX:
+        # CUDA events around the first matrix's kernels of one more iteration: its density16
+        # launch is the dominant kernel; the tiles, and so the algorithmic bytes, are the build's
+        g.profile(True)
+        step(prec, F)
+        ms = g.stage_ms()
+        g.profile(False)
+        info = g.info()
+        kms = [ms[0], 0.0, 0.0, ms[1], ms[2], ms[3]]
+        roof = mixed_roofline(info, kms, [ms[0], 0.0, 0.0, ms[1] + ms[2] + ms[3]], measured_peaks(), xc.type, 1)
+        roof["kernel_ms"] = {"split_d + density16 + combine": ms[0], "response_coef + prep16": ms[1],
+                             "fock16": ms[2], "wsum": ms[3]}
+        roof.pop("stage_ms", None)
+        tf = os.path.join(REPO, "profiles", "traffic_c18_b3lyp_sg2.json")
+        if os.path.exists(tf) and roof["kernel"] == "density16":
+            tr = json.load(open(tf)).get("dram_bytes_per_launch", {}).get("density16")
+            roof["traffic"] = tr
+            roof["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of density16 on the same "
+                                      "tiles (C18 build), profiles/traffic_c18_b3lyp_sg2.json")
     cfg = {"workload": "C18 RKS B3LYP/def2-TZVP SG-2, 54 symmetric perturbations, one CPSCF iteration",
            "precision": args.precision, "nbasis": n, "nmat": nmat, "grid": "shells screened at 1e-11",
            "ground_state": "fp64 (density, functional, second derivatives), prepared once before the steps",
@@ -584,7 +604,7 @@ def run_response(args):
             "e2e": {"value": nmat / t, "unit": "matrices/s", "h2d_bytes_per_step": int(Du.nbytes),
                     "d2h_bytes_per_step": int(F.nbytes)},
             "gpu_launches": nmat * 7 if prec == PMX else 4,  # per matrix: split_d, density16, combine, response_coef, prep16, fock16, wsum
-            "clocks": clocks}
+            "roofline": roof, "clocks": clocks}
     print(json.dumps(line), flush=True)
 
 

@@ -793,17 +793,25 @@ void Grid::response_mixed(const double* dDU, int nmat, double* dFU) {
     const int n = basis.nbasis;
     const size_t nn = (size_t)n * n;
     for (int k = 0; k < nmat; k++) {
+        // stage timers (xc_grid_profile) on the first matrix: [split_d + density + combine,
+        // coefficients + R planes, V partials, V sum] of spin 0
+        const bool first = k == 0;
         for (int s = 0; s < nspin; s++)
             CGB_CUDA(cudaMemcpyAsync(d_rt_D.p + s * nn, dDU + ((size_t)s * nmat + k) * nn, nn * sizeof(double),
                                      cudaMemcpyDeviceToDevice, stream));
+        if (first) mark(0);
         launch_split_d(d_rt_D.p, m.d_mols.p, 1, nspin, md.drows, m.dcols, n, m.d_Dp.p, stream);
         density_passes(m.d_Dp.p);
+        if (first) mark(1);
         launch_response_coef(fxc_family, nspin, Gt, 1, m.d_w.p, d_rt_rho1.p, d_rt_vsig.p, d_rt_f2.p, m.rho.p,
                              m.rho1.p, d_rt_fcU.p, stream);
         for (int s = 0; s < nspin; s++) {
             v_prep(d_rt_fcU.p + (size_t)s * 5 * Gt, fxc_family);
+            if (first && s == 0) mark(2);
             v_partials(1);
+            if (first && s == 0) mark(3);
             launch_wsum(m.d_wpart.p, m.d_item_live.p, m.d_mols.p, 1, n, s, nspin, d_rt_V.p, stream);
+            if (first && s == 0) mark(4);
         }
         for (int s = 0; s < nspin; s++)
             CGB_CUDA(cudaMemcpyAsync(dFU + ((size_t)s * nmat + k) * nn, d_rt_V.p + s * nn, nn * sizeof(double),

@@ -268,7 +268,10 @@ int xc_grid_get_fock_u(xc_grid* g, double* FU);
  * FP64 ground state of Evaluate("ev") / Evaluate("f"), gathered once into the
  * tensor-core tiles, and forms each matrix's response density (symmetric part
  * of D_U) and V_U on the tensor cores inside xc_grid_get_fock_u: the
- * per-iteration work of a CPSCF loop (CoupledPerturbed.cpp:131-134). */
+ * per-iteration work of a CPSCF loop (CoupledPerturbed.cpp:131-134).  With
+ * xc_grid_profile on, xc_grid_stage_ms after such a getFockU returns the first
+ * matrix's [response density, coefficients + V operand planes, V partials,
+ * V sum] of spin 0. */
 int xc_grid_set_response_precision(xc_grid* g, int precision);
 
 /* getDensity(D) + Evaluate("ev") + Evaluate("f") + getDensityU(D_U) +
