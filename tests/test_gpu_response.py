@@ -278,3 +278,26 @@ def test_response_mixed_split_calls_equal_fused(h2o):
     g.getDensityU(Us)
     f64 = np.array(g.getFockU())
     assert np.abs(f64 - split).max() < MIXED_RTOL * np.abs(f64).max()
+
+
+@pytest.mark.parametrize("name", ["PBE", "B3LYP"])
+def test_unrestricted_response_at_equal_spins_is_restricted(h2o, name):
+    """CUDA FP64: D_a = D_b = D / 2, D_U,a = D_U,b = D_U / 2 give each spin the
+    restricted V_U of (D, D_U) (sigma_ab on its clamp: the jets keep the
+    unclamped branch, as the first derivatives do)."""
+    Z, xyz, b, ob, og = h2o
+    n = b.nbasis
+    D = model_density(og, 5)
+    rng = np.random.default_rng(17)
+    A = rng.normal(size=(n, n)) * 0.05
+    U = A + A.T
+    gr = cg.Grid(b, "SG-1")
+    gr.setType(1)
+    gr.getAO(0)
+    r = np.array(gr.build_response(cg.ExchangeCorrelation().Read(name), [D], [U]))[0, 0]
+    gu = cg.Grid(b, "SG-1", nspin=2)
+    gu.setType(1)
+    gu.getAO(0)
+    u = np.array(gu.build_response(cg.ExchangeCorrelation(spin=2).Read(name), [D / 2, D / 2], [[U / 2], [U / 2]]))
+    for s in range(2):
+        assert np.abs(u[s, 0] - r).max() < 1e-12 * max(1.0, np.abs(r).max())

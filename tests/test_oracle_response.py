@@ -97,3 +97,24 @@ def test_oracle_response_nonsymmetric_orientation(h2o_oracle):
     FU = og.response(D, U, ids, 1)
     assert np.abs(FU[0, 0] - FU[0, 1]).max() > 1e-6
     assert np.allclose(0.5 * (FU[0, 0] + FU[0, 1]), FU[0, 2], rtol=0, atol=1e-13)
+
+
+@pytest.mark.parametrize("name", ["SVWN5", "PBE", "BLYP"])
+def test_oracle_unrestricted_response_at_equal_spins_is_restricted(h2o_oracle, name):
+    """With D_a = D_b = D / 2 and D_U,a = D_U,b = D_U / 2 each spin's V_U is the
+    restricted V_U of (D, D_U): the unrestricted expression (libxc layouts, the
+    S = 2 factor on the output sigma pair) is the derivative of V_xc at a
+    closed shell too.  sigma_ab sits on its clamp there, so the oracle's
+    one-sided steps carry the check (~1e-9)."""
+    Z, xyz, basis, og = h2o_oracle
+    n = basis.nbasis
+    ids = O.FUNCTIONAL_FILES[name]
+    D = model_density(og, 5)
+    rng = np.random.default_rng(13)
+    A = rng.normal(size=(n, n)) * 0.05
+    U = A + A.T
+    r = og.response(D[None], U[None, None], ids, 1)[0, 0]
+    u = og.response(np.stack([D / 2, D / 2]), np.stack([U / 2, U / 2])[:, None], ids, 2)
+    scale = np.abs(r).max()
+    for s in range(2):
+        assert np.abs(u[s, 0] - r).max() < 1e-8 * scale, (name, s, np.abs(u[s, 0] - r).max())
