@@ -504,6 +504,28 @@ def run_gradient(args):
     print(json.dumps(line), flush=True)
 
 
+def response_cpu_baseline(wl, D, U, sample_blocks=24):
+    """The oracle's response (the reference's getDensityU + getFockU<u_t>
+    restated, one thread, with its FP64 ground state and second derivatives
+    per block) on the first sample_blocks blocks of the same grid for one
+    perturbation, scaled to one matrix over the whole grid."""
+    from oracle import oracle as O
+    basis = O.Basis(wl["Z"], wl["xyz"], wl["basis"])
+    px, py, pz, w = O.grid_points(wl["Z"], wl["xyz"], wl["grid"])
+    allb = O.padded_blocks(px, py, pz, w)
+    g = O.OracleGrid.__new__(O.OracleGrid)
+    g.basis = basis
+    g.blocks = allb[:sample_blocks]
+    g.ao = [basis.ao(b[0], b[1], b[2], 1) for b in g.blocks]
+    t = time.perf_counter()
+    g.response(D[None], U[None, None], wl["ids"], 1)
+    dt = time.perf_counter() - t
+    per_matrix = dt * len(allb) / len(g.blocks)
+    return {"value": 1.0 / per_matrix, "unit": "matrices/s", "cores": 1, "kind": "port",
+            "sample": "%d of %d blocks, one perturbation, %.2f s (one matrix over the grid: %.0f s)" % (
+                len(g.blocks), len(allb), dt, per_matrix)}
+
+
 def run_response(args):
     """C18 RKS B3LYP/def2-TZVP SG-2 (shells screened at 1e-11), the response
     work of one CPSCF iteration for the 3 N_atoms = 54 symmetric perturbations
@@ -605,6 +627,8 @@ def run_response(args):
                     "d2h_bytes_per_step": int(F.nbytes)},
             "gpu_launches": nmat * 7 if prec == PMX else 4,  # per matrix: split_d, density16, combine, response_coef, prep16, fock16, wsum
             "roofline": roof, "clocks": clocks}
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = response_cpu_baseline(wl, D, Du[0, 0])
     print(json.dumps(line), flush=True)
 
 
