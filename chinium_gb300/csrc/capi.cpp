@@ -14,6 +14,7 @@
 #include "common.h"
 #include "kernels.h"
 #include "model.h"
+#include "nvtx.h"
 #include "xc_state.h"
 
 namespace cgb {
@@ -97,6 +98,7 @@ static void halve(long lo, long n, std::vector<std::pair<long, long>>& out) {
 }
 
 void Grid::build(const BasisSet& bs, const std::string& grid_name, int ns, double thr) {
+    NvtxRange nvtx_("xc.grid");
     basis = bs;
     nspin = ns;
     screen_thr = thr;
@@ -303,6 +305,7 @@ DevShells Grid::dev_shells() const {
 }
 
 void Grid::get_ao(int derivative) {
+    NvtxRange nvtx_("xc.getAO");
     CGB_CHECK(derivative >= 0, XC_ERR_ARG, "negative derivative order");
     if (batched) return;  // the mixed path evaluates its own FP32 AO store at the first build
     const int order = type + derivative;
@@ -351,6 +354,7 @@ Grid::~Grid() {
 }
 
 void Grid::density_device(const double* dD) {
+    NvtxRange nvtx_("xc.getDensity");
     CGB_CHECK(!batched, XC_ERR_UNSUPPORTED, "batch grids run mixed-precision builds only");
     CGB_CHECK(ao_order >= type, XC_ERR_STATE, "getAO must run (for the current type) before getDensity");
     ensure_work();
@@ -364,6 +368,7 @@ void Grid::density_device(const double* dD) {
 }
 
 void Grid::evaluate_fxc(const Functional& f) {
+    NvtxRange nvtx_("xc.Evaluate.f");
     CGB_CHECK(have_density, XC_ERR_STATE, "Evaluate needs a density (getDensity first)");
     CGB_CHECK(f.nspin == nspin, XC_ERR_ARG, "functional and grid disagree on the number of spins");
     CGB_CHECK(f.family <= 1, XC_ERR_UNSUPPORTED,
@@ -377,6 +382,7 @@ void Grid::evaluate_fxc(const Functional& f) {
 }
 
 void Grid::density_u_device(const double* dDU, int nmat) {
+    NvtxRange nvtx_("xc.getDensityU");
     CGB_CHECK(!batched, XC_ERR_UNSUPPORTED, "response densities are per molecule");
     CGB_CHECK(ao_order >= type, XC_ERR_STATE, "getAO must run (for the current type) before getDensityU");
     CGB_CHECK(nmat >= 1, XC_ERR_ARG, "at least one response matrix");
@@ -405,6 +411,7 @@ void Grid::density_u_device(const double* dDU, int nmat) {
 }
 
 void Grid::fock_u_device(double* dFU) {
+    NvtxRange nvtx_("xc.getFockU");
     CGB_CHECK(have_fxc, XC_ERR_STATE, "getFockU needs Evaluate(\"f\") on the current density");
     CGB_CHECK(have_density_u, XC_ERR_STATE, "getFockU needs getDensityU first");
     CGB_CHECK(fxc_family == 0 || (have_potential && eval_family >= 1), XC_ERR_STATE,
@@ -428,6 +435,7 @@ void Grid::fock_u_device(double* dFU) {
 }
 
 void Grid::evaluate(const Functional& f, double float_above) {
+    NvtxRange nvtx_("xc.Evaluate");
     CGB_CHECK(have_density, XC_ERR_STATE, "Evaluate needs a density (getDensity first)");
     CGB_CHECK(f.nspin == nspin, XC_ERR_ARG, "functional and grid disagree on the number of spins");
     CGB_CHECK(f.family <= type, XC_ERR_STATE, "grid type is below the functional family (setType/getAO)");
@@ -445,6 +453,7 @@ void Grid::energy_device(double* dE) {
 }
 
 void Grid::fock_device(double* dV, int fam) {
+    NvtxRange nvtx_("xc.getFock");
     const size_t nn = (size_t)basis.nbasis * basis.nbasis * nspin;
     mark(3);
     CGB_CUDA(cudaMemsetAsync(dV, 0, nn * sizeof(double), stream));
@@ -1014,6 +1023,7 @@ int xc_grid_energy_grad(xc_grid* g, xc_functional* f, const double* D, int nspin
         const long nlist = (long)G.basis_lists.size();
         DevBuf<double> part;
         part.alloc((size_t)nspin * nlist * 3);
+        NvtxRange nvtx_("xc.getEnergyGrad");
         G.mark(2);  // stage timers: ms[2] = the gradient kernel, ms[3] = 0
         launch_xc_grad((int)G.blocks.size(), G.d_blocks.p, G.d_lists.p, nlist, n, nspin, f->f.family, G.d_D.p,
                        G.d_ao.p, G.Gp, G.d_fcoef.p, part.p, G.stream);

@@ -12,6 +12,7 @@
 #include <queue>
 
 #include "mixed.h"
+#include "nvtx.h"
 #include "xc_state.h"
 
 namespace cgb {
@@ -160,6 +161,7 @@ void Grid::collect_sources() {
 }
 
 void Grid::prepare_mixed(const MixedConfig& cfg) {
+    NvtxRange nvtx_("xc.mixed.prepare");
     MixedState& m = mx;
     m.drop_graph();
     m.ready = false;
@@ -553,6 +555,7 @@ void Grid::density_passes(const __nv_bfloat16*) {
 }
 
 void Grid::build_mixed(const double* dD, const Functional& f, double* dE, double* dV, double float_above) {
+    NvtxRange nvtx_("xc.mixed.build");
     mixed_ready();
     MixedState& m = mx;
     const MixedDev& md = m.md;
@@ -629,6 +632,7 @@ void Grid::build_mixed_graph(const Functional& f) {
 // or the first call; gathered into tile order) or a full tensor-core build
 // with the functional in FP64 everywhere (anchor 2; already in tile order).
 void Grid::build_incremental(const double* dD, const Functional& f, double* dE, double* dV, int anchor) {
+    NvtxRange nvtx_("xc.mixed.incremental");
     CGB_CHECK(!batched, XC_ERR_UNSUPPORTED, "incremental builds need the FP64 path (one molecule per grid)");
     CGB_CHECK(ao_order >= type, XC_ERR_STATE, "getAO must run (for the current type) before a build");
     ensure_work();
@@ -787,6 +791,7 @@ void Grid::response_tiles_prepare() {
 // split-BF16 density of its symmetric part (rho_U, grad rho_U in tile order),
 // the response coefficients (FP64) and V_U through the V kernels, FP64 sums.
 void Grid::response_mixed(const double* dDU, int nmat, double* dFU) {
+    NvtxRange nvtx_("xc.mixed.response");
     MixedState& m = mx;
     const MixedDev& md = m.md;
     const long Gt = md.Gt;
