@@ -175,6 +175,23 @@ class Basis:
                         _p(np.ascontiguousarray(z)), ctypes.c_int(deriv), _p(ao), _p(ao1))
         return ao.reshape(self.nbasis, ng), (ao1.reshape(3, self.nbasis, ng) if deriv else None)
 
+    def ao2(self, x, y, z):
+        """Second derivatives (6, n, g): xx, xy, yy, xz, yz, zz (SubGrid::AO2's packing)."""
+        ng = len(x)
+        out = np.zeros(6 * self.nbasis * ng)
+        lib().oracle_ao2(ctypes.c_int(len(self.types)), _p(self.types), _p(self.nprim), _p(self.off),
+                         _p(self.centers), _p(self.exps), _p(self.coefs), ctypes.c_int(self.nbasis),
+                         ctypes.c_int(ng), _p(np.ascontiguousarray(x)), _p(np.ascontiguousarray(y)),
+                         _p(np.ascontiguousarray(z)), _p(out))
+        return out.reshape(6, self.nbasis, ng)
+
+    def function_atoms(self):
+        """Atom of every basis function."""
+        out = []
+        for t, a in zip(self.types, self.shell_atom):
+            out.extend([a] * (1 if t == 0 else (3 if abs(t) == 1 else 2 * abs(t) + 1)))
+        return np.array(out, dtype=np.int32)
+
 
 # ----------------------------------------------------------------- grid --
 
@@ -412,6 +429,80 @@ class OracleGrid:
                             ctypes.c_int(nmat), ctypes.c_int(fam), _p(w), _p(ao), _p(ao1), _p(rho1), _p(vsigma),
                             _p(v2rho2), _p(v2rhosigma), _p(v2sigma2), _p(rhoU), _p(rho1U), _p(sigmaU), _p(F))
         return F.transpose(0, 1, 3, 2).copy()
+
+
+    def fock_skeleton(self, D, ids, nspin):
+        """The Hessian's skeleton V_xc derivatives for every atom A and direction t with the grid
+        fixed: getFockSkeleton (GridFock.cpp:52-95) and getFockU<s_t> on the skeleton density
+        derivatives of getDensitySkeleton (GridDensity.cpp:79-130, GridFock.cpp:97-160), block by
+        block.  D (nspin, n, n).  Returns (F_skeleton, F_U) as (nspin, 3 natoms, n, n), matrix
+        3 A + t; their sum is dV_xc / dR_(A,t) at fixed D."""
+        fam = family(ids)
+        nb = self.basis.nbasis
+        natoms = len(self.basis.Z)
+        D = np.asarray(D, dtype=np.float64).reshape(nspin, nb, nb)
+        Dc = np.ascontiguousarray(D.transpose(0, 2, 1))
+        nmat = 3 * natoms
+        Fs = np.zeros((nspin, natoms, 3, nb, nb))
+        Fu = np.zeros((nspin, nmat, nb, nb))
+        blist = np.arange(nb, dtype=np.int32)
+        atom_of = self.basis.function_atoms()
+        nsig = 1 if nspin == 1 else 3
+        L = lib()
+        for b, blk in enumerate(self.blocks):
+            ng = len(blk[0])
+            w = np.ascontiguousarray(blk[3], dtype=np.float64)
+            ao = np.ascontiguousarray(self.ao[b][0], dtype=np.float64)
+            ao1 = np.ascontiguousarray(self.ao[b][1], dtype=np.float64)
+            ao2 = np.ascontiguousarray(self.basis.ao2(blk[0], blk[1], blk[2])) if fam >= 1 else np.zeros(1)
+            rho, rho1 = np.zeros(nspin * ng), np.zeros(nspin * 3 * ng)
+            sigma, tau = np.zeros(nsig * ng), np.zeros(nspin * ng)
+            L.oracle_density(ctypes.c_int(ng), ctypes.c_int(nb), ctypes.c_int(nspin), ctypes.c_int(fam), _p(Dc),
+                             _p(ao), _p(ao1), _p(rho), _p(rho1), _p(sigma), _p(tau))
+            _, vrho, vsigma, _ = functional(ids, nspin, rho, sigma)
+            vrho, vsigma = np.ascontiguousarray(vrho), np.ascontiguousarray(vsigma)
+            v2rho2, v2rhosigma, v2sigma2 = functional_fxc(ids, nspin, rho, sigma)
+            rg, r1g, sg = np.zeros(nmat * nspin * ng), np.zeros(3 * nmat * nspin * ng), np.zeros(nmat * nsig * ng)
+            L.oracle_density_skeleton(ctypes.c_int(ng), ctypes.c_int(nb), ctypes.c_int(nspin), ctypes.c_int(natoms),
+                                      _p(atom_of), ctypes.c_int(fam), _p(Dc), _p(ao), _p(ao1), _p(ao2), _p(rho1),
+                                      _p(rg), _p(r1g), _p(sg))
+            L.oracle_fock_skeleton(ctypes.c_int(ng), ctypes.c_int(nb), ctypes.c_int(nb), _p(blist),
+                                   ctypes.c_int(nspin), ctypes.c_int(natoms), _p(atom_of), ctypes.c_int(fam), _p(w),
+                                   _p(ao), _p(ao1), _p(ao2), _p(rho1), _p(vrho), _p(vsigma), _p(Fs))
+            L.oracle_fock_u(ctypes.c_int(ng), ctypes.c_int(nb), ctypes.c_int(nb), _p(blist), ctypes.c_int(nspin),
+                            ctypes.c_int(nmat), ctypes.c_int(fam), _p(w), _p(ao), _p(ao1), _p(rho1), _p(vsigma),
+                            _p(v2rho2), _p(v2rhosigma), _p(v2sigma2), _p(rg), _p(r1g), _p(sg), _p(Fu))
+        Fs = Fs.reshape(nspin, nmat, nb, nb).transpose(0, 1, 3, 2).copy()
+        return Fs, Fu.transpose(0, 1, 3, 2).copy()
+
+
+def fock_fd(og, Z, xyz_bohr, basis_name, D, ids, nspin, h=1e-4):
+    """dV_xc / dR_(A,t) at fixed D with the grid held fixed, by central
+    differences of the oracle's V_xc with atom A's basis functions displaced
+    by +-h and +-h/2 (Richardson); (nspin, 3 natoms, n, n).  Test reference
+    for fock_skeleton."""
+    xyz = np.asarray(xyz_bohr, dtype=np.float64).reshape(-1, 3)
+    saved = og.ao, og.basis
+    n = og.basis.nbasis
+    out = np.zeros((nspin, 3 * len(Z), n, n))
+    try:
+        for a in range(len(Z)):
+            for t in range(3):
+                cds = []
+                for hh in (h, 0.5 * h):
+                    vs = []
+                    for sgn in (1.0, -1.0):
+                        moved = xyz.copy()
+                        moved[a, t] += sgn * hh
+                        bm = Basis(Z, moved, basis_name)
+                        og.basis = bm
+                        og.ao = [bm.ao(bx, by, bz, og.deriv) for bx, by, bz, bw in og.blocks]
+                        vs.append(np.array(og.build(D, ids, nspin)[1]))
+                    cds.append((vs[0] - vs[1]) / (2 * hh))
+                out[:, 3 * a + t] = (4 * cds[1] - cds[0]) / 3
+    finally:
+        og.ao, og.basis = saved
+    return out
 
 
 def skeleton_grad_fd(og, Z, xyz_bohr, basis_name, D, ids, nspin, h=1e-4):

@@ -102,6 +102,25 @@ void oracle_fock_u(int ng, int nbasis_block, int nbasis_total, const int* basis_
                    const double* v2rhosigma, const double* v2sigma2, const double* rhoU,
                    const double* rho1U, const double* sigmaU, double* F);
 
+/* AO second derivatives of one block: ao2[(c * nbasis + mu) * ng + g] with c = xx, xy, yy, xz,
+ * yz, zz (the packing of SubGrid::AO2, GridAO.cpp:254-259). */
+void oracle_ao2(int nshells, const int* shell_type, const int* shell_nprim, const int* shell_prim_off,
+                const double* shell_center, const double* exps, const double* coefs, int nbasis, int ng,
+                const double* x, const double* y, const double* z, double* ao2);
+
+/* Skeleton density derivatives of one block (GridDensity.cpp:79-130): RhoGrad (g,t,A,s),
+ * Rho1Grad (g,r,t,A,s), SigmaGrad (g,t,A,uv) for the block functions' atoms atom_of[mu]. */
+void oracle_density_skeleton(int ng, int nbasis, int nspin, int natoms, const int* atom_of, int type,
+                             const double* D, const double* ao, const double* ao1, const double* ao2,
+                             const double* rho1, double* rhog, double* rho1g, double* sigmag);
+
+/* Skeleton Fock derivatives of one block accumulated into F (ntot,ntot,3,natoms,s)
+ * (GridFock.cpp:52-95, getFockSkeleton). */
+void oracle_fock_skeleton(int ng, int nbasis_block, int nbasis_total, const int* basis_list, int nspin,
+                          int natoms, const int* atom_of, int type, const double* w, const double* ao,
+                          const double* ao1, const double* ao2, const double* rho1, const double* vrho,
+                          const double* vsigma, double* F);
+
 #ifdef __cplusplus
 }
 #endif

@@ -183,3 +183,225 @@ void oracle_fock_u(int ng, int nb, int ntot, const int* list, int ns, int nmat, 
     free(tmp);
     free(F);
 }
+
+/* ----------------------------------------------------- Hessian skeleton terms */
+
+#include <math.h>
+
+/* Angular polynomials (the same restatement as xc_oracle.c's AO/ *.hpp tables)
+ * evaluated through oracle_ao on single points: their first derivatives come
+ * from the complex step there; here the second derivatives are
+ * Richardson-extrapolated central differences of those first derivatives,
+ * exact to rounding for polynomials of degree <= 4. */
+void oracle_ao(int nshells, const int* shell_type, const int* shell_nprim, const int* shell_prim_off,
+               const double* shell_center, const double* exps, const double* coefs, int nbasis, int ng,
+               const double* x, const double* y, const double* z, int deriv, double* ao, double* ao1);
+
+/* AO second derivatives ao2[(c * nbasis + mu) * ng + g], c = xx, xy, yy, xz, yz, zz (the packing
+ * of SubGrid::AO2, GridAO.cpp:254-259; values as GridAO.cpp:185-196):
+ *   d_a d_b phi = A_ab Q + A_a Q_b + A_b Q_a + A Q_ab,
+ *   A = sum c e^(-alpha r^2), A_a = -2 x_a sum c alpha e, A_ab = 4 x_a x_b sum c alpha^2 e - 2 delta_ab sum c alpha e
+ * (GridAO.cpp:113-135).  Q_a, Q_ab from oracle_ao on a unit radial part: a one-primitive shell with
+ * exponent 0 and coefficient 1 gives phi = Q. */
+void oracle_ao2(int nshells, const int* shell_type, const int* shell_nprim, const int* shell_prim_off,
+                const double* shell_center, const double* exps, const double* coefs, int nbasis, int ng,
+                const double* xs, const double* ys, const double* zs, double* ao2) {
+    int ibasis = 0;
+    const double zero_exp = 0.0, one_coef = 1.0;
+    const int one_nprim = 1, zero_off = 0;
+    double q[16], q1[48], qp[48], qm[48], qp2[48], qm2[48];
+    for (int s = 0; s < nshells; s++) {
+        const int type = shell_type[s];
+        const double* e = exps + shell_prim_off[s];
+        const double* c = coefs + shell_prim_off[s];
+        const double* C = shell_center + 3 * s;
+        const int size = type == 0 ? 1 : (type == 1 || type == -1) ? 3 : 2 * (-type) + 1;
+        for (int k = 0; k < ng; k++) {
+            const double r[3] = {xs[k] - C[0], ys[k] - C[1], zs[k] - C[2]};
+            const double r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+            double t0 = 0, t1 = 0, t2 = 0;
+            for (int p = 0; p < shell_nprim[s]; p++) {
+                const double t = c[p] * exp(-e[p] * r2);
+                t0 += t;
+                t1 += t * e[p];
+                t2 += t * e[p] * e[p];
+            }
+            /* Q and grad Q at the point, shell centred at the origin */
+            const double org[3] = {0, 0, 0};
+            oracle_ao(1, &type, &one_nprim, &zero_off, org, &zero_exp, &one_coef, size, 1, &r[0], &r[1], &r[2], 1,
+                      q, q1);
+            double Qab[6][16];
+            for (int b = 0; b < 3; b++) {
+                const double h = 1e-2;
+                double rp[3] = {r[0], r[1], r[2]}, rm[3] = {r[0], r[1], r[2]};
+                double rp2[3] = {r[0], r[1], r[2]}, rm2[3] = {r[0], r[1], r[2]};
+                rp[b] += h;
+                rm[b] -= h;
+                rp2[b] += 0.5 * h;
+                rm2[b] -= 0.5 * h;
+                double tq[16];
+                oracle_ao(1, &type, &one_nprim, &zero_off, org, &zero_exp, &one_coef, size, 1, &rp[0], &rp[1], &rp[2],
+                          1, tq, qp);
+                oracle_ao(1, &type, &one_nprim, &zero_off, org, &zero_exp, &one_coef, size, 1, &rm[0], &rm[1], &rm[2],
+                          1, tq, qm);
+                oracle_ao(1, &type, &one_nprim, &zero_off, org, &zero_exp, &one_coef, size, 1, &rp2[0], &rp2[1],
+                          &rp2[2], 1, tq, qp2);
+                oracle_ao(1, &type, &one_nprim, &zero_off, org, &zero_exp, &one_coef, size, 1, &rm2[0], &rm2[1],
+                          &rm2[2], 1, tq, qm2);
+                for (int a = 0; a <= b; a++) {
+                    const int pk = a + b * (b + 1) / 2;
+                    for (int i = 0; i < size; i++) {
+                        const double d1 = (qp[a * size + i] - qm[a * size + i]) / (2 * h);
+                        const double d2 = (qp2[a * size + i] - qm2[a * size + i]) / h;
+                        Qab[pk][i] = (4 * d2 - d1) / 3;
+                    }
+                }
+            }
+            for (int b = 0; b < 3; b++)
+                for (int a = 0; a <= b; a++) {
+                    const int pk = a + b * (b + 1) / 2;
+                    const double Aa = -2 * r[a] * t1, Ab = -2 * r[b] * t1;
+                    const double Aab = 4 * r[a] * r[b] * t2 - (a == b ? 2 * t1 : 0.0);
+                    for (int i = 0; i < size; i++)
+                        ao2[((long)pk * nbasis + ibasis + i) * ng + k] =
+                            Aab * q[i] + Aa * q1[b * size + i] + Ab * q1[a * size + i] + t0 * Qab[pk][i];
+                }
+        }
+        ibasis += size;
+    }
+}
+
+static int pair_pack(int a, int b) {
+    const int lo = a < b ? a : b, hi = a < b ? b : a;
+    return lo + hi * (hi + 1) / 2;
+}
+
+/* SubGrid::getDensitySkeleton (GridDensity.cpp:79-130) for one block: D (n,n,s) column-major,
+ * atom_of[mu] the atom of block function mu.  Outputs (g fastest):
+ * RhoGrad (g,t,A,s), Rho1Grad (g,r,t,A,s), SigmaGrad (g,t,A,uv). */
+void oracle_density_skeleton(int ng, int nb, int ns, int natoms, const int* atom_of, int type, const double* D,
+                             const double* ao, const double* ao1, const double* ao2, const double* rho1,
+                             double* rhog, double* rho1g, double* sigmag) {
+    const long nn = (long)nb * nb;
+    memset(rhog, 0, sizeof(double) * ng * 3 * natoms * ns);
+    double* T = (double*)malloc(sizeof(double) * ng);
+    /* RhoGrada(g,t,w) = -2 sum_(mu in A) sum_nu Da(mu,nu,w) AO1a(g,mu,t) AO(g,nu) (:90-101) */
+    for (int w = 0; w < ns; w++)
+        for (int mu = 0; mu < nb; mu++) {
+            const int A = atom_of[mu];
+            memset(T, 0, sizeof(double) * ng);
+            for (int nu = 0; nu < nb; nu++) {
+                const double d = D[(long)w * nn + (long)nu * nb + mu];
+                for (int g = 0; g < ng; g++) T[g] += d * ao[(long)nu * ng + g];
+            }
+            for (int t = 0; t < 3; t++) {
+                double* o = rhog + (((long)w * natoms + A) * 3 + t) * ng;
+                const double* a1 = ao1 + ((long)t * nb + mu) * ng;
+                for (int g = 0; g < ng; g++) o[g] += -2.0 * a1[g] * T[g];
+            }
+        }
+    if (type >= 1) {
+        /* Rho1Grada(g,r,t,w) = -2 sum Da [AO2a(g,mu,r+t) AO(g,nu) + AO1a(g,mu,t) AO1(g,nu,r)] (:103-118) */
+        memset(rho1g, 0, sizeof(double) * ng * 9 * natoms * ns);
+        double* Tr = (double*)malloc(sizeof(double) * ng * 3);
+        for (int w = 0; w < ns; w++)
+            for (int mu = 0; mu < nb; mu++) {
+                const int A = atom_of[mu];
+                memset(T, 0, sizeof(double) * ng);
+                memset(Tr, 0, sizeof(double) * ng * 3);
+                for (int nu = 0; nu < nb; nu++) {
+                    const double d = D[(long)w * nn + (long)nu * nb + mu];
+                    for (int g = 0; g < ng; g++) T[g] += d * ao[(long)nu * ng + g];
+                    for (int r = 0; r < 3; r++)
+                        for (int g = 0; g < ng; g++) Tr[r * ng + g] += d * ao1[((long)r * nb + nu) * ng + g];
+                }
+                for (int t = 0; t < 3; t++)
+                    for (int r = 0; r < 3; r++) {
+                        double* o = rho1g + ((((long)w * natoms + A) * 3 + t) * 3 + r) * ng;
+                        const double* h2 = ao2 + ((long)pair_pack(r, t) * nb + mu) * ng;
+                        const double* a1 = ao1 + ((long)t * nb + mu) * ng;
+                        for (int g = 0; g < ng; g++) o[g] += -2.0 * (h2[g] * T[g] + a1[g] * Tr[r * ng + g]);
+                    }
+            }
+        free(Tr);
+        /* SigmaGradaFull(g,t,u,v) = Rho1(g,r,u) Rho1Grada(g,r,t,v), symmetrised over (u,v), kept for
+         * u <= v (:119-128) */
+        const int nsig = ns * (ns + 1) / 2;
+        memset(sigmag, 0, sizeof(double) * ng * 3 * natoms * nsig);
+        for (int A = 0; A < natoms; A++)
+            for (int t = 0; t < 3; t++)
+                for (int v = 0; v < ns; v++)
+                    for (int u = 0; u <= v; u++) {
+                        double* o = sigmag + (((long)pair_pack(u, v) * natoms + A) * 3 + t) * ng;
+                        for (int r = 0; r < 3; r++) {
+                            const double* ru = rho1 + ((long)u * 3 + r) * ng;
+                            const double* rv = rho1 + ((long)v * 3 + r) * ng;
+                            const double* gu = rho1g + ((((long)u * natoms + A) * 3 + t) * 3 + r) * ng;
+                            const double* gv = rho1g + ((((long)v * natoms + A) * 3 + t) * 3 + r) * ng;
+                            for (int g = 0; g < ng; g++) o[g] += ru[g] * gv[g] + rv[g] * gu[g];
+                        }
+                    }
+    }
+    free(T);
+}
+
+/* SubGrid::getFockSkeleton (GridFock.cpp:52-95) for one block, accumulated into
+ * F (ntot,ntot,3,natoms,s) through basis_list:
+ *   F0a(mu in A, nu, t, w) = sum_g W Eps1Rho_w AO1a(g,mu,t) AO(g,nu)
+ *   Fa1(mu in A, nu, t, u) = sum_g W S_(u+v) Eps1Sigma_(u+v) Rho1(g,r,v)
+ *                            [AO2a(g,mu,r+t) AO(g,nu) + AO1a(g,mu,t) AO1(g,nu,r)]
+ *   F(:,:,t,A,s) -= F0a + Fa1 (rows of A), then F += F^T over (mu, nu). */
+void oracle_fock_skeleton(int ng, int nb, int ntot, const int* list, int ns, int natoms, const int* atom_of,
+                          int type, const double* w, const double* ao, const double* ao1, const double* ao2,
+                          const double* rho1, const double* vrho, const double* vsigma, double* Fout) {
+    const long nn = (long)nb * nb;
+    double* F = (double*)calloc((size_t)nn * 3 * natoms * ns, sizeof(double));
+    double* L = (double*)malloc(sizeof(double) * ng);
+    double* c1 = (double*)malloc(sizeof(double) * ng * 3);
+    for (int s = 0; s < ns; s++) {
+        /* c1_r(g) = W sum_v S_(s+v) vsigma_(s+v) Rho1(g,r,v) */
+        memset(c1, 0, sizeof(double) * ng * 3);
+        if (type >= 1)
+            for (int v = 0; v < ns; v++) {
+                const int uv = pair_pack(s, v);
+                const double S = (s == v) ? 2.0 : 1.0;
+                for (int r = 0; r < 3; r++)
+                    for (int g = 0; g < ng; g++)
+                        c1[r * ng + g] += w[g] * S * vsigma[(long)uv * ng + g] * rho1[((long)v * 3 + r) * ng + g];
+            }
+        for (int mu = 0; mu < nb; mu++) {
+            const int A = atom_of[mu];
+            for (int t = 0; t < 3; t++) {
+                double* Fm = F + (((long)s * natoms + A) * 3 + t) * nn;
+                /* L(g) multiplies AO(g,nu): W vrho d_t phi_mu + sum_r c1_r d_r d_t phi_mu */
+                const double* a1 = ao1 + ((long)t * nb + mu) * ng;
+                for (int g = 0; g < ng; g++) L[g] = w[g] * vrho[(long)s * ng + g] * a1[g];
+                if (type >= 1)
+                    for (int r = 0; r < 3; r++) {
+                        const double* h2 = ao2 + ((long)pair_pack(r, t) * nb + mu) * ng;
+                        for (int g = 0; g < ng; g++) L[g] += c1[r * ng + g] * h2[g];
+                    }
+                for (int nu = 0; nu < nb; nu++) {
+                    double acc = 0;
+                    for (int g = 0; g < ng; g++) acc += L[g] * ao[(long)nu * ng + g];
+                    if (type >= 1)
+                        for (int r = 0; r < 3; r++) {
+                            const double* b1 = ao1 + ((long)r * nb + nu) * ng;
+                            for (int g = 0; g < ng; g++) acc += c1[r * ng + g] * a1[g] * b1[g];
+                        }
+                    Fm[(long)nu * nb + mu] -= acc;
+                }
+            }
+        }
+    }
+    for (long m = 0; m < (long)3 * natoms * ns; m++) {
+        const double* Fm = F + m * nn;
+        double* O = Fout + m * ntot * (long)ntot;
+        for (int nu = 0; nu < nb; nu++)
+            for (int mu = 0; mu < nb; mu++)
+                O[(long)list[nu] * ntot + list[mu]] += Fm[(long)nu * nb + mu] + Fm[(long)mu * nb + nu];
+    }
+    free(c1);
+    free(L);
+    free(F);
+}
