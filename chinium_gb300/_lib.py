@@ -94,6 +94,7 @@ SIGNATURES = {
     "xc_sap_fock": [_P, _P],
     "xc_sap_fock_tc": [_P, _P],
     "xc_grid_energy_grad": [_P, _P, _P, _I, _P],
+    "xc_grid_fock_skeleton": [_P, _P, _P, _I, _P, _P],
     "xc_functional_fxc_points": [_P, _L, _P, _P, _P, _P, _P],
     "xc_grid_get_density_u": [_P, _P, _I, _I],
     "xc_grid_get_fock_u": [_P, _P],

@@ -1047,6 +1047,65 @@ int xc_grid_energy_grad(xc_grid* g, xc_functional* f, const double* D, int nspin
     });
 }
 
+int xc_grid_fock_skeleton(xc_grid* g, xc_functional* f, const double* D, int nspin, double* FS, double* FU) {
+    return guard([&] {
+        CGB_CHECK(g && f && D && FS && FU, XC_ERR_ARG, "null argument");
+        Grid& G = g->g;
+        CGB_CHECK(!G.batched, XC_ERR_UNSUPPORTED, "skeleton terms are per molecule");
+        CGB_CHECK(nspin == G.nspin && f->f.nspin == G.nspin, XC_ERR_ARG, "Wrong number of spin types!");
+        CGB_CHECK(f->f.family <= 1, XC_ERR_UNSUPPORTED,
+                  "skeleton terms cover LDA and GGA functionals (as the reference's Hessian)");
+        CGB_CHECK(f->f.family <= G.type, XC_ERR_STATE, "grid type is below the functional family (setType/getAO)");
+        CGB_CHECK(G.ncomp >= (f->f.family >= 1 ? 10 : 4), XC_ERR_STATE,
+                  "the skeleton terms need AO derivatives one order above the functional's (getAO(1))");
+        NvtxRange nvtx_("xc.getFockSkeleton");
+        G.ensure_work();
+        const int n = G.basis.nbasis, na = G.basis.natoms();
+        const int nmat = 3 * na;
+        const long q = (long)nspin * nmat;
+        CGB_CHECK(q <= 65535, XC_ERR_ARG, "at most 65535 (spin, atom, direction) matrices");
+        const size_t nn = (size_t)n * n;
+        CGB_CUDA(cudaMemcpyAsync(G.d_D.p, D, nn * nspin * sizeof(double), cudaMemcpyHostToDevice, G.stream));
+        G.density_device(G.d_D.p);
+        G.evaluate(f->f);
+        G.evaluate_fxc(f->f);
+        // the atom of every block list entry
+        std::vector<int> atom_of(n, 0);
+        for (const Shell& sh : G.basis.shells)
+            for (int k = 0; k < shell_size(sh.type); k++) atom_of[sh.first + k] = sh.atom;
+        std::vector<int> la(G.basis_lists.size());
+        for (size_t e = 0; e < la.size(); e++) la[e] = atom_of[G.basis_lists[e]];
+        DevBuf<int> d_la;
+        d_la.upload(la.data(), la.size());
+        DevBuf<double> rg, r1g, fcU, dFS, dFU;
+        rg.alloc((size_t)q * G.Gp);
+        r1g.alloc((size_t)q * 3 * G.Gp);
+        fcU.alloc((size_t)q * 5 * G.Gp);
+        dFS.alloc((size_t)q * nn);
+        dFU.alloc((size_t)q * nn);
+        CGB_CUDA(cudaMemsetAsync(rg.p, 0, (size_t)q * G.Gp * sizeof(double), G.stream));
+        CGB_CUDA(cudaMemsetAsync(r1g.p, 0, (size_t)q * 3 * G.Gp * sizeof(double), G.stream));
+        CGB_CUDA(cudaMemsetAsync(dFS.p, 0, (size_t)q * nn * sizeof(double), G.stream));
+        CGB_CUDA(cudaMemsetAsync(dFU.p, 0, (size_t)q * nn * sizeof(double), G.stream));
+        const int fam = f->f.family;
+        const int nbk = (int)G.blocks.size();
+        // getDensitySkeleton, then getFockU<s_t> (response of V_xc to the skeleton densities)
+        launch_skel_density(nbk, G.d_blocks.p, G.d_lists.p, d_la.p, n, nspin, nmat, fam, G.d_D.p, G.d_ao.p, G.Gp,
+                            rg.p, r1g.p, G.stream);
+        launch_response_coef(fam, nspin, G.Gp, nmat, G.d_w.p, G.d_rho1.p, G.d_vsigma.p, G.d_f2.p, rg.p, r1g.p, fcU.p,
+                             G.stream);
+        launch_fock_fp64(nbk, G.d_blocks.p, G.d_lists.p, G.max_nb, n, (int)q, fam, G.d_ao.p, G.Gp, fcU.p, dFU.p,
+                         G.stream);
+        // getFockSkeleton
+        launch_fock_skel(nbk, G.d_blocks.p, G.d_lists.p, d_la.p, G.max_nb, n, nspin, nmat, fam, G.d_ao.p, G.Gp,
+                         G.d_fcoef.p, dFS.p, G.stream);
+        CGB_CUDA(cudaMemcpyAsync(FS, dFS.p, (size_t)q * nn * sizeof(double), cudaMemcpyDeviceToHost, G.stream));
+        CGB_CUDA(cudaMemcpyAsync(FU, dFU.p, (size_t)q * nn * sizeof(double), cudaMemcpyDeviceToHost, G.stream));
+        CGB_CUDA(cudaStreamSynchronize(G.stream));
+        G.have_density_u = false;  // the response scratch of getDensityU is not these matrices
+    });
+}
+
 int xc_build(xc_grid* g, xc_functional* f, const double* D, int nspin, int precision, double* E, double* V) {
     return guard([&] {
         CGB_CHECK(g && f && D && E && V, XC_ERR_ARG, "null argument");

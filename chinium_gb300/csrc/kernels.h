@@ -87,6 +87,17 @@ void launch_response_coef(int family, int nspin, long Gp, int nmat, const double
                           const double* vsigma, const double* f2, const double* rhoU, const double* rho1U,
                           double* fcoefU, cudaStream_t s);
 
+// Hessian skeleton terms (grid fixed, LDA / GGA; AO store with Hessians): the skeleton density
+// derivatives rhog (q, Gp) and rho1g (q, 3, Gp), accumulated (zero them first), and the skeleton
+// Fock derivatives F (q, n, n), accumulated, for q = s nmat + 3 A + t with the atom of every list
+// entry in d_atom_list.
+void launch_skel_density(int nblocks, const BlockDesc* d_blocks, const int* d_lists, const int* d_atom_list,
+                         int nbasis, int nspin, int nmat, int family, const double* D, const double* ao, long Gp,
+                         double* rhog, double* rho1g, cudaStream_t s);
+void launch_fock_skel(int nblocks, const BlockDesc* d_blocks, const int* d_lists, const int* d_atom_list,
+                      int max_nb, int nbasis, int nspin, int nmat, int family, const double* ao, long Gp,
+                      const double* fcoef, double* F, cudaStream_t s);
+
 // Pointwise functional on caller arrays (parity tests).
 void launch_functional_points(const xcf::FuncDesc& f, int family, int nspin, long n, const double* rho,
                               const double* sigma, const double* tau, double* eps, double* vrho,

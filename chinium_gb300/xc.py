@@ -230,6 +230,17 @@ class Grid:
         check(lib().xc_build_response(self._h, xc._h, _p(Dst), self.nspin, int(precision), nmat, _p(Du), _p(F)))
         return self._unstack_u(F, nmat)
 
+    def getFockSkeleton(self, xc, D):
+        """getFockSkeleton and getFockU<s_t> (grid fixed, FP64, LDA / GGA) for every atom and
+        direction: (FS, FU), each (nspin, 3 natoms, n, n) with matrix 3 A + t; FS + FU is
+        dV_xc / dR at fixed D.  Needs getAO(1)."""
+        Dst = self._stack(D)
+        n, na = self.nbasis, len(self.basis.Z)
+        FS = np.zeros((self.nspin, 3 * na, n, n))
+        FU = np.zeros((self.nspin, 3 * na, n, n))
+        check(lib().xc_grid_fock_skeleton(self._h, xc._h, _p(Dst), self.nspin, _p(FS), _p(FU)))
+        return FS.transpose(0, 1, 3, 2).copy(), FU.transpose(0, 1, 3, 2).copy()
+
     def sap_fock(self, precision=PRECISION_FP64):
         """SuperpositionAtomicPotential (GuessSCF.cpp:17-75); PRECISION_MIXED
         assembles it on the tensor cores (FP32-level accuracy)."""

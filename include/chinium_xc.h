@@ -233,6 +233,16 @@ int xc_grid_kernel_ms(xc_grid* g, double* ms);
  * gradient kernel, 0]. */
 int xc_grid_energy_grad(xc_grid* g, xc_functional* f, const double* D, int nspin, double* grad);
 
+/* The Hessian's skeleton V_xc derivatives with the grid held fixed, FP64, LDA
+ * and GGA (Restricted/Hess.cpp:83-97): FS = getFockSkeleton (GridFock.cpp:52-95)
+ * and FU = getFockU<s_t> (GridFock.cpp:97-160) on the skeleton density
+ * derivatives of getDensitySkeleton (GridDensity.cpp:79-130), for every atom A
+ * and direction t: nspin x 3 natoms column-major n x n matrices, matrix
+ * (s * 3 natoms + 3 A + t).  FS + FU is dV_xc / dR_(A,t) at fixed D.  Needs
+ * getAO(1) after setType (AO derivatives one order above the functional's).
+ * D as for xc_build. */
+int xc_grid_fock_skeleton(xc_grid* g, xc_functional* f, const double* D, int nspin, double* FS, double* FU);
+
 /* --------------------------------------------- response (coupled-perturbed)
  * FP64, LDA and GGA.  D_U and V_U hold nspin x nmat column-major n x n
  * matrices, spin-major: matrix m of spin s starts at (s * nmat + m) n^2, as

@@ -301,3 +301,23 @@ def test_unrestricted_response_at_equal_spins_is_restricted(h2o, name):
     u = np.array(gu.build_response(cg.ExchangeCorrelation(spin=2).Read(name), [D / 2, D / 2], [[U / 2], [U / 2]]))
     for s in range(2):
         assert np.abs(u[s, 0] - r).max() < 1e-12 * max(1.0, np.abs(r).max())
+
+
+@pytest.mark.parametrize("name,nspin", [("SVWN5", 1), ("PBE", 1), ("PBE", 2)])
+def test_hessian_skeleton_fock_terms_match_oracle(h2o, name, nspin):
+    """getFockSkeleton and getFockU<s_t> (grid fixed, FP64) against the oracle's
+    restatement, whose sum the CPU tests pin to finite differences of V_xc."""
+    Z, xyz, b, ob, og = h2o
+    ids = O.FUNCTIONAL_FILES[name]
+    fam = O.family(ids)
+    D = [model_density(og, 5)] if nspin == 1 else model_density(og, (5, 4), nspin=2, seed=2)
+    g = cg.Grid(b, "SG-1", nspin=nspin)
+    g.setType(fam)
+    g.getAO(1)
+    xc = cg.ExchangeCorrelation(spin=nspin).Read(name)
+    FS, FU = g.getFockSkeleton(xc, D)
+    rs, ru = og.fock_skeleton(np.stack(D), ids, nspin)
+    es, eu = np.abs(FS - rs).max(), np.abs(FU - ru).max()
+    print(name, nspin, "skeleton max |dF| %.2e (max %.2e), s_t response %.2e (max %.2e)"
+          % (es, np.abs(rs).max(), eu, np.abs(ru).max()))
+    assert es < V_TOL and eu < V_TOL
