@@ -483,6 +483,15 @@ def run_gradient(args):
         flops = float(np.sum(4 * ng * nb * nb + 35 * ng * nb))
         out[key] = {"ms_per_gradient": t * 1e3, "kernel_ms": ms[2], "density_ms": ms[0], "functional_ms": ms[1],
                     "kernel_fp64_tflops": flops / (ms[2] * 1e-3) / 1e12, "grad": G}
+        if thr > 0:
+            # the Hessian's skeleton V_xc terms on the same grid (getFockSkeleton + getFockU<s_t>, 3 N_atoms
+            # matrices each): one warm-up call, one timed
+            g.getFockSkeleton(xc, [D])
+            t0 = time.perf_counter()
+            FS, FU = g.getFockSkeleton(xc, [D])
+            out[key]["fock_skeleton_ms"] = (time.perf_counter() - t0) * 1e3
+            out[key]["fock_skeleton_matrices"] = int(FS.shape[1])
+            del FS, FU
         del g
     peak = fp64_gemm_peak(torch)
     sc = out["screened_1e-11"]
