@@ -1102,7 +1102,7 @@ int xc_grid_fock_skeleton(xc_grid* g, xc_functional* f, const double* D, int nsp
         CGB_CUDA(cudaMemcpyAsync(FS, dFS.p, (size_t)q * nn * sizeof(double), cudaMemcpyDeviceToHost, G.stream));
         CGB_CUDA(cudaMemcpyAsync(FU, dFU.p, (size_t)q * nn * sizeof(double), cudaMemcpyDeviceToHost, G.stream));
         CGB_CUDA(cudaStreamSynchronize(G.stream));
-        G.have_density_u = false;  // the response scratch of getDensityU is not these matrices
+        G.have_density_u = false;  // a new ground state: response densities of an earlier getDensityU belong to the old one
     });
 }
 
