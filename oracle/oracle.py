@@ -185,6 +185,16 @@ class Basis:
                          _p(np.ascontiguousarray(z)), _p(out))
         return out.reshape(6, self.nbasis, ng)
 
+    def ao3(self, x, y, z):
+        """Third derivatives (10, n, g), the packed sorted triples (xxx, xxy, xyy, yyy, xxz, ...)."""
+        ng = len(x)
+        out = np.zeros(10 * self.nbasis * ng)
+        lib().oracle_ao3(ctypes.c_int(len(self.types)), _p(self.types), _p(self.nprim), _p(self.off),
+                         _p(self.centers), _p(self.exps), _p(self.coefs), ctypes.c_int(self.nbasis),
+                         ctypes.c_int(ng), _p(np.ascontiguousarray(x)), _p(np.ascontiguousarray(y)),
+                         _p(np.ascontiguousarray(z)), _p(out))
+        return out.reshape(10, self.nbasis, ng)
+
     def function_atoms(self):
         """Atom of every basis function."""
         out = []
@@ -474,6 +484,71 @@ class OracleGrid:
                             _p(v2rho2), _p(v2rhosigma), _p(v2sigma2), _p(rg), _p(r1g), _p(sg), _p(Fu))
         Fs = Fs.reshape(nspin, nmat, nb, nb).transpose(0, 1, 3, 2).copy()
         return Fs, Fu.transpose(0, 1, 3, 2).copy()
+
+
+def energy_hess(og, D, ids):
+    """XC skeleton energy Hessian with the grid fixed, restricted: getDensitySkeleton2 +
+    getEnergyHess (GridDensity.cpp:132-212, GridEnergy.cpp:32-46) block by block.  D the total
+    density (n, n).  Returns (3 natoms, 3 natoms), index 3 a + t."""
+    fam = family(ids)
+    b = og.basis
+    nb, natoms = b.nbasis, len(b.Z)
+    nm = 3 * natoms
+    Dc = np.ascontiguousarray(np.asarray(D, dtype=np.float64).reshape(nb, nb).T)
+    atom_of = b.function_atoms()
+    E = np.zeros(nm * nm)
+    L = lib()
+    for k, blk in enumerate(og.blocks):
+        ng = len(blk[0])
+        w = np.ascontiguousarray(blk[3], dtype=np.float64)
+        ao = np.ascontiguousarray(og.ao[k][0])
+        ao1 = np.ascontiguousarray(og.ao[k][1])
+        ao2 = np.ascontiguousarray(b.ao2(blk[0], blk[1], blk[2]))
+        ao3 = np.ascontiguousarray(b.ao3(blk[0], blk[1], blk[2])) if fam >= 1 else np.zeros(1)
+        rho, rho1, sigma, tau = np.zeros(ng), np.zeros(3 * ng), np.zeros(ng), np.zeros(ng)
+        L.oracle_density(ctypes.c_int(ng), ctypes.c_int(nb), ctypes.c_int(1), ctypes.c_int(fam), _p(Dc), _p(ao),
+                         _p(ao1), _p(rho), _p(rho1), _p(sigma), _p(tau))
+        _, vrho, vsigma, _ = functional(ids, 1, rho, sigma)
+        vrho, vsigma = np.ascontiguousarray(vrho), np.ascontiguousarray(vsigma)
+        f2 = [np.ascontiguousarray(a) for a in functional_fxc(ids, 1, rho, sigma)]
+        rg, r1g, sg = np.zeros(nm * ng), np.zeros(3 * nm * ng), np.zeros(nm * ng)
+        L.oracle_density_skeleton(ctypes.c_int(ng), ctypes.c_int(nb), ctypes.c_int(1), ctypes.c_int(natoms),
+                                  _p(atom_of), ctypes.c_int(fam), _p(Dc), _p(ao), _p(ao1), _p(ao2), _p(rho1), _p(rg),
+                                  _p(r1g), _p(sg))
+        L.oracle_energy_hess(ctypes.c_int(ng), ctypes.c_int(nb), ctypes.c_int(natoms), _p(atom_of), ctypes.c_int(fam),
+                             _p(Dc), _p(w), _p(ao), _p(ao1), _p(ao2), _p(ao3), _p(rho1), _p(vrho), _p(vsigma), _p(f2[0]),
+                             _p(f2[1]), _p(f2[2]), _p(rg), _p(r1g), _p(sg), _p(E))
+    return E.reshape(nm, nm).T.copy()
+
+
+def energy_hess_fd(og, Z, xyz_bohr, basis_name, D, ids, pairs, h=1e-3):
+    """d^2 E_xc / dR_i dR_j at fixed D with the grid fixed (i, j = 3 atom + direction) for the
+    given pairs, by the four-point difference of E_xc with the basis functions of the atoms
+    displaced, steps h and h/2 combined by Richardson extrapolation.  Test reference for
+    energy_hess."""
+    xyz = np.asarray(xyz_bohr, dtype=np.float64).reshape(-1, 3)
+    saved = og.ao, og.basis
+
+    def energy(moves):
+        moved = xyz.copy()
+        for (i, d) in moves:
+            moved[i // 3, i % 3] += d
+        bm = Basis(Z, moved, basis_name)
+        og.basis = bm
+        og.ao = [bm.ao(bx, by, bz, og.deriv) for bx, by, bz, bw in og.blocks]
+        return og.build(np.asarray(D)[None], ids, 1)[0]
+
+    out = {}
+    try:
+        for i, j in pairs:
+            vals = []
+            for hh in (h, 0.5 * h):
+                e = [energy([(i, si * hh), (j, sj * hh)]) for si, sj in ((1, 1), (1, -1), (-1, 1), (-1, -1))]
+                vals.append((e[0] - e[1] - e[2] + e[3]) / (4 * hh * hh))
+            out[(i, j)] = (4 * vals[1] - vals[0]) / 3
+    finally:
+        og.ao, og.basis = saved
+    return out
 
 
 def fock_fd(og, Z, xyz_bohr, basis_name, D, ids, nspin, h=1e-4):

@@ -121,6 +121,20 @@ void oracle_fock_skeleton(int ng, int nbasis_block, int nbasis_total, const int*
                           const double* ao1, const double* ao2, const double* rho1, const double* vrho,
                           const double* vsigma, double* F);
 
+/* AO third derivatives of one block: ao3[(c * nbasis + mu) * ng + g], c the packed sorted triple
+ * i0 + i1 (i1 + 1) / 2 + i2 (i2 + 1) (i2 + 2) / 6. */
+void oracle_ao3(int nshells, const int* shell_type, const int* shell_nprim, const int* shell_prim_off,
+                const double* shell_center, const double* exps, const double* coefs, int nbasis, int ng,
+                const double* x, const double* y, const double* z, double* ao3);
+
+/* XC skeleton energy Hessian of one block, restricted (GridDensity.cpp:132-212, GridEnergy.cpp:32-46),
+ * added to E (3 natoms x 3 natoms, column-major, index 3 a + t). */
+void oracle_energy_hess(int ng, int nbasis, int natoms, const int* atom_of, int type, const double* D,
+                        const double* w, const double* ao, const double* ao1, const double* ao2,
+                        const double* ao3, const double* rho1, const double* vrho, const double* vsigma,
+                        const double* v2rho2, const double* v2rhosigma, const double* v2sigma2,
+                        const double* rhog, const double* rho1g, const double* sigmag, double* E);
+
 #ifdef __cplusplus
 }
 #endif

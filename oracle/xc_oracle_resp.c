@@ -405,3 +405,184 @@ void oracle_fock_skeleton(int ng, int nb, int ntot, const int* list, int ns, int
     free(L);
     free(F);
 }
+
+/* ------------------------------------------------ energy Hessian (restricted) */
+
+static int triple_pack(int a, int b, int c) {
+    int v[3] = {a, b, c};
+    for (int i = 0; i < 2; i++)
+        for (int j = 0; j < 2 - i; j++)
+            if (v[j] > v[j + 1]) {
+                const int t = v[j];
+                v[j] = v[j + 1];
+                v[j + 1] = t;
+            }
+    return v[0] + v[1] * (v[1] + 1) / 2 + v[2] * (v[2] + 1) * (v[2] + 2) / 6;
+}
+
+/* AO third derivatives ao3[(c * nbasis + mu) * ng + g], c the packed sorted triple
+ * i0 + i1 (i1 + 1) / 2 + i2 (i2 + 1) (i2 + 2) / 6 (xxx, xxy, xyy, yyy, xxz, xyz, yyz, xzz, yzz, zzz):
+ *   d_abc phi = A_abc Q + A_ab Q_c + A_ac Q_b + A_bc Q_a + A_a Q_bc + A_b Q_ac + A_c Q_ab + A Q_abc
+ * with A_abc = -8 x_a x_b x_c sum c alpha^3 e + 4 (d_ab x_c + d_ac x_b + d_bc x_a) sum c alpha^2 e
+ * (GridAO.cpp:134-146, 197-208); Q's derivatives from oracle_ao2 on a unit radial part and central
+ * differences of its second derivatives (exact: they are at most quadratic). */
+void oracle_ao3(int nshells, const int* shell_type, const int* shell_nprim, const int* shell_prim_off,
+                const double* shell_center, const double* exps, const double* coefs, int nbasis, int ng,
+                const double* xs, const double* ys, const double* zs, double* ao3) {
+    int ibasis = 0;
+    const double zero_exp = 0.0, one_coef = 1.0;
+    const int one_nprim = 1, zero_off = 0;
+    const double org[3] = {0, 0, 0};
+    double q[16], q1[48], q2[96], q2p[96], q2m[96];
+    for (int s = 0; s < nshells; s++) {
+        const int type = shell_type[s];
+        const double* e = exps + shell_prim_off[s];
+        const double* c = coefs + shell_prim_off[s];
+        const double* C = shell_center + 3 * s;
+        const int size = type == 0 ? 1 : (type == 1 || type == -1) ? 3 : 2 * (-type) + 1;
+        for (int k = 0; k < ng; k++) {
+            const double r[3] = {xs[k] - C[0], ys[k] - C[1], zs[k] - C[2]};
+            const double r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+            double t[4] = {0, 0, 0, 0};
+            for (int p = 0; p < shell_nprim[s]; p++) {
+                const double v = c[p] * exp(-e[p] * r2);
+                t[0] += v;
+                t[1] += v * e[p];
+                t[2] += v * e[p] * e[p];
+                t[3] += v * e[p] * e[p] * e[p];
+            }
+            oracle_ao(1, &type, &one_nprim, &zero_off, org, &zero_exp, &one_coef, size, 1, &r[0], &r[1], &r[2], 1, q,
+                      q1);
+            oracle_ao2(1, &type, &one_nprim, &zero_off, org, &zero_exp, &one_coef, size, 1, &r[0], &r[1], &r[2], q2);
+            double Q3[10][16];
+            for (int cdir = 0; cdir < 3; cdir++) {
+                const double h = 1e-2;
+                double rp[3] = {r[0], r[1], r[2]}, rm[3] = {r[0], r[1], r[2]};
+                rp[cdir] += h;
+                rm[cdir] -= h;
+                oracle_ao2(1, &type, &one_nprim, &zero_off, org, &zero_exp, &one_coef, size, 1, &rp[0], &rp[1],
+                           &rp[2], q2p);
+                oracle_ao2(1, &type, &one_nprim, &zero_off, org, &zero_exp, &one_coef, size, 1, &rm[0], &rm[1],
+                           &rm[2], q2m);
+                for (int b = 0; b < 3; b++)
+                    for (int a = 0; a <= b; a++) {
+                        if (cdir < b) continue; /* each sorted triple (a <= b <= cdir) once */
+                        const int pk2 = a + b * (b + 1) / 2, pk3 = triple_pack(a, b, cdir);
+                        for (int i = 0; i < size; i++)
+                            Q3[pk3][i] = (q2p[pk2 * size + i] - q2m[pk2 * size + i]) / (2 * h);
+                    }
+            }
+            for (int cc = 0; cc < 3; cc++)
+                for (int b = 0; b <= cc; b++)
+                    for (int a = 0; a <= b; a++) {
+                        const int idx[3] = {a, b, cc};
+                        const double x[3] = {r[idx[0]], r[idx[1]], r[idx[2]]};
+                        const double dab = a == b, dac = a == cc, dbc = b == cc;
+                        const double A1[3] = {-2 * x[0] * t[1], -2 * x[1] * t[1], -2 * x[2] * t[1]};
+                        const double Aab = 4 * x[0] * x[1] * t[2] - 2 * dab * t[1];
+                        const double Aac = 4 * x[0] * x[2] * t[2] - 2 * dac * t[1];
+                        const double Abc = 4 * x[1] * x[2] * t[2] - 2 * dbc * t[1];
+                        const double Aabc = -8 * x[0] * x[1] * x[2] * t[3] + 4 * (dab * x[2] + dac * x[1] + dbc * x[0]) * t[2];
+                        const int pk3 = triple_pack(a, b, cc);
+                        for (int i = 0; i < size; i++) {
+                            const double Qa = q1[a * size + i], Qb = q1[b * size + i], Qc = q1[cc * size + i];
+                            const double Qbc = q2[pair_pack(b, cc) * size + i], Qac = q2[pair_pack(a, cc) * size + i],
+                                         Qab = q2[pair_pack(a, b) * size + i];
+                            ao3[((long)pk3 * nbasis + ibasis + i) * ng + k] =
+                                Aabc * q[i] + Aab * Qc + Aac * Qb + Abc * Qa + A1[0] * Qbc + A1[1] * Qac + A1[2] * Qab +
+                                t[0] * Q3[pk3][i];
+                        }
+                    }
+        }
+        ibasis += size;
+    }
+}
+
+/* SubGrid::getDensitySkeleton2 + SubGrid::getEnergyHess (GridDensity.cpp:132-212,
+ * GridEnergy.cpp:32-46) for one block, restricted (the reference marks its sigma Hessian
+ * as incorrect for open shells, GridDensity.cpp:210): adds
+ *   E(t,a,s,b) += sum_g W [f_rr rho_at rho_bs + v_r rho_at,bs + f_rs (rho_at sigma_bs + sigma_at rho_bs)
+ *                          + f_ss sigma_at sigma_bs + v_s sigma_at,bs]
+ * to E (3 natoms x 3 natoms, index (3 a + t) + 3 natoms (3 b + s)), with the skeleton first
+ * derivatives of oracle_density_skeleton (rhog, rho1g, sigmag) and
+ *   rho_at,bs   = 2 [d_ab sum_(mu on a) H_ts,mu T0_mu + sum_(mu on a, nu on b) D d_t phi_mu d_s phi_nu]
+ *   (grad_r rho)_at,bs = 2 [d_ab sum_(mu on a) (T3_rts,mu T0_mu + H_ts,mu Tr_mu)
+ *                          + sum_(mu on a, nu on b) D (H_rt,mu d_s phi_nu + d_t phi_mu H_rs,nu)]
+ *   sigma_at,bs = 2 (grad rho . (grad rho)_at,bs + (grad rho)_at . (grad rho)_bs)
+ * where T0_mu = sum_nu D phi_nu, Tr_mu = sum_nu D d_r phi_nu. */
+void oracle_energy_hess(int ng, int nb, int natoms, const int* atom_of, int type, const double* D,
+                        const double* w, const double* ao, const double* ao1, const double* ao2, const double* ao3,
+                        const double* rho1, const double* vrho, const double* vsigma, const double* v2rho2,
+                        const double* v2rhosigma, const double* v2sigma2, const double* rhog, const double* rho1g,
+                        const double* sigmag, double* E) {
+    const int nm = 3 * natoms;
+    double* T0 = (double*)calloc((size_t)nb * ng, sizeof(double));
+    double* Tr = (double*)calloc((size_t)3 * nb * ng, sizeof(double));
+    for (int mu = 0; mu < nb; mu++)
+        for (int nu = 0; nu < nb; nu++) {
+            const double d = D[(long)nu * nb + mu];
+            for (int g = 0; g < ng; g++) {
+                T0[(long)mu * ng + g] += d * ao[(long)nu * ng + g];
+                if (type >= 1)
+                    for (int r = 0; r < 3; r++) Tr[((long)r * nb + mu) * ng + g] += d * ao1[((long)r * nb + nu) * ng + g];
+            }
+        }
+    double* rh = (double*)malloc(sizeof(double) * ng);
+    double* r1h = (double*)malloc(sizeof(double) * ng * 3);
+    for (int a = 0; a < natoms; a++)
+        for (int t = 0; t < 3; t++)
+            for (int b = 0; b < natoms; b++)
+                for (int s = 0; s < 3; s++) {
+                    memset(rh, 0, sizeof(double) * ng);
+                    memset(r1h, 0, sizeof(double) * ng * 3);
+                    for (int mu = 0; mu < nb; mu++) {
+                        if (atom_of[mu] != a) continue;
+                        const double* dt = ao1 + ((long)t * nb + mu) * ng;
+                        if (a == b) {
+                            const double* hts = ao2 + ((long)pair_pack(t, s) * nb + mu) * ng;
+                            for (int g = 0; g < ng; g++) rh[g] += hts[g] * T0[(long)mu * ng + g];
+                            if (type >= 1)
+                                for (int r = 0; r < 3; r++) {
+                                    const double* t3 = ao3 + ((long)triple_pack(r, t, s) * nb + mu) * ng;
+                                    for (int g = 0; g < ng; g++)
+                                        r1h[r * ng + g] += t3[g] * T0[(long)mu * ng + g] + hts[g] * Tr[((long)r * nb + mu) * ng + g];
+                                }
+                        }
+                        for (int nu = 0; nu < nb; nu++) {
+                            if (atom_of[nu] != b) continue;
+                            const double d = D[(long)nu * nb + mu];
+                            if (d == 0) continue;
+                            const double* ds = ao1 + ((long)s * nb + nu) * ng;
+                            for (int g = 0; g < ng; g++) rh[g] += d * dt[g] * ds[g];
+                            if (type >= 1)
+                                for (int r = 0; r < 3; r++) {
+                                    const double* hrt = ao2 + ((long)pair_pack(r, t) * nb + mu) * ng;
+                                    const double* hrs = ao2 + ((long)pair_pack(r, s) * nb + nu) * ng;
+                                    for (int g = 0; g < ng; g++) r1h[r * ng + g] += d * (hrt[g] * ds[g] + dt[g] * hrs[g]);
+                                }
+                        }
+                    }
+                    const long i = 3 * a + t, j = 3 * b + s;
+                    const double* ra = rhog + i * ng;
+                    const double* rb = rhog + j * ng;
+                    double acc = 0;
+                    for (int g = 0; g < ng; g++) {
+                        double v = v2rho2[g] * ra[g] * rb[g] + vrho[g] * 2.0 * rh[g];
+                        if (type >= 1) {
+                            const double sa = sigmag[i * ng + g], sb = sigmag[j * ng + g];
+                            double shess = 0;
+                            for (int r = 0; r < 3; r++)
+                                shess += rho1[r * ng + g] * 2.0 * r1h[r * ng + g] +
+                                         rho1g[(i * 3 + r) * ng + g] * rho1g[(j * 3 + r) * ng + g];
+                            shess *= 2.0;
+                            v += v2rhosigma[g] * (ra[g] * sb + sa * rb[g]) + v2sigma2[g] * sa * sb + vsigma[g] * shess;
+                        }
+                        acc += w[g] * v;
+                    }
+                    E[i + nm * j] += acc;
+                }
+    free(r1h);
+    free(rh);
+    free(Tr);
+    free(T0);
+}
