@@ -203,6 +203,7 @@ def test_response_entry_points_validate_arguments_on_the_host():
     assert L.xc_build_response(nul, nul, p, 1, 0, 1, p, p) == -1
     assert L.xc_functional_fxc_points(nul, 1, p, p, p, p, p) == -1
     assert L.xc_dipole(nul, p, p) == -1
+    assert L.xc_grid_fock_skeleton(nul, nul, p, 1, p, p) == -1
     f = ctypes.c_void_p()
     ids = (ctypes.c_int * 2)(202, 231)
     assert L.xc_functional_create(ids, 2, 1, ctypes.byref(f)) == 0
