@@ -404,6 +404,33 @@ class OracleGrid:
         return E.value, F.transpose(0, 2, 1).copy()
 
 
+    def build_response(self, D, DU, ids, nspin, nblocks=None, nthreads=0):
+        """response() over the first nblocks blocks with the C driver (OpenMP over blocks):
+        the timed CPU baseline.  Returns V_U (nspin, nmat, n, n)."""
+        fam = family(ids)
+        nb = self.basis.nbasis
+        blocks = self.blocks[: nblocks or len(self.blocks)]
+        ngs = np.array([len(b[0]) for b in blocks], dtype=np.int32)
+        pt_off = np.concatenate([[0], np.cumsum(ngs)[:-1]]).astype(np.int64)
+        ao_off = (pt_off * nb).astype(np.int64)
+        w = np.concatenate([b[3] for b in blocks])
+        ao = np.concatenate([a[0].ravel() for a in self.ao[: len(blocks)]])
+        ao1 = np.concatenate([a[1].ravel() for a in self.ao[: len(blocks)]]) if fam >= 1 else np.zeros(1)
+        D = np.asarray(D, dtype=np.float64).reshape(nspin, nb, nb)
+        DU = np.asarray(DU, dtype=np.float64).reshape(nspin, -1, nb, nb)
+        nmat = DU.shape[1]
+        Dc = np.ascontiguousarray(D.transpose(0, 2, 1))
+        DUc = np.ascontiguousarray(DU.transpose(0, 1, 3, 2))
+        F = np.zeros((nspin, nmat, nb, nb))
+        idsa = np.asarray(ids, dtype=np.int32)
+        st = lib().oracle_build_response(ctypes.c_int(len(blocks)), _p(ngs), _p(pt_off), _p(ao_off), _p(w), _p(ao),
+                                         _p(ao1), ctypes.c_int(nb), ctypes.c_int(nspin), ctypes.c_int(fam), _p(Dc),
+                                         ctypes.c_int(nmat), _p(DUc), ctypes.c_int(len(idsa)), _p(idsa),
+                                         ctypes.c_int(nthreads), _p(F))
+        if st:
+            raise ValueError("oracle response build failed")
+        return F.transpose(0, 1, 3, 2).copy()
+
     def response(self, D, DU, ids, nspin):
         """getDensity(D) + Evaluate("v", "f") + getDensityU(DU) + getFockU<u_t>
         block by block with the C oracle (GridDensity.cpp:47-77,

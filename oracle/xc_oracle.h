@@ -135,6 +135,13 @@ void oracle_energy_hess(int ng, int nbasis, int natoms, const int* atom_of, int 
                         const double* v2rho2, const double* v2rhosigma, const double* v2sigma2,
                         const double* rhog, const double* rho1g, const double* sigmag, double* E);
 
+/* The response V_U of nmat matrices over a list of blocks (layouts as oracle_build; D_U
+ * (n,n,nmat,s) column-major), OpenMP over blocks: the timed CPU baseline of the response. */
+int oracle_build_response(int nblocks, const int* blk_ng, const long* blk_pt_off, const long* blk_ao_off,
+                          const double* w, const double* ao, const double* ao1, int nbasis, int nspin,
+                          int type, const double* D, int nmat, const double* DU, int nids, const int* ids,
+                          int nthreads, double* F_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -586,3 +586,80 @@ void oracle_energy_hess(int ng, int nb, int natoms, const int* atom_of, int type
     free(Tr);
     free(T0);
 }
+
+/* ------------------------------------------------------ response build (OpenMP) */
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* The response over a list of blocks (the blocks' AO values concatenated as in oracle_build):
+ * per block the ground-state density, vsigma and second derivatives, the response densities
+ * of the nmat matrices D_U (n,n,nmat,s) and their V_U accumulated into F (n,n,nmat,s), OpenMP
+ * over blocks (the reference's static bins, GridGeneration.cpp:293-300, with per-thread copies
+ * of F reduced at the end, as Grid::getFockU does, Grid.cpp:194-218).  Returns 0, or -1 for a
+ * meta-GGA or unknown functional id. */
+int oracle_build_response(int nblocks, const int* blk_ng, const long* blk_pt_off, const long* blk_ao_off,
+                          const double* w, const double* ao, const double* ao1, int nb, int ns, int type,
+                          const double* D, int nmat, const double* DU, int nids, const int* ids, int nthreads,
+                          double* F_out) {
+    if (type > 1) return -1;
+    int* list = (int*)malloc(sizeof(int) * nb);
+    for (int i = 0; i < nb; i++) list[i] = i;
+    const long nf = (long)nb * nb * nmat * ns;
+    for (long i = 0; i < nf; i++) F_out[i] = 0;
+    int status = 0;
+    const int nsig = ns == 1 ? 1 : 3, nrs = ns == 1 ? 1 : 6, nrr = ns == 1 ? 1 : 3;
+#ifdef _OPENMP
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+#else
+    nthreads = 1;
+#endif
+#pragma omp parallel num_threads(nthreads)
+    {
+        double* Fp = (double*)calloc(nf, sizeof(double));
+        const int cap = 128;
+        double* rho = (double*)malloc(sizeof(double) * cap * ns);
+        double* rho1 = (double*)malloc(sizeof(double) * cap * 3 * ns);
+        double* sigma = (double*)malloc(sizeof(double) * cap * nsig);
+        double* tau = (double*)malloc(sizeof(double) * cap * ns);
+        double* eps = (double*)malloc(sizeof(double) * cap);
+        double* vrho = (double*)malloc(sizeof(double) * cap * ns);
+        double* vsigma = (double*)malloc(sizeof(double) * cap * nsig);
+        double* vtau = (double*)malloc(sizeof(double) * cap * ns);
+        double* f1 = (double*)malloc(sizeof(double) * cap * nrr);
+        double* f2 = (double*)malloc(sizeof(double) * cap * nrs);
+        double* f3 = (double*)malloc(sizeof(double) * cap * nrs);
+        double* rU = (double*)malloc(sizeof(double) * cap * nmat * ns);
+        double* r1U = (double*)malloc(sizeof(double) * cap * 3 * nmat * ns);
+        double* sU = (double*)malloc(sizeof(double) * cap * nmat * nsig);
+#pragma omp for schedule(static)
+        for (int b = 0; b < nblocks; b++) {
+            const int ng = blk_ng[b];
+            if (ng > cap) {
+#pragma omp atomic write
+                status = -1;
+                continue;
+            }
+            const double* a0 = ao + blk_ao_off[b];
+            const double* a1 = type >= 1 ? ao1 + 3 * blk_ao_off[b] : NULL;
+            const double* wb = w + blk_pt_off[b];
+            oracle_density(ng, nb, ns, type, D, a0, a1, rho, rho1, sigma, tau);
+            int st = oracle_functional(nids, ids, ns, ng, rho, sigma, tau, eps, vrho, vsigma, vtau);
+            st |= oracle_functional_fxc(nids, ids, ns, ng, rho, sigma, f1, f2, f3);
+            if (st) {
+#pragma omp atomic write
+                status = -1;
+            }
+            oracle_density_u(ng, nb, ns, nmat, type, DU, a0, a1, rho1, rU, r1U, sU);
+            oracle_fock_u(ng, nb, nb, list, ns, nmat, type, wb, a0, a1, rho1, vsigma, f1, f2, f3, rU, r1U, sU, Fp);
+        }
+#pragma omp critical
+        for (long i = 0; i < nf; i++) F_out[i] += Fp[i];
+        free(Fp);
+        free(rho); free(rho1); free(sigma); free(tau); free(eps); free(vrho); free(vsigma); free(vtau);
+        free(f1); free(f2); free(f3); free(rU); free(r1U); free(sU);
+    }
+    free(list);
+    return status;
+}

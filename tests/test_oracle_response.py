@@ -118,3 +118,18 @@ def test_oracle_unrestricted_response_at_equal_spins_is_restricted(h2o_oracle, n
     scale = np.abs(r).max()
     for s in range(2):
         assert np.abs(u[s, 0] - r).max() < 1e-8 * scale, (name, s, np.abs(u[s, 0] - r).max())
+
+
+@pytest.mark.parametrize("name,nspin", [("PBE", 1), ("SVWN5", 2)])
+def test_parallel_response_driver_equals_block_loop(h2o_oracle, name, nspin):
+    """The OpenMP response driver (the timed CPU baseline) gives the per-block restatement's V_U."""
+    Z, xyz, basis, og = h2o_oracle
+    n = basis.nbasis
+    ids = O.FUNCTIONAL_FILES[name]
+    D = model_density(og, 5)[None] if nspin == 1 else np.stack(model_density(og, (5, 4), nspin=2, seed=2))
+    rng = np.random.default_rng(3)
+    U = rng.normal(size=(nspin, 2, n, n)) * 0.05
+    U = U + U.transpose(0, 1, 3, 2)
+    a = og.response(D, U, ids, nspin)
+    b = og.build_response(D, U, ids, nspin, nthreads=4)
+    assert np.abs(a - b).max() < 1e-13
