@@ -34,7 +34,7 @@ def workload(name="c18"):
     if name == "fe4s4":
         Z, xyz = M.fe4s4()
         return dict(name="Fe4S4 UKS TPSS/def2-TZVP SG-3, multiplicity 9", Z=Z, xyz=xyz, basis="def2-tzvp",
-                    grid="SG-3", functional="TPSS", nspin=2, nocc=(88, 80),
+                    grid="SG-3", functional="TPSS", ids=[202, 231], nspin=2, nocc=(88, 80),
                     metric="XC grid-pts/s (one UKS TPSS/def2-TZVP XC build of Fe4S4 on SG-3)")
     Z, xyz = M.c18()
     return dict(name="C18 RKS B3LYP/def2-TZVP SG-2", Z=Z, xyz=xyz, basis="def2-tzvp", grid="SG-2",
@@ -49,6 +49,14 @@ def model_density(nbasis, nocc, seed=0):
     A[np.arange(nocc), np.arange(nocc)] += 1.0
     Q, _ = np.linalg.qr(A)
     return 2.0 * Q @ Q.T
+
+
+def workload_density(wl, nbasis):
+    """The workload's density matrices (row-major n x n, one per spin):
+    restricted 2 C C^T, or per-spin C_s C_s^T of an open-shell occupation."""
+    if wl["nspin"] == 1:
+        return [model_density(nbasis, wl["nocc"])]
+    return [0.5 * model_density(nbasis, no, seed=k) for k, no in enumerate(wl["nocc"])]
 
 
 def clocks_start(path):
@@ -118,65 +126,78 @@ def fp64_gemm_peak(torch):
 class CpuArm:
     """The oracle (CPU restatement of the reference's per-block einsum loops,
     OpenMP over blocks) on the first sample_blocks blocks of the same
-    workload (0 = every block): grid, blocks and AO values set up once."""
+    workload (0 = every block): grid, blocks and AO values set up once.
+    Throughput counts the real (unpadded) points of the blocks built."""
 
     def __init__(self, wl, D, sample_blocks, threads):
         from oracle import oracle as O
         basis = O.Basis(wl["Z"], wl["xyz"], wl["basis"])
         px, py, pz, w = O.grid_points(wl["Z"], wl["xyz"], wl["grid"])
         allb = O.padded_blocks(px, py, pz, w)
+        ranges = O.block_ranges(len(px))
         self.total = len(allb)
-        blocks = allb[:sample_blocks] if sample_blocks > 0 else allb
+        nblk = sample_blocks if 0 < sample_blocks < len(allb) else len(allb)
+        blocks = allb[:nblk]
         g = O.OracleGrid.__new__(O.OracleGrid)
         g.basis = basis
         g.blocks = blocks
         g.ao = [basis.ao(b[0], b[1], b[2], 1) for b in blocks]
         g.npoints = sum(len(b[0]) for b in blocks)
         self.g, self.D, self.ids, self.threads = g, D, wl["ids"], threads
+        self.nspin = wl["nspin"]
         self.npad = g.npoints
-        g.build([D], wl["ids"], 1, nblocks=1, nthreads=threads)  # warm
+        self.nreal = int(sum(n for _, n in ranges[:nblk]))
+        self.whole = nblk == len(allb)
+        self.E, self.F = g.build(D, wl["ids"], self.nspin, nblocks=1, nthreads=threads)  # warm
 
     def step(self):
-        """One timed build of the sample: (grid-points/s, seconds)."""
+        """One timed build of the sample: (real grid-points/s, seconds); keeps E_xc, V_xc."""
         t = time.perf_counter()
-        self.g.build([self.D], self.ids, 1, nthreads=self.threads)
+        self.E, self.F = self.g.build(self.D, self.ids, self.nspin, nthreads=self.threads)
         dt = time.perf_counter() - t
-        return self.npad / dt, dt
+        return self.nreal / dt, dt
 
     def describe(self, dt):
         return {"unit": UNIT, "cores": self.threads, "kind": "port",
-                "sample": "%d of %d blocks (%d padded points), one build, %.2f s" % (
-                    len(self.g.blocks), self.total, self.npad, dt)}
+                "sample": "%d of %d blocks (%d real points), one build, %.2f s" % (
+                    len(self.g.blocks), self.total, self.nreal, dt)}
 
 
 def cpu_baseline(wl, D, sample_blocks, threads):
     arm = CpuArm(wl, D, sample_blocks, threads)
     v, dt = arm.step()
-    return dict(value=v, **arm.describe(dt))
+    return dict(value=v, **arm.describe(dt)), arm
 
 
 def run_reference(args):
+    """The reference arm: the oracle port of the reference's CPU XC build
+    (per-block einsum loops, OpenMP over blocks on every host thread) on the
+    same workload, one whole build per step.  Nothing of the product is
+    loaded: the basis size comes from the oracle's own basis."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    wl = workload()
-    import chinium_gb300 as cg  # basis size only (host side)
-    nb = cg.Basis(wl["Z"], wl["xyz"], wl["basis"]).nbasis
-    D = model_density(nb, wl["nocc"])
+    from oracle import oracle as O
+    wl = workload(args.workload if args.workload in ("c18", "fe4s4") else "c18")
+    nb = O.Basis(wl["Z"], wl["xyz"], wl["basis"]).nbasis
+    Dm = workload_density(wl, nb)
     threads = os.cpu_count() or 1
-    arm = CpuArm(wl, D, args.ref_blocks, threads)
+    arm = CpuArm(wl, Dm, args.ref_blocks, threads)
     vals, times = [], []
     for i in range(args.warmup + args.steps):
         v, dt = arm.step()
         if i >= args.warmup:
             vals.append(v)
             times.append(dt)
-    v = float(np.median(vals))
+    t = float(np.sum(times))
+    v = arm.nreal * len(times) / t
     cb = dict(value=v, **arm.describe(float(np.median(times))))
-    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 147456 / v * 1e3,
+    line = {"impl": "reference", "metric": wl["metric"], "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t / len(times) * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": wl["name"], "sample_blocks": args.ref_blocks},
+            "data": "synthetic", "config": {"workload": wl["name"], "npoints": arm.nreal,
+                                            "blocks": "%d of %d" % (len(arm.g.blocks), arm.total),
+                                            "whole_build": arm.whole, "E_xc": arm.E},
             "cpu_baseline": cb, "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -653,8 +674,8 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--cpu-blocks", type=int, default=0,
                     help="blocks of the workload in the CPU baseline of this arm (0 = all: one whole build)")
-    ap.add_argument("--ref-blocks", type=int, default=512,
-                    help="blocks per step of the --impl reference arm (a bounded sample of the workload)")
+    ap.add_argument("--ref-blocks", type=int, default=0,
+                    help="blocks per step of the --impl reference arm (0 = all: one whole build per step)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="c18", choices=["c18", "fe4s4", "alkanes64", "scf-water", "c18-response",
                                                          "c18-gradient"])
@@ -700,13 +721,10 @@ def main():
     P64, PMX = cg.PRECISION_FP64, cg.PRECISION_MIXED
     precision = P64 if args.precision == "fp64" else PMX
 
-    if ns == 1:
-        D = model_density(n, wl["nocc"])
-        Dst = np.ascontiguousarray(D.T)[None]
-    else:  # one-spin densities C_s C_s^T of an open-shell occupation
-        Dsp = [0.5 * model_density(n, no, seed=k) for k, no in enumerate(wl["nocc"])]
-        D = Dsp[0] + Dsp[1]
-        Dst = np.ascontiguousarray(np.stack([d.T for d in Dsp]))
+    Dl = workload_density(wl, n)
+    Dst = np.ascontiguousarray(np.stack([d.T for d in Dl]))
+    D = Dl[0] if ns == 1 else Dl[0] + Dl[1]
+    Dsp = Dl
     dD = torch.from_numpy(Dst).cuda()
     dE = torch.zeros(1, dtype=torch.float64, device="cuda")
     dV = torch.zeros((ns, n, n), dtype=torch.float64, device="cuda")
@@ -822,7 +840,7 @@ def main():
     torch.cuda.synchronize()
     t_e2e = time.perf_counter() - t0
 
-    G = info["npoints_padded"]
+    G = info["npoints"]  # real points (the reference's padded blocks carry zero-weight copies)
     value = world * G * args.steps / t_dev
     e2e = world * G * args.steps / t_e2e
     plain = G * plain_steps / t_plain
@@ -853,7 +871,7 @@ def main():
             "dtype": "f64" if precision == P64 else "bf16x3 (split) + f64 accumulation",
             "data": "synthetic",
             "config": {"workload": wl["name"], "precision": args.precision, "npoints": info["npoints"],
-                       "npoints_padded": G, "nblocks": info["nblocks"], "nbasis": n,
+                       "npoints_padded": info["npoints_padded"], "nblocks": info["nblocks"], "nbasis": n,
                        "mixed_tiles": info["mixed_tiles"],
                        "l2": "inputs larger than L2 (FP64 AO store %.2f GB; FP32 AO store + Z %.2f GB)"
                              % (info["ao_elements"] * 4 * 8 / 1e9, info["mixed_store_bytes"] / 1e9),
@@ -872,8 +890,16 @@ def main():
                     "d2h_bytes_per_step": 8 * ns * n * n + 8},
             "gpu_launches": args.steps * (info["mixed_launches"] if precision == PMX else 4),
             "roofline": roof, "clocks": clocks}
-    if rank == 0 and not args.no_cpu_baseline and ns == 1:
-        line["cpu_baseline"] = cpu_baseline(wl, D, args.cpu_blocks, os.cpu_count() or 1)
+    if rank == 0 and not args.no_cpu_baseline:
+        cb, arm = cpu_baseline(wl, Dl, args.cpu_blocks, os.cpu_count() or 1)
+        line["cpu_baseline"] = cb
+        if arm.whole:
+            # parity of the plain FP64 path with the oracle on this workload (same grid, basis,
+            # functional and density): the plain path's bar is 1e-10 in both
+            V64h = V64.cpu().numpy()
+            line["config"]["abs_dE_xc_fp64_vs_oracle"] = abs(E64 - arm.E)
+            line["config"]["max_abs_dV_xc_fp64_vs_oracle"] = float(max(
+                np.abs(V64h[s_].T - arm.F[s_]).max() for s_ in range(ns)))
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

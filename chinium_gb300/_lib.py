@@ -63,6 +63,7 @@ SIGNATURES = {
     "xc_last_error": [_P, ctypes.c_size_t],
     "xc_set_data_path": [_S],
     "xc_basis_create": [_I, _P, _P, _S, _PP],
+    "xc_basis_create_shells": [_I, _P, _P, _I, _P, _P, _P, _P, _P, _I, _PP],
     "xc_basis_nbasis": [_P, _P],
     "xc_basis_nshells": [_P, _P],
     "xc_basis_shells": [_P, _P, _P, _P, _P],

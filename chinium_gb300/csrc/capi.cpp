@@ -536,6 +536,56 @@ int xc_basis_create(int natoms, const int* Z, const double* xyz, const char* nam
     });
 }
 
+int xc_basis_create_shells(int natoms, const int* Z, const double* xyz, int nshells, const int* shell_atom,
+                           const int* shell_type, const int* nprim, const double* exps, const double* coefs,
+                           int normalize, xc_basis** out) {
+    return guard([&] {
+        CGB_CHECK(natoms > 0 && Z && xyz && nshells > 0 && shell_atom && shell_type && nprim && exps && coefs && out,
+                  XC_ERR_ARG, "bad basis arguments");
+        CGB_CHECK(normalize == 0 || normalize == 1, XC_ERR_ARG, "normalize must be 0 or 1");
+        BasisSet b;
+        b.Z.assign(Z, Z + natoms);
+        b.xyz.assign(xyz, xyz + 3 * natoms);
+        for (double v : b.xyz) CGB_CHECK(std::isfinite(v), XC_ERR_NUMERIC, "non-finite coordinate");
+        int first = 0;
+        long po = 0;
+        for (int i = 0; i < nshells; i++) {
+            const int a = shell_atom[i], t = shell_type[i], np = nprim[i];
+            CGB_CHECK(a >= 0 && a < natoms, XC_ERR_ARG, "shell atom index out of range");
+            CGB_CHECK(np > 0, XC_ERR_ARG, "shell without primitives");
+            // Mwfn shell types the reference's AO code evaluates (GridAO.cpp:153-178):
+            // 0 s, 1 Cartesian p (x, y, z), -l pure l >= 1 (m = -l..l; pure p is y, z, x)
+            CGB_CHECK(t == 0 || t == 1 || (t < 0 && -t <= kMaxL), XC_ERR_UNSUPPORTED,
+                      "shell type " + std::to_string(t) + " is not supported (0, 1 or -1..-" +
+                          std::to_string(kMaxL) + ")");
+            Shell s{};
+            s.atom = a;
+            s.l = t < 0 ? -t : t;
+            s.type = t;
+            s.first = first;
+            s.nprim = np;
+            s.prim_off = (int)po;
+            s.x = xyz[3 * a];
+            s.y = xyz[3 * a + 1];
+            s.z = xyz[3 * a + 2];
+            std::vector<double> e(exps + po, exps + po + np), c(coefs + po, coefs + po + np);
+            for (int p = 0; p < np; p++)
+                CGB_CHECK(std::isfinite(e[p]) && e[p] > 0 && std::isfinite(c[p]), XC_ERR_NUMERIC,
+                          "exponents must be positive and finite, coefficients finite");
+            if (normalize) c = renorm_contraction(s.l, e, c);
+            b.exps.insert(b.exps.end(), e.begin(), e.end());
+            b.coefs.insert(b.coefs.end(), c.begin(), c.end());
+            first += shell_size(t);
+            po += np;
+            b.shells.push_back(s);
+        }
+        b.nbasis = first;
+        auto* h = new xc_basis;
+        h->b = std::move(b);
+        *out = h;
+    });
+}
+
 int xc_basis_nbasis(const xc_basis* b, int* n) {
     return guard([&] {
         CGB_CHECK(b && n, XC_ERR_ARG, "null argument");
@@ -694,7 +744,7 @@ int xc_grid_info_get(const xc_grid* g, xc_grid_info* info) {
         info->mixed_empty_tiles = G.mx.ready ? G.mx.empty_tiles : 0;
         info->mixed_presplit = G.mx.ready && G.mx.use16 ? 1 : 0;
         info->mixed_presplit_bytes =
-            info->mixed_presplit ? (long)((G.mx.d_e16.n + G.mx.d_R16.n) * sizeof(__nv_bfloat16)) : 0;
+            info->mixed_presplit ? (long)((G.mx.d_e16.n + G.mx.d_e16d.n + G.mx.d_R16.n) * sizeof(__nv_bfloat16)) : 0;
     });
 }
 

@@ -177,7 +177,7 @@ void sap_table(int Z, std::vector<double>& radii, std::vector<double>& rv) {
 // libint2 Shell::renorm (the normalisation Normalization.cpp:11-18 copies):
 // primitive factor for x^l exp(-a r^2), then the contraction's self-overlap
 // is scaled to one.
-static std::vector<double> renorm(int l, const std::vector<double>& e, std::vector<double> c) {
+std::vector<double> renorm_contraction(int l, const std::vector<double>& e, std::vector<double> c) {
     const double sqrt_pi3 = std::pow(M_PI, 1.5);
     const double df = dfact(2 * l - 1);
     for (size_t p = 0; p < e.size(); p++) {
@@ -246,7 +246,7 @@ BasisSet load_basis(const std::string& name, const std::vector<int>& Z, const st
             s.x = xyz[3 * a];
             s.y = xyz[3 * a + 1];
             s.z = xyz[3 * a + 2];
-            auto c = renorm(r.l, r.e, r.c);
+            auto c = renorm_contraction(r.l, r.e, r.c);
             b.exps.insert(b.exps.end(), r.e.begin(), r.e.end());
             b.coefs.insert(b.coefs.end(), c.begin(), c.end());
             first += shell_size(s.type);

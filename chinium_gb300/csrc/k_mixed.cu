@@ -174,6 +174,27 @@ __device__ __forceinline__ void store_chunk(uint32_t planes, int r, int j, const
     tc::sts128(planes + 2 * kPlaneA + off, l);
 }
 
+// The same for a K range that shares one fixed-point exponent e
+// (tc::split3_fixed_f).
+__device__ __forceinline__ void store_chunk_fixed(uint32_t planes, int r, int j, const float* v, int e) {
+    uint32_t hh[4], mm[4], ll[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        bf16 h0, m0, l0, h1, m1, l1;
+        tc::split3_fixed_f(v[2 * k], e, h0, m0, l0);
+        tc::split3_fixed_f(v[2 * k + 1], e, h1, m1, l1);
+        const __nv_bfloat162 H = __halves2bfloat162(h0, h1), Mv = __halves2bfloat162(m0, m1),
+                             Lv = __halves2bfloat162(l0, l1);
+        hh[k] = *reinterpret_cast<const uint32_t*>(&H);
+        mm[k] = *reinterpret_cast<const uint32_t*>(&Mv);
+        ll[k] = *reinterpret_cast<const uint32_t*>(&Lv);
+    }
+    const uint32_t off = (uint32_t)r * 128u + ((uint32_t)(j ^ (r & 7)) << 4);
+    tc::sts128(planes + off, make_uint4(hh[0], hh[1], hh[2], hh[3]));
+    tc::sts128(planes + kPlaneA + off, make_uint4(mm[0], mm[1], mm[2], mm[3]));
+    tc::sts128(planes + 2 * kPlaneA + off, make_uint4(ll[0], ll[1], ll[2], ll[3]));
+}
+
 // The six split products of one stage into TMEM buffer `buf`: term hh into
 // the hh accumulator, the five corrections into the correction accumulator.
 // `first` starts both accumulators (unit boundary).
@@ -416,30 +437,34 @@ __global__ void __launch_bounds__(kThreads, 1) density_tc_kernel(const __grid_co
     } else if (warp >= 2) {
         // converter warps: the raw Phi tile [64 functions][128 points] is read
         // into registers (releasing the buffer for the next TMA load), split
-        // and stored transposed (point-major) as the stage's A planes
+        // on the fixed-point grid of each point (one exponent over the 64
+        // functions, as split_store_fixed_kernel does for the pre-split
+        // planes: the same slices) and stored transposed (point-major) as the
+        // stage's A planes.  Thread ct < 128 takes point ct; the other
+        // converter threads only take part in the barrier arrivals.
         const int ct = conv_index() * 32 + lane;
         uint32_t uu = 0;
         for (DensCursor c(job_off, jobs, EPI != 1); c.valid(); c.advance(jobs), uu++) {
             if (!warp_wait(sm, &sm.rfull[0], uu & 1, err)) break;
-            float v[kDensItems][8];
+            float v[64];
+            int e = tc::kFixedZero;
             const uint32_t rf = ssm + 2 * kStageBytes;
+            if (ct < 128) {
+                float mx = 0.f;
 #pragma unroll
-            for (int k = 0; k < kDensItems; k++) {
-                const int q = ct + kConvThreads * k;
-                if (q < 1024) {
-                    const int gg = q & 127, jj = q >> 7;
-#pragma unroll
-                    for (int i = 0; i < 8; i++) v[k][i] = tc::lds32f(rf + ((8 * jj + i) * 128 + gg) * 4);
+                for (int f = 0; f < 64; f++) {
+                    v[f] = tc::lds32f(rf + (f * 128 + ct) * 4);
+                    mx = fmaxf(mx, fabsf(v[f]));
                 }
+                e = tc::fixed_exponent((double)mx);
             }
             warp_arrive(&sm.rempty[0]);
             const int s = uu & 1;
             if (!warp_wait(sm, &sm.empty[s], ((uu >> 1) & 1) ^ 1, err)) break;
             const uint32_t st = ssm + s * kStageBytes;
+            if (ct < 128) {
 #pragma unroll
-            for (int k = 0; k < kDensItems; k++) {
-                const int q = ct + kConvThreads * k;
-                if (q < 1024) store_chunk(st, q & 127, q >> 7, v[k]);
+                for (int jj = 0; jj < 8; jj++) store_chunk_fixed(st, ct, jj, v + 8 * jj, e);
             }
             conv_publish(&sm.full[s]);
         }
@@ -974,15 +999,21 @@ __global__ void __launch_bounds__(1024) wsum_kernel(const double* __restrict__ w
 
 // Packed D_m (s, n, n) column-major FP64 -> three BF16 planes per spin of the
 // strip: row f0(m) + nu, col mu, of (D + D^T) / 2 (zero outside the
-// molecule's n x n block).
+// molecule's n x n block).  One warp per (spin, row, 64-column chunk): the
+// chunk's values share one fixed-point exponent (tc::split3_fixed), the K
+// range of one accumulation unit of the density kernel, whose A operand
+// (e16d) shares one exponent per point over the same 64 functions -- so the
+// hh products of a unit accumulate exactly on the tensor core.
 __global__ void split_d_kernel(const double* __restrict__ D, const MolRange* __restrict__ mols, int nmol, int nspin,
                                long drows, int dcols, bf16* __restrict__ Dp) {
-    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long total = (long)nspin * drows * dcols;
-    if (idx >= total) return;
-    const int mu = (int)(idx % dcols);
-    const long row = (idx / dcols) % drows;
-    const int s = (int)(idx / ((long)dcols * drows));
+    const long wid = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const int nch = dcols / 64;
+    const long total = (long)nspin * drows * nch;
+    if (wid >= total) return;  // whole warps leave together (blockDim is a multiple of 32)
+    const int ch = (int)(wid % nch);
+    const long row = (wid / nch) % drows;
+    const int s = (int)(wid / ((long)nch * drows));
     int lo = 0, hi = nmol - 1;  // molecule owning the row (f0 ascending)
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
@@ -993,14 +1024,26 @@ __global__ void split_d_kernel(const double* __restrict__ D, const MolRange* __r
     const long nu = row - m.f0;
     // symmetric part (the tensor-core density uses one triangle of D for rho and tau)
     const double* Ds = D + m.voff + (long)s * m.n * m.n;
-    const double v = (mu < m.n && nu < m.n) ? 0.5 * (Ds[nu * m.n + mu] + Ds[(long)mu * m.n + nu]) : 0.0;
-    bf16 h, md_, l;
-    tc::split3(v, h, md_, l);
+    double v[2];
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        const int mu = ch * 64 + k * 32 + lane;
+        v[k] = (mu < m.n && nu < m.n) ? 0.5 * (Ds[nu * m.n + mu] + Ds[(long)mu * m.n + nu]) : 0.0;
+    }
+    double mx = fmax(fabs(v[0]), fabs(v[1]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    const int e = tc::fixed_exponent(mx);
     const size_t plane = (size_t)drows * dcols;
-    const size_t o = (size_t)row * dcols + mu;
-    Dp[(size_t)(s * 3 + 0) * plane + o] = h;
-    Dp[(size_t)(s * 3 + 1) * plane + o] = md_;
-    Dp[(size_t)(s * 3 + 2) * plane + o] = l;
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        bf16 h, md_, l;
+        tc::split3_fixed(v[k], e, h, md_, l);
+        const size_t o = (size_t)row * dcols + ch * 64 + k * 32 + lane;
+        Dp[(size_t)(s * 3 + 0) * plane + o] = h;
+        Dp[(size_t)(s * 3 + 1) * plane + o] = md_;
+        Dp[(size_t)(s * 3 + 2) * plane + o] = l;
+    }
 }
 
 // Z = c0 phi + c1 . grad phi per kept row (FP32); c2 per point (meta-GGA).
@@ -1051,6 +1094,34 @@ __global__ void split_store_kernel(const float* __restrict__ e32, long n, int nc
     e16[(size_t)(c * 3 + 0) * n + o] = h;
     e16[(size_t)(c * 3 + 1) * n + o] = m;
     e16[(size_t)(c * 3 + 2) * n + o] = l;
+}
+
+// The density kernel's A operand planes: components 0..ncomp-1 of the FP32
+// store split on the fixed-point grid of each (point, 64-function slot): the
+// 64 values of one point in one slot (the K range of a density unit) share
+// one exponent (tc::split3_fixed).  Layout as e16: e16d[(c * 3 + p) * n +
+// row * 128 + g].  One CTA per (component, 64-row slot), thread = point.
+__global__ void __launch_bounds__(128) split_store_fixed_kernel(const float* __restrict__ e32, long rows, int ncomp,
+                                                                bf16* __restrict__ e16d) {
+    const long nslot = rows / 64;
+    const int c = (int)(blockIdx.x / nslot);
+    const long sl = blockIdx.x - (long)c * nslot;
+    const int g = threadIdx.x;
+    if (c >= ncomp) return;
+    const size_t n = (size_t)rows * 128;
+    const float* src = e32 + (size_t)c * n + (size_t)sl * 64 * 128 + g;
+    float mx = 0.f;
+    for (int f = 0; f < 64; f++) mx = fmaxf(mx, fabsf(src[(size_t)f * 128]));
+    const int e = tc::fixed_exponent((double)mx);
+    bf16* dst = e16d + (size_t)(c * 3) * n + (size_t)sl * 64 * 128 + g;
+    for (int f = 0; f < 64; f++) {
+        bf16 h, m, l;
+        tc::split3_fixed_f(src[(size_t)f * 128], e, h, m, l);
+        const size_t o = (size_t)f * 128;
+        dst[o] = h;
+        dst[n + o] = m;
+        dst[2 * n + o] = l;
+    }
 }
 
 // Two consecutive points of one row into the three planes (one 4-byte
@@ -1215,8 +1286,10 @@ void launch_ao_mixed(const MixedDev& md, DevShells sh, const int* tile_shells, c
 
 void launch_split_d(const double* D, const MolRange* mols, int nmol, int nspin, long drows, int dcols, int /*maxn*/,
                     bf16* Dp, cudaStream_t s) {
-    const long total = (long)nspin * drows * dcols;
-    split_d_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(D, mols, nmol, nspin, drows, dcols, Dp);
+    CGB_CHECK(dcols % 64 == 0, XC_ERR_INTERNAL, "density strip width is not a multiple of 64");
+    const long threads = (long)nspin * drows * (dcols / 64) * 32;
+    if (threads == 0) return;
+    split_d_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(D, mols, nmol, nspin, drows, dcols, Dp);
     CGB_CUDA(cudaGetLastError());
 }
 
@@ -1288,6 +1361,13 @@ void launch_fock_tc(const CUtensorMap& tm_e32, const CUtensorMap& tm_z, long row
     if (ctas == 0) return;
     fock_tc_kernel<<<ctas, kThreads, mixed_smem_bytes(), s>>>(tm_e32, tm_z, rows, job_off, jobs, c2, ncomp, wpart,
                                                              err);
+    CGB_CUDA(cudaGetLastError());
+}
+
+void launch_split_store_fixed(const float* e32, long rows, int ncomp, bf16* e16d, cudaStream_t s) {
+    const long blocks = (long)ncomp * (rows / 64);  // kept rows come in 64-row slots
+    if (blocks == 0) return;
+    split_store_fixed_kernel<<<(unsigned)blocks, 128, 0, s>>>(e32, rows, ncomp, e16d);
     CGB_CUDA(cudaGetLastError());
 }
 

@@ -295,7 +295,8 @@ void Grid::prepare_mixed(const MixedConfig& cfg) {
     {
         const int ncv = type >= 2 ? 4 : 1;
         const size_t n16 = (size_t)md.rows * kTilePts;
-        const size_t need = (size_t)(3 * m.ao_comp + 3 * ncv) * n16 * sizeof(__nv_bfloat16);
+        const int ncd = type >= 2 ? 4 : 1;  // components the density kernel takes as its A operand
+        const size_t need = (size_t)(3 * m.ao_comp + 3 * ncv + 3 * ncd) * n16 * sizeof(__nv_bfloat16);
         const size_t e32b = (size_t)m.ao_comp * n16 * sizeof(float);
         size_t freeb = 0, totalb = 0;
         CGB_CUDA(cudaMemGetInfo(&freeb, &totalb));
@@ -460,15 +461,20 @@ void Grid::prepare_mixed(const MixedConfig& cfg) {
         const int ncv = type >= 2 ? 4 : 1;
         const size_t n16 = (size_t)md.rows * kTilePts;
         if (m.use16) {
+            const int ncd = type >= 2 ? 4 : 1;
             m.d_e16.alloc((size_t)3 * m.ao_comp * n16);
+            m.d_e16d.alloc((size_t)3 * ncd * n16);
             m.d_R16.alloc((size_t)3 * ncv * n16);
             launch_split_store(m.d_e32.p, (long)n16, m.ao_comp, m.d_e16.p, s);
+            launch_split_store_fixed(m.d_e32.p, md.rows, ncd, m.d_e16d.p, s);
             make_tmap_bf16(&m.tm_e16, m.d_e16.p, kTilePts, (uint64_t)3 * m.ao_comp * md.rows, 64, 64);
+            make_tmap_bf16(&m.tm_e16d, m.d_e16d.p, kTilePts, (uint64_t)3 * ncd * md.rows, 64, 64);
             make_tmap_bf16(&m.tm_r16, m.d_R16.p, kTilePts, (uint64_t)3 * ncv * md.rows, 64, 64);
             m.d_Z.alloc(1);
             m.d_c2.alloc(1);
         } else {
             m.d_e16.alloc(1);
+            m.d_e16d.alloc(1);
             m.d_R16.alloc(1);
             m.d_Z.alloc((size_t)md.rows * kTilePts);
             m.d_c2.alloc(type >= 2 ? (size_t)md.Gt : 1);
@@ -540,7 +546,7 @@ void Grid::density_passes(const __nv_bfloat16*) {
     }
     const auto pass = [&](int epi, int acomp, int s) {
         if (m.use16)
-            launch_density16(m.tm_d, m.tm_e16, md, m.dens_ctas, m.d_dens_off.p, m.d_dens_jobs.p, epi, acomp, s, m.rho.p,
+            launch_density16(m.tm_d, m.tm_e16d, md, m.dens_ctas, m.d_dens_off.p, m.d_dens_jobs.p, epi, acomp, s, m.rho.p,
                              m.rho1.p, m.tau.p, m.rho_b.p, m.rho1_b.p, m.tau_b.p, m.d_err.p, stream);
         else
             launch_density_tc(m.tm_d, m.tm_raw_d, md, m.dens_ctas, m.d_dens_off.p, m.d_dens_jobs.p, epi, acomp, s,

@@ -107,6 +107,7 @@ struct MixedState {
     DevBuf<float> d_e32, d_Z, d_c2;
     bool use16 = false;                  // V kernel on pre-split planes
     DevBuf<__nv_bfloat16> d_e16, d_R16;  // AO store planes [c][p][rows][128]; R planes [c][p][rows][128]
+    DevBuf<__nv_bfloat16> d_e16d;        // density A planes [c][p][rows][128], fixed point per (point, slot)
     DevBuf<__nv_bfloat16> d_Dp;
     DevBuf<double> d_wpart;
     DevBuf<int> d_err;
@@ -122,6 +123,7 @@ struct MixedState {
     CUtensorMap tm_raw_f;                  // e32, box 32 points x 64 rows (V_xc L / R boxes)
     CUtensorMap tm_z;                      // Z, box 32 points x 64 rows
     CUtensorMap tm_e16, tm_r16;            // BF16 planes of e16 / R16, box 64 points x 64 rows
+    CUtensorMap tm_e16d;                   // BF16 planes of e16d, box 64 points x 64 rows
     // CUDA graph of one build (replayed while the functional and buffers are unchanged)
     cudaGraphExec_t graph = nullptr;
     std::vector<int> graph_ids;  // functional (libxc ids) and grid type the graph was captured for
@@ -157,6 +159,9 @@ void launch_fock_tc(const CUtensorMap& tm_e32, const CUtensorMap& tm_z, long row
                     const FockJob* jobs, const float* c2, int ncomp, double* wpart, int* err, cudaStream_t s);
 // FP32 store (ncomp planes of n) -> BF16 planes e16[(c * 3 + p) * n + i].
 void launch_split_store(const float* e32, long n, int ncomp, __nv_bfloat16* e16, cudaStream_t s);
+// Components 0..ncomp-1 of the FP32 store (rows x 128 each) -> the density
+// kernel's A planes, one fixed-point exponent per (point, 64-row slot).
+void launch_split_store_fixed(const float* e32, long rows, int ncomp, __nv_bfloat16* e16d, cudaStream_t s);
 // R planes of the pre-split V kernel: Z (component 0) and c2 d_c phi (1-3, meta-GGA).
 void launch_prep16(const MixedDev& md, int type, const double* fcoef, __nv_bfloat16* R16, cudaStream_t s);
 void launch_fock16(const CUtensorMap& tm_l, const CUtensorMap& tm_r, long rows, int ctas, const int* job_off,

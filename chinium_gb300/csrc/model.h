@@ -51,6 +51,9 @@ void set_data_path(const std::string& p);
 const std::vector<double>& lebedev_rule(int npoints);  // 4*npoints: x y z w
 const GridRecipe& grid_recipe(const std::string& grid, int Z);
 BasisSet load_basis(const std::string& name, const std::vector<int>& Z, const std::vector<double>& xyz);
+// libint2's renormalisation of one contracted shell (primitive factors for
+// x^l exp(-a r^2), then unit self-overlap), as Normalization.cpp:11-18 applies it.
+std::vector<double> renorm_contraction(int l, const std::vector<double>& e, std::vector<double> c);
 void sap_table(int Z, std::vector<double>& radii, std::vector<double>& rv);  // 751 entries each
 
 // Solid-harmonic coefficient table: coef[l][i][k] for function i (m = i - l)

@@ -234,5 +234,62 @@ __device__ __forceinline__ void split3f(float x, __nv_bfloat16& h, __nv_bfloat16
     l = __float2bfloat16_rn(r);
 }
 
+// Binary exponent shared by a group of values for split3_fixed: e with
+// 2^e <= max|x| < 2^(e+1), or kFixedZero when the group is negligible
+// (max|x| < 2^-100: its slices are zero).
+constexpr int kFixedZero = -100000;
+__device__ __forceinline__ int fixed_exponent(double maxabs) {
+    return maxabs >= 0x1p-100 ? ilogb(maxabs) : kFixedZero;
+}
+
+// Three-term split on the fixed-point grid of a group (x ~= h + m + l, error
+// <= 2^(e-24)): h, m and l are integer multiples of 2^(e-7), 2^(e-15) and
+// 2^(e-23) with at most 8 significant bits (|h| <= 256 units, |m|, |l| <= 128),
+// each rounded to nearest and so exact in BF16.  When both operands of a
+// product are split this way with one exponent per row of A and per column
+// of B over the K range of an accumulation, every hh product of that sum is
+// an integer (|.| <= 2^16) times one common power of two, so a K <= 256 sum
+// of them is exact in FP32 whatever the order or rounding mode of the
+// accumulator: the tensor core's FP32 accumulation adds no error (and no
+// truncation bias) to the leading term.
+__device__ __forceinline__ void split3_fixed(double x, int e, __nv_bfloat16& h, __nv_bfloat16& m,
+                                             __nv_bfloat16& l) {
+    if (e == kFixedZero) {
+        h = m = l = __double2bfloat16(0.0);
+        return;
+    }
+    const double a = ldexp(rint(ldexp(x, 7 - e)), e - 7);
+    const double r1 = x - a;
+    const double b = ldexp(rint(ldexp(r1, 15 - e)), e - 15);
+    const double r2 = r1 - b;
+    const double c = ldexp(rint(ldexp(r2, 23 - e)), e - 23);
+    h = __double2bfloat16(a);
+    m = __double2bfloat16(b);
+    l = __double2bfloat16(c);
+}
+
+// 2^k as a float for -126 <= k <= 127.
+__device__ __forceinline__ float pow2f(int k) { return __int_as_float((127 + k) << 23); }
+
+// split3_fixed for a float x, in float arithmetic: every step is exact (scaling
+// by powers of two within the normal range, rounding to an integer, exact
+// differences), so it gives the same slices as the double version.  Needs
+// -100 <= e <= 103 or e == kFixedZero (fixed_exponent of a float group).
+__device__ __forceinline__ void split3_fixed_f(float x, int e, __nv_bfloat16& h, __nv_bfloat16& m,
+                                               __nv_bfloat16& l) {
+    if (e == kFixedZero) {
+        h = m = l = __float2bfloat16_rn(0.f);
+        return;
+    }
+    const float a = rintf(x * pow2f(7 - e)) * pow2f(e - 7);
+    const float r1 = x - a;
+    const float b = rintf(r1 * pow2f(15 - e)) * pow2f(e - 15);
+    const float r2 = r1 - b;
+    const float c = rintf(r2 * pow2f(23 - e)) * pow2f(e - 23);
+    h = __float2bfloat16_rn(a);
+    m = __float2bfloat16_rn(b);
+    l = __float2bfloat16_rn(c);
+}
+
 }  // namespace tc
 }  // namespace cgb

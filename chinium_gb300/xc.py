@@ -28,22 +28,51 @@ def _p(a):
 
 class Basis:
     """Centres plus libint2-normalised contracted shells for a named basis
-    set (the Mwfn basis after Normalize(), Representation.cpp:30-53)."""
+    set (the Mwfn basis after Normalize(), Representation.cpp:30-53), or,
+    through ``Basis.from_shells``, the caller's own shells."""
 
     def __init__(self, Z, xyz_bohr, name):
+        Z, xyz = self._centres(Z, xyz_bohr)
+        self.Z, self.xyz, self.name = Z, xyz, name
+        h = ctypes.c_void_p()
+        check(lib().xc_basis_create(len(Z), _p(Z), _p(xyz), name.encode(), ctypes.byref(h)))
+        self._adopt(h)
+
+    @staticmethod
+    def _centres(Z, xyz_bohr):
         Z = np.ascontiguousarray(Z, dtype=np.int32)
         xyz = np.ascontiguousarray(np.asarray(xyz_bohr, dtype=np.float64).reshape(-1, 3))
         if len(Z) != len(xyz):
             raise ValueError("Z and coordinates differ in length")
-        self.Z = Z
-        self.xyz = xyz
-        self.name = name
-        h = ctypes.c_void_p()
-        check(lib().xc_basis_create(len(Z), _p(Z), _p(xyz), name.encode(), ctypes.byref(h)))
+        return Z, xyz
+
+    def _adopt(self, h):
         self._h = h
         n = ctypes.c_int()
         check(lib().xc_basis_nbasis(h, ctypes.byref(n)))
         self.nbasis = n.value
+
+    @classmethod
+    def from_shells(cls, Z, xyz_bohr, atom, type, nprim, exps, coefs, normalize=False):
+        """The caller's shells (the Mwfn's centres and shells): per shell its
+        atom, type (0 s, 1 Cartesian p, -l pure) and primitive count, with
+        exps / coefs shell by shell; coefs normalised by the caller
+        (NormalizedCoefficients) unless normalize=True."""
+        self = cls.__new__(cls)
+        Z, xyz = cls._centres(Z, xyz_bohr)
+        self.Z, self.xyz, self.name = Z, xyz, None
+        atom = np.ascontiguousarray(atom, dtype=np.int32)
+        typ = np.ascontiguousarray(type, dtype=np.int32)
+        npr = np.ascontiguousarray(nprim, dtype=np.int32)
+        e = np.ascontiguousarray(exps, dtype=np.float64)
+        c = np.ascontiguousarray(coefs, dtype=np.float64)
+        if not (len(atom) == len(typ) == len(npr)) or len(e) != int(npr.sum()) or len(c) != len(e):
+            raise ValueError("shell arrays differ in length")
+        h = ctypes.c_void_p()
+        check(lib().xc_basis_create_shells(len(Z), _p(Z), _p(xyz), len(atom), _p(atom), _p(typ), _p(npr), _p(e),
+                                           _p(c), int(bool(normalize)), ctypes.byref(h)))
+        self._adopt(h)
+        return self
 
     def shells(self):
         L = lib()

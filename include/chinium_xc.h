@@ -67,6 +67,20 @@ int xc_set_data_path(const char* path);
  * Cartesian (x, y, z); d and higher are pure (m = -l..l). */
 int xc_basis_create(int natoms, const int* Z, const double* xyz_bohr, const char* basis_name,
                     xc_basis** out);
+/* Centres and shells from the caller's own basis, as Grid::Grid(Mwfn*, ...)
+ * reads them (GridGeneration.cpp:232-271 through SubGrid::getAO,
+ * GridAO.cpp:14-215: per MwfnShell its centre, Type, Exponents and
+ * NormalizedCoefficients).  Shells in basis-function order; per shell its
+ * atom (0..natoms-1), type (0 s, 1 Cartesian p in x, y, z order, -l pure
+ * l = 1..4 with m = -l..l, pure p being y, z, x) and primitive count;
+ * exps/coefs of length sum(nprim), shell by shell.  normalize = 0 takes
+ * coefs as normalised by the caller (the Mwfn's NormalizedCoefficients
+ * after Normalize(), Normalization.cpp:11-18); normalize = 1 applies that
+ * libint2 renormalisation to raw contraction coefficients.  Z gives the
+ * Becke partition and the SG-n recipe of each atom. */
+int xc_basis_create_shells(int natoms, const int* Z, const double* xyz_bohr, int nshells,
+                           const int* shell_atom, const int* shell_type, const int* nprim,
+                           const double* exps, const double* coefs, int normalize, xc_basis** out);
 int xc_basis_nbasis(const xc_basis* b, int* nbasis);
 /* Shell layout: per shell its atom, type (0 S, 1 Cartesian P, -l pure l),
  * first function index and primitive count; arrays of length nshells. */

@@ -211,3 +211,54 @@ def test_response_entry_points_validate_arguments_on_the_host():
         assert L.xc_functional_fxc_points(f, 1, p, p, p, p, p) == -6  # TPSS: no "f" (as the reference)
     finally:
         L.xc_functional_destroy(f)
+
+
+@pytest.mark.parametrize("mol,basis", [("h2o", "def2-svp"), ("c18", "def2-tzvp"), ("fe4s4", "def2-tzvp")])
+def test_basis_from_caller_shells_equals_named_basis(mol, basis):
+    """xc_basis_create_shells on the shells a named basis exports (its
+    normalised coefficients, as the Mwfn's NormalizedCoefficients) gives the
+    same basis; with raw contraction coefficients and normalize=1 the
+    libint2 renormalisation reproduces the normalised ones."""
+    Z, xyz = getattr(M, mol)()
+    b = cg.Basis(Z, xyz, basis)
+    sh = b.shells()
+    b2 = cg.Basis.from_shells(Z, xyz, sh["atom"], sh["type"], sh["nprim"], sh["exps"], sh["coefs"])
+    assert b2.nbasis == b.nbasis
+    sh2 = b2.shells()
+    for k in ("atom", "type", "first", "nprim", "exps", "coefs"):
+        assert np.array_equal(sh2[k], sh[k]), k
+    # raw coefficients from the basis table, renormalised by the library
+    table = O.load_basis(basis)
+    raw = np.concatenate([c for z in Z for (_, _, c) in table[z]])
+    b3 = cg.Basis.from_shells(Z, xyz, sh["atom"], sh["type"], sh["nprim"], sh["exps"], raw, normalize=True)
+    assert np.allclose(b3.shells()["coefs"], sh["coefs"], rtol=1e-14, atol=0)
+
+
+def test_basis_from_shells_validates_arguments():
+    Z, xyz = M.h2o()
+    L = lib()
+    h = ctypes.c_void_p()
+    Zi = np.array(Z, dtype=np.int32)
+    X = np.ascontiguousarray(xyz, dtype=np.float64)
+    atom = np.array([0, 7], dtype=np.int32)
+    typ = np.array([0, 0], dtype=np.int32)
+    npr = np.array([1, 1], dtype=np.int32)
+    e = np.array([1.0, 2.0])
+    c = np.array([1.0, 1.0])
+    p = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    # atom index out of range
+    assert L.xc_basis_create_shells(3, p(Zi), p(X), 2, p(atom), p(typ), p(npr), p(e), p(c), 0, ctypes.byref(h)) == -1
+    atom[1] = 1
+    # Cartesian d (type 2) is not a shell type the reference's grid evaluates
+    typ[1] = 2
+    assert L.xc_basis_create_shells(3, p(Zi), p(X), 2, p(atom), p(typ), p(npr), p(e), p(c), 0, ctypes.byref(h)) == -6
+    typ[1] = -1  # pure p (y, z, x) is
+    e[1] = -2.0
+    assert L.xc_basis_create_shells(3, p(Zi), p(X), 2, p(atom), p(typ), p(npr), p(e), p(c), 0, ctypes.byref(h)) == -7
+    e[1] = 2.0
+    assert L.xc_basis_create_shells(3, p(Zi), p(X), 2, p(atom), p(typ), p(npr), p(e), p(c), 2, ctypes.byref(h)) == -1
+    assert L.xc_basis_create_shells(3, p(Zi), p(X), 2, p(atom), p(typ), p(npr), p(e), p(c), 1, None) == -1
+    assert L.xc_basis_create_shells(3, p(Zi), p(X), 2, p(atom), p(typ), p(npr), p(e), p(c), 1, ctypes.byref(h)) == 0
+    n = ctypes.c_int()
+    assert L.xc_basis_nbasis(h, ctypes.byref(n)) == 0 and n.value == 4
+    L.xc_basis_destroy(h)

@@ -270,3 +270,19 @@ def test_xc_gradient_rejects_meta_gga(h2o):
     with pytest.raises(cg.XCError) as e:
         g.getEnergyGrad(xc, [model_density(og, 5)])
     assert e.value.code == -6
+
+
+def test_grid_from_caller_shells_is_bitwise_the_named_basis(h2o):
+    """xc_basis_create_shells with the shells of the named basis (normalised
+    coefficients, as the Mwfn's NormalizedCoefficients): bitwise the same
+    E_xc and V_xc, FP64 and tensor-core paths."""
+    Z, xyz, b, ob, og = h2o
+    sh = b.shells()
+    b2 = cg.Basis.from_shells(Z, xyz, sh["atom"], sh["type"], sh["nprim"], sh["exps"], sh["coefs"])
+    D = model_density(og, 5)
+    xc = cg.ExchangeCorrelation().Read("PBE")
+    for prec in (cg.PRECISION_FP64, cg.PRECISION_MIXED):
+        E1, V1 = make_grid(b).build(xc, [D], precision=prec)
+        E2, V2 = make_grid(b2).build(xc, [D], precision=prec)
+        assert E1 == E2
+        assert np.array_equal(V1[0], V2[0])
