@@ -114,6 +114,12 @@ SIGNATURES = {
     "xc_int1e": [_P, _P, _P, _P],
     "xc_dipole": [_P, _P, _P],
     "xc_eri": [_P, _P, _D],
+    "xc_jk_create": [_P, _D, _D, _PP],
+    "xc_jk_destroy": [_P],
+    "xc_jk_info": [_P, _P, _P, _P],
+    "xc_jk_set_stream": [_P, _P],
+    "xc_jk_build": [_P, _I, _P, _P, _P],
+    "xc_jk_build_device": [_P, _I, _P, _P, _P],
     "xc_grid_profile": [_P, _I],
     "xc_grid_stage_ms": [_P, _P],
     "xc_grid_kernel_ms": [_P, _P],

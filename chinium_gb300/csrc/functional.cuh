@@ -35,7 +35,7 @@ namespace xcf {
 template <class R, int N>
 struct Dual {
     R v;
-    R d[N];
+    R d[N > 0 ? N : 1];  // N = 0: value only (the slot is never read)
     CGB_HD Dual() {}
     CGB_HD Dual(R x) : v(x) {
 #pragma unroll
@@ -597,11 +597,13 @@ CGB_HD T e_sum(const FuncDesc& f, const XIn<T>& v) {
     return e;
 }
 
-// Restricted point: inputs rho, sigma, tau (totals).  Outputs eps and
-// d e / d (rho, sigma, tau).  Returns false when below the density threshold.
-template <class R, int FAM>
-CGB_HDN bool eval_unpol(const FuncDesc& f, R rho, R sigma, R tau, R& eps, R* dv) {
-    constexpr int N = FAM == 0 ? 1 : (FAM == 1 ? 2 : 3);
+// Restricted point: inputs rho, sigma, tau (totals).  Outputs eps and, with
+// DERIV, d e / d (rho, sigma, tau).  Returns false when below the density
+// threshold.  Without DERIV no direction is seeded (Dual<R, 0>: the value
+// alone, a fraction of the arithmetic).
+template <class R, int FAM, bool DERIV>
+CGB_HDN bool eval_unpol_t(const FuncDesc& f, R rho, R sigma, R tau, R& eps, R* dv) {
+    constexpr int N = !DERIV ? 0 : (FAM == 0 ? 1 : (FAM == 1 ? 2 : 3));
     using T = Dual<R, N>;
     if (!(rho >= R(kDensThr))) {
         eps = R(0);
@@ -609,9 +611,9 @@ CGB_HDN bool eval_unpol(const FuncDesc& f, R rho, R sigma, R tau, R& eps, R* dv)
         return false;
     }
     T r(rho), s(sigma), t(tau);
-    r.d[0] = R(1);
-    if (N > 1) s.d[1 % N] = R(1);
-    if (N > 2) t.d[2 % N] = R(1);
+    if constexpr (N > 0) r.d[0] = R(1);
+    if constexpr (N > 1) s.d[1] = R(1);
+    if constexpr (N > 2) t.d[2] = R(1);
     s = tmax(s, T(R(1.0000000000000011e-40)));  // kDensThr^(8/3)
     if (FAM >= 2) {
         t = tmax(t, T(R(kTauThr)));
@@ -623,11 +625,21 @@ CGB_HDN bool eval_unpol(const FuncDesc& f, R rho, R sigma, R tau, R& eps, R* dv)
     for (int i = 0; i < N; i++) dv[i] = e.d[i];
     return true;
 }
-
-// Unrestricted point: in = (ra, rb, saa, sab, sbb, ta, tb); dv in the same order.
 template <class R, int FAM>
-CGB_HDN bool eval_pol(const FuncDesc& f, const R* in, R& eps, R* dv) {
-    constexpr int N = FAM == 0 ? 2 : (FAM == 1 ? 5 : 7);
+CGB_HD bool eval_unpol(const FuncDesc& f, R rho, R sigma, R tau, R& eps, R* dv) {
+    return eval_unpol_t<R, FAM, true>(f, rho, sigma, tau, eps, dv);
+}
+// eps alone.
+template <class R, int FAM>
+CGB_HD bool eval_unpol_value(const FuncDesc& f, R rho, R sigma, R tau, R& eps) {
+    return eval_unpol_t<R, FAM, false>(f, rho, sigma, tau, eps, nullptr);
+}
+
+// Unrestricted point: in = (ra, rb, saa, sab, sbb, ta, tb); dv in the same
+// order (with DERIV; without it eps alone, as eval_unpol_t).
+template <class R, int FAM, bool DERIV>
+CGB_HDN bool eval_pol_t(const FuncDesc& f, const R* in, R& eps, R* dv) {
+    constexpr int N = !DERIV ? 0 : (FAM == 0 ? 2 : (FAM == 1 ? 5 : 7));
     using T = Dual<R, N>;
     const R rt = in[0] + in[1];
     if (!(rt >= R(kDensThr))) {
@@ -638,7 +650,8 @@ CGB_HDN bool eval_pol(const FuncDesc& f, const R* in, R& eps, R* dv) {
     T x[7];
     for (int i = 0; i < 7; i++) {
         x[i] = T(in[i]);
-        if (i < N) x[i].d[i] = R(1);
+        if constexpr (N > 0)
+            if (i < N) x[i].d[i] = R(1);
     }
     XIn<T> v{x[0], x[1], x[2], x[3], x[4], x[5], x[6]};
     v.ra = tmax(v.ra, T(R(kDensThr)));
@@ -657,6 +670,14 @@ CGB_HDN bool eval_pol(const FuncDesc& f, const R* in, R& eps, R* dv) {
     eps = e.v / rt;
     for (int i = 0; i < N; i++) dv[i] = e.d[i];
     return true;
+}
+template <class R, int FAM>
+CGB_HD bool eval_pol(const FuncDesc& f, const R* in, R& eps, R* dv) {
+    return eval_pol_t<R, FAM, true>(f, in, eps, dv);
+}
+template <class R, int FAM>
+CGB_HD bool eval_pol_value(const FuncDesc& f, const R* in, R& eps) {
+    return eval_pol_t<R, FAM, false>(f, in, eps, nullptr);
 }
 
 // ------------------------------------------------ second derivatives ("f")

@@ -16,6 +16,7 @@
 #include "common.h"
 #include "model.h"
 #include "xc_state.h"
+#include "eri.h"
 
 namespace cgb {
 namespace {
@@ -394,6 +395,77 @@ void scatter_quartet(const CShell& a, const CShell& b, const CShell& c, const CS
 }
 
 }  // namespace
+
+// Hermite data of the pure function products of shell pairs for the GPU
+// integral engine (eri.h): per primitive pair kept (overlap charge
+// |c_i c_j| exp(-mu R^2) (pi / p)^(3/2) >= prim_cut) its exponent sum, product
+// centre and Ep[fa * nb + fb][h(t, u, v)] with the coefficients folded in.
+// OpenMP over the pairs.
+void eri_pairs_hermite(const BasisSet& b, const std::vector<std::pair<int, int>>& pairs, double prim_cut,
+                       std::vector<PairHermite>& out) {
+    const std::vector<CShell> sh = make_shells(b);
+    out.assign(pairs.size(), PairHermite{});
+#pragma omp parallel for schedule(dynamic)
+    for (long ip = 0; ip < (long)pairs.size(); ip++) {
+        const CShell &a = sh[pairs[ip].first], &c = sh[pairs[ip].second];
+        PairHermite& o = out[ip];
+        const int L = a.l + c.l, H = (L + 1) * (L + 2) * (L + 3) / 6;
+        const int nab = a.nfunc * c.nfunc;
+        Herm1 hx, hy, hz;
+        std::vector<double> cartE((size_t)a.ncart * c.ncart * H);
+        double R2 = 0;
+        for (int k = 0; k < 3; k++) R2 += (a.A[k] - c.A[k]) * (a.A[k] - c.A[k]);
+        for (size_t i = 0; i < a.exps.size(); i++)
+            for (size_t j = 0; j < c.exps.size(); j++) {
+                const double ea = a.exps[i], eb = c.exps[j], p = ea + eb;
+                const double cc = a.coefs[i] * c.coefs[j];
+                if (std::fabs(cc) * std::exp(-ea * eb / p * R2) * std::pow(M_PI / p, 1.5) < prim_cut) continue;
+                hermite_e(a.l, c.l, ea, eb, a.A[0], c.A[0], hx);
+                hermite_e(a.l, c.l, ea, eb, a.A[1], c.A[1], hy);
+                hermite_e(a.l, c.l, ea, eb, a.A[2], c.A[2], hz);
+                std::fill(cartE.begin(), cartE.end(), 0.0);
+                for (int ka = 0; ka < a.ncart; ka++)
+                    for (int kb = 0; kb < c.ncart; kb++) {
+                        const int ix = a.ca[ka], iy = a.cb[ka], iz = a.cc[ka];
+                        const int jx = c.ca[kb], jy = c.cb[kb], jz = c.cc[kb];
+                        double* dst = &cartE[((size_t)ka * c.ncart + kb) * H];
+                        for (int t = 0; t <= ix + jx; t++)
+                            for (int u = 0; u <= iy + jy; u++)
+                                for (int v = 0; v <= iz + jz; v++) {
+                                    const int N = t + u + v, m = N - t;
+                                    dst[N * (N + 1) * (N + 2) / 6 + m * (m + 1) / 2 + (m - u)] =
+                                        cc * hx.E[ix][jx][t] * hy.E[iy][jy][u] * hz.E[iz][jz][v];
+                                }
+                    }
+                o.p.push_back(p);
+                for (int k = 0; k < 3; k++) o.P.push_back((ea * a.A[k] + eb * c.A[k]) / p);
+                const size_t off = o.ep.size();
+                o.ep.resize(off + (size_t)nab * H, 0.0);
+                for (int fa = 0; fa < a.nfunc; fa++)
+                    for (int fb = 0; fb < c.nfunc; fb++) {
+                        double* dst = &o.ep[off + ((size_t)fa * c.nfunc + fb) * H];
+                        for (int ka = 0; ka < a.ncart; ka++) {
+                            const double ta = a.T[(size_t)fa * a.ncart + ka];
+                            if (ta == 0) continue;
+                            for (int kb = 0; kb < c.ncart; kb++) {
+                                const double tb = c.T[(size_t)fb * c.ncart + kb];
+                                if (tb == 0) continue;
+                                const double* src = &cartE[((size_t)ka * c.ncart + kb) * H];
+                                for (int h = 0; h < H; h++) dst[h] += ta * tb * src[h];
+                            }
+                        }
+                    }
+            }
+    }
+}
+
+// Boys function table F_n(i * step), n < cols, i < rows (series and downward
+// recursion of boys(), ~1e-16 relative).
+void boys_table(int rows, int cols, double step, double* out) {
+#pragma omp parallel for
+    for (int i = 0; i < rows; i++) boys(cols - 1, i * step, out + (size_t)i * cols);
+}
+
 }  // namespace cgb
 
 using namespace cgb;

@@ -1,0 +1,312 @@
+// Electron-repulsion integrals (McMurchie-Davidson, FP64) and their
+// contraction into Coulomb and exchange matrices: the GPU counterpart of the
+// reference's in-core Int4C2E (CalculateIntegrals, then ContractInts /
+// Gunified every SCF iteration, src/Integral/Int4C2E.cpp:567-683).
+//
+// eri_kernel: one CTA (128 threads) per shell quartet of the screened list.
+// Per primitive quartet the threads evaluate the Boys function F_0..F_L
+// (tabulated Taylor expansion), the Hermite Coulomb integrals R_tuv by the
+// MD recursion level by level in shared memory, the ket half-transform
+//   X[cd][h] = sum_h' (-1)^|h'| Ep_cd[cd][h'] R_{h + h'}
+// and the bra contraction I[ab][cd] += pre sum_h Ep_ab[ab][h] X[cd][h].
+// The block of pure integrals [fa][fb][fc][fd] is written once.
+//
+// jk_contract_kernel: one CTA per quartet block; the block is staged in
+// shared memory (one read from HBM) and each thread forms one element of
+// the six J / K sub-blocks it feeds (2 J, 4 K), scaled by the quartet's
+// degeneracy, with one FP64 atomic per element.
+#include "common.h"
+#include "eri.h"
+
+namespace cgb {
+namespace {
+
+constexpr int kEriThreads = 128;
+constexpr int kHMax = herm_count(kEriMaxLt);        // 455
+constexpr int kHabMax = herm_count(2 * kEriMaxL);   // 84
+constexpr int kNf = 2 * kEriMaxL + 1;               // 7 pure functions per shell at most
+constexpr int kXMax = kNf * kNf * kHabMax;          // 4116
+constexpr int kIMax = kNf * kNf * kNf * kNf;        // 2401
+
+// (t | u << 8 | v << 16 | (t + u + v) << 24) of Hermite index h.
+__constant__ unsigned c_tuv[kHMax];
+
+__device__ __forceinline__ int hidx(int t, int u, int v) {
+    const int N = t + u + v, a = N - t;
+    return N * (N + 1) * (N + 2) / 6 + a * (a + 1) / 2 + (a - u);
+}
+
+// F_n(T): Taylor expansion about the nearest table point (|dT| <= 0.025,
+// seven terms: relative error ~1e-15), asymptotic form beyond the table.
+__device__ __forceinline__ double boys_n(int n, double T, const double* __restrict__ tab) {
+    if (T >= kBoysTmax) {
+        double f = 0.5 * sqrt(3.14159265358979323846 / T);
+        for (int k = 1; k <= n; k++) f *= (2 * k - 1) / (2.0 * T);
+        return f;
+    }
+    const int i = (int)(T * (1.0 / kBoysStep) + 0.5);
+    const double x = i * kBoysStep - T;
+    const double* row = tab + (size_t)i * kBoysCols + n;
+    double r = __ldg(row + 6);
+#pragma unroll
+    for (int k = 5; k >= 0; k--) r = __ldg(row + k) + r * x * (1.0 / (k + 1));
+    return r;
+}
+
+struct EriSmem {
+    double R[2][kHMax];
+    double X[kXMax];
+    double I[kIMax];
+    double F[kEriMaxLt + 1];
+    double sc[6];  // alpha, X_PQ, Y_PQ, Z_PQ, T, prefactor
+};
+
+__global__ void __launch_bounds__(kEriThreads) eri_kernel(EriDev e, const int2* __restrict__ quartets,
+                                                          const long long* __restrict__ out_off, long long q0,
+                                                          long long base, double* __restrict__ out) {
+    extern __shared__ double smem_d[];
+    EriSmem& sm = *reinterpret_cast<EriSmem*>(smem_d);
+    const long long q = q0 + blockIdx.x;
+    const int tid = threadIdx.x;
+    const int2 pq = quartets[q];
+    const EriPair P = e.pairs[pq.x], Q = e.pairs[pq.y];
+    const int Lab = P.la + P.lb, Lcd = Q.la + Q.lb, L = Lab + Lcd;
+    const int Hab = herm_count(Lab), Hcd = herm_count(Lcd);
+    const int nab = P.na * P.nb, ncd = Q.na * Q.nb, nI = nab * ncd, nX = ncd * Hab;
+    for (int i = tid; i < nI; i += kEriThreads) sm.I[i] = 0.0;
+    for (int ij = 0; ij < P.npp; ij++) {
+        const int pi = P.pp0 + ij;
+        const double p = e.pp_p[pi];
+        const double* __restrict__ Eab = e.ep + P.ep0 + (long long)ij * nab * Hab;
+        for (int kl = 0; kl < Q.npp; kl++) {
+            const int qi = Q.pp0 + kl;
+            const double* __restrict__ Ecd = e.ep + Q.ep0 + (long long)kl * ncd * Hcd;
+            if (tid == 0) {
+                const double qq = e.pp_p[qi];
+                const double alpha = p * qq / (p + qq);
+                const double X = e.pp_P[3 * pi] - e.pp_P[3 * qi], Y = e.pp_P[3 * pi + 1] - e.pp_P[3 * qi + 1],
+                             Z = e.pp_P[3 * pi + 2] - e.pp_P[3 * qi + 2];
+                sm.sc[0] = alpha;
+                sm.sc[1] = X;
+                sm.sc[2] = Y;
+                sm.sc[3] = Z;
+                sm.sc[4] = alpha * (X * X + Y * Y + Z * Z);
+                sm.sc[5] = 34.98683665524972 / (p * qq * sqrt(p + qq));  // 2 pi^(5/2)
+            }
+            __syncthreads();
+            const double alpha = sm.sc[0], Xp = sm.sc[1], Yp = sm.sc[2], Zp = sm.sc[3], T = sm.sc[4];
+            if (tid <= L) {
+                // (-2 alpha)^n F_n(T): the level-n value of R_000
+                double m = 1.0;
+                for (int k = 0; k < tid; k++) m *= -2.0 * alpha;
+                sm.F[tid] = m * boys_n(tid, T, e.boys);
+            }
+            __syncthreads();
+            // MD recursion, level n = L .. 0 (level n holds N <= L - n), ping-pong buffers
+            if (tid == 0) sm.R[L & 1][0] = sm.F[L];
+            __syncthreads();
+            for (int n = L - 1; n >= 0; n--) {
+                const int b = n & 1, hn = herm_count(L - n);
+                const double* __restrict__ up = sm.R[b ^ 1];
+                for (int h = tid; h < hn; h += kEriThreads) {
+                    double v;
+                    if (h == 0) {
+                        v = sm.F[n];
+                    } else {
+                        const unsigned c = c_tuv[h];
+                        const int t = c & 255, u = (c >> 8) & 255, w = (c >> 16) & 255;
+                        if (t > 0) {
+                            v = Xp * up[hidx(t - 1, u, w)];
+                            if (t > 1) v += (t - 1) * up[hidx(t - 2, u, w)];
+                        } else if (u > 0) {
+                            v = Yp * up[hidx(t, u - 1, w)];
+                            if (u > 1) v += (u - 1) * up[hidx(t, u - 2, w)];
+                        } else {
+                            v = Zp * up[hidx(t, u, w - 1)];
+                            if (w > 1) v += (w - 1) * up[hidx(t, u, w - 2)];
+                        }
+                    }
+                    sm.R[b][h] = v;
+                }
+                __syncthreads();
+            }
+            const double* __restrict__ R0 = sm.R[0];
+            // ket half-transform
+            for (int i = tid; i < nX; i += kEriThreads) {
+                const int cd = i / Hab, ha = i - cd * Hab;
+                const unsigned c1 = c_tuv[ha];
+                const int t1 = c1 & 255, u1 = (c1 >> 8) & 255, v1 = (c1 >> 16) & 255;
+                const double* __restrict__ ec = Ecd + cd * Hcd;
+                double acc = 0.0;
+                for (int hc = 0; hc < Hcd; hc++) {
+                    const unsigned c2 = c_tuv[hc];
+                    const double term = __ldg(ec + hc) * R0[hidx(t1 + (c2 & 255), u1 + ((c2 >> 8) & 255),
+                                                                v1 + ((c2 >> 16) & 255))];
+                    acc += ((c2 >> 24) & 1) ? -term : term;
+                }
+                sm.X[i] = acc;
+            }
+            __syncthreads();
+            const double pre = sm.sc[5];
+            for (int i = tid; i < nI; i += kEriThreads) {
+                const int ab = i / ncd, cd = i - ab * ncd;
+                const double* __restrict__ ea = Eab + ab * Hab;
+                const double* __restrict__ x = sm.X + cd * Hab;
+                double acc = 0.0;
+                for (int h = 0; h < Hab; h++) acc = fma(__ldg(ea + h), x[h], acc);
+                sm.I[i] = fma(pre, acc, sm.I[i]);
+            }
+            __syncthreads();
+        }
+    }
+    double* o = out + (out_off[q] - base);
+    for (int i = tid; i < nI; i += kEriThreads) o[i] = sm.I[i];
+}
+
+// One CTA per quartet block: stage it, then each thread forms elements of
+// the sub-blocks rawJ(a, b), rawJ(c, d), rawK(a, c), rawK(b, d), rawK(a, d),
+// rawK(b, c) of every matrix (D symmetric, n x n row-major = column-major).
+__global__ void __launch_bounds__(kEriThreads) jk_contract_kernel(EriDev e, const int2* __restrict__ quartets,
+                                                                  const long long* __restrict__ out_off, long long q0,
+                                                                  long long base, const double* __restrict__ ints,
+                                                                  int n, int nmat, const double* __restrict__ D,
+                                                                  double* __restrict__ rawJ, double* __restrict__ rawK) {
+    __shared__ double blk[kIMax];
+    const long long q = q0 + blockIdx.x;
+    const int tid = threadIdx.x;
+    const int2 pq = quartets[q];
+    const EriPair P = e.pairs[pq.x], Q = e.pairs[pq.y];
+    const int na = P.na, nb = P.nb, nc = Q.na, nd = Q.nb;
+    const int nI = na * nb * nc * nd;
+    const double* src = ints + (out_off[q] - base);
+    for (int i = tid; i < nI; i += kEriThreads) blk[i] = src[i];
+    __syncthreads();
+    // degeneracy of the canonical quartet (a >= b, c >= d, bra pair >= ket pair)
+    const int sa = P.fa, sb = P.fb, sc_ = Q.fa, sd = Q.fb;
+    double f = 1.0;
+    if (sa == sb) f *= 0.5;
+    if (sc_ == sd) f *= 0.5;
+    if (pq.x == pq.y) f *= 0.5;
+    const int nJ1 = na * nb, nJ2 = nc * nd, nK1 = na * nc, nK2 = nb * nd, nK3 = na * nd, nK4 = nb * nc;
+    const int tot = (rawJ ? nJ1 + nJ2 : 0) + (rawK ? nK1 + nK2 + nK3 + nK4 : 0);
+    const size_t nn = (size_t)n * n;
+    for (int m = 0; m < nmat; m++) {
+        const double* Dm = D + m * nn;
+        for (int e_ = tid; e_ < tot; e_ += kEriThreads) {
+            int k = e_;
+            double acc = 0.0;
+            size_t dst;
+            double* base_out;
+            if (rawJ && k < nJ1) {  // rawJ(a, b) += f sum_cd I D(c, d)
+                const int ia = k / nb, ib = k - ia * nb;
+                for (int ic = 0; ic < nc; ic++)
+                    for (int id = 0; id < nd; id++)
+                        acc += blk[((ia * nb + ib) * nc + ic) * nd + id] * __ldg(Dm + (size_t)(sc_ + ic) * n + sd + id);
+                dst = (size_t)(sa + ia) * n + sb + ib;
+                base_out = rawJ;
+            } else if (rawJ && (k -= nJ1) < nJ2) {  // rawJ(c, d) += f sum_ab I D(a, b)
+                const int ic = k / nd, id = k - ic * nd;
+                for (int ia = 0; ia < na; ia++)
+                    for (int ib = 0; ib < nb; ib++)
+                        acc += blk[((ia * nb + ib) * nc + ic) * nd + id] * __ldg(Dm + (size_t)(sa + ia) * n + sb + ib);
+                dst = (size_t)(sc_ + ic) * n + sd + id;
+                base_out = rawJ;
+            } else {
+                if (rawJ) k -= nJ2;
+                base_out = rawK;
+                if (k < nK1) {  // rawK(a, c) += f sum_bd I D(b, d)
+                    const int ia = k / nc, ic = k - ia * nc;
+                    for (int ib = 0; ib < nb; ib++)
+                        for (int id = 0; id < nd; id++)
+                            acc += blk[((ia * nb + ib) * nc + ic) * nd + id] *
+                                   __ldg(Dm + (size_t)(sb + ib) * n + sd + id);
+                    dst = (size_t)(sa + ia) * n + sc_ + ic;
+                } else if ((k -= nK1) < nK2) {  // rawK(b, d) += f sum_ac I D(a, c)
+                    const int ib = k / nd, id = k - ib * nd;
+                    for (int ia = 0; ia < na; ia++)
+                        for (int ic = 0; ic < nc; ic++)
+                            acc += blk[((ia * nb + ib) * nc + ic) * nd + id] *
+                                   __ldg(Dm + (size_t)(sa + ia) * n + sc_ + ic);
+                    dst = (size_t)(sb + ib) * n + sd + id;
+                } else if ((k -= nK2) < nK3) {  // rawK(a, d) += f sum_bc I D(b, c)
+                    const int ia = k / nd, id = k - ia * nd;
+                    for (int ib = 0; ib < nb; ib++)
+                        for (int ic = 0; ic < nc; ic++)
+                            acc += blk[((ia * nb + ib) * nc + ic) * nd + id] *
+                                   __ldg(Dm + (size_t)(sb + ib) * n + sc_ + ic);
+                    dst = (size_t)(sa + ia) * n + sd + id;
+                } else {  // rawK(b, c) += f sum_ad I D(a, d)
+                    k -= nK3;
+                    const int ib = k / nc, ic = k - ib * nc;
+                    for (int ia = 0; ia < na; ia++)
+                        for (int id = 0; id < nd; id++)
+                            acc += blk[((ia * nb + ib) * nc + ic) * nd + id] *
+                                   __ldg(Dm + (size_t)(sa + ia) * n + sd + id);
+                    dst = (size_t)(sb + ib) * n + sc_ + ic;
+                }
+            }
+            atomicAdd(base_out + m * nn + dst, f * acc);
+        }
+    }
+}
+
+__global__ void jk_symmetrise_kernel(int n, int nmat, const double* __restrict__ rawJ, const double* __restrict__ rawK,
+                                     double* __restrict__ J, double* __restrict__ K) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long nn = (long long)n * n;
+    if (i >= nn * nmat) return;
+    const long long m = i / nn, r = i - m * nn;
+    const int a = (int)(r / n), b = (int)(r - (long long)a * n);
+    const long long t = m * nn + (long long)b * n + a;
+    if (J) J[i] = 2.0 * (rawJ[i] + rawJ[t]);
+    if (K) K[i] = rawK[i] + rawK[t];
+}
+
+}  // namespace
+
+void set_eri_kernel_attributes() {
+    CGB_CUDA(cudaFuncSetAttribute(eri_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(EriSmem)));
+    static bool tables = false;
+    if (!tables) {
+        unsigned h[kHMax];
+        for (int N = 0; N <= kEriMaxLt; N++)
+            for (int t = N; t >= 0; t--)
+                for (int u = N - t; u >= 0; u--) {
+                    const int v = N - t - u, a = N - t;
+                    const int i = N * (N + 1) * (N + 2) / 6 + a * (a + 1) / 2 + (a - u);
+                    h[i] = (unsigned)t | ((unsigned)u << 8) | ((unsigned)v << 16) | ((unsigned)N << 24);
+                }
+        CGB_CUDA(cudaMemcpyToSymbol(c_tuv, h, sizeof(h)));
+        tables = true;
+    }
+}
+
+void launch_eri(const EriDev& e, const int2* quartets, const long long* out_off, long long q0, long long nq,
+                long long base, double* out, cudaStream_t s) {
+    for (long long c = 0; c < nq; c += (1LL << 30)) {
+        const long long m = nq - c < (1LL << 30) ? nq - c : (1LL << 30);
+        eri_kernel<<<(unsigned)m, kEriThreads, sizeof(EriSmem), s>>>(e, quartets, out_off, q0 + c, base, out);
+        CGB_CUDA(cudaGetLastError());
+    }
+}
+
+void launch_jk_contract(const EriDev& e, const int2* quartets, const long long* out_off, long long q0, long long nq,
+                        long long base, const double* ints, int n, int nmat, const double* D, double* rawJ,
+                        double* rawK, cudaStream_t s) {
+    for (long long c = 0; c < nq; c += (1LL << 30)) {
+        const long long m = nq - c < (1LL << 30) ? nq - c : (1LL << 30);
+        jk_contract_kernel<<<(unsigned)m, kEriThreads, 0, s>>>(e, quartets, out_off, q0 + c, base, ints, n, nmat, D,
+                                                               rawJ, rawK);
+        CGB_CUDA(cudaGetLastError());
+    }
+}
+
+void launch_jk_symmetrise(int n, int nmat, const double* rawJ, const double* rawK, double* J, double* K,
+                          cudaStream_t s) {
+    const long long tot = (long long)n * n * nmat;
+    if (tot == 0) return;
+    jk_symmetrise_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(n, nmat, rawJ, rawK, J, K);
+    CGB_CUDA(cudaGetLastError());
+}
+
+}  // namespace cgb

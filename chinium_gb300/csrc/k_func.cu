@@ -37,7 +37,12 @@ __device__ double cta_sum(double v) {
     return r;
 }
 
-// MODE 1: only the points whose total density is >= float_above, in FP32;
+// MODE 1: only the points whose total density is >= float_above: the
+// potentials in FP32 (forward-mode derivatives of the FP32 expression) and
+// the energy density eps in FP64 (the value alone) -- float constants and
+// float k/3 exponents shift an FP32 eps systematically by 1e-8..1e-7
+// relative, which E_xc = sum w rho eps would accumulate, while V takes
+// FP32-level errors;
 // MODE 2: only the others, in FP64 (float_above = +inf: every point).  The
 // mixed path runs both launches (separate kernels: each gets the registers
 // and occupancy of its own precision); accumulate adds the CTA's energy
@@ -73,10 +78,10 @@ __global__ void __launch_bounds__(kThreads) functional_kernel(xcf::FuncDesc f, l
             }
             if (FAM >= 2) t = tau[g];
             double e, dv[3] = {0, 0, 0};
-            if (MODE == 1) {  // mixed path: FP32 functional above the low-density bound
+            if (MODE == 1) {  // mixed path: FP32 potentials, FP64 eps, above the low-density bound
                 float ef, df[3] = {0, 0, 0};
                 xcf::eval_unpol<float, FAM>(f, (float)r, (float)s, (float)t, ef, df);
-                e = ef;
+                xcf::eval_unpol_value<double, FAM>(f, r, s, t, e);
                 for (int i = 0; i < 3; i++) dv[i] = df[i];
             } else {
                 xcf::eval_unpol<double, FAM>(f, r, s, t, e, dv);
@@ -117,7 +122,7 @@ __global__ void __launch_bounds__(kThreads) functional_kernel(xcf::FuncDesc f, l
                 float inf_[7], ef, df[7] = {0, 0, 0, 0, 0, 0, 0};
                 for (int i = 0; i < 7; i++) inf_[i] = (float)in[i];
                 xcf::eval_pol<float, FAM>(f, inf_, ef, df);
-                e = ef;
+                xcf::eval_pol_value<double, FAM>(f, in, e);
                 for (int i = 0; i < 7; i++) dv[i] = df[i];
             } else {
                 xcf::eval_pol<double, FAM>(f, in, e, dv);

@@ -57,7 +57,6 @@ constexpr int kF16Threads = 384;               // kernels on pre-split operands:
 constexpr int kEpiWarp0 = 4;                   // epilogue warps 4-11 (two per TMEM lane quadrant)
 constexpr int kEpiThreads = 256;
 constexpr int kConvWarps = 6;                  // warps 2-3 and 12-15
-constexpr int kConvThreads = kConvWarps * 32;
 constexpr uint32_t kPlaneA = 128 * 64 * 2;     // bytes of one 128x64 bf16 operand plane
 constexpr uint32_t kStageBytes = 6 * kPlaneA;  // A (3 planes) + B (3 planes)
 constexpr uint32_t kRawD = 64 * 128 * 4;       // density raw tile: 64 functions x 128 points FP32
@@ -284,7 +283,6 @@ struct DensCursor {
     }
 };
 
-constexpr int kDensItems = (1024 + kConvThreads - 1) / kConvThreads;  // (point, 8-function chunk) items
 constexpr int kMaxChunks = 256;                                       // chunks of one molecule (n <= 16384)
 
 struct DensOut {

@@ -33,11 +33,12 @@ constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) double g_energy_partials[kStaticPartials];
 
-// Device address of g_energy_partials per device, looked up once per device
-// with that device current (the host-side symbol is only a stand-in).
+// Device address of g_energy_partials per device, looked up with that device
+// current (the host-side symbol is only a stand-in).  Only a successful
+// lookup is kept: a failed one (for instance a first call made while the
+// stream is being captured) is retried by the next call.
+std::mutex g_partials_mu;
 double* g_partials_addr[kMaxDevices] = {};
-std::once_flag g_partials_once[kMaxDevices];
-cudaError_t g_partials_status[kMaxDevices] = {};
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -139,15 +140,22 @@ extern "C" int xc_functional_energy_static(const xc_functional* fh, long npoints
         int dev = -1;
         CGB_CUDA(cudaGetDevice(&dev));
         CGB_CHECK(dev >= 0 && dev < kMaxDevices, XC_ERR_CUDA, "device index out of range");
-        // first call on this device: resolve the array's device address
-        std::call_once(g_partials_once[dev], [dev] {
-            void* p = nullptr;
-            g_partials_status[dev] = cudaGetSymbolAddress(&p, g_energy_partials);
-            g_partials_addr[dev] = (double*)p;
-        });
-        CGB_CHECK(g_partials_status[dev] == cudaSuccess && g_partials_addr[dev], XC_ERR_CUDA,
-                  "cudaGetSymbolAddress of the static energy scratch failed");
-        double* partials = g_partials_addr[dev];
+        // first successful call on this device: resolve the array's device address
+        double* partials = nullptr;
+        {
+            std::lock_guard<std::mutex> lk(g_partials_mu);
+            if (!g_partials_addr[dev]) {
+                void* p = nullptr;
+                const cudaError_t st = cudaGetSymbolAddress(&p, g_energy_partials);
+                if (st != cudaSuccess || !p) {
+                    cudaGetLastError();  // not sticky: the next call looks the address up again
+                    throw Error(XC_ERR_CUDA, std::string("cudaGetSymbolAddress of the static energy scratch failed (") +
+                                                 cudaGetErrorString(st) + "); the next call retries the lookup");
+                }
+                g_partials_addr[dev] = (double*)p;
+            }
+            partials = g_partials_addr[dev];
+        }
         cudaStream_t s = (cudaStream_t)stream;
         const unsigned grid = (unsigned)((npoints + kStaticThreads - 1) / kStaticThreads);
 #define CGB_ST(FAM_, NS_)                                                                                  \

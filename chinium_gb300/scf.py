@@ -130,6 +130,61 @@ class JKDevice:
         return (self.K @ d).reshape(n, n).cpu().numpy()
 
 
+class JKEngine:
+    """Coulomb and exchange matrices from the library's GPU integral engine
+    (include/chinium_int.h, xc_jk_*: the reference's Int4C2E): the screened
+    unique integrals are computed on the GPU once and kept in HBM, or
+    recomputed per build when they do not fit, and every build contracts them
+    with the density matrices.  begin() enqueues J (of the summed densities)
+    and, when asked, K of each density on the engine's own stream and returns
+    at once, so that the XC build can run meanwhile; end() waits."""
+
+    def __init__(self, basis, threshold=1e-14, max_bytes=0.0):
+        import torch
+        self.torch = torch
+        self.n = basis.nbasis
+        h = ctypes.c_void_p()
+        check(lib().xc_jk_create(basis._h, float(threshold), float(max_bytes), ctypes.byref(h)))
+        self._h = h
+        self.stream = torch.cuda.Stream()
+        check(lib().xc_jk_set_stream(h, ctypes.c_void_p(self.stream.cuda_stream)))
+
+    def info(self):
+        nq, ni, ic = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_int()
+        check(lib().xc_jk_info(self._h, ctypes.byref(nq), ctypes.byref(ni), ctypes.byref(ic)))
+        return {"quartets": nq.value, "integrals": ni.value, "incore": bool(ic.value)}
+
+    def begin(self, Ds, want_k):
+        torch = self.torch
+        n, m = self.n, len(Ds)
+        with torch.cuda.stream(self.stream):
+            d = torch.from_numpy(np.ascontiguousarray(np.stack(Ds))).pin_memory().cuda(non_blocking=True)
+            J = torch.empty((m, n, n), dtype=torch.float64, device="cuda")
+            K = torch.empty((m, n, n), dtype=torch.float64, device="cuda") if want_k else None
+        ptr = lambda t: ctypes.c_void_p(t.data_ptr()) if t is not None else None
+        check(lib().xc_jk_build_device(self._h, m, ptr(d), ptr(J), ptr(K)))
+        return d, J, K
+
+    def end(self, h):
+        d, J, K = h
+        self.stream.synchronize()
+        Jh = J.cpu().numpy().sum(axis=0)
+        Ks = [K[s].cpu().numpy() for s in range(K.shape[0])] if K is not None else None
+        return Jh, Ks
+
+    def coulomb(self, D):
+        return self.end(self.begin([D], False))[0]
+
+    def exchange(self, D):
+        return self.end(self.begin([D], True))[1][0]
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().xc_jk_destroy(h)
+            self._h = None
+
+
 def overlap_metric(S, ctx=None):
     """(X, S^-1/2, S^1/2) of the overlap matrix: X the canonical
     orthogonaliser (eigenvectors with eigenvalue > 1e-8, scaled), the other
@@ -217,7 +272,9 @@ def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, m
     half of max_iter), or a density matrix (total for RKS, [Da, Db] for UKS).
     context: reuse integrals and grid from a previous call on the same
     molecule ({"basis","S","H","jk","grid","Enuc"}).
-    jk_device: "cpu" (numpy) or "cuda" (repulsion integrals kept in HBM)."""
+    jk_device: "cpu" (host repulsion integrals, numpy contraction), "cuda"
+    (host repulsion integrals moved to HBM, torch contraction) or "engine"
+    (integrals computed and contracted on the GPU by the library, JKEngine)."""
     t_start = time.perf_counter()
     timings = {"setup": 0.0, "xc": 0.0, "jk": 0.0, "diag": 0.0}
     na, nb = occupations(Z, charge, mult)
@@ -228,17 +285,17 @@ def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, m
     if "basis" not in ctx:
         b = Basis(Z, xyz, basis)
         S, T, Vn = one_electron(b)
-        ctx.update(basis=b, S=S, H=T + Vn, jk=make_jk(repulsion(b, eri_threshold), jk_device),
-                   Enuc=M.nuclear_repulsion(Z, xyz))
+        jk_ = JKEngine(b) if jk_device == "engine" else make_jk(repulsion(b, eri_threshold), jk_device)
+        ctx.update(basis=b, S=S, H=T + Vn, jk=jk_, Enuc=M.nuclear_repulsion(Z, xyz))
     key = ("grid", nspin, functional, grid, screen)
     xc = ExchangeCorrelation(spin=nspin).Read(functional)
     if ctx.get("grid_key") != key:
         g = Grid(ctx["basis"], grid, nspin=nspin, screen_threshold=screen)
         g.setType(xc.type)
         g.getAO(0)
-        if jk_device == "cuda":
+        if jk_device in ("cuda", "engine"):
             # the XC build on its own stream, so that the device J of the same
-            # iteration (torch's stream) runs alongside it
+            # iteration (torch's or the engine's stream) runs alongside it
             import torch
             torch.cuda.synchronize()
             ctx["grid_stream"] = torch.cuda.Stream()
@@ -302,8 +359,11 @@ def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, m
     for it in range(1, max_iter + 1):
         t0 = time.perf_counter()
         Dtot = Ds[0] if not unrestricted else Ds[0] + Ds[1]
-        J_pending = jk.coulomb_begin(Dtot)  # overlaps the XC build below
-        Ks = [jk.exchange(d) for d in Ds] if exx > 0 else [np.zeros((n, n))] * nspin
+        if isinstance(jk, JKEngine):  # J and K on the GPU engine's stream, overlapping the XC build below
+            J_pending = jk.begin(Ds, exx > 0)
+        else:
+            J_pending = jk.coulomb_begin(Dtot)  # overlaps the XC build below
+            Ks = [jk.exchange(d) for d in Ds] if exx > 0 else [np.zeros((n, n))] * nspin
         timings["jk"] += time.perf_counter() - t0
         t0 = time.perf_counter()
         if precision == "fp64":
@@ -318,7 +378,12 @@ def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, m
             Exc, Vxc = e.value, [Vb[s].T.copy() for s in range(nspin)]
         timings["xc"] += time.perf_counter() - t0
         t0 = time.perf_counter()
-        J = jk.coulomb_end(J_pending)
+        if isinstance(jk, JKEngine):
+            J, Ks = jk.end(J_pending)
+            if Ks is None:
+                Ks = [np.zeros((n, n))] * nspin
+        else:
+            J = jk.coulomb_end(J_pending)
         timings["jk"] += time.perf_counter() - t0
         if unrestricted:
             Fs = [H + J - exx * Ks[s] + Vxc[s] for s in range(2)]

@@ -34,6 +34,35 @@ int xc_dipole(const xc_basis* b, const double* origin, double* M);
  * bound is below schwarz_threshold are left zero. */
 int xc_eri(const xc_basis* b, double* eri, double schwarz_threshold);
 
+/* --------------------------------------------- Coulomb and exchange (GPU)
+ * The reference's Int4C2E (src/Integral/Int4C2E.cpp) on the GPU: Schwarz
+ * bounds from the diagonal integrals (getRepulsionDiag, :19-77), the
+ * screened list of unique shell quartets (getRepulsionLength /
+ * getRepulsionIndices, :79-130), the integrals themselves
+ * (CalculateIntegrals, :567-584; McMurchie-Davidson in FP64 here, s to f
+ * shells) and their contraction with density matrices every SCF iteration
+ * (ContractInts / Gunified, :601-683).  Quartets whose Schwarz product is
+ * below `threshold` are dropped (the reference's SCF keeps all of them,
+ * threshold -1 at SelfConsistentField.cpp:47; 0 does the same here).  The
+ * integrals are computed once and kept in HBM when they take at most
+ * max_bytes (0: half of the free device memory); otherwise every build
+ * recomputes them in chunks (integral-direct). */
+typedef struct xc_jk xc_jk;
+int xc_jk_create(const xc_basis* b, double threshold, double max_bytes, xc_jk** out);
+int xc_jk_destroy(xc_jk* jk);
+/* Quartets and integrals kept, and 1 if the integrals are resident in HBM. */
+int xc_jk_info(const xc_jk* jk, long long* nquartets, long long* nints, int* incore);
+/* CUDA stream (cudaStream_t as void*) of the builds; NULL = legacy default. */
+int xc_jk_set_stream(xc_jk* jk, void* stream);
+/* J_m = sum (mu nu|la si) D_m(la, si) and K_m = sum (mu la|nu si) D_m(la, si)
+ * for nmat symmetric n x n density matrices (host buffers); J or K may be
+ * NULL.  Gunified returns J of the total density and K per spin; a caller
+ * forms those from J_m and K_m. */
+int xc_jk_build(xc_jk* jk, int nmat, const double* D, double* J, double* K);
+/* Same on caller-owned device buffers, issued on the handle's stream
+ * without synchronising. */
+int xc_jk_build_device(xc_jk* jk, int nmat, const double* d_D, double* d_J, double* d_K);
+
 #ifdef __cplusplus
 }
 #endif

@@ -144,7 +144,7 @@ typedef struct xc_grid_info {
     long mixed_fock_jobs;  /* V (item, tile) jobs, each 128 x 128 x 128 per component */
     long mixed_fock_tau_jobs; /* jobs that also carry the meta-GGA components (I <= J) */
     long mixed_presplit;      /* 1: the tensor-core kernels read pre-split BF16 planes (v_operands) */
-    long mixed_presplit_bytes; /* bytes of those planes (AO store + per-build R planes) */
+    long mixed_presplit_bytes; /* bytes of those planes (AO store, density A planes, per-build R planes) */
     long mixed_fock_items;    /* V work items with at least one job (one W partial written each) */
     long mixed_empty_tiles;   /* tiles whose points no kept chunk reaches (zero density there) */
 } xc_grid_info;
@@ -201,8 +201,10 @@ int xc_functional_eval_points(xc_functional* f, long npoints, const double* rho,
  * inside the library, so npoints <= 2 097 152; larger calls fail with
  * XC_ERR_ARG.  The first call on a device looks up that array's device
  * address (with that device current); make that first call before any stream
- * capture.  Calls share the array, so calls whose kernels overlap on the GPU
- * race and must be serialised by the caller.  Work is enqueued on `stream`
+ * capture.  A lookup that fails returns XC_ERR_CUDA and is not remembered:
+ * the next call on that device tries again.  Calls share the array, so calls
+ * whose kernels overlap on the GPU race and must be serialised by the
+ * caller.  Work is enqueued on `stream`
  * (cudaStream_t as void*, NULL = legacy default) without synchronising. */
 int xc_functional_energy_static(const xc_functional* f, long npoints, const double* d_w,
                                 const double* d_rho, const double* d_sigma, const double* d_tau,

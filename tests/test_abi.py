@@ -262,3 +262,27 @@ def test_basis_from_shells_validates_arguments():
     n = ctypes.c_int()
     assert L.xc_basis_nbasis(h, ctypes.byref(n)) == 0 and n.value == 4
     L.xc_basis_destroy(h)
+
+
+def test_static_entry_point_validates_arguments_on_the_host():
+    """xc_functional_energy_static rejects bad arguments before touching the
+    GPU: null pointers, npoints <= 0, a GGA or meta-GGA call without its
+    sigma / tau arrays, and calls above its fixed scratch of 2 097 152 points
+    (the pointers below are never dereferenced)."""
+    L = lib()
+    one = ctypes.c_void_p(16)
+    pbe = cg.ExchangeCorrelation().Read("PBE")
+    tpss = cg.ExchangeCorrelation().Read("TPSS")
+    args = lambda f, n, sig=one, tau=one: (f._h, n, one, one, sig, tau, one, one, sig, tau, one, None)
+    msg = lambda: (lambda b: (L.xc_last_error(b, 512), b.value)[1])(ctypes.create_string_buffer(512))
+    assert L.xc_functional_energy_static(*args(pbe, 2097152 + 1)) == -1
+    assert b"static scratch limit" in msg()
+    assert L.xc_functional_energy_static(*args(pbe, 0)) == -1
+    assert L.xc_functional_energy_static(*args(pbe, -5)) == -1
+    assert L.xc_functional_energy_static(None, 10, one, one, one, one, one, one, one, one, one, None) == -1
+    assert L.xc_functional_energy_static(pbe._h, 10, None, one, one, one, one, one, one, one, one, None) == -1
+    assert L.xc_functional_energy_static(pbe._h, 10, one, one, one, one, one, one, one, one, None, None) == -1
+    assert L.xc_functional_energy_static(*args(pbe, 10, sig=None)) == -1
+    assert b"sigma" in msg()
+    assert L.xc_functional_energy_static(*args(tpss, 10, tau=None)) == -1
+    assert b"tau" in msg()

@@ -275,7 +275,7 @@ def test_xc_gradient_rejects_meta_gga(h2o):
 def test_grid_from_caller_shells_is_bitwise_the_named_basis(h2o):
     """xc_basis_create_shells with the shells of the named basis (normalised
     coefficients, as the Mwfn's NormalizedCoefficients): bitwise the same
-    E_xc and V_xc, FP64 and tensor-core paths."""
+    E_xc and V_xc equal to rounding (FP64 atomics), FP64 and tensor-core paths."""
     Z, xyz, b, ob, og = h2o
     sh = b.shells()
     b2 = cg.Basis.from_shells(Z, xyz, sh["atom"], sh["type"], sh["nprim"], sh["exps"], sh["coefs"])
@@ -284,5 +284,5 @@ def test_grid_from_caller_shells_is_bitwise_the_named_basis(h2o):
     for prec in (cg.PRECISION_FP64, cg.PRECISION_MIXED):
         E1, V1 = make_grid(b).build(xc, [D], precision=prec)
         E2, V2 = make_grid(b2).build(xc, [D], precision=prec)
-        assert E1 == E2
-        assert np.array_equal(V1[0], V2[0])
+        assert E1 == E2  # E_xc is summed in a fixed order
+        assert np.abs(V1[0] - V2[0]).max() < 1e-14  # V_xc takes FP64 atomics: equal to rounding

@@ -137,7 +137,8 @@ def _grid_overlap_trace_weights(c):
 def test_grid_from_caller_shells_is_bitwise_the_named_basis(config):
     """A grid built from the caller's shells (xc_basis_create_shells, the
     Mwfn-shell form of Grid::Grid) gives bitwise the same E_xc and V_xc as
-    the grid of the named basis, on the shells that basis exports."""
+    the grid of the named basis, on the shells that basis exports (V_xc to
+    rounding: its FP64 sums use atomics)."""
     if config["name"] != "c18":
         pytest.skip("one large configuration suffices (H2O in test_gpu_parity.py)")
     c = config
@@ -150,5 +151,6 @@ def test_grid_from_caller_shells_is_bitwise_the_named_basis(config):
         g.setType(xc.type)
         g.getAO(0)
         out.append(g.build(xc, c["D"]))
-    assert out[0][0] == out[1][0]
-    assert all(np.array_equal(a, b) for a, b in zip(out[0][1], out[1][1]))
+    assert out[0][0] == out[1][0]  # E_xc is summed in a fixed order
+    # V_xc takes FP64 atomics: equal to rounding
+    assert all(np.abs(a - b).max() < 1e-13 for a, b in zip(out[0][1], out[1][1]))
