@@ -400,9 +400,9 @@ def run_scf_water(args):
     screening 1e-11 — and (b) incremental mixed builds from the learned guess
     (its SAP base on the tensor cores; references from screened FP64
     densities with a tensor-core V), plus the other combinations.  Integrals,
-    the overlap metric and the grids are shared setup (ERIs resident in HBM
-    for J/K); the timed SCF includes the guess and every iteration (XC build,
-    J/K, DIIS, diagonalisation)."""
+    the overlap metric and the grids are shared setup (repulsion integrals
+    computed on the GPU and resident in HBM); the timed SCF includes the guess
+    and every iteration (XC build, J/K contraction, DIIS, diagonalisation)."""
     import torch
     import chinium_gb300 as cg
     from chinium_gb300 import guess as G
@@ -423,7 +423,7 @@ def run_scf_water(args):
     t_setup = 0.0
     xc = cg.ExchangeCorrelation().Read("PBE")
     for Z, xyz in mols:
-        kw = dict(functional="PBE", grid="SG-2", jk_device="cuda")
+        kw = dict(functional="PBE", grid="SG-2", jk_device="engine")
         t0 = time.perf_counter()
         ctxs = {}
         for scr in (0.0, 1e-11):  # integrals shared; one grid (AO store, mixed tiles) per screening

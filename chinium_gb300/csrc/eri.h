@@ -62,6 +62,15 @@ void launch_jk_contract(const EriDev& e, const int2* quartets, const long long* 
                         long long base, const double* ints, int n, int nmat, const double* D, double* rawJ,
                         double* rawK, cudaStream_t s);
 
+// rawJ of nmat matrices from in-core blocks without global atomics: pass A
+// over every bra pair's consecutive quartets (bra_seg: npairs + 1 offsets
+// into the quartet list), pass B over every ket pair's quartets (ket_seg
+// offsets into ket_idx, the quartet indices grouped by ket pair).  rawJ must
+// start at zero.
+void launch_coulomb_passes(const EriDev& e, const int2* quartets, const long long* out_off, const long long* bra_seg,
+                           const long long* ket_seg, const long long* ket_idx, int npairs, const double* ints, int n,
+                           int nmat, const double* D, double* rawJ, cudaStream_t s);
+
 // rawJ, rawK -> J = 2 (rawJ + rawJ^T), K = rawK + rawK^T (nmat matrices each, either may be null).
 void launch_jk_symmetrise(int n, int nmat, const double* rawJ, const double* rawK, double* J, double* K,
                           cudaStream_t s);

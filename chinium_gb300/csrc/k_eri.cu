@@ -11,10 +11,10 @@
 // and the bra contraction I[ab][cd] += pre sum_h Ep_ab[ab][h] X[cd][h].
 // The block of pure integrals [fa][fb][fc][fd] is written once.
 //
-// jk_contract_kernel: one CTA per quartet block; the block is staged in
-// shared memory (one read from HBM) and each thread forms one element of
-// the six J / K sub-blocks it feeds (2 J, 4 K), scaled by the quartet's
-// degeneracy, with one FP64 atomic per element.
+// jk_contract_kernel: one warp per quartet block; each lane forms elements
+// of the six J / K sub-blocks it feeds (2 J, 4 K), scaled by the quartet's
+// degeneracy, with one FP64 atomic per element.  coulomb_pass_kernel: J of
+// in-core blocks in two atomic-free passes (per bra pair, per ket pair).
 #include "common.h"
 #include "eri.h"
 
@@ -163,90 +163,153 @@ __global__ void __launch_bounds__(kEriThreads) eri_kernel(EriDev e, const int2* 
     for (int i = tid; i < nI; i += kEriThreads) o[i] = sm.I[i];
 }
 
-// One CTA per quartet block: stage it, then each thread forms elements of
-// the sub-blocks rawJ(a, b), rawJ(c, d), rawK(a, c), rawK(b, d), rawK(a, d),
-// rawK(b, c) of every matrix (D symmetric, n x n row-major = column-major).
-__global__ void __launch_bounds__(kEriThreads) jk_contract_kernel(EriDev e, const int2* __restrict__ quartets,
-                                                                  const long long* __restrict__ out_off, long long q0,
-                                                                  long long base, const double* __restrict__ ints,
-                                                                  int n, int nmat, const double* __restrict__ D,
-                                                                  double* __restrict__ rawJ, double* __restrict__ rawK) {
-    __shared__ double blk[kIMax];
-    const long long q = q0 + blockIdx.x;
-    const int tid = threadIdx.x;
-    const int2 pq = quartets[q];
-    const EriPair P = e.pairs[pq.x], Q = e.pairs[pq.y];
-    const int na = P.na, nb = P.nb, nc = Q.na, nd = Q.nb;
-    const int nI = na * nb * nc * nd;
-    const double* src = ints + (out_off[q] - base);
-    for (int i = tid; i < nI; i += kEriThreads) blk[i] = src[i];
-    __syncthreads();
-    // degeneracy of the canonical quartet (a >= b, c >= d, bra pair >= ket pair)
-    const int sa = P.fa, sb = P.fb, sc_ = Q.fa, sd = Q.fb;
-    double f = 1.0;
-    if (sa == sb) f *= 0.5;
-    if (sc_ == sd) f *= 0.5;
-    if (pq.x == pq.y) f *= 0.5;
-    const int nJ1 = na * nb, nJ2 = nc * nd, nK1 = na * nc, nK2 = nb * nd, nK3 = na * nd, nK4 = nb * nc;
-    const int tot = (rawJ ? nJ1 + nJ2 : 0) + (rawK ? nK1 + nK2 + nK3 + nK4 : 0);
+// One warp per quartet block (persistent grid, quartets strided over the
+// warps): each lane forms elements of the sub-blocks rawJ(a, b), rawJ(c, d),
+// rawK(a, c), rawK(b, d), rawK(a, d), rawK(b, c) of every matrix -- one
+// slice sum of the block times D each -- and adds it with one FP64 atomic.
+// The block's lines are read from HBM once and re-read from L1 by the six
+// slices (D symmetric, n x n; row-major and column-major alike).  rawJ or
+// rawK may be null (that half is skipped).
+constexpr int kJkWarps = 8;
+__global__ void __launch_bounds__(32 * kJkWarps) jk_contract_kernel(EriDev e, const int2* __restrict__ quartets,
+                                                                    const long long* __restrict__ out_off,
+                                                                    long long q0, long long nq, long long base,
+                                                                    const double* __restrict__ ints, int n, int nmat,
+                                                                    const double* __restrict__ D,
+                                                                    double* __restrict__ rawJ,
+                                                                    double* __restrict__ rawK) {
+    const int lane = threadIdx.x & 31;
+    const long long w0 = (long long)blockIdx.x * kJkWarps + (threadIdx.x >> 5);
+    const long long nw = (long long)gridDim.x * kJkWarps;
     const size_t nn = (size_t)n * n;
-    for (int m = 0; m < nmat; m++) {
-        const double* Dm = D + m * nn;
-        for (int e_ = tid; e_ < tot; e_ += kEriThreads) {
-            int k = e_;
-            double acc = 0.0;
-            size_t dst;
-            double* base_out;
-            if (rawJ && k < nJ1) {  // rawJ(a, b) += f sum_cd I D(c, d)
-                const int ia = k / nb, ib = k - ia * nb;
-                for (int ic = 0; ic < nc; ic++)
-                    for (int id = 0; id < nd; id++)
-                        acc += blk[((ia * nb + ib) * nc + ic) * nd + id] * __ldg(Dm + (size_t)(sc_ + ic) * n + sd + id);
-                dst = (size_t)(sa + ia) * n + sb + ib;
-                base_out = rawJ;
-            } else if (rawJ && (k -= nJ1) < nJ2) {  // rawJ(c, d) += f sum_ab I D(a, b)
-                const int ic = k / nd, id = k - ic * nd;
-                for (int ia = 0; ia < na; ia++)
-                    for (int ib = 0; ib < nb; ib++)
-                        acc += blk[((ia * nb + ib) * nc + ic) * nd + id] * __ldg(Dm + (size_t)(sa + ia) * n + sb + ib);
-                dst = (size_t)(sc_ + ic) * n + sd + id;
-                base_out = rawJ;
-            } else {
-                if (rawJ) k -= nJ2;
-                base_out = rawK;
-                if (k < nK1) {  // rawK(a, c) += f sum_bd I D(b, d)
-                    const int ia = k / nc, ic = k - ia * nc;
-                    for (int ib = 0; ib < nb; ib++)
+    for (long long qq = w0; qq < nq; qq += nw) {
+        const long long q = q0 + qq;
+        const int2 pq = quartets[q];
+        const EriPair P = e.pairs[pq.x], Q = e.pairs[pq.y];
+        const int na = P.na, nb = P.nb, nc = Q.na, nd = Q.nb;
+        const double* __restrict__ blk = ints + (out_off[q] - base);
+        // degeneracy of the canonical quartet (a >= b, c >= d, bra pair >= ket pair)
+        const int sa = P.fa, sb = P.fb, sc = Q.fa, sd = Q.fb;
+        double f = 1.0;
+        if (sa == sb) f *= 0.5;
+        if (sc == sd) f *= 0.5;
+        if (pq.x == pq.y) f *= 0.5;
+        const int nJ1 = na * nb, nJ2 = nc * nd, nK1 = na * nc, nK2 = nb * nd, nK3 = na * nd, nK4 = nb * nc;
+        const int nJ = rawJ ? nJ1 + nJ2 : 0;
+        const int tot = nJ + (rawK ? nK1 + nK2 + nK3 + nK4 : 0);
+        const int sab = nb * nc * nd, sbb = nc * nd;  // strides of ia, ib in the block
+        for (int m = 0; m < nmat; m++) {
+            const double* __restrict__ Dm = D + m * nn;
+            for (int k = lane; k < tot; k += 32) {
+                double acc = 0.0;
+                size_t dst;
+                double* out;
+                if (k < nJ && k < nJ1) {  // rawJ(a, b) += f sum_cd I D(c, d)
+                    const int ia = k / nb, ib = k - ia * nb;
+                    const double* bl = blk + ia * sab + ib * sbb;
+                    for (int ic = 0; ic < nc; ic++)
                         for (int id = 0; id < nd; id++)
-                            acc += blk[((ia * nb + ib) * nc + ic) * nd + id] *
-                                   __ldg(Dm + (size_t)(sb + ib) * n + sd + id);
-                    dst = (size_t)(sa + ia) * n + sc_ + ic;
-                } else if ((k -= nK1) < nK2) {  // rawK(b, d) += f sum_ac I D(a, c)
-                    const int ib = k / nd, id = k - ib * nd;
+                            acc = fma(__ldg(bl + ic * nd + id), __ldg(Dm + (size_t)(sc + ic) * n + sd + id), acc);
+                    dst = (size_t)(sa + ia) * n + sb + ib;
+                    out = rawJ;
+                } else if (k < nJ) {  // rawJ(c, d) += f sum_ab I D(a, b)
+                    const int r = k - nJ1, ic = r / nd, id = r - ic * nd;
+                    const double* bl = blk + ic * nd + id;
                     for (int ia = 0; ia < na; ia++)
-                        for (int ic = 0; ic < nc; ic++)
-                            acc += blk[((ia * nb + ib) * nc + ic) * nd + id] *
-                                   __ldg(Dm + (size_t)(sa + ia) * n + sc_ + ic);
-                    dst = (size_t)(sb + ib) * n + sd + id;
-                } else if ((k -= nK2) < nK3) {  // rawK(a, d) += f sum_bc I D(b, c)
-                    const int ia = k / nd, id = k - ia * nd;
-                    for (int ib = 0; ib < nb; ib++)
-                        for (int ic = 0; ic < nc; ic++)
-                            acc += blk[((ia * nb + ib) * nc + ic) * nd + id] *
-                                   __ldg(Dm + (size_t)(sb + ib) * n + sc_ + ic);
-                    dst = (size_t)(sa + ia) * n + sd + id;
-                } else {  // rawK(b, c) += f sum_ad I D(a, d)
-                    k -= nK3;
-                    const int ib = k / nc, ic = k - ib * nc;
-                    for (int ia = 0; ia < na; ia++)
-                        for (int id = 0; id < nd; id++)
-                            acc += blk[((ia * nb + ib) * nc + ic) * nd + id] *
-                                   __ldg(Dm + (size_t)(sa + ia) * n + sd + id);
-                    dst = (size_t)(sb + ib) * n + sc_ + ic;
+                        for (int ib = 0; ib < nb; ib++)
+                            acc = fma(__ldg(bl + ia * sab + ib * sbb), __ldg(Dm + (size_t)(sa + ia) * n + sb + ib), acc);
+                    dst = (size_t)(sc + ic) * n + sd + id;
+                    out = rawJ;
+                } else {
+                    int r = k - nJ;
+                    out = rawK;
+                    if (r < nK1) {  // rawK(a, c) += f sum_bd I D(b, d)
+                        const int ia = r / nc, ic = r - ia * nc;
+                        for (int ib = 0; ib < nb; ib++)
+                            for (int id = 0; id < nd; id++)
+                                acc = fma(__ldg(blk + ia * sab + ib * sbb + ic * nd + id),
+                                          __ldg(Dm + (size_t)(sb + ib) * n + sd + id), acc);
+                        dst = (size_t)(sa + ia) * n + sc + ic;
+                    } else if ((r -= nK1) < nK2) {  // rawK(b, d) += f sum_ac I D(a, c)
+                        const int ib = r / nd, id = r - ib * nd;
+                        for (int ia = 0; ia < na; ia++)
+                            for (int ic = 0; ic < nc; ic++)
+                                acc = fma(__ldg(blk + ia * sab + ib * sbb + ic * nd + id),
+                                          __ldg(Dm + (size_t)(sa + ia) * n + sc + ic), acc);
+                        dst = (size_t)(sb + ib) * n + sd + id;
+                    } else if ((r -= nK2) < nK3) {  // rawK(a, d) += f sum_bc I D(b, c)
+                        const int ia = r / nd, id = r - ia * nd;
+                        for (int ib = 0; ib < nb; ib++)
+                            for (int ic = 0; ic < nc; ic++)
+                                acc = fma(__ldg(blk + ia * sab + ib * sbb + ic * nd + id),
+                                          __ldg(Dm + (size_t)(sb + ib) * n + sc + ic), acc);
+                        dst = (size_t)(sa + ia) * n + sd + id;
+                    } else {  // rawK(b, c) += f sum_ad I D(a, d)
+                        r -= nK3;
+                        const int ib = r / nc, ic = r - ib * nc;
+                        for (int ia = 0; ia < na; ia++)
+                            for (int id = 0; id < nd; id++)
+                                acc = fma(__ldg(blk + ia * sab + ib * sbb + ic * nd + id),
+                                          __ldg(Dm + (size_t)(sa + ia) * n + sd + id), acc);
+                        dst = (size_t)(sb + ib) * n + sc + ic;
+                    }
                 }
+                atomicAdd(out + m * nn + dst, f * acc);
             }
-            atomicAdd(base_out + m * nn + dst, f * acc);
         }
+    }
+}
+
+// Coulomb contraction without global atomics, in two passes over the
+// in-core blocks.  Pass A: one warp per bra pair P walks P's quartets (they
+// are consecutive in the list) and accumulates y[ab] = sum_q f_q sum_cd
+// I_q[ab][cd] D(c, d) in shared memory; pass B: one warp per ket pair Q walks
+// the quartets whose ket is Q (a transposed index) and accumulates
+// z[cd] = sum_q f_q sum_ab I_q[ab][cd] D(a, b).  Each warp owns its pair's
+// block of rawJ (pass B runs after pass A); lanes read the blocks coalesced.
+constexpr int kJWarps = 8;
+constexpr int kPairMax = 49;  // functions of a shell pair (f f)
+template <bool KET>
+__global__ void __launch_bounds__(32 * kJWarps) coulomb_pass_kernel(EriDev e, const int2* __restrict__ quartets,
+                                                                     const long long* __restrict__ out_off,
+                                                                     const long long* __restrict__ seg,
+                                                                     const long long* __restrict__ idx, int npairs,
+                                                                     const double* __restrict__ ints, int n,
+                                                                     const double* __restrict__ D,
+                                                                     double* __restrict__ rawJ) {
+    __shared__ double acc_s[kJWarps][kPairMax];
+    const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+    double* acc = acc_s[wl];
+    for (int p = blockIdx.x * kJWarps + wl; p < npairs; p += gridDim.x * kJWarps) {
+        const EriPair O = e.pairs[p];  // the pair that owns the output block
+        const int nown = O.na * O.nb;
+        for (int i = lane; i < nown; i += 32) acc[i] = 0.0;
+        __syncwarp();
+        for (long long s = seg[p]; s < seg[p + 1]; s++) {
+            const long long q = KET ? idx[s] : s;
+            const int2 pq = quartets[q];
+            const EriPair Pb = e.pairs[pq.x], Qk = e.pairs[pq.y];
+            double f = 1.0;
+            if (Pb.fa == Pb.fb) f *= 0.5;
+            if (Qk.fa == Qk.fb) f *= 0.5;
+            if (pq.x == pq.y) f *= 0.5;
+            const int ncd = Qk.na * Qk.nb, nI = Pb.na * Pb.nb * ncd;
+            const int ofa = KET ? Pb.fa : Qk.fa, ofb = KET ? Pb.fb : Qk.fb, onb = KET ? Pb.nb : Qk.nb;
+            const double* __restrict__ blk = ints + out_off[q];
+            for (int k = lane; k < nI; k += 32) {
+                const int ab = k / ncd, cd = k - ab * ncd;
+                const int own = KET ? cd : ab, oth = KET ? ab : cd;
+                const int o1 = oth / onb, o2 = oth - o1 * onb;
+                const double v = __ldg(blk + k) * __ldg(D + (size_t)(ofa + o1) * n + ofb + o2);
+                atomicAdd(acc + own, f * v);  // shared memory
+            }
+        }
+        __syncwarp();
+        for (int i = lane; i < nown; i += 32) {
+            const int i1 = i / O.nb, i2 = i - i1 * O.nb;
+            rawJ[(size_t)(O.fa + i1) * n + O.fb + i2] += acc[i];
+        }
+        __syncwarp();
     }
 }
 
@@ -293,10 +356,33 @@ void launch_eri(const EriDev& e, const int2* quartets, const long long* out_off,
 void launch_jk_contract(const EriDev& e, const int2* quartets, const long long* out_off, long long q0, long long nq,
                         long long base, const double* ints, int n, int nmat, const double* D, double* rawJ,
                         double* rawK, cudaStream_t s) {
-    for (long long c = 0; c < nq; c += (1LL << 30)) {
-        const long long m = nq - c < (1LL << 30) ? nq - c : (1LL << 30);
-        jk_contract_kernel<<<(unsigned)m, kEriThreads, 0, s>>>(e, quartets, out_off, q0 + c, base, ints, n, nmat, D,
-                                                               rawJ, rawK);
+    if (nq <= 0 || (!rawJ && !rawK)) return;
+    int dev = 0, sms = 0;
+    CGB_CUDA(cudaGetDevice(&dev));
+    CGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const long long want = (nq + kJkWarps - 1) / kJkWarps;
+    const unsigned blocks = (unsigned)(want < (long long)sms * 8 ? want : (long long)sms * 8);
+    jk_contract_kernel<<<blocks, 32 * kJkWarps, 0, s>>>(e, quartets, out_off, q0, nq, base, ints, n, nmat, D, rawJ,
+                                                      rawK);
+    CGB_CUDA(cudaGetLastError());
+}
+
+void launch_coulomb_passes(const EriDev& e, const int2* quartets, const long long* out_off, const long long* bra_seg,
+                           const long long* ket_seg, const long long* ket_idx, int npairs, const double* ints, int n,
+                           int nmat, const double* D, double* rawJ, cudaStream_t s) {
+    if (npairs <= 0) return;
+    int dev = 0, sms = 0;
+    CGB_CUDA(cudaGetDevice(&dev));
+    CGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int want = (npairs + kJWarps - 1) / kJWarps;
+    const unsigned blocks = (unsigned)(want < sms * 8 ? want : sms * 8);
+    const size_t nn = (size_t)n * n;
+    for (int m = 0; m < nmat; m++) {
+        coulomb_pass_kernel<false><<<blocks, 32 * kJWarps, 0, s>>>(e, quartets, out_off, bra_seg, nullptr, npairs,
+                                                                   ints, n, D + m * nn, rawJ + m * nn);
+        CGB_CUDA(cudaGetLastError());
+        coulomb_pass_kernel<true><<<blocks, 32 * kJWarps, 0, s>>>(e, quartets, out_off, ket_seg, ket_idx, npairs,
+                                                                  ints, n, D + m * nn, rawJ + m * nn);
         CGB_CUDA(cudaGetLastError());
     }
 }

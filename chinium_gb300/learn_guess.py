@@ -37,7 +37,7 @@ def main():
     ap.add_argument("--out", default=G.DEFAULT_WEIGHTS)
     ap.add_argument("--residual", type=int, default=1, help="learn (converged - SAP) blocks")
     ap.add_argument("--test-kmax", type=int, default=0)
-    ap.add_argument("--jk", default="cuda", choices=["cpu", "cuda"])
+    ap.add_argument("--jk", default="engine", choices=["cpu", "engine"])
     ap.add_argument("--eval-only", action="store_true", help="evaluate the weights at --out on held-out clusters")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
                     help="XC builds of the held-out SCFs (mixed: incremental tensor-core builds)")

@@ -3,9 +3,10 @@
 Restates the reference's restricted / unrestricted DIIS SCF
 (src/HartreeFockKohnSham/Restricted/SP.cpp:20-81, Unrestricted/SP.cpp:19-104):
 per iteration, diagonalise the orthogonalised Fock matrix, form the density,
-build Coulomb / exact exchange from the repulsion integrals
-(Int4C2E::ContractInts, src/Integral/Int4C2E.cpp:601-683: J from the total
-density, K scaled by the functional's EXX fraction), call the XC build, and
+build Coulomb / exact exchange from the repulsion integrals (the library's
+GPU engine, the role of Int4C2E::CalculateIntegrals + ContractInts,
+src/Integral/Int4C2E.cpp:567-683: J from the total density, K scaled by the
+functional's EXX fraction), call the XC build, and
 extrapolate with Pulay's commutator DIIS (src/DIIS/CDIIS.cpp:24-47).  The
 energy expression is the reference's E = D.(Hcore + F_hf) + E_xc
 (Restricted/SP.cpp:59) written with the total density.
@@ -67,67 +68,6 @@ class JK:
 
     def exchange(self, D):
         return (self.K @ D.ravel()).reshape(self.n, self.n)
-
-
-def coulomb_pairs(eri):
-    """Pair form of the Coulomb contraction: the (n(n+1)/2)^2 matrix
-    [(mu nu), (l s)] over mu <= nu, l <= s, the pair indices, and the weights
-    (1 on the diagonal, 2 off it) that fold D_ls + D_sl into one element."""
-    n = eri.shape[0]
-    iu, ju = np.triu_indices(n)
-    pair = iu * n + ju
-    return eri.reshape(n * n, n * n)[np.ix_(pair, pair)], iu, ju, np.where(iu == ju, 1.0, 2.0)
-
-
-def coulomb_from_pairs(Jp, iu, ju, n):
-    J = np.empty((n, n))
-    J[iu, ju] = Jp
-    J[ju, iu] = Jp
-    return J
-
-
-class JKDevice:
-    """Coulomb and exchange matrices from repulsion integrals resident in HBM.
-    J uses the pair symmetry (mu nu|ls) = (nu mu|ls) = (mu nu|sl): one
-    (n(n+1)/2)^2 FP64 matrix times the packed density (off-diagonal elements
-    doubled), a quarter of the full n^4 array.  The exchange layout
-    (mu l|nu s) -> [mu nu, l s] is made on the first exchange() call (hybrid
-    functionals only).  Caller-side plumbing for the SCF: torch only moves and
-    multiplies the arrays."""
-
-    def __init__(self, eri):
-        import torch
-        self.torch = torch
-        n = eri.shape[0]
-        self.n = n
-        Jpairs, self.iu, self.ju, self.pair_w = coulomb_pairs(eri)
-        self.J = torch.from_numpy(Jpairs).cuda()
-        del Jpairs
-        self._eri = eri
-        self.K = None
-
-    def coulomb(self, D):
-        return self.coulomb_end(self.coulomb_begin(D))
-
-    def coulomb_begin(self, D):
-        """Enqueue J on torch's current stream and return at once (the XC
-        build, on the grid's own stream, can run meanwhile)."""
-        torch = self.torch
-        d = torch.from_numpy(np.ascontiguousarray(D[self.iu, self.ju] * self.pair_w)).pin_memory()
-        return self.J @ d.cuda(non_blocking=True)
-
-    def coulomb_end(self, h):
-        return coulomb_from_pairs(h.cpu().numpy(), self.iu, self.ju, self.n)
-
-    def exchange(self, D):
-        torch = self.torch
-        n = self.n
-        if self.K is None:
-            t = torch.from_numpy(np.ascontiguousarray(self._eri)).cuda()
-            self.K = t.permute(0, 2, 1, 3).contiguous().reshape(n * n, n * n)
-            del t
-        d = torch.from_numpy(np.ascontiguousarray(D).ravel()).cuda()
-        return (self.K @ d).reshape(n, n).cpu().numpy()
 
 
 class JKEngine:
@@ -199,10 +139,15 @@ def overlap_metric(S, ctx=None):
     return m
 
 
-def make_jk(eri, device):
-    if device == "cuda":
-        return JKDevice(eri)
-    return JK(eri)
+def make_jk(basis, device, eri_threshold=1e-12):
+    """J/K provider of an SCF: "engine" (or "cuda"): the library's GPU
+    integrals and contraction; "cpu": the full host integral tensor with numpy
+    contractions (small molecules, host-side checks)."""
+    if device in ("engine", "cuda"):
+        return JKEngine(basis)
+    if device == "cpu":
+        return JK(repulsion(basis, eri_threshold))
+    raise ValueError("jk_device must be 'engine', 'cuda' or 'cpu'")
 
 
 class DIIS:
@@ -260,7 +205,7 @@ def occupations(Z, charge, mult):
 
 def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, mult=1, precision="fp64",
             guess="sap", conv_energy=1e-8, conv_grad=1e-6, max_iter=100, diis_size=20, screen=0.0,
-            eri_threshold=1e-12, anchor_every=0, context=None, verbose=False, jk_device="cpu", anchor="fp64"):
+            eri_threshold=1e-12, anchor_every=0, context=None, verbose=False, jk_device="engine", anchor="fp64"):
     """Kohn-Sham SCF.  precision: "fp64" (plain XC build every iteration) or
     "mixed" (incremental tensor-core XC builds after a first build that sets
     the references: anchor "fp64", a full FP64 build, or "density", FP64
@@ -272,9 +217,9 @@ def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, m
     half of max_iter), or a density matrix (total for RKS, [Da, Db] for UKS).
     context: reuse integrals and grid from a previous call on the same
     molecule ({"basis","S","H","jk","grid","Enuc"}).
-    jk_device: "cpu" (host repulsion integrals, numpy contraction), "cuda"
-    (host repulsion integrals moved to HBM, torch contraction) or "engine"
-    (integrals computed and contracted on the GPU by the library, JKEngine)."""
+    jk_device: "engine" (alias "cuda": integrals computed on the GPU, kept in
+    HBM and contracted there by the library, JKEngine) or "cpu" (the full
+    host integral tensor, numpy contraction; small molecules)."""
     t_start = time.perf_counter()
     timings = {"setup": 0.0, "xc": 0.0, "jk": 0.0, "diag": 0.0}
     na, nb = occupations(Z, charge, mult)
@@ -285,8 +230,7 @@ def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, m
     if "basis" not in ctx:
         b = Basis(Z, xyz, basis)
         S, T, Vn = one_electron(b)
-        jk_ = JKEngine(b) if jk_device == "engine" else make_jk(repulsion(b, eri_threshold), jk_device)
-        ctx.update(basis=b, S=S, H=T + Vn, jk=jk_, Enuc=M.nuclear_repulsion(Z, xyz))
+        ctx.update(basis=b, S=S, H=T + Vn, jk=make_jk(b, jk_device, eri_threshold), Enuc=M.nuclear_repulsion(Z, xyz))
     key = ("grid", nspin, functional, grid, screen)
     xc = ExchangeCorrelation(spin=nspin).Read(functional)
     if ctx.get("grid_key") != key:

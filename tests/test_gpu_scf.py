@@ -48,26 +48,27 @@ def test_sap_guess_beats_core_guess():
     assert r_sap.iterations <= r_core.iterations
 
 
-def test_device_jk_matches_host_jk():
-    """J/K from integrals resident in HBM give the same SCF as the host path."""
+def test_gpu_jk_engine_matches_host_jk_in_scf():
+    """J/K from the GPU integral engine give the same SCF as the host
+    integral tensor (B3LYP: Coulomb and exact exchange)."""
     pytest.importorskip("torch")
     Z, xyz = M.h2o()
-    r_cpu = run_scf(Z, xyz, functional="B3LYP", jk_device="cpu")
-    r_gpu = run_scf(Z, xyz, functional="B3LYP", jk_device="cuda")
+    r_cpu = run_scf(Z, xyz, functional="B3LYP", jk_device="cpu", eri_threshold=0.0)
+    r_gpu = run_scf(Z, xyz, functional="B3LYP", jk_device="engine")
     assert r_cpu.converged and r_gpu.converged
     assert abs(r_cpu.energy - r_gpu.energy) < 1e-9
 
 
-def test_device_coulomb_pairs_and_exchange_match_host():
+def test_engine_coulomb_and_exchange_match_host():
     pytest.importorskip("torch")
-    from chinium_gb300.scf import JK, JKDevice, repulsion
+    from chinium_gb300.scf import JK, JKEngine, repulsion
     from chinium_gb300.xc import Basis
     Z, xyz = M.h2o()
-    eri = repulsion(Basis(Z, xyz, "def2-svp"))
+    b = Basis(Z, xyz, "def2-svp")
     rng = np.random.default_rng(5)
     D = rng.normal(size=(24, 24))
     D = D + D.T
-    host, dev = JK(eri), JKDevice(eri)
+    host, dev = JK(repulsion(b, 0.0)), JKEngine(b)
     assert np.abs(dev.coulomb(D) - host.coulomb(D)).max() < 1e-11
     assert np.abs(dev.exchange(D) - host.exchange(D)).max() < 1e-11
 
@@ -76,9 +77,9 @@ def test_mixed_scf_with_learned_guess_uses_tensor_core_sap():
     """precision="mixed" builds the learned guess's SAP base on the tensor
     cores; the SCF still converges to the FP64 energy."""
     Z, xyz = M.water_clusters(1, seed=99, kmin=2, kmax=2)[0]
-    r64 = run_scf(Z, xyz, functional="PBE", precision="fp64", jk_device="cuda")
+    r64 = run_scf(Z, xyz, functional="PBE", precision="fp64", jk_device="engine")
     rl = run_scf(Z, xyz, functional="PBE", precision="mixed", guess="learned", anchor="density",
-                 context=r64.context, jk_device="cuda")
+                 context=r64.context, jk_device="engine")
     assert rl.converged and rl.guess_used == "learned"
     assert abs(rl.energy - r64.energy) < 1e-6
 

@@ -4,7 +4,7 @@ commutator DIIS (src/DIIS/CDIIS.cpp:24-47), and the packed-pair Coulomb
 contraction used by the HBM-resident J."""
 import numpy as np
 
-from chinium_gb300.scf import DIIS, coulomb_from_pairs, coulomb_pairs
+from chinium_gb300.scf import DIIS
 
 
 def _pulay(Fs, Es):
@@ -39,18 +39,40 @@ def test_diis_kept_products_match_full_recompute():
             np.testing.assert_allclose(a, b, rtol=1e-10, atol=1e-12)
 
 
-def test_packed_pair_coulomb_matches_full_contraction():
-    """J_mn = sum_ls (mn|ls) D_ls through the (n(n+1)/2)^2 pair matrix and
-    the packed density with doubled off-diagonal elements."""
+def test_canonical_quartet_jk_algebra_matches_full_contraction():
+    """The contraction rule of the GPU J/K engine (k_eri.cu), restated: every
+    unique shell quartet (a >= b, c >= d, bra pair >= ket pair, pairs in any
+    order) contributes its full function block once, scaled by 1/2 for each
+    of a == b, c == d and equal pairs, to rawJ(a,b), rawJ(c,d), rawK(a,c),
+    rawK(b,d), rawK(a,d), rawK(b,c); then J = 2 (rawJ + rawJ^T) and
+    K = rawK + rawK^T are the full contractions J_mn = sum (mn|ls) D_ls and
+    K_mn = sum (ml|ns) D_ls."""
     rng = np.random.default_rng(3)
-    n = 7
+    sizes = [1, 3, 1, 5, 3, 7]
+    first = np.concatenate([[0], np.cumsum(sizes)[:-1]])
+    n = sum(sizes)
     A = rng.normal(size=(n, n, n, n))
     eri = A + A.transpose(1, 0, 2, 3)
     eri = eri + eri.transpose(0, 1, 3, 2)
     eri = eri + eri.transpose(2, 3, 0, 1)
     D = rng.normal(size=(n, n))
     D = D + D.T
-    P, iu, ju, w = coulomb_pairs(eri)
-    assert P.shape == (n * (n + 1) // 2,) * 2
-    J = coulomb_from_pairs(P @ (D[iu, ju] * w), iu, ju, n)
-    np.testing.assert_allclose(J, np.einsum("mnls,ls->mn", eri, D), rtol=1e-12, atol=1e-12)
+    pairs = [(a, b) for a in range(len(sizes)) for b in range(a + 1)]
+    rng.shuffle(pairs)  # the engine orders pairs by their Schwarz bound: any order works
+    rawJ, rawK = np.zeros((n, n)), np.zeros((n, n))
+    sl = lambda s: slice(first[s], first[s] + sizes[s])
+    for i, (a, b) in enumerate(pairs):
+        for j in range(i + 1):
+            c, d = pairs[j]
+            f = (0.5 if a == b else 1.0) * (0.5 if c == d else 1.0) * (0.5 if i == j else 1.0)
+            I = f * eri[sl(a), sl(b), sl(c), sl(d)]
+            rawJ[sl(a), sl(b)] += np.einsum("abcd,cd->ab", I, D[sl(c), sl(d)])
+            rawJ[sl(c), sl(d)] += np.einsum("abcd,ab->cd", I, D[sl(a), sl(b)])
+            rawK[sl(a), sl(c)] += np.einsum("abcd,bd->ac", I, D[sl(b), sl(d)])
+            rawK[sl(b), sl(d)] += np.einsum("abcd,ac->bd", I, D[sl(a), sl(c)])
+            rawK[sl(a), sl(d)] += np.einsum("abcd,bc->ad", I, D[sl(b), sl(c)])
+            rawK[sl(b), sl(c)] += np.einsum("abcd,ad->bc", I, D[sl(a), sl(d)])
+    J = 2 * (rawJ + rawJ.T)
+    K = rawK + rawK.T
+    np.testing.assert_allclose(J, np.einsum("mnls,ls->mn", eri, D), rtol=1e-12, atol=1e-11)
+    np.testing.assert_allclose(K, np.einsum("mlns,ls->mn", eri, D), rtol=1e-12, atol=1e-11)
