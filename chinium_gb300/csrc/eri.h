@@ -62,14 +62,14 @@ void launch_jk_contract(const EriDev& e, const int2* quartets, const long long* 
                         long long base, const double* ints, int n, int nmat, const double* D, double* rawJ,
                         double* rawK, cudaStream_t s);
 
-// rawJ of nmat matrices from in-core blocks without global atomics: pass A
-// over every bra pair's consecutive quartets (bra_seg: npairs + 1 offsets
-// into the quartet list), pass B over every ket pair's quartets (ket_seg
-// offsets into ket_idx, the quartet indices grouped by ket pair).  rawJ must
-// start at zero.
-void launch_coulomb_passes(const EriDev& e, const int2* quartets, const long long* out_off, const long long* bra_seg,
-                           const long long* ket_seg, const long long* ket_idx, int npairs, const double* ints, int n,
-                           int nmat, const double* D, double* rawJ, cudaStream_t s);
+// Dense Coulomb operator M (ld x ld, ld = n (n + 1) / 2 rounded up to even,
+// packed pairs mu >= nu) from the in-core blocks of all quartets; M must
+// start at zero.  Then J of nmat densities: pack (x2 off-diagonal) into x
+// (nmat vectors of stride ld, zeroed once by the caller), GEMV into y, unpack.
+void launch_coulomb_scatter(const EriDev& e, const int2* quartets, const long long* out_off, long long nq,
+                            const double* ints, long long ld, double* M, cudaStream_t s);
+void launch_coulomb_dense(int n, int nmat, long long ld, const double* M, const double* D, double* x, double* y,
+                          double* J, cudaStream_t s);
 
 // rawJ, rawK -> J = 2 (rawJ + rawJ^T), K = rawK + rawK^T (nmat matrices each, either may be null).
 void launch_jk_symmetrise(int n, int nmat, const double* rawJ, const double* rawK, double* J, double* K,

@@ -44,7 +44,10 @@ struct JkEngine {
     DevBuf<double> d_pp_p, d_pp_P, d_ep, d_boys;
     DevBuf<int2> d_quartets;
     DevBuf<long long> d_off;
-    DevBuf<long long> d_bra_seg, d_ket_seg, d_ket_idx;  // quartets grouped by bra pair / by ket pair
+    bool dense_j = false;                     // J from the dense Coulomb operator over function pairs
+    long long npair = 0;                      // row stride of the dense operator (pairs, rounded up to even)
+    int dense_nmat = 0;
+    DevBuf<double> d_M, d_x, d_y;             // dense operator; packed densities and results
     DevBuf<double> d_ints;                    // in-core integrals, or the direct-mode chunk buffer
     DevBuf<double> d_D, d_rawJ, d_rawK, d_J, d_K;
     int nmat_alloc = 0;
@@ -167,23 +170,6 @@ void JkEngine::setup(const BasisSet& b, double thr, double max_bytes) {
     CGB_CHECK(nquartets > 0, XC_ERR_ARG, "no shell quartet above the threshold");
     d_quartets.upload(quart.data(), quart.size(), stream);
     d_off.upload(off.data(), off.size(), stream);
-    {
-        // bra segments (the list is bra-major) and the ket-grouped index (counting sort)
-        std::vector<long long> bseg(npk + 1, 0), kseg(npk + 1, 0), kidx(quart.size());
-        for (const int2& t : quart) {
-            bseg[t.x + 1]++;
-            kseg[t.y + 1]++;
-        }
-        for (int i = 0; i < npk; i++) {
-            bseg[i + 1] += bseg[i];
-            kseg[i + 1] += kseg[i];
-        }
-        std::vector<long long> fill(kseg.begin(), kseg.end() - 1);
-        for (long long q = 0; q < (long long)quart.size(); q++) kidx[fill[quart[q].y]++] = q;
-        d_bra_seg.upload(bseg.data(), bseg.size(), stream);
-        d_ket_seg.upload(kseg.data(), kseg.size(), stream);
-        d_ket_idx.upload(kidx.data(), kidx.size(), stream);
-    }
     // in-core when the integrals fit in the budget (default: half of the free memory)
     size_t freeb = 0, totalb = 0;
     CGB_CUDA(cudaMemGetInfo(&freeb, &totalb));
@@ -193,6 +179,18 @@ void JkEngine::setup(const BasisSet& b, double thr, double max_bytes) {
     if (incore) {
         d_ints.alloc(nints);
         launch_eri(dev(), d_quartets.p, d_off.p, 0, nquartets, 0, d_ints.p, stream);
+        // small molecules: the dense Coulomb operator when it takes at most a
+        // quarter of the memory left (J then streams it once per build)
+        npair = (long long)n * (n + 1) / 2;
+        npair += npair & 1;  // even row stride (16-byte rows for the GEMV)
+        CGB_CUDA(cudaStreamSynchronize(stream));
+        CGB_CUDA(cudaMemGetInfo(&freeb, &totalb));
+        dense_j = (double)npair * npair * sizeof(double) <= 0.25 * (double)freeb;
+        if (dense_j) {
+            d_M.alloc((size_t)npair * npair);
+            d_M.zero(stream);
+            launch_coulomb_scatter(dev(), d_quartets.p, d_off.p, nquartets, d_ints.p, npair, d_M.p, stream);
+        }
         CGB_CUDA(cudaStreamSynchronize(stream));
     } else {
         // chunks of consecutive quartets whose blocks fit in the chunk buffer
@@ -225,14 +223,25 @@ void JkEngine::build_device(int nmat, const double* dD, double* dJ, double* dK) 
     double* rK = dK ? d_rawK.p : nullptr;
     if (rJ) CGB_CUDA(cudaMemsetAsync(rJ, 0, nn * nmat * sizeof(double), stream));
     if (rK) CGB_CUDA(cudaMemsetAsync(rK, 0, nn * nmat * sizeof(double), stream));
-    if (incore) {
-        // J by the two atomic-free passes; K (hybrids) by the per-quartet kernel
-        if (rJ)
-            launch_coulomb_passes(dev(), d_quartets.p, d_off.p, d_bra_seg.p, d_ket_seg.p, d_ket_idx.p,
-                                  (int)pairs.size(), d_ints.p, n, nmat, dD, rJ, stream);
+    if (incore && dense_j) {
+        // J from the dense operator (written straight into dJ); K from the blocks
+        if (dJ) {
+            if (nmat > dense_nmat) {
+                d_x.alloc((size_t)npair * nmat);
+                d_x.zero(stream);  // pad entries stay zero
+                d_y.alloc((size_t)npair * nmat);
+                dense_nmat = nmat;
+            }
+            launch_coulomb_dense(n, nmat, npair, d_M.p, dD, d_x.p, d_y.p, dJ, stream);
+        }
         if (rK)
             launch_jk_contract(dev(), d_quartets.p, d_off.p, 0, nquartets, 0, d_ints.p, n, nmat, dD, nullptr, rK,
                                stream);
+        launch_jk_symmetrise(n, nmat, nullptr, rK, nullptr, dK, stream);
+        return;
+    }
+    if (incore) {
+        launch_jk_contract(dev(), d_quartets.p, d_off.p, 0, nquartets, 0, d_ints.p, n, nmat, dD, rJ, rK, stream);
     } else {
         for (size_t c = 0; c + 1 < chunk_q.size(); c++) {
             const long long q0 = chunk_q[c], q1 = chunk_q[c + 1];

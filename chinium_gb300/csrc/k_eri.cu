@@ -13,8 +13,9 @@
 //
 // jk_contract_kernel: one warp per quartet block; each lane forms elements
 // of the six J / K sub-blocks it feeds (2 J, 4 K), scaled by the quartet's
-// degeneracy, with one FP64 atomic per element.  coulomb_pass_kernel: J of
-// in-core blocks in two atomic-free passes (per bra pair, per ket pair).
+// degeneracy, with one FP64 atomic per element.  Small molecules take J from
+// a dense Coulomb operator over function pairs filled once from the blocks
+// (coulomb_scatter_kernel) and a GEMV per build (coulomb_gemv_kernel).
 #include "common.h"
 #include "eri.h"
 
@@ -260,57 +261,108 @@ __global__ void __launch_bounds__(32 * kJkWarps) jk_contract_kernel(EriDev e, co
     }
 }
 
-// Coulomb contraction without global atomics, in two passes over the
-// in-core blocks.  Pass A: one warp per bra pair P walks P's quartets (they
-// are consecutive in the list) and accumulates y[ab] = sum_q f_q sum_cd
-// I_q[ab][cd] D(c, d) in shared memory; pass B: one warp per ket pair Q walks
-// the quartets whose ket is Q (a transposed index) and accumulates
-// z[cd] = sum_q f_q sum_ab I_q[ab][cd] D(a, b).  Each warp owns its pair's
-// block of rawJ (pass B runs after pass A); lanes read the blocks coalesced.
-constexpr int kJWarps = 8;
-constexpr int kPairMax = 49;  // functions of a shell pair (f f)
-template <bool KET>
-__global__ void __launch_bounds__(32 * kJWarps) coulomb_pass_kernel(EriDev e, const int2* __restrict__ quartets,
-                                                                     const long long* __restrict__ out_off,
-                                                                     const long long* __restrict__ seg,
-                                                                     const long long* __restrict__ idx, int npairs,
-                                                                     const double* __restrict__ ints, int n,
-                                                                     const double* __restrict__ D,
-                                                                     double* __restrict__ rawJ) {
-    __shared__ double acc_s[kJWarps][kPairMax];
-    const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
-    double* acc = acc_s[wl];
-    for (int p = blockIdx.x * kJWarps + wl; p < npairs; p += gridDim.x * kJWarps) {
-        const EriPair O = e.pairs[p];  // the pair that owns the output block
-        const int nown = O.na * O.nb;
-        for (int i = lane; i < nown; i += 32) acc[i] = 0.0;
-        __syncwarp();
-        for (long long s = seg[p]; s < seg[p + 1]; s++) {
-            const long long q = KET ? idx[s] : s;
-            const int2 pq = quartets[q];
-            const EriPair Pb = e.pairs[pq.x], Qk = e.pairs[pq.y];
-            double f = 1.0;
-            if (Pb.fa == Pb.fb) f *= 0.5;
-            if (Qk.fa == Qk.fb) f *= 0.5;
-            if (pq.x == pq.y) f *= 0.5;
-            const int ncd = Qk.na * Qk.nb, nI = Pb.na * Pb.nb * ncd;
-            const int ofa = KET ? Pb.fa : Qk.fa, ofb = KET ? Pb.fb : Qk.fb, onb = KET ? Pb.nb : Qk.nb;
-            const double* __restrict__ blk = ints + out_off[q];
-            for (int k = lane; k < nI; k += 32) {
-                const int ab = k / ncd, cd = k - ab * ncd;
-                const int own = KET ? cd : ab, oth = KET ? ab : cd;
-                const int o1 = oth / onb, o2 = oth - o1 * onb;
-                const double v = __ldg(blk + k) * __ldg(D + (size_t)(ofa + o1) * n + ofb + o2);
-                atomicAdd(acc + own, f * v);  // shared memory
+// Dense Coulomb operator of small molecules: M[(mu nu), (la si)] =
+// (mu nu|la si) over packed pairs mu >= nu (p = mu (mu + 1) / 2 + nu), filled
+// once from the in-core quartet blocks (warp per quartet, both (P, Q) and
+// (Q, P) entries; screened-out quartets stay zero), rows of stride ld (npair
+// rounded up to even, the pad column zero).  J of a density is then M d with
+// d_p = D(mu, nu) (x 2 off the diagonal): a GEMV that streams M from HBM once
+// per build.
+__device__ __forceinline__ long long pair_index(int i, int j) {
+    return i >= j ? (long long)i * (i + 1) / 2 + j : (long long)j * (j + 1) / 2 + i;
+}
+
+__global__ void __launch_bounds__(256) coulomb_scatter_kernel(EriDev e, const int2* __restrict__ quartets,
+                                                              const long long* __restrict__ out_off, long long nq,
+                                                              const double* __restrict__ ints, long long ld,
+                                                              double* __restrict__ M) {
+    const int lane = threadIdx.x & 31;
+    const long long w0 = (long long)blockIdx.x * 8 + (threadIdx.x >> 5), nw = (long long)gridDim.x * 8;
+    for (long long q = w0; q < nq; q += nw) {
+        const int2 pq = quartets[q];
+        const EriPair P = e.pairs[pq.x], Q = e.pairs[pq.y];
+        const int nb = P.nb, nc = Q.na, nd = Q.nb, ncd = nc * nd, nI = P.na * nb * ncd;
+        const double* __restrict__ blk = ints + out_off[q];
+        for (int k = lane; k < nI; k += 32) {
+            const int ab = k / ncd, cd = k - ab * ncd;
+            const int ia = ab / nb, ib = ab - ia * nb, ic = cd / nd, id = cd - ic * nd;
+            const long long p1 = pair_index(P.fa + ia, P.fb + ib), p2 = pair_index(Q.fa + ic, Q.fb + id);
+            const double v = blk[k];
+            M[p1 * ld + p2] = v;
+            M[p2 * ld + p1] = v;
+        }
+    }
+}
+
+// d_p of nmat densities (n x n each) -> x[m][p] (vectors of stride ld)
+__global__ void coulomb_pack_kernel(int n, int nmat, long long npair, const double* __restrict__ D,
+                                    double* __restrict__ x) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)n * n * nmat) return;
+    const int m = (int)(t / ((long long)n * n));
+    const long long r = t - (long long)m * n * n;
+    const int i = (int)(r / n), j = (int)(r - (long long)i * n);
+    if (j > i) return;
+    x[m * npair + pair_index(i, j)] = (i == j ? 1.0 : 2.0) * D[t];
+}
+
+// y[m] = M x[m] for NM <= 4 vectors in one pass over M (npair rows of
+// stride npair here being the even row stride ld): one warp per row, four
+// independent 16-byte loads of M per lane in flight per step (a single
+// outstanding load per warp leaves HBM at ~10% of its rate).
+constexpr int kGemvMaxVec = 4;
+template <int NM>
+__global__ void __launch_bounds__(256) coulomb_gemv_kernel(long long npair, const double* __restrict__ M,
+                                                           const double* __restrict__ x, double* __restrict__ y) {
+    const int lane = threadIdx.x & 31;
+    const long long w0 = (long long)blockIdx.x * 8 + (threadIdx.x >> 5), nw = (long long)gridDim.x * 8;
+    const long long nc2 = npair / 2;
+    for (long long r = w0; r < npair; r += nw) {
+        const double2* __restrict__ row2 = reinterpret_cast<const double2*>(M + r * npair);
+        double acc[NM];
+#pragma unroll
+        for (int m = 0; m < NM; m++) acc[m] = 0.0;
+        long long c = lane;
+        for (; c + 96 < nc2; c += 128) {
+            double2 v[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) v[u] = __ldcs(row2 + c + 32 * u);
+#pragma unroll
+            for (int m = 0; m < NM; m++) {
+                const double2* __restrict__ x2 = reinterpret_cast<const double2*>(x + m * npair);
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const double2 xv = __ldg(x2 + c + 32 * u);
+                    acc[m] = fma(v[u].x, xv.x, fma(v[u].y, xv.y, acc[m]));
+                }
             }
         }
-        __syncwarp();
-        for (int i = lane; i < nown; i += 32) {
-            const int i1 = i / O.nb, i2 = i - i1 * O.nb;
-            rawJ[(size_t)(O.fa + i1) * n + O.fb + i2] += acc[i];
+        for (; c < nc2; c += 32) {
+            const double2 v = __ldcs(row2 + c);
+#pragma unroll
+            for (int m = 0; m < NM; m++) {
+                const double2 xv = __ldg(reinterpret_cast<const double2*>(x + m * npair) + c);
+                acc[m] = fma(v.x, xv.x, fma(v.y, xv.y, acc[m]));
+            }
         }
-        __syncwarp();
+#pragma unroll
+        for (int m = 0; m < NM; m++) {
+            double v = acc[m];
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+            if (lane == 0) y[m * npair + r] = v;
+        }
     }
+}
+
+// J[m](i, j) = y[m][p(i, j)]
+__global__ void coulomb_unpack_kernel(int n, int nmat, long long npair, const double* __restrict__ y,
+                                      double* __restrict__ J) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)n * n * nmat) return;
+    const int m = (int)(t / ((long long)n * n));
+    const long long r = t - (long long)m * n * n;
+    const int i = (int)(r / n), j = (int)(r - (long long)i * n);
+    J[t] = y[m * npair + pair_index(i, j)];
 }
 
 __global__ void jk_symmetrise_kernel(int n, int nmat, const double* __restrict__ rawJ, const double* __restrict__ rawK,
@@ -367,24 +419,41 @@ void launch_jk_contract(const EriDev& e, const int2* quartets, const long long* 
     CGB_CUDA(cudaGetLastError());
 }
 
-void launch_coulomb_passes(const EriDev& e, const int2* quartets, const long long* out_off, const long long* bra_seg,
-                           const long long* ket_seg, const long long* ket_idx, int npairs, const double* ints, int n,
-                           int nmat, const double* D, double* rawJ, cudaStream_t s) {
-    if (npairs <= 0) return;
+static unsigned persistent_blocks(long long items, int per_block) {
     int dev = 0, sms = 0;
     CGB_CUDA(cudaGetDevice(&dev));
     CGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    const int want = (npairs + kJWarps - 1) / kJWarps;
-    const unsigned blocks = (unsigned)(want < sms * 8 ? want : sms * 8);
-    const size_t nn = (size_t)n * n;
-    for (int m = 0; m < nmat; m++) {
-        coulomb_pass_kernel<false><<<blocks, 32 * kJWarps, 0, s>>>(e, quartets, out_off, bra_seg, nullptr, npairs,
-                                                                   ints, n, D + m * nn, rawJ + m * nn);
-        CGB_CUDA(cudaGetLastError());
-        coulomb_pass_kernel<true><<<blocks, 32 * kJWarps, 0, s>>>(e, quartets, out_off, ket_seg, ket_idx, npairs,
-                                                                  ints, n, D + m * nn, rawJ + m * nn);
+    const long long want = (items + per_block - 1) / per_block;
+    return (unsigned)(want < (long long)sms * 8 ? (want > 0 ? want : 1) : (long long)sms * 8);
+}
+
+void launch_coulomb_scatter(const EriDev& e, const int2* quartets, const long long* out_off, long long nq,
+                            const double* ints, long long ld, double* M, cudaStream_t s) {
+    if (nq <= 0) return;
+    coulomb_scatter_kernel<<<persistent_blocks(nq, 8), 256, 0, s>>>(e, quartets, out_off, nq, ints, ld, M);
+    CGB_CUDA(cudaGetLastError());
+}
+
+void launch_coulomb_dense(int n, int nmat, long long ld, const double* M, const double* D, double* x, double* y,
+                          double* J, cudaStream_t s) {
+    CGB_CHECK(ld % 2 == 0 && ld >= (long long)n * (n + 1) / 2, XC_ERR_INTERNAL, "bad dense Coulomb row stride");
+    const long long tot = (long long)n * n * nmat;
+    // x: nmat vectors of stride ld whose pad entry stays zero (the caller zeroes x once)
+    coulomb_pack_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(n, nmat, ld, D, x);
+    CGB_CUDA(cudaGetLastError());
+    const unsigned blocks = persistent_blocks(ld, 8);
+    for (int m0 = 0; m0 < nmat; m0 += kGemvMaxVec) {
+        const int nm = nmat - m0 < kGemvMaxVec ? nmat - m0 : kGemvMaxVec;
+        const double* xm = x + m0 * ld;
+        double* ym = y + m0 * ld;
+        if (nm == 1) coulomb_gemv_kernel<1><<<blocks, 256, 0, s>>>(ld, M, xm, ym);
+        else if (nm == 2) coulomb_gemv_kernel<2><<<blocks, 256, 0, s>>>(ld, M, xm, ym);
+        else if (nm == 3) coulomb_gemv_kernel<3><<<blocks, 256, 0, s>>>(ld, M, xm, ym);
+        else coulomb_gemv_kernel<4><<<blocks, 256, 0, s>>>(ld, M, xm, ym);
         CGB_CUDA(cudaGetLastError());
     }
+    coulomb_unpack_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(n, nmat, ld, y, J);
+    CGB_CUDA(cudaGetLastError());
 }
 
 void launch_jk_symmetrise(int n, int nmat, const double* rawJ, const double* rawK, double* J, double* K,

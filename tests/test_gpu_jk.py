@@ -31,6 +31,8 @@ CASES = {
     "h2o_svp": (M.h2o, "def2-svp"),
     "h2o_tzvp": (M.h2o, "def2-tzvp"),  # f shells on O
     "water4_svp": (lambda: M.water_clusters(1, seed=5, kmin=4, kmax=4)[0], "def2-svp"),
+    # 34 functions: an odd number of function pairs (the dense Coulomb operator's padded row stride)
+    "methane_svp": (lambda: M.alkane(1, np.random.default_rng(0)), "def2-svp"),
 }
 
 
