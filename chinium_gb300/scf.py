@@ -88,6 +88,7 @@ class JKEngine:
         self._h = h
         self.stream = torch.cuda.Stream()
         check(lib().xc_jk_set_stream(h, ctypes.c_void_p(self.stream.cuda_stream)))
+        self._pinned = None  # page-locked upload buffer, reused (pinning per call costs ~1 ms)
 
     def info(self):
         nq, ni, ic = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_int()
@@ -97,8 +98,15 @@ class JKEngine:
     def begin(self, Ds, want_k):
         torch = self.torch
         n, m = self.n, len(Ds)
+        if self._pinned is None or self._pinned.shape[0] < m:
+            self.stream.synchronize()
+            self._pinned = torch.empty((m, n, n), dtype=torch.float64).pin_memory()
+        self.stream.synchronize()  # the previous upload from the buffer has completed
+        host = self._pinned[:m]
+        for i, Dm in enumerate(Ds):
+            host[i].numpy()[...] = Dm
         with torch.cuda.stream(self.stream):
-            d = torch.from_numpy(np.ascontiguousarray(np.stack(Ds))).pin_memory().cuda(non_blocking=True)
+            d = host.cuda(non_blocking=True)
             J = torch.empty((m, n, n), dtype=torch.float64, device="cuda")
             K = torch.empty((m, n, n), dtype=torch.float64, device="cuda") if want_k else None
         ptr = lambda t: ctypes.c_void_p(t.data_ptr()) if t is not None else None
@@ -151,17 +159,22 @@ def make_jk(basis, device, eri_threshold=1e-12):
 
 
 class DIIS:
-    """Pulay's commutator DIIS; the error inner products are kept from one
-    push to the next (each push adds one row)."""
+    """Pulay's commutator DIIS (src/DIIS/CDIIS.cpp:24-47); the error inner
+    products are kept from one push to the next (each push adds one row).
+    The history also keeps each iterate's densities and energy, which the
+    ADIIS stage that precedes it uses (the reference's ADIIS run hands its
+    history to CDIIS, Restricted/SP.cpp:75-79)."""
 
     def __init__(self, size=20):
         self.size = size
-        self.F, self.E = [], []
+        self.F, self.E, self.D, self.En = [], [], [], []
         self.G = np.zeros((0, 0))
 
-    def push(self, F, err):
+    def push(self, F, err, D=None, energy=None):
         self.F.append(F)
         self.E.append(err)
+        self.D.append(D)
+        self.En.append(energy)
         row = np.array([sum(np.vdot(a, b) for a, b in zip(e, err)) for e in self.E])
         m = len(self.E)
         G = np.zeros((m, m))
@@ -170,8 +183,8 @@ class DIIS:
         G[:, m - 1] = row
         self.G = G
         if len(self.F) > self.size:
-            self.F.pop(0)
-            self.E.pop(0)
+            for lst in (self.F, self.E, self.D, self.En):
+                lst.pop(0)
             self.G = self.G[1:, 1:]
 
     def extrapolate(self):
@@ -189,6 +202,82 @@ class DIIS:
             return self.F[-1]
         return [sum(ci * Fi[s] for ci, Fi in zip(c, self.F)) for s in range(len(self.F[0]))]
 
+    def extrapolate_adiis(self):
+        """Augmented DIIS (Hu and Yang, J. Chem. Phys. 132, 054109 (2010);
+        src/DIIS/AEDIIS.cpp:29-104): weights x on the simplex minimising
+        x.(A + B x / 2) with A_i = (D_i - D_n).F_n and B_ij = (D_i - D_n).(F_j
+        - F_n), summed over the spin matrices (n the latest iterate), from
+        the reference's start (0.9 on the latest, the rest shared)."""
+        m = len(self.F)
+        if m < 2 or any(d is None for d in self.D):
+            return self.F[-1]
+        ns = len(self.F[0])
+        A = np.zeros(m)
+        B = np.zeros((m, m))
+        for s in range(ns):
+            Dn, Fn = self.D[-1][s], self.F[-1][s]
+            dD = [self.D[i][s] - Dn for i in range(m)]
+            dF = [self.F[j][s] - Fn for j in range(m)]
+            A += np.array([np.vdot(dD[i], Fn) for i in range(m)])
+            B += np.array([[np.vdot(dD[i], dF[j]) for j in range(m)] for i in range(m)])
+        x = minimise_on_simplex(A, B)
+        return [sum(xi * Fi[s] for xi, Fi in zip(x, self.F)) for s in range(ns)]
+
+
+def project_simplex(v):
+    """Euclidean projection onto {x >= 0, sum x = 1} (sort-based)."""
+    u = np.sort(v)[::-1]
+    css = np.cumsum(u) - 1.0
+    k = np.nonzero(u * np.arange(1, len(v) + 1) > css)[0][-1]
+    return np.maximum(v - css[k] / (k + 1), 0.0)
+
+
+def minimise_on_simplex(A, B, iters=400):
+    """min_x x.A + x.B x / 2 over the simplex: accelerated projected gradient
+    (FISTA) from the reference's start, keeping the best iterate (B need not
+    be positive definite).  Small dense numpy only (m <= DIIS size)."""
+    m = len(A)
+    Bs = 0.5 * (B + B.T)
+    L = max(np.abs(np.linalg.eigvalsh(Bs)).max(), 1e-12)
+    f = lambda x: x @ A + 0.5 * x @ Bs @ x
+    x = np.full(m, 0.1 / (m - 1))
+    x[-1] = 0.9
+    y, t, best, fbest = x.copy(), 1.0, x.copy(), f(x)
+    for _ in range(iters):
+        xn = project_simplex(y - (A + Bs @ y) / L)
+        tn = 0.5 * (1.0 + np.sqrt(1.0 + 4.0 * t * t))
+        y = xn + ((t - 1.0) / tn) * (xn - x)
+        step = np.abs(xn - x).max()
+        x, t = xn, tn
+        fx = f(x)
+        if fx < fbest:
+            best, fbest = x.copy(), fx
+        if step < 1e-12:
+            break
+    return best
+
+
+def cayley_update(C, F, nocc):
+    """One orbital update without diagonalisation: the occupied-virtual block
+    of F in the current orbitals C (S-orthonormal columns) gives first-order
+    rotation angles kappa_ai = -F_ai / (F_aa - F_ii), applied as the exactly
+    orthogonal Cayley transform U = (1 - K/2)^-1 (1 + K/2) of the
+    antisymmetric K = [[0, -kappa^T], [kappa, 0]].  At the SCF fixed point
+    (F_ai = 0) it leaves C unchanged, so the converged state is the one a full
+    diagonalisation reaches; the SCF uses it once the DIIS error is small."""
+    Fm = C.T @ F @ C
+    e = np.diag(Fm)
+    o, v = slice(0, nocc), slice(nocc, C.shape[1])
+    denom = np.maximum(e[v][:, None] - e[o][None, :], 1e-2)
+    kap = -Fm[v, o] / denom
+    m = C.shape[1]
+    K = np.zeros((m, m))
+    K[v, o] = kap
+    K[o, v] = -kap.T
+    eye = np.eye(m)
+    U = np.linalg.solve(eye - 0.5 * K, eye + 0.5 * K)
+    return C @ U
+
 
 class Result(dict):
     __getattr__ = dict.__getitem__
@@ -205,7 +294,8 @@ def occupations(Z, charge, mult):
 
 def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, mult=1, precision="fp64",
             guess="sap", conv_energy=1e-8, conv_grad=1e-6, max_iter=100, diis_size=20, screen=0.0,
-            eri_threshold=1e-12, anchor_every=0, context=None, verbose=False, jk_device="engine", anchor="fp64"):
+            eri_threshold=1e-12, anchor_every=0, context=None, verbose=False, jk_device="engine", anchor="fp64",
+            adiis_until=1e-1, rotate_below=1e-2):
     """Kohn-Sham SCF.  precision: "fp64" (plain XC build every iteration) or
     "mixed" (incremental tensor-core XC builds after a first build that sets
     the references: anchor "fp64", a full FP64 build, or "density", FP64
@@ -219,7 +309,12 @@ def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, m
     molecule ({"basis","S","H","jk","grid","Enuc"}).
     jk_device: "engine" (alias "cuda": integrals computed on the GPU, kept in
     HBM and contracted there by the library, JKEngine) or "cpu" (the full
-    host integral tensor, numpy contraction; small molecules)."""
+    host integral tensor, numpy contraction; small molecules).
+    adiis_until: ADIIS extrapolation while the largest commutator element is
+    above this (the reference's 1e-1), CDIIS below; 0 = CDIIS throughout.
+    rotate_below: once that element is below this, new orbitals come from a
+    Cayley rotation of the previous ones (cayley_update) instead of a full
+    diagonalisation; 0 = always diagonalise."""
     t_start = time.perf_counter()
     timings = {"setup": 0.0, "xc": 0.0, "jk": 0.0, "diag": 0.0}
     na, nb = occupations(Z, charge, mult)
@@ -259,7 +354,7 @@ def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, m
         kw = dict(basis=basis, functional=functional, grid=grid, charge=charge, mult=mult, precision=precision,
                   conv_energy=conv_energy, conv_grad=conv_grad, diis_size=diis_size, screen=screen,
                   eri_threshold=eri_threshold, anchor_every=anchor_every, context=ctx, verbose=verbose,
-                  jk_device=jk_device, anchor=anchor)
+                  jk_device=jk_device, anchor=anchor, adiis_until=adiis_until, rotate_below=rotate_below)
         if unrestricted or charge != 0 or not G.supported(Z, b):
             r = run_scf(Z, xyz, guess="sap", max_iter=max_iter, **kw)
             r["guess_used"] = "sap (outside the learned model's scope)"
@@ -295,6 +390,7 @@ def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, m
         raise ValueError("anchor must be 'fp64' or 'density'")
     anchor_code = 1 if anchor == "fp64" else 2
     diis = DIIS(diis_size)
+    Cs = None  # orbitals of the last update (per spin)
     E_old = None
     history = []
     converged = False
@@ -349,17 +445,17 @@ def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, m
             converged = True
             break
         E_old = E
-        diis.push(Fs, errs)
-        Fx = diis.extrapolate()
+        diis.push(Fs, errs, Ds, E)
+        Fx = diis.extrapolate_adiis() if adiis_until > 0 and gmax > adiis_until else diis.extrapolate()
         t0 = time.perf_counter()
-        if unrestricted:
-            Ds = []
-            for s, occ in enumerate((na, nb)):
-                _, C = solve(Fx[s])
-                Ds.append(C[:, :occ] @ C[:, :occ].T)
-        else:
-            _, C = solve(Fx[0])
-            Ds = [2 * C[:, :na] @ C[:, :na].T]
+        occs = (na, nb) if unrestricted else (na,)
+        rotate = rotate_below > 0 and gmax < rotate_below and Cs is not None
+        Cs = [cayley_update(Cs[s], Fx[s], occ) if rotate else solve(Fx[s])[1] for s, occ in enumerate(occs)]
+        if rotate:
+            timings["rotations"] = timings.get("rotations", 0) + 1
+        Ds = [C[:, :occ] @ C[:, :occ].T for C, occ in zip(Cs, occs)]
+        if not unrestricted:
+            Ds = [2 * Ds[0]]
         timings["diag"] += time.perf_counter() - t0
     wall = time.perf_counter() - t_start
     return Result(energy=E, converged=converged, iterations=it, wall=wall, timings=timings, D=Ds,

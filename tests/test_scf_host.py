@@ -76,3 +76,47 @@ def test_canonical_quartet_jk_algebra_matches_full_contraction():
     K = rawK + rawK.T
     np.testing.assert_allclose(J, np.einsum("mnls,ls->mn", eri, D), rtol=1e-12, atol=1e-11)
     np.testing.assert_allclose(K, np.einsum("mlns,ls->mn", eri, D), rtol=1e-12, atol=1e-11)
+
+
+def test_adiis_start_and_cayley_rotations_reach_the_diagonalisation_fixed_point(monkeypatch):
+    """Restricted Hartree-Fock on the host (XC switched off, host integrals):
+    the SCF with the reference's ADIIS start (until the commutator is below
+    1e-1) and Cayley rotations of the orbitals in place of diagonalisations
+    (below 1e-2) converges to the energy and density of plain CDIIS with a
+    full diagonalisation every iteration."""
+    import chinium_gb300 as cg
+    from chinium_gb300 import molecules as M
+    from chinium_gb300 import scf
+
+    class NoXC:
+        EXX = 1.0  # Hartree-Fock exchange
+        type = 0
+
+        def __init__(self, spin=1):
+            pass
+
+        def Read(self, name):
+            return self
+
+    class NoXCGrid:
+        def __init__(self, n):
+            self.n = n
+
+        def build(self, xc, D, precision=0):
+            return 0.0, [np.zeros((self.n, self.n)) for _ in D]
+
+    monkeypatch.setattr(scf, "ExchangeCorrelation", NoXC)
+    Z, xyz = M.h2o()
+    b = cg.Basis(Z, xyz, "def2-svp")
+    S, T, V = scf.one_electron(b)
+    out = {}
+    for name, kw in (("plain", dict(adiis_until=0.0, rotate_below=0.0)), ("adiis_cayley", {})):
+        ctx = {"basis": b, "S": S, "H": T + V, "jk": scf.JK(scf.repulsion(b, 0.0)), "grid": NoXCGrid(b.nbasis),
+               "Enuc": M.nuclear_repulsion(Z, xyz), "grid_key": ("grid", 1, "HF", "SG-1", 0.0)}
+        r = scf.run_scf(Z, xyz, functional="HF", guess="core", context=ctx, conv_energy=1e-10, jk_device="cpu", **kw)
+        assert r.converged
+        out[name] = r
+    assert out["adiis_cayley"].timings.get("rotations", 0) > 0
+    assert abs(out["plain"].energy - out["adiis_cayley"].energy) < 1e-9
+    assert np.abs(out["plain"].D[0] - out["adiis_cayley"].D[0]).max() < 1e-5
+    assert -76.1 < out["plain"].energy < -75.8  # RHF / def2-SVP water
