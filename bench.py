@@ -464,6 +464,50 @@ def run_scf_water(args):
     print(json.dumps(line), flush=True)
 
 
+C18_SCF_METRIC = "SCF wall time to 1e-8 Eh, C18 RKS B3LYP/def2-TZVP SG-2, mixed vs plain FP64 XC"
+
+
+def run_c18_scf(args):
+    """cyclo[18]carbon, restricted B3LYP/def2-TZVP (558 functions) on SG-2:
+    full Kohn-Sham SCFs to 1e-8 Eh from the SAP guess, Coulomb and exact
+    exchange from the library's GPU integrals (4.3e9 unique integrals kept in
+    HBM, computed once in the shared set-up).  Legs: the plain FP64 XC build
+    every iteration (per-block shell screening 1e-11, the same energies as
+    unscreened to 1e-14 Eh) and incremental tensor-core XC builds (references
+    from FP64 densities).  The timed SCF includes the guess and every
+    iteration (XC build, J/K contraction, DIIS, orbital update)."""
+    import torch
+    from chinium_gb300 import molecules as M
+    from chinium_gb300.scf import run_scf
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    torch.cuda.set_device(0)
+    Z, xyz = M.c18()
+    kw = dict(basis="def2-tzvp", functional="B3LYP", grid="SG-2", jk_device="engine", screen=1e-11)
+    t0 = time.perf_counter()
+    warm = run_scf(Z, xyz, precision="fp64", guess="core", max_iter=1, **kw)
+    ctx = warm.context
+    t_setup = time.perf_counter() - t0
+    jk_info = ctx["jk"].info()
+    legs = {}
+    for leg, prec in (("fp64", "fp64"), ("mixed", "mixed")):
+        t0 = time.perf_counter()
+        r = run_scf(Z, xyz, precision=prec, guess="sap", context=ctx, anchor="density", **kw)
+        wall = time.perf_counter() - t0
+        legs[leg] = {"wall_s": wall, "iterations": r.iterations, "converged": bool(r.converged), "E": r.energy,
+                     "xc_s": r.timings["xc"], "jk_s": r.timings["jk"], "orbital_update_s": r.timings["diag"]}
+    dE = abs(legs["mixed"]["E"] - legs["fp64"]["E"])
+    value = legs["mixed"]["wall_s"]
+    line = {"metric": C18_SCF_METRIC, "value": value, "unit": "s", "n_gpus": 1, "steps": 1, "warmup": 0,
+            "ms_per_step": value * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16x3 (split) + f64 accumulation (XC); f64 integrals, J/K, DIIS", "data": "synthetic",
+            "config": {"workload": "C18 RKS B3LYP/def2-TZVP SG-2, SCF to 1e-8 Eh from the SAP guess",
+                       "setup_s": t_setup, "integrals": jk_info, "legs": legs,
+                       "speedup_vs_plain_fp64": legs["fp64"]["wall_s"] / value,
+                       "abs_dE_total_mixed_vs_fp64": dE}}
+    print(json.dumps(line), flush=True)
+
+
 def run_gradient(args):
     """C18 RKS B3LYP/def2-TZVP SG-2: the XC nuclear gradient with the grid fixed
     (getDensitySkeleton + getEnergyGrad, FP64) through the C ABI, host buffers;
@@ -680,7 +724,7 @@ def main():
                     help="blocks per step of the --impl reference arm (0 = all: one whole build per step)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="c18", choices=["c18", "fe4s4", "alkanes64", "scf-water", "c18-response",
-                                                         "c18-gradient"])
+                                                         "c18-gradient", "c18-scf"])
     ap.add_argument("--no-fp64", action="store_true", help="c18-response: skip the FP64 comparison")
     ap.add_argument("--scf-mols", type=int, default=4)
     ap.add_argument("--fp64-mols", type=int, default=0, help="alkanes64: molecules checked in FP64 (0 = all)")
@@ -696,6 +740,8 @@ def main():
         return run_response(args)
     if args.workload == "c18-gradient":
         return run_gradient(args)
+    if args.workload == "c18-scf":
+        return run_c18_scf(args)
 
     import ctypes
     import torch

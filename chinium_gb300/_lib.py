@@ -127,6 +127,7 @@ SIGNATURES = {
     "xc_grid_molecules": [_P, _P, _P, _P, _P],
     "xc_grid_set_mixed_config": [_P, _P],
     "xc_grid_get_mixed_config": [_P, _P],
+    "xc_grid_wait_probe": [_P, _D],
     "xc_grid_tune": [_P, _P, _P, _I, _D, _D, _I, _P],
 }
 

@@ -1283,6 +1283,17 @@ int xc_grid_molecules(const xc_grid* g, int* nmol, int* nbasis, long* npoints, l
     });
 }
 
+int xc_grid_wait_probe(xc_grid* g, double budget_ms) {
+    return guard([&] {
+        CGB_CHECK(g, XC_ERR_ARG, "null grid");
+        CGB_CHECK(budget_ms > 0 && budget_ms <= 1000, XC_ERR_ARG, "budget_ms must be in (0, 1000]");
+        Grid& G = g->g;
+        CGB_CHECK(G.mx.ready, XC_ERR_STATE, "the wait probe needs the grid's tensor-core state (a mixed build first)");
+        launch_wait_probe(budget_ms, G.mx.d_err.p, G.stream);
+        if (G.mixed_error()) throw Error(XC_ERR_TIMEOUT, "a bounded wait of the tensor-core pipeline gave up");
+    });
+}
+
 int xc_grid_set_mixed_config(xc_grid* g, const xc_mixed_config* cfg) {
     return guard([&] {
         CGB_CHECK(g && cfg, XC_ERR_ARG, "null argument");

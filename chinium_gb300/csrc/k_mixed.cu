@@ -1273,7 +1273,27 @@ __global__ void __launch_bounds__(128) ao_mixed_kernel(MixedDev md, DevShells sh
     }
 }
 
+// Diagnostic of the bounded waits: one CTA sets up as the tensor-core
+// kernels do (their mbarriers and 512 TMEM columns), one thread waits on a
+// barrier that nothing ever arrives on, for budget_ns, flags the timeout in
+// err as the pipelines do and the CTA unwinds, releasing TMEM.  No TMA load
+// or MMA is issued, so nothing is in flight when the wait gives up.
+__global__ void __launch_bounds__(128, 1) wait_probe_kernel(unsigned long long budget_ns, int* err) {
+    __shared__ Smem sm;
+    init_cta(sm, 1, 1);
+    const uint32_t tmem = sm.tmem;
+    if (threadIdx.x == 32 && !tc::mbar_wait_budget(&sm.full[0], 0, budget_ns)) flag_timeout(err, &sm);
+    tc::fence_before_sync();
+    __syncthreads();
+    if ((threadIdx.x >> 5) == 0) tc::tmem_dealloc(tmem, kTmemCols);
+}
+
 }  // namespace
+
+void launch_wait_probe(double budget_ms, int* err, cudaStream_t s) {
+    wait_probe_kernel<<<1, 128, 0, s>>>((unsigned long long)(budget_ms * 1e6), err);
+    CGB_CUDA(cudaGetLastError());
+}
 
 void launch_ao_mixed(const MixedDev& md, DevShells sh, const int* tile_shells, const int* tile_shell_off, const double* x,
                      const double* y, const double* z, const double* shtab, int ao_comp, float* e32, cudaStream_t s) {

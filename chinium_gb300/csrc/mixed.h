@@ -177,6 +177,9 @@ void launch_axpby(long n, double a, const double* x, double b, const double* y, 
 void launch_gather(const long* perm, long Gt, long Gp, int ncomp, const double* src, double* dst, bool zero_pads,
                    cudaStream_t s);
 void set_mixed_kernel_attributes();
+// One CTA that waits on an mbarrier nothing arrives on for budget_ms, then
+// records XC_ERR_TIMEOUT in err and unwinds (the pipelines' failure path).
+void launch_wait_probe(double budget_ms, int* err, cudaStream_t s);
 
 // 2D bf16 tensor map with 128-byte swizzle over a row-major [rows][cols] array.
 void make_tmap_bf16(CUtensorMap* map, const void* base, uint64_t cols, uint64_t rows, uint32_t box_cols,

@@ -45,16 +45,18 @@ __device__ __forceinline__ uint64_t globaltimer_ns() {
     return t;
 }
 
-// Bounded wait for the phase of the given parity; false after kWaitNs.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// Bounded wait for the phase of the given parity; false after budget_ns.
+__device__ __forceinline__ bool mbar_wait_budget(uint64_t* bar, uint32_t parity, uint64_t budget_ns) {
     if (mbar_try_wait(bar, parity)) return true;
     const uint64_t t0 = globaltimer_ns();
     for (;;) {
         for (int i = 0; i < 256; i++)
             if (mbar_try_wait(bar, parity)) return true;
-        if (globaltimer_ns() - t0 > kWaitNs) return false;
+        if (globaltimer_ns() - t0 > budget_ns) return false;
     }
 }
+// The pipelines' wait: false after kWaitNs.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) { return mbar_wait_budget(bar, parity, kWaitNs); }
 
 // 2D TMA tile load global -> shared, completing bytes on bar.
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {

@@ -429,7 +429,9 @@ def guess_density(model, Z, xyz, ctx, bf16=True, precision="fp64"):
     from .scf import overlap_metric
     nocc = sum(Z) // 2
     metric = overlap_metric(ctx["S"], ctx)
-    base = sap_density(ctx["grid"], ctx["H"], ctx["S"], nocc, metric, precision) if model.residual else None
+    # tensor-core V_SAP only for a well-conditioned overlap (as the SCF's own SAP guess)
+    prec = precision if ctx.get("S_min", 0.0) >= 1e-3 else "fp64"
+    base = sap_density(ctx["grid"], ctx["H"], ctx["S"], nocc, metric, prec) if model.residual else None
     return predict_density(model, Z, xyz, ctx["basis"], ctx["S"], nocc, bf16=bf16, D_base=base, metric=metric)
 
 

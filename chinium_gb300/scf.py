@@ -144,6 +144,7 @@ def overlap_metric(S, ctx=None):
     m = (V[:, keep] / np.sqrt(w[keep]), (V * w ** -0.5) @ V.T, (V * w ** 0.5) @ V.T)
     if ctx is not None:
         ctx["S_metric"] = m
+        ctx["S_min"] = float(w[0])  # smallest overlap eigenvalue (near-linear dependence)
     return m
 
 
@@ -264,11 +265,16 @@ def cayley_update(C, F, nocc):
     orthogonal Cayley transform U = (1 - K/2)^-1 (1 + K/2) of the
     antisymmetric K = [[0, -kappa^T], [kappa, 0]].  At the SCF fixed point
     (F_ai = 0) it leaves C unchanged, so the converged state is the one a full
-    diagonalisation reaches; the SCF uses it once the DIIS error is small."""
+    diagonalisation reaches; the SCF uses it once the DIIS error is small.
+    Returns None when a virtual orbital's diagonal energy is not above every
+    occupied one (within 1e-3 Eh): the occupations would no longer follow the
+    aufbau order, and the caller diagonalises instead."""
     Fm = C.T @ F @ C
     e = np.diag(Fm)
     o, v = slice(0, nocc), slice(nocc, C.shape[1])
-    denom = np.maximum(e[v][:, None] - e[o][None, :], 1e-2)
+    if nocc < C.shape[1] and e[v].min() <= e[o].max() + 1e-3:
+        return None  # the occupied set is no longer the lowest: the caller diagonalises (aufbau)
+    denom = e[v][:, None] - e[o][None, :]
     kap = -Fm[v, o] / denom
     m = C.shape[1]
     K = np.zeros((m, m))
@@ -295,7 +301,7 @@ def occupations(Z, charge, mult):
 def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, mult=1, precision="fp64",
             guess="sap", conv_energy=1e-8, conv_grad=1e-6, max_iter=100, diis_size=20, screen=0.0,
             eri_threshold=1e-12, anchor_every=0, context=None, verbose=False, jk_device="engine", anchor="fp64",
-            adiis_until=1e-1, rotate_below=1e-2):
+            adiis_until=1e-1, rotate_below=1e-2, callback=None, reanchor_above=1.0):
     """Kohn-Sham SCF.  precision: "fp64" (plain XC build every iteration) or
     "mixed" (incremental tensor-core XC builds after a first build that sets
     the references: anchor "fp64", a full FP64 build, or "density", FP64
@@ -314,7 +320,10 @@ def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, m
     above this (the reference's 1e-1), CDIIS below; 0 = CDIIS throughout.
     rotate_below: once that element is below this, new orbitals come from a
     Cayley rotation of the previous ones (cayley_update) instead of a full
-    diagonalisation; 0 = always diagonalise."""
+    diagonalisation; 0 = always diagonalise.
+    callback: called every iteration as callback(it, Ds, Exc, Vxc, E) (monitoring).
+    reanchor_above: mixed precision re-anchors the incremental XC build when a
+    density element changed by more than this since the previous build."""
     t_start = time.perf_counter()
     timings = {"setup": 0.0, "xc": 0.0, "jk": 0.0, "diag": 0.0}
     na, nb = occupations(Z, charge, mult)
@@ -354,7 +363,8 @@ def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, m
         kw = dict(basis=basis, functional=functional, grid=grid, charge=charge, mult=mult, precision=precision,
                   conv_energy=conv_energy, conv_grad=conv_grad, diis_size=diis_size, screen=screen,
                   eri_threshold=eri_threshold, anchor_every=anchor_every, context=ctx, verbose=verbose,
-                  jk_device=jk_device, anchor=anchor, adiis_until=adiis_until, rotate_below=rotate_below)
+                  jk_device=jk_device, anchor=anchor, adiis_until=adiis_until, rotate_below=rotate_below,
+                  callback=callback, reanchor_above=reanchor_above)
         if unrestricted or charge != 0 or not G.supported(Z, b):
             r = run_scf(Z, xyz, guess="sap", max_iter=max_iter, **kw)
             r["guess_used"] = "sap (outside the learned model's scope)"
@@ -372,7 +382,10 @@ def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, m
     # initial guess
     if isinstance(guess, str):
         if guess == "sap":
-            V0 = g.sap_fock(PRECISION_MIXED if precision == "mixed" else PRECISION_FP64)
+            # the tensor-core SAP matrix (FP32-level error) only when the overlap is well
+            # conditioned: the orthogonaliser amplifies an error in V by 1 / s_min
+            tc_sap = precision == "mixed" and ctx.get("S_min", 0.0) >= 1e-3
+            V0 = g.sap_fock(PRECISION_MIXED if tc_sap else PRECISION_FP64)
             F0 = H + V0
         elif guess == "core":
             F0 = H
@@ -391,6 +404,7 @@ def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, m
     anchor_code = 1 if anchor == "fp64" else 2
     diis = DIIS(diis_size)
     Cs = None  # orbitals of the last update (per spin)
+    D_ref = None  # densities of the last XC build (the incremental reference)
     E_old = None
     history = []
     converged = False
@@ -409,7 +423,13 @@ def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, m
         if precision == "fp64":
             Exc, Vxc = g.build(xc, Ds)
         else:
-            reset = it == 1 or (anchor_every and (it - 1) % anchor_every == 0)
+            # re-anchor after a large density change: an incremental build's error scales with
+            # the change (max |D - D_ref|), and stays in the reconstructed densities
+            reset = (it == 1 or (anchor_every and (it - 1) % anchor_every == 0)
+                     or max(np.abs(d - r).max() for d, r in zip(Ds, D_ref)) > reanchor_above)
+            D_ref = [d.copy() for d in Ds]
+            if reset:
+                timings["anchors"] = timings.get("anchors", 0) + 1
             Dst = np.ascontiguousarray(np.stack([d.T for d in Ds]))
             Vb = np.zeros((nspin, n, n))
             e = ctypes.c_double()
@@ -439,6 +459,8 @@ def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, m
         gmax = max(np.abs(e).max() for e in errs)
         dE = None if E_old is None else E - E_old
         history.append((E, gmax))
+        if callback is not None:
+            callback(it, Ds, Exc, Vxc, E)
         if verbose:
             print("iter %3d  E = %.12f  dE = %s  |grad| = %.3e" % (it, E, "%.3e" % dE if dE is not None else "-", gmax))
         if dE is not None and abs(dE) < conv_energy and gmax < conv_grad:
@@ -450,9 +472,9 @@ def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, m
         t0 = time.perf_counter()
         occs = (na, nb) if unrestricted else (na,)
         rotate = rotate_below > 0 and gmax < rotate_below and Cs is not None
-        Cs = [cayley_update(Cs[s], Fx[s], occ) if rotate else solve(Fx[s])[1] for s, occ in enumerate(occs)]
-        if rotate:
-            timings["rotations"] = timings.get("rotations", 0) + 1
+        new = [cayley_update(Cs[s], Fx[s], occ) if rotate else None for s, occ in enumerate(occs)]
+        Cs = [c if c is not None else solve(Fx[s])[1] for s, c in enumerate(new)]
+        timings["rotations"] = timings.get("rotations", 0) + sum(c is not None for c in new)
         Ds = [C[:, :occ] @ C[:, :occ].T for C, occ in zip(Cs, occs)]
         if not unrestricted:
             Ds = [2 * Ds[0]]

@@ -155,6 +155,11 @@ class Grid:
         ptr = lambda t: ctypes.c_void_p(t if isinstance(t, int) else t.data_ptr())
         check(lib().xc_build_device(self._h, xc._h, ptr(d_D), self.nspin, int(precision), ptr(d_E), ptr(d_V)))
 
+    def wait_probe(self, budget_ms=2.0):
+        """Diagnostic: a tensor-core wait that runs out (xc_grid_wait_probe);
+        raises XCError with XC_ERR_TIMEOUT."""
+        check(lib().xc_grid_wait_probe(self._h, float(budget_ms)))
+
     def profile(self, enable=True):
         check(lib().xc_grid_profile(self._h, int(bool(enable))))
 

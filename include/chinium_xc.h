@@ -352,6 +352,16 @@ int xc_grid_create_batch(int nmol, const xc_basis* const* bases, const char* gri
  * basis functions, real grid points, offset of its block in packed D / V. */
 int xc_grid_molecules(const xc_grid* g, int* nmol, int* nbasis, long* npoints, long* offset);
 
+/* Diagnostic of the failure path, no reference counterpart.  Every wait of
+ * the tensor-core pipelines is bounded (2 s); one that gives up records
+ * XC_ERR_TIMEOUT and its kernel unwinds (TMEM released) instead of hanging,
+ * and the build returns XC_ERR_TIMEOUT with the context still usable.  This
+ * call runs the same set-up and wait in a one-CTA kernel on a barrier that
+ * nothing arrives on, for budget_ms (<= 1000), and returns what a build whose
+ * wait gave up returns: XC_ERR_TIMEOUT.  Needs a mixed build on the grid
+ * first; later builds on the grid are unaffected. */
+int xc_grid_wait_probe(xc_grid* g, double budget_ms);
+
 /* Knobs of the mixed path.  screen: chunk screening threshold on |phi| and
  * |grad phi| (0 keeps every chunk); fock_tiles: point tiles per V work item
  * (0 = from the SM count); spatial: 1 forms tiles from k-d cells of each

@@ -286,3 +286,8 @@ def test_static_entry_point_validates_arguments_on_the_host():
     assert b"sigma" in msg()
     assert L.xc_functional_energy_static(*args(tpss, 10, tau=None)) == -1
     assert b"tau" in msg()
+
+
+def test_wait_probe_validates_arguments_on_the_host():
+    L = lib()
+    assert L.xc_grid_wait_probe(None, 1.0) == -1
