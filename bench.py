@@ -464,6 +464,105 @@ def run_scf_water(args):
     print(json.dumps(line), flush=True)
 
 
+JK_METRIC = "Coulomb (J) builds/s, (H2O)8 def2-SVP, repulsion integrals on the GPU (in-core)"
+
+
+def run_jk(args):
+    """The SCF caller's Coulomb / exchange engine on one held-out (H2O)_8
+    (seed 424242, def2-SVP, n = 192): integrals computed once on the GPU and
+    kept in HBM (set-up), then a step is one J build of the dense Coulomb
+    operator (pack, GEMV, unpack) on a density resident in HBM; K builds are
+    timed beside it.  Roofline: the operator's bytes over the GEMV's CUDA-event
+    time against the measured HBM rate, and its FMAs against the FP64 rate of
+    cuBLAS DGEMM measured here (a GEMV does one FMA per 8 bytes)."""
+    import ctypes
+    import torch
+    import chinium_gb300 as cg
+    from chinium_gb300 import molecules as M
+    from chinium_gb300._lib import check, lib
+    from chinium_gb300.scf import JKEngine
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    torch.cuda.set_device(0)
+    Z, xyz = M.water_clusters(1, seed=424242, kmin=8, kmax=8)[0]
+    b = cg.Basis(Z, xyz, "def2-svp")
+    n = b.nbasis
+    t0 = time.perf_counter()
+    jk = JKEngine(b, threshold=1e-12)
+    torch.cuda.synchronize()
+    t_setup = time.perf_counter() - t0
+    info = jk.info()
+    D = torch.from_numpy(model_density(n, sum(Z) // 2)[None].copy()).cuda()
+    J = torch.empty((1, n, n), dtype=torch.float64, device="cuda")
+    K = torch.empty((1, n, n), dtype=torch.float64, device="cuda")
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+    st = jk.stream
+
+    def timed(steps, with_k):
+        for _ in range(max(args.warmup, 1)):
+            check(lib().xc_jk_build_device(jk._h, 1, p(D), p(J), p(K) if with_k else None))
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(steps):
+            check(lib().xc_jk_build_device(jk._h, 1, p(D), p(J), p(K) if with_k else None))
+        e1.record(st)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3 / steps
+
+    t_j = timed(args.steps, False)
+    t_jk = timed(max(args.steps // 4, 1), True)
+    npair = n * (n + 1) // 2
+    npair += npair & 1
+    op_bytes = 8.0 * npair * npair
+    peaks = measured_peaks()
+    hbm = op_bytes / t_j / 1e9
+    fp64 = fp64_gemm_peak(torch)
+    tflops = 2.0 * npair * npair / t_j / 1e12
+    line = {"metric": JK_METRIC, "value": 1.0 / t_j, "unit": "builds/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_j * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "(H2O)_8 (seed 424242) RKS def2-SVP, J of one density per step", "nbasis": n,
+                       "integrals": info, "setup_s": t_setup, "j_plus_k_ms": t_jk * 1e3,
+                       "l2": "inputs larger than L2 (dense Coulomb operator %.2f GB)" % (op_bytes / 1e9)},
+            "roofline": {"bound": "fp64", "kernel": "coulomb_gemv_kernel", "achieved": tflops, "peak": fp64,
+                         "unit": "TFLOP/s", "frac": tflops / fp64, "traffic": None,
+                         "peak_source": "cuBLAS DGEMM 4096^3 measured in this run",
+                         "hbm": {"achieved": hbm, "peak": peaks.get("hbm_gbs", 6800.0), "unit": "GB/s",
+                                 "frac": hbm / peaks.get("hbm_gbs", 6800.0),
+                                 "peak_source": "MEASURED_PEAKS.json hbm_gbs -- of measured"}}}
+    print(json.dumps(line), flush=True)
+
+
+def run_c18_mixed(args):
+    """C18 B3LYP/def2-TZVP SG-2: grid, AO store and tiles set up, then only
+    mixed-precision builds (the kernels of the headline, for profiling)."""
+    import torch
+    import chinium_gb300 as cg
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    torch.cuda.set_device(0)
+    wl = workload("c18")
+    b = cg.Basis(wl["Z"], wl["xyz"], wl["basis"])
+    xc = cg.ExchangeCorrelation().Read(wl["functional"])
+    g = cg.Grid(b, wl["grid"])
+    g.setType(xc.type)
+    g.getAO(0)
+    D = model_density(b.nbasis, wl["nocc"])
+    for _ in range(args.warmup):
+        g.build(xc, [D], precision=cg.PRECISION_MIXED)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        E, _ = g.build(xc, [D], precision=cg.PRECISION_MIXED)
+    t = (time.perf_counter() - t0) / args.steps
+    print(json.dumps({"metric": wl["metric"] + ", host-buffer mixed builds only", "value": g.info()["npoints"] / t,
+                      "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+                      "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                      "dtype": "bf16x3 (split) + f64 accumulation", "data": "synthetic",
+                      "config": {"workload": wl["name"], "E_xc": E}}), flush=True)
+
+
 C18_SCF_METRIC = "SCF wall time to 1e-8 Eh, C18 RKS B3LYP/def2-TZVP SG-2, mixed vs plain FP64 XC"
 
 
@@ -724,7 +823,7 @@ def main():
                     help="blocks per step of the --impl reference arm (0 = all: one whole build per step)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="c18", choices=["c18", "fe4s4", "alkanes64", "scf-water", "c18-response",
-                                                         "c18-gradient", "c18-scf"])
+                                                         "c18-gradient", "c18-scf", "jk-water8", "c18-mixed"])
     ap.add_argument("--no-fp64", action="store_true", help="c18-response: skip the FP64 comparison")
     ap.add_argument("--scf-mols", type=int, default=4)
     ap.add_argument("--fp64-mols", type=int, default=0, help="alkanes64: molecules checked in FP64 (0 = all)")
@@ -742,6 +841,10 @@ def main():
         return run_gradient(args)
     if args.workload == "c18-scf":
         return run_c18_scf(args)
+    if args.workload == "jk-water8":
+        return run_jk(args)
+    if args.workload == "c18-mixed":
+        return run_c18_mixed(args)
 
     import ctypes
     import torch
