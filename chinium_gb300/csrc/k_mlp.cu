@@ -1,9 +1,14 @@
-// Per-atom-pair MLP of the learned starting density: training (FP32 forward,
-// backward, Adam) and inference (BF16 weights, FP32 accumulation) kernels.
+// Per-atom-pair MLP of the learned starting density: training (FP32-level
+// forward, backward, Adam) and inference (BF16 weights, FP32 activations).
 //
 // Network: x (nin) -> [Linear, SiLU] x nlayers (width nh) -> Linear (nout).
 // Parameters are one flat FP32 vector, layer by layer: W (fan_in x fan_out,
 // row-major) then b (fan_out).  Activations are row-major (batch x width).
+//
+// Every product runs on the tensor cores (tc_gemm, k_tcgemm.cu): training
+// splits both operands into three BF16 planes (six cross products, FP32-level
+// sums); inference keeps the weights as one BF16 plane (cached until the
+// parameters change) against three activation planes.
 #include <cuda_bf16.h>
 
 #include <cmath>
@@ -11,62 +16,11 @@
 #include <vector>
 
 #include "common.h"
+#include "mixed.h"
 #include "xc_state.h"
 
 namespace cgb {
 namespace {
-
-constexpr int kT = 64, kTK = 16, kGemmThreads = 256;
-
-// C (M x N) = op(A) (M x K) * op(B) (K x N) [+ bias] ; row-major storage.
-// TA: A stored K x M; TB: B stored N x K.  WB: B element type (float or bf16).
-template <bool TA, bool TB, class WB>
-__global__ void __launch_bounds__(kGemmThreads) gemm_kernel(int M, int N, int K, const float* __restrict__ A,
-                                                            const WB* __restrict__ B, const float* __restrict__ bias,
-                                                            float* __restrict__ C, int accumulate) {
-    __shared__ float As[kTK][kT + 1], Bs[kTK][kT + 1];
-    const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
-    const int m0 = blockIdx.y * kT, n0 = blockIdx.x * kT;
-    float acc[4][4] = {};
-    for (int k0 = 0; k0 < K; k0 += kTK) {
-        for (int i = threadIdx.x; i < kTK * kT; i += kGemmThreads) {
-            const int kk = i / kT, mm = i % kT;
-            const int m = m0 + mm, k = k0 + kk;
-            float a = 0.f;
-            if (m < M && k < K) a = TA ? A[(size_t)k * M + m] : A[(size_t)m * K + k];
-            As[kk][mm] = a;
-            const int n = n0 + mm;
-            float b = 0.f;
-            if (n < N && k < K) b = (float)(TB ? B[(size_t)n * K + k] : B[(size_t)k * N + n]);
-            Bs[kk][mm] = b;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int kk = 0; kk < kTK; kk++) {
-            float a[4], b[4];
-#pragma unroll
-            for (int i = 0; i < 4; i++) a[i] = As[kk][ty * 4 + i];
-#pragma unroll
-            for (int j = 0; j < 4; j++) b[j] = Bs[kk][tx * 4 + j];
-#pragma unroll
-            for (int i = 0; i < 4; i++)
-#pragma unroll
-                for (int j = 0; j < 4; j++) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
-        }
-        __syncthreads();
-    }
-#pragma unroll
-    for (int i = 0; i < 4; i++)
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            const int m = m0 + ty * 4 + i, n = n0 + tx * 4 + j;
-            if (m < M && n < N) {
-                float v = acc[i][j] + (bias ? (float)bias[n] : 0.f);
-                if (accumulate) v += C[(size_t)m * N + n];
-                C[(size_t)m * N + n] = v;
-            }
-        }
-}
 
 __device__ __forceinline__ float silu(float z) { return z / (1.f + __expf(-z)); }
 __device__ __forceinline__ float dsilu(float z) {
@@ -126,18 +80,6 @@ __global__ void adam_kernel(long n, float* __restrict__ p, const float* __restri
     p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
 }
 
-__global__ void to_bf16_kernel(long n, const float* __restrict__ x, __nv_bfloat16* __restrict__ y) {
-    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) y[i] = __float2bfloat16_rn(x[i]);
-}
-
-template <bool TA, bool TB, class WB>
-void gemm(int M, int N, int K, const float* A, const WB* B, const float* bias, float* C, bool acc, cudaStream_t s) {
-    dim3 grid((N + kT - 1) / kT, (M + kT - 1) / kT);
-    gemm_kernel<TA, TB, WB><<<grid, kGemmThreads, 0, s>>>(M, N, K, A, B, bias, C, acc ? 1 : 0);
-    CGB_CUDA(cudaGetLastError());
-}
-
 unsigned blocks_for(long n) { return (unsigned)((n + 255) / 256); }
 
 }  // namespace
@@ -149,8 +91,10 @@ struct Mlp {
     long np = 0;
     int batch_cap = 0;
     DevBuf<float> p, g, m, v, x, y, t, mask, dy, loss_part;
-    DevBuf<__nv_bfloat16> pb;  // bf16 copy of the parameters for inference
-    bool pb_valid = false;
+    DevBuf<__nv_bfloat16> pa, pb;          // operand planes of the current product
+    std::vector<DevBuf<__nv_bfloat16>> wt;  // inference: W^T of each layer, one BF16 plane
+    bool wt_valid = false;
+    DevBuf<int> err;
     std::vector<DevBuf<float>> z, h, dh, dz;  // per layer
     long step = 0;
 
@@ -172,10 +116,13 @@ struct Mlp {
         m.zero();
         v.zero();
         p.zero();
+        err.alloc(1);
+        err.zero();
         z.resize(nl + 1);
         h.resize(nl + 1);
         dh.resize(nl + 1);
         dz.resize(nl + 1);
+        wt.resize(nl + 1);
     }
     void ensure_batch(int B) {
         if (B <= batch_cap) return;
@@ -193,54 +140,79 @@ struct Mlp {
             dz[l].alloc((size_t)B * fan_out[l]);
         }
     }
-    // FP32 forward on x (device); result in y.
-    void forward(int B, cudaStream_t s) {
+    // Planes of src(r, k) = src[r*ld_r + k*ld_k] (rows x kdim) in buf.
+    static void planes(DevBuf<__nv_bfloat16>& buf, const float* src, int rows, int kdim, long ld_r, long ld_k, int np_,
+                       cudaStream_t s) {
+        const size_t need = (size_t)np_ * tc_pad_rows(rows) * tc_pad_k(kdim);
+        if (buf.n < need) buf.alloc(need);
+        tc_to_planes(src, rows, kdim, ld_r, ld_k, np_, buf.p, s);
+    }
+    // Y (B x fo) = X (B x fi) W + b for layer l; weights 3 planes (training) or
+    // the cached BF16 plane (inference).
+    void linear(int l, int B, const float* in, float* out, bool bf16, cudaStream_t s) {
+        const int fi = fan_in[l], fo = fan_out[l];
+        planes(pa, in, B, fi, fi, 1, 3, s);
+        const __nv_bfloat16* wb;
+        if (bf16) {
+            wb = wt[l].p;
+        } else {
+            planes(pb, p.p + w_off[l], fo, fi, 1, fo, 3, s);  // W^T: row n, column k = W[k][n]
+            wb = pb.p;
+        }
+        tc_gemm(pa.p, 3, wb, bf16 ? 1 : 3, B, fo, fi, p.p + b_off[l], out, fo, false, err.p, s);
+    }
+    void forward_any(int B, bool bf16, cudaStream_t s) {
+        if (bf16 && !wt_valid) {
+            for (int l = 0; l <= nl; l++) planes(wt[l], p.p + w_off[l], fan_out[l], fan_in[l], 1, fan_out[l], 1, s);
+            wt_valid = true;
+        }
         const float* in = x.p;
         for (int l = 0; l <= nl; l++) {
             float* out = l == nl ? y.p : z[l].p;
-            gemm<false, false, float>(B, fan_out[l], fan_in[l], in, p.p + w_off[l], p.p + b_off[l], out, false, s);
+            linear(l, B, in, out, bf16, s);
             if (l < nl) {
                 silu_kernel<<<blocks_for((long)B * fan_out[l]), 256, 0, s>>>((long)B * fan_out[l], z[l].p, h[l].p);
                 in = h[l].p;
             }
         }
     }
+    // FP32-level forward on x (device); result in y.
+    void forward(int B, cudaStream_t s) { forward_any(B, false, s); }
     // BF16-weight forward (inference).
-    void forward_bf16(int B, cudaStream_t s) {
-        if (!pb_valid) {
-            pb.alloc(np);
-            to_bf16_kernel<<<blocks_for(np), 256, 0, s>>>(np, p.p, pb.p);
-            pb_valid = true;
-        }
-        const float* in = x.p;
-        for (int l = 0; l <= nl; l++) {
-            float* out = l == nl ? y.p : z[l].p;
-            // bias stays FP32 (read from p)
-            gemm<false, false, __nv_bfloat16>(B, fan_out[l], fan_in[l], in, pb.p + w_off[l], p.p + b_off[l], out, false, s);
-            if (l < nl) {
-                silu_kernel<<<blocks_for((long)B * fan_out[l]), 256, 0, s>>>((long)B * fan_out[l], z[l].p, h[l].p);
-                in = h[l].p;
-            }
-        }
-    }
+    void forward_bf16(int B, cudaStream_t s) { forward_any(B, true, s); }
     // Backward from dy (device) after forward(B); gradient into g.
     void backward(int B, cudaStream_t s) {
         const float* dout = dy.p;
         for (int l = nl; l >= 0; l--) {
+            const int fi = fan_in[l], fo = fan_out[l];
             const float* dzl = dout;
             if (l < nl) {
-                dsilu_kernel<<<blocks_for((long)B * fan_out[l]), 256, 0, s>>>((long)B * fan_out[l], z[l].p, dout, dz[l].p);
+                dsilu_kernel<<<blocks_for((long)B * fo), 256, 0, s>>>((long)B * fo, z[l].p, dout, dz[l].p);
                 dzl = dz[l].p;
             }
             const float* in = l == 0 ? x.p : h[l - 1].p;
-            // dW = in^T dz  (fan_in x fan_out)
-            gemm<true, false, float>(fan_in[l], fan_out[l], B, in, dzl, nullptr, g.p + w_off[l], false, s);
-            colsum_kernel<<<(fan_out[l] + 127) / 128, 128, 0, s>>>(B, fan_out[l], dzl, g.p + b_off[l]);
+            // dW (fi x fo) = in^T dz: A(i, b) = in[b][i], B(j, b) = dz[b][j]
+            planes(pa, in, fi, B, 1, fi, 3, s);
+            planes(pb, dzl, fo, B, 1, fo, 3, s);
+            tc_gemm(pa.p, 3, pb.p, 3, fi, fo, B, nullptr, g.p + w_off[l], fo, false, err.p, s);
+            colsum_kernel<<<(fo + 127) / 128, 128, 0, s>>>(B, fo, dzl, g.p + b_off[l]);
             if (l > 0) {
-                // dh_{l-1} = dz W^T  (B x fan_in)
-                gemm<false, true, float>(B, fan_in[l], fan_out[l], dzl, p.p + w_off[l], nullptr, dh[l - 1].p, false, s);
+                // dh_{l-1} (B x fi) = dz W^T: A(b, j) = dz[b][j], B(i, j) = W[i][j]
+                planes(pa, dzl, B, fo, fo, 1, 3, s);
+                planes(pb, p.p + w_off[l], fi, fo, fo, 1, 3, s);
+                tc_gemm(pa.p, 3, pb.p, 3, B, fi, fo, nullptr, dh[l - 1].p, fi, false, err.p, s);
                 dout = dh[l - 1].p;
             }
+        }
+    }
+    // XC_ERR_TIMEOUT (and a cleared flag) when a tensor-core wait gave up.
+    void check_error(cudaStream_t s) {
+        int e = 0;
+        CGB_CUDA(cudaMemcpyAsync(&e, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+        CGB_CUDA(cudaStreamSynchronize(s));
+        if (e) {
+            CGB_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), s));
+            throw Error(e, "MLP tensor-core GEMM: a pipeline wait timed out");
         }
     }
 };
@@ -290,7 +262,7 @@ int xc_mlp_set_params(xc_mlp* h, const float* params) {
         h->m.m.zero();
         h->m.v.zero();
         h->m.step = 0;
-        h->m.pb_valid = false;
+        h->m.wt_valid = false;
     });
 }
 
@@ -309,6 +281,7 @@ int xc_mlp_forward(xc_mlp* h, int batch, const float* X, float* Y, int bf16) {
         CGB_CUDA(cudaMemcpy(m.x.p, X, (size_t)batch * m.nin * sizeof(float), cudaMemcpyHostToDevice));
         if (bf16) m.forward_bf16(batch, h->s);
         else m.forward(batch, h->s);
+        m.check_error(h->s);
         CGB_CUDA(cudaMemcpy(Y, m.y.p, (size_t)batch * m.nout * sizeof(float), cudaMemcpyDeviceToHost));
     });
 }
@@ -322,6 +295,7 @@ int xc_mlp_backward(xc_mlp* h, int batch, const float* X, const float* dY, float
         m.forward(batch, h->s);
         CGB_CUDA(cudaMemcpy(m.dy.p, dY, (size_t)batch * m.nout * sizeof(float), cudaMemcpyHostToDevice));
         m.backward(batch, h->s);
+        m.check_error(h->s);
         CGB_CUDA(cudaMemcpy(grad, m.g.p, m.np * sizeof(float), cudaMemcpyDeviceToHost));
     });
 }
@@ -346,7 +320,8 @@ int xc_mlp_train_step(xc_mlp* h, int batch, const float* X, const float* T, cons
         const float b1 = 0.9f, b2 = 0.999f;
         adam_kernel<<<blocks_for(m.np), 256, 0, h->s>>>(m.np, m.p.p, m.g.p, m.m.p, m.v.p, lr, b1, b2, 1e-8f,
                                                         1.f - std::pow(b1, (float)m.step), 1.f - std::pow(b2, (float)m.step));
-        m.pb_valid = false;
+        m.wt_valid = false;
+        m.check_error(h->s);
         std::vector<float> parts(nb);
         CGB_CUDA(cudaMemcpy(parts.data(), m.loss_part.p, nb * sizeof(float), cudaMemcpyDeviceToHost));
         double l = 0;

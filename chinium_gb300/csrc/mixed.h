@@ -188,4 +188,16 @@ void make_tmap_bf16(CUtensorMap* map, const void* base, uint64_t cols, uint64_t 
 void make_tmap_f32(CUtensorMap* map, const void* base, uint64_t cols, uint64_t rows, uint32_t box_cols,
                    uint32_t box_rows);
 
+// Tensor-core GEMM of the pair MLP (k_tcgemm.cu).  Operands are BF16 planes,
+// K-major, rows padded by tc_pad_rows and K by tc_pad_k; 1 or 3 planes each.
+int tc_pad_rows(int n);
+int tc_pad_k(int n);
+// dst planes (nplanes x pad(rows) x pad(kdim)) of src(r, k) = src[r*ld_r + k*ld_k]; pads are 0.
+void tc_to_planes(const float* src, int rows, int kdim, long ld_r, long ld_k, int nplanes, __nv_bfloat16* dst,
+                  cudaStream_t s);
+// C[m*ldc + n] (+)= sum_k A(m, k) B(n, k) [+ bias[n]] for m < M, n < N; a
+// timed-out wait records XC_ERR_TIMEOUT in err.
+void tc_gemm(const __nv_bfloat16* A, int npa, const __nv_bfloat16* B, int npb, int M, int N, int K, const float* bias,
+             float* C, int ldc, bool accumulate, int* err, cudaStream_t s);
+
 }  // namespace cgb

@@ -85,6 +85,55 @@ def test_mlp_forward_backward_match_oracle():
     assert np.abs(Yb - Yo).max() < 3e-2 * np.abs(Yo).max()
 
 
+def _bf16_round(p):
+    """FP32 -> nearest BF16 (ties to even), returned as FP64."""
+    u = np.asarray(p, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    u = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return u.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+@pytest.mark.gpu
+def test_mlp_tensor_core_products_at_network_shape():
+    """The production network (79 -> 256 x 3 -> 196) on a ragged batch of
+    1000 pairs: every dimension off the 128 x 64 tiles.  Training products
+    (three BF16 planes each side) match FP64 to FP32 rounding; inference
+    (BF16 weights, FP32 activations) matches an FP64 network whose weights
+    are rounded to BF16, so the only error left is FP32 accumulation."""
+    if not _gpu():
+        pytest.skip("needs a GPU")
+    from oracle import mlp_oracle as MO
+    model = G.PairMLP(seed=5)
+    dims = [model.nin] + [model.hidden] * model.layers + [model.nout]
+    rng = np.random.default_rng(7)
+    p = model.params()
+    o = 0
+    for fi, fo in zip(dims[:-1], dims[1:]):  # non-zero biases
+        o += fi * fo
+        p[o:o + fo] = 0.1 * rng.normal(size=fo)
+        o += fo
+    model.set_params(p)
+    p = p.astype(np.float64)
+    X = rng.normal(size=(1000, model.nin)).astype(np.float32)
+    Yo, _ = MO.forward(p, dims, X)
+    scale = np.abs(Yo).max()
+    Y = model.forward(X)
+    assert np.abs(Y - Yo).max() <= 2e-5 * scale, np.abs(Y - Yo).max() / scale
+    dY = rng.normal(size=Yo.shape).astype(np.float32)
+    g = model.grad(X, dY)
+    go = MO.backward(p, dims, X, dY)
+    assert np.abs(g - go).max() <= 2e-5 * np.abs(go).max(), np.abs(g - go).max() / np.abs(go).max()
+    # inference: weights to BF16, biases stay FP32
+    pb = p.copy()
+    o = 0
+    for fi, fo in zip(dims[:-1], dims[1:]):
+        pb[o:o + fi * fo] = _bf16_round(p[o:o + fi * fo])
+        o += fi * fo + fo
+    Ybo, _ = MO.forward(pb, dims, X)
+    Yb = model.forward(X, bf16=True)
+    assert np.abs(Yb - Ybo).max() <= 2e-5 * scale, np.abs(Yb - Ybo).max() / scale
+    assert np.abs(Yb - Yo).max() > 10 * np.abs(Yb - Ybo).max()  # BF16 weights do differ from FP32
+
+
 @pytest.mark.gpu
 def test_mlp_training_reduces_loss():
     if not _gpu():
