@@ -472,9 +472,10 @@ def run_jk(args):
     (seed 424242, def2-SVP, n = 192): integrals computed once on the GPU and
     kept in HBM (set-up), then a step is one J build of the dense Coulomb
     operator (pack, GEMV, unpack) on a density resident in HBM; K builds are
-    timed beside it.  Roofline: the operator's bytes over the GEMV's CUDA-event
-    time against the measured HBM rate, and its FMAs against the FP64 rate of
-    cuBLAS DGEMM measured here (a GEMV does one FMA per 8 bytes)."""
+    timed beside it.  The operator is held as float-float pairs (8 bytes per
+    element, 48-bit significands) and the GEMV runs on the FP32 pipe, so its
+    roof is HBM: the operator's bytes over the build's CUDA-event time
+    against the measured HBM rate."""
     import ctypes
     import torch
     import chinium_gb300 as cg
@@ -517,20 +518,16 @@ def run_jk(args):
     op_bytes = 8.0 * npair * npair
     peaks = measured_peaks()
     hbm = op_bytes / t_j / 1e9
-    fp64 = fp64_gemm_peak(torch)
-    tflops = 2.0 * npair * npair / t_j / 1e12
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
     line = {"metric": JK_METRIC, "value": 1.0 / t_j, "unit": "builds/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_j * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "vs_baseline": None, "dtype": "f32x2 (float-float operator and density, FP64 sums)", "data": "synthetic",
             "config": {"workload": "(H2O)_8 (seed 424242) RKS def2-SVP, J of one density per step", "nbasis": n,
                        "integrals": info, "setup_s": t_setup, "j_plus_k_ms": t_jk * 1e3,
                        "l2": "inputs larger than L2 (dense Coulomb operator %.2f GB)" % (op_bytes / 1e9)},
-            "roofline": {"bound": "fp64", "kernel": "coulomb_gemv_kernel", "achieved": tflops, "peak": fp64,
-                         "unit": "TFLOP/s", "frac": tflops / fp64, "traffic": None,
-                         "peak_source": "cuBLAS DGEMM 4096^3 measured in this run",
-                         "hbm": {"achieved": hbm, "peak": peaks.get("hbm_gbs", 6800.0), "unit": "GB/s",
-                                 "frac": hbm / peaks.get("hbm_gbs", 6800.0),
-                                 "peak_source": "MEASURED_PEAKS.json hbm_gbs -- of measured"}}}
+            "roofline": {"bound": "hbm", "kernel": "coulomb_gemv_kernel", "achieved": hbm, "peak": hbm_peak,
+                         "unit": "GB/s", "frac": hbm / hbm_peak, "traffic": None,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs -- of measured"}}
     print(json.dumps(line), flush=True)
 
 

@@ -1234,7 +1234,8 @@ int xc_build_incremental(xc_grid* g, xc_functional* f, const double* D, int nspi
         Grid& G = g->g;
         CGB_CHECK(nspin == G.nspin && f->f.nspin == G.nspin, XC_ERR_ARG, "Wrong number of spin types!");
         CGB_CHECK(f->f.family <= G.type, XC_ERR_STATE, "grid type is below the functional family (setType/getAO)");
-        CGB_CHECK(anchor >= 0 && anchor <= 2, XC_ERR_ARG, "anchor must be 0, 1 or 2");
+        CGB_CHECK((anchor & ~(XC_INCREMENTAL_FP32_POTENTIALS | 15)) == 0 && (anchor & 15) <= XC_ANCHOR_MIXED, XC_ERR_ARG,
+                  "anchor must be 0..3, optionally with XC_INCREMENTAL_FP32_POTENTIALS");
         G.ensure_work();
         const size_t nn = (size_t)G.basis.nbasis * G.basis.nbasis * nspin;
         CGB_CUDA(cudaMemcpyAsync(G.d_D.p, D, nn * sizeof(double), cudaMemcpyHostToDevice, G.stream));

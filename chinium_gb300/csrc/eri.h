@@ -64,10 +64,14 @@ void launch_jk_contract(const EriDev& e, const int2* quartets, const long long* 
 
 // Dense Coulomb operator M (ld x ld, ld = n (n + 1) / 2 rounded up to even,
 // packed pairs mu >= nu) from the in-core blocks of all quartets; M must
-// start at zero.  Then J of nmat densities: pack (x2 off-diagonal) into x
-// (nmat vectors of stride ld, zeroed once by the caller), GEMV into y, unpack.
+// start at zero.  launch_coulomb_split then turns each FP64 element in place
+// into a float-float pair (hi, lo), the form launch_coulomb_dense reads.
+// J of nmat densities: pack (x2 off-diagonal) into x (nmat float-float
+// vectors of stride ld in a buffer of nmat * ld doubles, zeroed once by the
+// caller), GEMV into y (FP64), unpack.
 void launch_coulomb_scatter(const EriDev& e, const int2* quartets, const long long* out_off, long long nq,
                             const double* ints, long long ld, double* M, cudaStream_t s);
+void launch_coulomb_split(long long n, double* M, cudaStream_t s);
 void launch_coulomb_dense(int n, int nmat, long long ld, const double* M, const double* D, double* x, double* y,
                           double* J, cudaStream_t s);
 

@@ -47,7 +47,8 @@ struct JkEngine {
     bool dense_j = false;                     // J from the dense Coulomb operator over function pairs
     long long npair = 0;                      // row stride of the dense operator (pairs, rounded up to even)
     int dense_nmat = 0;
-    DevBuf<double> d_M, d_x, d_y;             // dense operator; packed densities and results
+    DevBuf<double> d_M, d_x, d_y;             // dense operator and packed densities (float-float pairs
+                                              // in 8-byte elements); results (FP64)
     DevBuf<double> d_ints;                    // in-core integrals, or the direct-mode chunk buffer
     DevBuf<double> d_D, d_rawJ, d_rawK, d_J, d_K;
     int nmat_alloc = 0;
@@ -190,6 +191,7 @@ void JkEngine::setup(const BasisSet& b, double thr, double max_bytes) {
             d_M.alloc((size_t)npair * npair);
             d_M.zero(stream);
             launch_coulomb_scatter(dev(), d_quartets.p, d_off.p, nquartets, d_ints.p, npair, d_M.p, stream);
+            launch_coulomb_split((long long)npair * npair, d_M.p, stream);
         }
         CGB_CUDA(cudaStreamSynchronize(stream));
     } else {

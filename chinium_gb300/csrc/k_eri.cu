@@ -15,7 +15,8 @@
 // of the six J / K sub-blocks it feeds (2 J, 4 K), scaled by the quartet's
 // degeneracy, with one FP64 atomic per element.  Small molecules take J from
 // a dense Coulomb operator over function pairs filled once from the blocks
-// (coulomb_scatter_kernel) and a GEMV per build (coulomb_gemv_kernel).
+// (coulomb_scatter_kernel, then split into float-float pairs) and a GEMV per
+// build in float-float arithmetic on the FP32 pipe (coulomb_gemv_kernel).
 #include "common.h"
 #include "eri.h"
 
@@ -294,60 +295,94 @@ __global__ void __launch_bounds__(256) coulomb_scatter_kernel(EriDev e, const in
     }
 }
 
-// d_p of nmat densities (n x n each) -> x[m][p] (vectors of stride ld)
+// The dense operator and the packed densities are float-float pairs: an FP64
+// value v is held as (hi, lo) = (fl32(v), fl32(v - hi)), 48 significant bits,
+// so the GEMV runs on the FP32 pipe (GB300's FP64 rate is 1/64 of it) at
+// FP64-level accuracy, in the same 8 bytes per element as FP64.
+__device__ __forceinline__ float2 ff_split(double v) {
+    const float hi = (float)v;
+    return make_float2(hi, (float)(v - (double)hi));
+}
+
+// In place: M[i] (FP64) -> (hi, lo) float pair in the same 8 bytes.
+__global__ void coulomb_split_kernel(long long n, double* __restrict__ M) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const double v = M[i];
+        reinterpret_cast<float2*>(M)[i] = ff_split(v);
+    }
+}
+
+// d_p of nmat densities (n x n each) -> x[m][p] as float-float pairs
+// (vectors of stride ld)
 __global__ void coulomb_pack_kernel(int n, int nmat, long long npair, const double* __restrict__ D,
-                                    double* __restrict__ x) {
+                                    float2* __restrict__ x) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)n * n * nmat) return;
     const int m = (int)(t / ((long long)n * n));
     const long long r = t - (long long)m * n * n;
     const int i = (int)(r / n), j = (int)(r - (long long)i * n);
     if (j > i) return;
-    x[m * npair + pair_index(i, j)] = (i == j ? 1.0 : 2.0) * D[t];
+    x[m * npair + pair_index(i, j)] = ff_split((i == j ? 1.0 : 2.0) * D[t]);
+}
+
+// s + c += (mh + ml)(xh + xl) in float-float: the product's rounding error
+// exactly (FMA), the sum's by TwoSum (Knuth); explicit _rn intrinsics keep
+// the compiler from contracting the error-free transformations.
+__device__ __forceinline__ void ff_fma(float mh, float ml, float xh, float xl, float& s, float& c) {
+    const float p = __fmul_rn(mh, xh);
+    const float e = __fmaf_rn(mh, xh, -p);
+    const float t = __fadd_rn(s, p);
+    const float z = __fsub_rn(t, s);
+    const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(p, z));
+    s = t;
+    c = __fadd_rn(c, __fadd_rn(__fadd_rn(err, e), __fmaf_rn(mh, xl, __fmul_rn(ml, xh))));
 }
 
 // y[m] = M x[m] for NM <= 4 vectors in one pass over M (npair rows of
 // stride npair here being the even row stride ld): one warp per row, four
-// independent 16-byte loads of M per lane in flight per step (a single
-// outstanding load per warp leaves HBM at ~10% of its rate).
+// independent 16-byte loads (two float-float elements each) of M per lane in
+// flight per step (a single outstanding load per warp leaves HBM at ~10% of
+// its rate).  Lanes accumulate in float-float and reduce in FP64.
 constexpr int kGemvMaxVec = 4;
 template <int NM>
-__global__ void __launch_bounds__(256) coulomb_gemv_kernel(long long npair, const double* __restrict__ M,
-                                                           const double* __restrict__ x, double* __restrict__ y) {
+__global__ void __launch_bounds__(256) coulomb_gemv_kernel(long long npair, const float2* __restrict__ M,
+                                                           const float2* __restrict__ x, double* __restrict__ y) {
     const int lane = threadIdx.x & 31;
     const long long w0 = (long long)blockIdx.x * 8 + (threadIdx.x >> 5), nw = (long long)gridDim.x * 8;
     const long long nc2 = npair / 2;
     for (long long r = w0; r < npair; r += nw) {
-        const double2* __restrict__ row2 = reinterpret_cast<const double2*>(M + r * npair);
-        double acc[NM];
+        const float4* __restrict__ row2 = reinterpret_cast<const float4*>(M + r * npair);
+        float s[NM], c[NM];
 #pragma unroll
-        for (int m = 0; m < NM; m++) acc[m] = 0.0;
-        long long c = lane;
-        for (; c + 96 < nc2; c += 128) {
-            double2 v[4];
+        for (int m = 0; m < NM; m++) s[m] = c[m] = 0.f;
+        long long k = lane;
+        for (; k + 96 < nc2; k += 128) {
+            float4 v[4];
 #pragma unroll
-            for (int u = 0; u < 4; u++) v[u] = __ldcs(row2 + c + 32 * u);
+            for (int u = 0; u < 4; u++) v[u] = __ldcs(row2 + k + 32 * u);
 #pragma unroll
             for (int m = 0; m < NM; m++) {
-                const double2* __restrict__ x2 = reinterpret_cast<const double2*>(x + m * npair);
+                const float4* __restrict__ x2 = reinterpret_cast<const float4*>(x + m * npair);
 #pragma unroll
                 for (int u = 0; u < 4; u++) {
-                    const double2 xv = __ldg(x2 + c + 32 * u);
-                    acc[m] = fma(v[u].x, xv.x, fma(v[u].y, xv.y, acc[m]));
+                    const float4 xv = __ldg(x2 + k + 32 * u);
+                    ff_fma(v[u].x, v[u].y, xv.x, xv.y, s[m], c[m]);
+                    ff_fma(v[u].z, v[u].w, xv.z, xv.w, s[m], c[m]);
                 }
             }
         }
-        for (; c < nc2; c += 32) {
-            const double2 v = __ldcs(row2 + c);
+        for (; k < nc2; k += 32) {
+            const float4 v = __ldcs(row2 + k);
 #pragma unroll
             for (int m = 0; m < NM; m++) {
-                const double2 xv = __ldg(reinterpret_cast<const double2*>(x + m * npair) + c);
-                acc[m] = fma(v.x, xv.x, fma(v.y, xv.y, acc[m]));
+                const float4 xv = __ldg(reinterpret_cast<const float4*>(x + m * npair) + k);
+                ff_fma(v.x, v.y, xv.x, xv.y, s[m], c[m]);
+                ff_fma(v.z, v.w, xv.z, xv.w, s[m], c[m]);
             }
         }
 #pragma unroll
         for (int m = 0; m < NM; m++) {
-            double v = acc[m];
+            double v = (double)s[m] + (double)c[m];
             for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
             if (lane == 0) y[m * npair + r] = v;
         }
@@ -434,22 +469,28 @@ void launch_coulomb_scatter(const EriDev& e, const int2* quartets, const long lo
     CGB_CUDA(cudaGetLastError());
 }
 
+void launch_coulomb_split(long long n, double* M, cudaStream_t s) {
+    coulomb_split_kernel<<<persistent_blocks(n, 2048), 256, 0, s>>>(n, M);
+    CGB_CUDA(cudaGetLastError());
+}
 void launch_coulomb_dense(int n, int nmat, long long ld, const double* M, const double* D, double* x, double* y,
                           double* J, cudaStream_t s) {
     CGB_CHECK(ld % 2 == 0 && ld >= (long long)n * (n + 1) / 2, XC_ERR_INTERNAL, "bad dense Coulomb row stride");
     const long long tot = (long long)n * n * nmat;
-    // x: nmat vectors of stride ld whose pad entry stays zero (the caller zeroes x once)
-    coulomb_pack_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(n, nmat, ld, D, x);
+    // x: nmat float-float vectors of stride ld whose pad entry stays zero (the caller zeroes x once)
+    float2* xf = reinterpret_cast<float2*>(x);
+    const float2* Mf = reinterpret_cast<const float2*>(M);
+    coulomb_pack_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(n, nmat, ld, D, xf);
     CGB_CUDA(cudaGetLastError());
     const unsigned blocks = persistent_blocks(ld, 8);
     for (int m0 = 0; m0 < nmat; m0 += kGemvMaxVec) {
         const int nm = nmat - m0 < kGemvMaxVec ? nmat - m0 : kGemvMaxVec;
-        const double* xm = x + m0 * ld;
+        const float2* xm = xf + m0 * ld;
         double* ym = y + m0 * ld;
-        if (nm == 1) coulomb_gemv_kernel<1><<<blocks, 256, 0, s>>>(ld, M, xm, ym);
-        else if (nm == 2) coulomb_gemv_kernel<2><<<blocks, 256, 0, s>>>(ld, M, xm, ym);
-        else if (nm == 3) coulomb_gemv_kernel<3><<<blocks, 256, 0, s>>>(ld, M, xm, ym);
-        else coulomb_gemv_kernel<4><<<blocks, 256, 0, s>>>(ld, M, xm, ym);
+        if (nm == 1) coulomb_gemv_kernel<1><<<blocks, 256, 0, s>>>(ld, Mf, xm, ym);
+        else if (nm == 2) coulomb_gemv_kernel<2><<<blocks, 256, 0, s>>>(ld, Mf, xm, ym);
+        else if (nm == 3) coulomb_gemv_kernel<3><<<blocks, 256, 0, s>>>(ld, Mf, xm, ym);
+        else coulomb_gemv_kernel<4><<<blocks, 256, 0, s>>>(ld, Mf, xm, ym);
         CGB_CUDA(cudaGetLastError());
     }
     coulomb_unpack_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(n, nmat, ld, y, J);

@@ -633,11 +633,13 @@ void Grid::build_mixed_graph(const Functional& f) {
 // per-point coefficients, so rho(D) = rho_ref + rho(D - D_ref) and
 // V = V_ref + V(c - c_ref), with only the differences on the tensor cores.
 // Their split-BF16 error is relative to the (shrinking, in an SCF) change;
-// the functional and E_xc are evaluated in FP64 on the reconstructed
-// densities.  An anchor resets the references: a full FP64 build (anchor 1,
-// or the first call; gathered into tile order) or a full tensor-core build
-// with the functional in FP64 everywhere (anchor 2; already in tile order).
-void Grid::build_incremental(const double* dD, const Functional& f, double* dE, double* dV, int anchor) {
+// the functional and E_xc are evaluated on the reconstructed densities, in
+// FP64 or (flag XC_INCREMENTAL_FP32_POTENTIALS) with FP32 potentials above
+// the config's func_float_above and an FP64 energy density.  An anchor resets
+// the references: a full FP64 build (anchor 1, or the first call), FP64
+// densities, functional and E_xc with V on the tensor cores (anchor 2) -- both
+// gathered into tile order -- or a full tensor-core build (anchor 3).
+void Grid::build_incremental(const double* dD, const Functional& f, double* dE, double* dV, int anchor_flags) {
     NvtxRange nvtx_("xc.mixed.incremental");
     CGB_CHECK(!batched, XC_ERR_UNSUPPORTED, "incremental builds need the FP64 path (one molecule per grid)");
     CGB_CHECK(ao_order >= type, XC_ERR_STATE, "getAO must run (for the current type) before a build");
@@ -658,6 +660,16 @@ void Grid::build_incremental(const double* dD, const Functional& f, double* dE, 
         m.d_dD.alloc(nn);
         m.d_dfcoef.alloc(5 * G1);
     };
+    const int anchor = anchor_flags & 15;
+    const double float_above =
+        (anchor_flags & XC_INCREMENTAL_FP32_POTENTIALS) ? m.cfg.func_float_above : __builtin_huge_val();
+    if (anchor == XC_ANCHOR_MIXED) {
+        alloc_refs();
+        build_mixed(dD, f, dE, dV);
+        save_refs(dD, dV);
+        m.have_ref = true;
+        return;
+    }
     if (anchor == 2) {
         // FP64 densities, functional and E_xc; V from the full coefficients
         // on the tensor cores
@@ -708,7 +720,7 @@ void Grid::build_incremental(const double* dD, const Functional& f, double* dE, 
     mark(1);
     // FP64 functional on the reconstructed densities
     launch_functional_fp64(f.desc, f.family, nspin, Gt, m.d_w.p, m.rho.p, m.rho1.p, m.tau.p, m.sigma.p, m.eps.p,
-                           m.vrho.p, m.vsigma.p, m.vtau.p, m.fcoef.p, m.partial.p, &m.n_partial, stream);
+                           m.vrho.p, m.vsigma.p, m.vtau.p, m.fcoef.p, m.partial.p, &m.n_partial, stream, float_above);
     mark(2);
     launch_energy_mols(m.partial.p, m.d_mols.p, 1, dE, stream);
     mark(3);

@@ -398,10 +398,12 @@ def assemble_blocks(pr, Y, Uas, Ubs, first, count, n):
     return D
 
 
-def predict_density(model, Z, xyz, basis, S, nocc, bf16=True, D_base=None, metric=None):
+def predict_density(model, Z, xyz, basis, S, nocc, bf16=True, D_base=None, metric=None, return_orbitals=False):
     """Learned closed-shell total density (2 C C^T, idempotent in the S metric):
     D_base (the SAP density for a residual model) plus the predicted pair
-    blocks, purified.  metric: overlap_metric(S) when the caller has it."""
+    blocks, purified.  metric: overlap_metric(S) when the caller has it.
+    return_orbitals: also return the natural orbitals (S-orthonormal columns,
+    occupied first), from which an SCF can rotate instead of diagonalising."""
     from .scf import overlap_metric
     types, first, count = atom_functions(basis)
     pr = pairs(xyz)
@@ -418,21 +420,25 @@ def predict_density(model, Z, xyz, basis, S, nocc, bf16=True, D_base=None, metri
     # purification: occupied natural orbitals in the overlap metric
     _, Xh, Sh = metric or overlap_metric(S)
     occ, C = np.linalg.eigh(Sh @ D @ Sh)
-    Co = Xh @ C[:, np.argsort(occ)[::-1][:nocc]]
-    return 2.0 * Co @ Co.T
+    Cn = Xh @ C[:, np.argsort(occ)[::-1]]
+    Co = Cn[:, :nocc]
+    D = 2.0 * Co @ Co.T
+    return (D, Cn) if return_orbitals else D
 
 
-def guess_density(model, Z, xyz, ctx, bf16=True, precision="fp64"):
+def guess_density(model, Z, xyz, ctx, bf16=True, precision="fp64", return_orbitals=False):
     """The learned starting density for a molecule whose SCF context (basis,
     S, H, grid) exists: the SAP base when the model is residual (its V_SAP on
-    the tensor cores for precision "mixed")."""
+    the tensor cores for precision "mixed").  return_orbitals: (D, natural
+    orbitals), as predict_density."""
     from .scf import overlap_metric
     nocc = sum(Z) // 2
     metric = overlap_metric(ctx["S"], ctx)
     # tensor-core V_SAP only for a well-conditioned overlap (as the SCF's own SAP guess)
     prec = precision if ctx.get("S_min", 0.0) >= 1e-3 else "fp64"
     base = sap_density(ctx["grid"], ctx["H"], ctx["S"], nocc, metric, prec) if model.residual else None
-    return predict_density(model, Z, xyz, ctx["basis"], ctx["S"], nocc, bf16=bf16, D_base=base, metric=metric)
+    return predict_density(model, Z, xyz, ctx["basis"], ctx["S"], nocc, bf16=bf16, D_base=base, metric=metric,
+                           return_orbitals=return_orbitals)
 
 
 def save(model, path):

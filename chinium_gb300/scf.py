@@ -266,23 +266,26 @@ def cayley_update(C, F, nocc):
     antisymmetric K = [[0, -kappa^T], [kappa, 0]].  At the SCF fixed point
     (F_ai = 0) it leaves C unchanged, so the converged state is the one a full
     diagonalisation reaches; the SCF uses it once the DIIS error is small.
+    With a = kappa / 2 and W = (1 + a^T a)^-1 (occupied x occupied), the
+    block inverse of 1 - K/2 gives U in closed form,
+        U_oo = 2 W - 1,  U_vo = 2 a W,  U_ov = -2 W a^T,  U_vv = 1 - 2 a W a^T,
+    so the update costs one F C product and occupied-sized solves:
+    C_o' = 2 G W - C_o and C_v' = C_v - (C_o' + C_o) a^T with G = C_o + C_v a.
     Returns None when a virtual orbital's diagonal energy is not above every
     occupied one (within 1e-3 Eh): the occupations would no longer follow the
     aufbau order, and the caller diagonalises instead."""
-    Fm = C.T @ F @ C
-    e = np.diag(Fm)
-    o, v = slice(0, nocc), slice(nocc, C.shape[1])
-    if nocc < C.shape[1] and e[v].min() <= e[o].max() + 1e-3:
-        return None  # the occupied set is no longer the lowest: the caller diagonalises (aufbau)
-    denom = e[v][:, None] - e[o][None, :]
-    kap = -Fm[v, o] / denom
     m = C.shape[1]
-    K = np.zeros((m, m))
-    K[v, o] = kap
-    K[o, v] = -kap.T
-    eye = np.eye(m)
-    U = np.linalg.solve(eye - 0.5 * K, eye + 0.5 * K)
-    return C @ U
+    Co, Cv = C[:, :nocc], C[:, nocc:]
+    FC = F @ C
+    e_o = np.einsum("ij,ij->j", Co, FC[:, :nocc])
+    e_v = np.einsum("ij,ij->j", Cv, FC[:, nocc:])
+    if nocc < m and e_v.min() <= e_o.max() + 1e-3:
+        return None  # the occupied set is no longer the lowest: the caller diagonalises (aufbau)
+    a = -0.5 * (Cv.T @ FC[:, :nocc]) / (e_v[:, None] - e_o[None, :])
+    W = np.linalg.inv(np.eye(nocc) + a.T @ a)
+    Co_new = 2.0 * (Co + Cv @ a) @ W - Co
+    Cv_new = Cv - (Co_new + Co) @ a.T
+    return np.hstack([Co_new, Cv_new])
 
 
 class Result(dict):
@@ -301,16 +304,24 @@ def occupations(Z, charge, mult):
 def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, mult=1, precision="fp64",
             guess="sap", conv_energy=1e-8, conv_grad=1e-6, max_iter=100, diis_size=20, screen=0.0,
             eri_threshold=1e-12, anchor_every=0, context=None, verbose=False, jk_device="engine", anchor="fp64",
-            adiis_until=1e-1, rotate_below=1e-2, callback=None, reanchor_above=1.0):
+            adiis_until=1e-1, rotate_below=1e-1, callback=None, reanchor_above=1.0, fp32_potentials=False,
+            orbitals=None):
     """Kohn-Sham SCF.  precision: "fp64" (plain XC build every iteration) or
     "mixed" (incremental tensor-core XC builds after a first build that sets
-    the references: anchor "fp64", a full FP64 build, or "density", FP64
-    densities, functional and E_xc with V_xc on the tensor cores: V's error
-    moves the converged energy only at second order).
+    the references: anchor "fp64", a full FP64 build, "density", FP64
+    densities, functional and E_xc with V_xc on the tensor cores (V's error
+    moves the converged energy only at second order), or "mixed", a full
+    tensor-core build, whose density error stays in E_xc at first order).
+    fp32_potentials: the incremental builds' functional takes FP32 potentials
+    where the density is above the mixed config's func_float_above (FP64
+    energy density everywhere).
     guess: "sap", "core", "learned" (the per-atom-pair network, with the SAP
     guess as fallback: for molecules outside the model's elements / basis, for
     open shells, and when the SCF started from it has not converged within
     half of max_iter), or a density matrix (total for RKS, [Da, Db] for UKS).
+    orbitals: with a density guess, S-orthonormal orbitals whose occupied
+    columns (first) span it ([C] for RKS, [Ca, Cb] for UKS), so that the first
+    update may be a rotation (the learned guess's natural orbitals).
     context: reuse integrals and grid from a previous call on the same
     molecule ({"basis","S","H","jk","grid","Enuc"}).
     jk_device: "engine" (alias "cuda": integrals computed on the GPU, kept in
@@ -364,13 +375,13 @@ def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, m
                   conv_energy=conv_energy, conv_grad=conv_grad, diis_size=diis_size, screen=screen,
                   eri_threshold=eri_threshold, anchor_every=anchor_every, context=ctx, verbose=verbose,
                   jk_device=jk_device, anchor=anchor, adiis_until=adiis_until, rotate_below=rotate_below,
-                  callback=callback, reanchor_above=reanchor_above)
+                  callback=callback, reanchor_above=reanchor_above, fp32_potentials=fp32_potentials)
         if unrestricted or charge != 0 or not G.supported(Z, b):
             r = run_scf(Z, xyz, guess="sap", max_iter=max_iter, **kw)
             r["guess_used"] = "sap (outside the learned model's scope)"
             return r
-        D0 = G.guess_density(G.default_model(), Z, xyz, ctx, precision=precision)
-        r = run_scf(Z, xyz, guess=D0, max_iter=max(1, max_iter // 2), **kw)
+        D0, C0 = G.guess_density(G.default_model(), Z, xyz, ctx, precision=precision, return_orbitals=True)
+        r = run_scf(Z, xyz, guess=D0, orbitals=[C0], max_iter=max(1, max_iter // 2), **kw)
         if r.converged:
             r["guess_used"] = "learned"
             r["wall"] += timings["setup"]
@@ -396,14 +407,20 @@ def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, m
             Ds = [C[:, :na] @ C[:, :na].T, C[:, :nb] @ C[:, :nb].T]
         else:
             Ds = [2 * C[:, :na] @ C[:, :na].T]
+        C_init = [C] * nspin
     else:
         Ds = [np.asarray(d, dtype=np.float64) for d in (guess if unrestricted else [guess])]
+        C_init = None if orbitals is None else [np.asarray(c, dtype=np.float64) for c in orbitals]
+        if C_init is not None and len(C_init) != nspin:
+            raise ValueError("orbitals: one matrix per spin")
 
-    if anchor not in ("fp64", "density"):
-        raise ValueError("anchor must be 'fp64' or 'density'")
-    anchor_code = 1 if anchor == "fp64" else 2
+    anchors = {"fp64": 1, "density": 2, "mixed": 3}
+    if anchor not in anchors:
+        raise ValueError("anchor must be 'fp64', 'density' or 'mixed'")
+    anchor_code = anchors[anchor]
+    incr_code = 16 if fp32_potentials else 0  # XC_INCREMENTAL_FP32_POTENTIALS
     diis = DIIS(diis_size)
-    Cs = None  # orbitals of the last update (per spin)
+    Cs = C_init  # orbitals of the last update (per spin)
     D_ref = None  # densities of the last XC build (the incremental reference)
     E_old = None
     history = []
@@ -433,7 +450,7 @@ def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, m
             Dst = np.ascontiguousarray(np.stack([d.T for d in Ds]))
             Vb = np.zeros((nspin, n, n))
             e = ctypes.c_double()
-            code = anchor_code if reset else 0
+            code = (anchor_code if reset else 0) | incr_code
             check(lib().xc_build_incremental(g._h, xc._h, _p(Dst), nspin, code, ctypes.byref(e), _p(Vb)))
             Exc, Vxc = e.value, [Vb[s].T.copy() for s in range(nspin)]
         timings["xc"] += time.perf_counter() - t0

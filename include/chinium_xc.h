@@ -324,7 +324,19 @@ int xc_build_response(xc_grid* g, xc_functional* f, const double* D, int nspin, 
  * first call on a grid with anchor 0) by a full FP64 build; 2 by FP64
  * densities, functional and E_xc with V on the tensor cores (about half the
  * cost: an error in V moves a converged SCF energy only at second order,
- * while E_xc takes the density's error at first order).  Host buffers. */
+ * while E_xc takes the density's error at first order); 3 by a full
+ * tensor-core build (as xc_build with XC_PRECISION_MIXED: the densities'
+ * split-BF16 error then stays in every later E_xc, ~1e-7 relative).  OR-ing
+ * XC_INCREMENTAL_FP32_POTENTIALS into anchor runs the functional of the
+ * incremental builds as a full mixed build does (FP32 potentials at points
+ * whose density is at least the mixed config's func_float_above, FP64 energy
+ * density everywhere): E_xc keeps FP64 arithmetic on the reconstructed
+ * densities, V_xc takes FP32-level noise.  Host buffers. */
+#define XC_ANCHOR_NONE 0
+#define XC_ANCHOR_FP64 1
+#define XC_ANCHOR_DENSITY 2
+#define XC_ANCHOR_MIXED 3
+#define XC_INCREMENTAL_FP32_POTENTIALS 16
 int xc_build_incremental(xc_grid* g, xc_functional* f, const double* D, int nspin, int anchor,
                          double* E, double* V);
 

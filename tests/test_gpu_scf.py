@@ -108,3 +108,52 @@ def test_incremental_builds_are_stationary_with_empty_tiles():
         Es.append(e.value)
     assert g.info()["mixed_empty_tiles"] > 0
     assert max(abs(x - Es[0]) for x in Es) < 1e-10
+
+
+def test_incremental_anchor_kinds_and_fp32_potentials():
+    """xc_build_incremental's anchors on (H2O)_3 PBE/SG-1: anchor 3 returns
+    the full tensor-core build's E_xc and V_xc; after each anchor, an
+    incremental build at a perturbed density is checked against the FP64
+    build there: anchor 2 (FP64 densities) to 1e-8 Eh in E_xc (the tensor
+    cores only see the change, elements of 2e-3 here), anchor 3 to the
+    tensor-core density's own 1e-6, and XC_INCREMENTAL_FP32_POTENTIALS
+    moves E_xc by less than 1e-9 Eh (its E stays FP64 arithmetic) while V_xc
+    takes FP32-level noise only."""
+    import ctypes
+    import chinium_gb300 as cg
+    from chinium_gb300._lib import check, lib, PRECISION_MIXED
+    Z, xyz = M.water_clusters(1, seed=3, kmin=3, kmax=3)[0]
+    r = run_scf(Z, xyz, functional="PBE", precision="fp64", max_iter=4)
+    g = r.context["grid"]
+    xc = cg.ExchangeCorrelation().Read("PBE")
+    n = r.nbasis
+    D0 = r.D[0]
+    P = np.random.default_rng(0).normal(size=(n, n)) * 1e-3
+    D1 = D0 + P + P.T
+
+    def inc(D, code):
+        Dc = np.ascontiguousarray(D.T)[None]
+        V = np.zeros((1, n, n))
+        e = ctypes.c_double()
+        check(lib().xc_build_incremental(g._h, xc._h, ctypes.c_void_p(Dc.ctypes.data), 1, code, ctypes.byref(e),
+                                         ctypes.c_void_p(V.ctypes.data)))
+        return e.value, V[0].T
+
+    Em, Vm = g.build(xc, [D0], precision=PRECISION_MIXED)
+    E3, V3 = inc(D0, 3)
+    assert E3 == Em and np.abs(V3 - Vm[0]).max() < 1e-12
+    E64, V64 = g.build(xc, [D1])
+    V64 = V64[0]
+    out = {}
+    for anchor in (2, 3):
+        for flag in (0, 16):
+            inc(D0, anchor)
+            out[anchor, flag] = inc(D1, flag)
+    for (anchor, flag), (E, V) in out.items():
+        print("anchor %d flag %2d: dE %.2e max|dV| %.2e" % (anchor, flag, E - E64, np.abs(V - V64).max()))
+    assert abs(out[2, 0][0] - E64) < 1e-8 and abs(out[2, 16][0] - E64) < 1e-8
+    assert abs(out[3, 0][0] - E64) < 1e-6 and abs(out[3, 16][0] - E64) < 1e-6
+    assert abs(out[2, 16][0] - out[2, 0][0]) < 1e-9
+    assert np.abs(out[2, 16][1] - V64).max() < 1e-5
+    with pytest.raises(Exception):
+        inc(D1, 4)

@@ -120,3 +120,31 @@ def test_adiis_start_and_cayley_rotations_reach_the_diagonalisation_fixed_point(
     assert abs(out["plain"].energy - out["adiis_cayley"].energy) < 1e-9
     assert np.abs(out["plain"].D[0] - out["adiis_cayley"].D[0]).max() < 1e-5
     assert -76.1 < out["plain"].energy < -75.8  # RHF / def2-SVP water
+
+
+def test_cayley_closed_form_matches_the_explicit_transform():
+    """cayley_update's occupied-block closed form equals C (1 - K/2)^-1 (1 + K/2)
+    built explicitly, and keeps the orbitals S-orthonormal."""
+    from chinium_gb300.scf import cayley_update
+    rng = np.random.default_rng(3)
+    n, nocc = 30, 7
+    A = rng.normal(size=(n, n))
+    S = A @ A.T / n + np.eye(n)
+    w, Q = np.linalg.eigh(S)
+    X = Q @ np.diag(w ** -0.5) @ Q.T  # S^-1/2
+    F0 = np.diag(np.sort(rng.normal(size=n)) * 3)  # well-separated orbital energies
+    C = X @ np.linalg.qr(rng.normal(size=(n, n)))[0]
+    F = np.linalg.inv(C.T) @ F0 @ np.linalg.inv(C)  # C^T F C = F0
+    P = rng.normal(size=(n, n)) * 0.02
+    F = F + P + P.T  # occupied-virtual coupling
+    got = cayley_update(C, F, nocc)
+    Fm = C.T @ F @ C
+    e = np.diag(Fm)
+    o, v = slice(0, nocc), slice(nocc, n)
+    kap = -Fm[v, o] / (e[v][:, None] - e[o][None, :])
+    K = np.zeros((n, n))
+    K[v, o] = kap
+    K[o, v] = -kap.T
+    want = C @ np.linalg.solve(np.eye(n) - 0.5 * K, np.eye(n) + 0.5 * K)
+    np.testing.assert_allclose(got, want, atol=1e-12)
+    np.testing.assert_allclose(got.T @ S @ got, np.eye(n), atol=1e-11)
