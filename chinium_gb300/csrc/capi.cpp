@@ -322,6 +322,7 @@ void Grid::get_ao(int derivative) {
     d_ao.alloc((size_t)off);
     launch_ao((int)blocks.size(), d_blocks.p, d_shell_lists.p, dev_shells(), d_x.p, d_y.p, d_z.p, ncomp, d_ao.p, stream);
     ao_order = order;
+    ao_ff_order = -1;  // the float-float copy is stale
     CGB_CUDA(cudaStreamSynchronize(stream));
 }
 
@@ -353,14 +354,27 @@ Grid::~Grid() {
     if (capture_stream) cudaStreamDestroy(capture_stream);
 }
 
-void Grid::density_device(const double* dD) {
+void Grid::density_device(const double* dD, bool float_float) {
     NvtxRange nvtx_("xc.getDensity");
     CGB_CHECK(!batched, XC_ERR_UNSUPPORTED, "batch grids run mixed-precision builds only");
     CGB_CHECK(ao_order >= type, XC_ERR_STATE, "getAO must run (for the current type) before getDensity");
     ensure_work();
     mark(0);
-    launch_density_fp64((int)blocks.size(), d_blocks.p, d_lists.p, basis.nbasis, nspin, type, dD, d_ao.p, Gp,
-                        d_rho.p, d_rho1.p, d_tau.p, stream);
+    if (float_float) {
+        if (ao_ff_order != ao_order) {  // split the AO store once per getAO
+            d_ao_ff.alloc(d_ao.n);
+            launch_split_ff((long)d_ao.n, d_ao.p, d_ao_ff.p, stream);
+            ao_ff_order = ao_order;
+        }
+        const size_t nn = (size_t)nspin * basis.nbasis * basis.nbasis;
+        d_D_ff.alloc(nn);
+        launch_split_ff((long)nn, dD, d_D_ff.p, stream);
+        launch_density_ff((int)blocks.size(), d_blocks.p, d_lists.p, basis.nbasis, nspin, type, d_D_ff.p, d_ao_ff.p,
+                          Gp, d_rho.p, d_rho1.p, d_tau.p, stream);
+    } else {
+        launch_density_fp64((int)blocks.size(), d_blocks.p, d_lists.p, basis.nbasis, nspin, type, dD, d_ao.p, Gp,
+                            d_rho.p, d_rho1.p, d_tau.p, stream);
+    }
     have_density = true;
     have_potential = false;
     have_fxc = false;

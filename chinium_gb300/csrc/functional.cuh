@@ -49,6 +49,7 @@ struct Scal {
     static CGB_HD R log_(R x) { return ::log(x); }
     static CGB_HD R sqrt_(R x) { return ::sqrt(x); }
     static CGB_HD R pow_(R x, R p) { return ::pow(x, p); }
+    static CGB_HD R cbrt_(R x) { return ::cbrt(x); }
     static CGB_HD R atan_(R x) { return ::atan(x); }
     static CGB_HD R asinh_(R x) { return ::asinh(x); }
 };
@@ -58,6 +59,7 @@ struct Scal<float> {
     static CGB_HD float log_(float x) { return ::logf(x); }
     static CGB_HD float sqrt_(float x) { return ::sqrtf(x); }
     static CGB_HD float pow_(float x, float p) { return ::powf(x, p); }
+    static CGB_HD float cbrt_(float x) { return ::cbrtf(x); }
     static CGB_HD float atan_(float x) { return ::atanf(x); }
     static CGB_HD float asinh_(float x) { return ::asinhf(x); }
 };
@@ -174,6 +176,25 @@ CGB_HD Dual<R, N> pow(const Dual<R, N>& a, R p) {
     const R f = Scal<R>::pow_(a.v, p);
     return chain(a, f, p * f / a.v);
 }
+// x^(k/3) for an integer k: cbrt and binary powering (FP64 pow is several
+// times the cost of cbrt; the functionals' exponents are all thirds).
+template <class R>
+CGB_HD R pow_third(R x, int k) {
+    const R c = Scal<R>::cbrt_(x);
+    R b = k < 0 ? R(1) / c : c, r = R(1);
+    for (int m = k < 0 ? -k : k; m; m >>= 1) {
+        if (m & 1) r *= b;
+        b *= b;
+    }
+    return r;
+}
+template <class R, int N>
+CGB_HD Dual<R, N> pow3(const Dual<R, N>& a, int k) {
+    const R f = pow_third(a.v, k);
+    return chain(a, f, R(k) / R(3) * f / a.v);
+}
+template <class R>
+CGB_HD R pow3(R a, int k) { return pow_third(a, k); }
 template <class R, int N>
 CGB_HD Dual<R, N> atan(const Dual<R, N>& a) { return chain(a, Scal<R>::atan_(a.v), R(1) / (R(1) + a.v * a.v)); }
 template <class R, int N>
@@ -205,12 +226,12 @@ CGB_HD T clamp_opz(const T& v) { return val(v) < R(kZetaThr) ? T(R(kZetaThr)) : 
 template <class T, class R>
 CGB_HD T ex_unif_half(const T& rs) {
     const R Cx = R(0.75 * 0.98474502184269654);  // 0.75 (3/pi)^(1/3)
-    return R(-0.5) * Cx * pow(R(2) * rs, R(4.0 / 3.0));
+    return R(-0.5) * Cx * pow3(R(2) * rs, 4);
 }
 
 template <class T, class R>
 CGB_HD T fzeta(const T& opz, const T& omz) {
-    return (pow(opz, R(4.0 / 3.0)) + pow(omz, R(4.0 / 3.0)) - R(2)) * R(1.0 / 0.51984209978974632953);
+    return (pow3(opz, 4) + pow3(omz, 4) - R(2)) * R(1.0 / 0.51984209978974632953);
 }
 
 template <class T, class R>
@@ -226,7 +247,7 @@ CGB_HD T vwn_f(const T& x, R A, R b, R c, R x0) {
 template <class T, class R>
 CGB_HD void rs_zeta(const XIn<T>& v, T& rho, T& rs, T& z, T& opz, T& omz) {
     rho = v.ra + v.rb;
-    rs = pow(R(3.0 / (4.0 * kPi)) / rho, R(1.0 / 3.0));
+    rs = pow3(R(3.0 / (4.0 * kPi)) / rho, 1);
     z = (v.ra - v.rb) / rho;
     opz = clamp_opz<T, R>(R(1) + z);
     omz = clamp_opz<T, R>(R(1) - z);
@@ -292,7 +313,7 @@ CGB_HDN T pw_eps(const T& rs, const T& z, const T& opz, const T& omz, T* deps) {
 template <class T, class R>
 CGB_HD T p_red(const T& n, const T& sig) {
     // sig / (4 (3 pi^2)^(2/3) n^(8/3))
-    return sig / (R(4.0 * 9.570780000627305) * pow(n, R(8.0 / 3.0)));
+    return sig / (R(4.0 * 9.570780000627305) * pow3(n, 8));
 }
 
 // sum over spins of 1/2 e_unif(2 rho_s) F(n = 2 rho_s, 4 sigma_ss, 2 tau_s)
@@ -320,7 +341,7 @@ CGB_HDN T e_b88(const XIn<T>& v) {
 #pragma unroll
     for (int s = 0; s < 2; s++) {
         if (val(rr[s]) <= R(0.5 * kDensThr)) continue;
-        const T r43 = pow(rr[s], R(4.0 / 3.0));
+        const T r43 = pow3(rr[s], 4);
         const T x = sqrt(ss[s]) / r43;
         out = out - cx * r43 - beta * r43 * x * x / (R(1) + R(6) * beta * x * asinh(x));
     }
@@ -333,12 +354,12 @@ CGB_HDN T e_lyp(const XIn<T>& v) {
     const R CF = R(0.3 * 9.570780000627305);  // 3/10 (3 pi^2)^(2/3)
     const T ra = v.ra, rb = v.rb, rho = ra + rb;
     const T saa = v.saa, sbb = v.sbb, sig = v.saa + R(2) * v.sab + v.sbb;
-    const T rm13 = pow(rho, R(-1.0 / 3.0));
+    const T rm13 = pow3(rho, -1);
     const T den = R(1) + d * rm13;
-    const T omega = exp(-c * rm13) / den * pow(rho, R(-11.0 / 3.0));
+    const T omega = exp(-c * rm13) / den * pow3(rho, -11);
     const T delta = c * rm13 + d * rm13 / den;
     const T t1 = R(-4) * a / den * ra * rb / rho;
-    const T inner = ra * rb * (R(12.699208415745595) * CF * (pow(ra, R(8.0 / 3.0)) + pow(rb, R(8.0 / 3.0))) +
+    const T inner = ra * rb * (R(12.699208415745595) * CF * (pow3(ra, 8) + pow3(rb, 8)) +
                                (R(47.0 / 18.0) - R(7.0 / 18.0) * delta) * sig -
                                (R(2.5) - delta / R(18)) * (saa + sbb) -
                                (delta - R(11)) / R(9) * (ra / rho * saa + rb / rho * sbb)) -
@@ -350,11 +371,11 @@ CGB_HDN T e_lyp(const XIn<T>& v) {
 template <class T, class R>
 CGB_HDN T pbe_c_eps(const T& rho, const T& z, const T& opz, const T& omz, const T& sig, R beta) {
     const R gamma = R(0.031090690869654895034);  // (1 - ln 2) / pi^2
-    const T rs = pow(R(3.0 / (4.0 * kPi)) / rho, R(1.0 / 3.0));
+    const T rs = pow3(R(3.0 / (4.0 * kPi)) / rho, 1);
     const T ec = pw_eps<T, R>(rs, z, opz, omz, nullptr);
-    const T phi = (pow(opz, R(2.0 / 3.0)) + pow(omz, R(2.0 / 3.0))) * R(0.5);
+    const T phi = (pow3(opz, 2) + pow3(omz, 2)) * R(0.5);
     const T phi3 = phi * phi * phi;
-    const T kf = pow(R(3.0 * kPi * kPi) * rho, R(1.0 / 3.0));
+    const T kf = pow3(R(3.0 * kPi * kPi) * rho, 1);
     const T t2 = sig * R(kPi) / (R(16) * phi * phi * kf * rho * rho);
     const T A = (beta / gamma) / (exp(-ec / (gamma * phi3)) - R(1));
     const T At2 = A * t2;
@@ -377,7 +398,7 @@ CGB_HDN T fx_tpss(const T& n, const T& sig, const T& tau) {
     const T p = p_red<T, R>(n, sig);
     const T tauw = sig / (R(8) * n);
     const T z = tauw / tau;
-    const T tunif = R(0.3 * 9.570780000627305) * pow(n, R(5.0 / 3.0));
+    const T tunif = R(0.3 * 9.570780000627305) * pow3(n, 5);
     const T alpha = (tau - tauw) / tunif;
     const T qb = R(0.45) * (alpha - R(1)) / sqrt(R(1) + b * alpha * (alpha - R(1))) + R(2.0 / 3.0) * p;
     const T z2 = z * z;
@@ -402,10 +423,10 @@ CGB_HDN T e_tpss_c(const XIn<T>& v) {
     const T epbe = pbe_c_eps<T, R>(rho, z, opz, omz, sig, beta);
     const T rho2 = rho * rho;
     const T gz2 = R(4) * (v.rb * v.rb * v.saa - R(2) * v.ra * v.rb * v.sab + v.ra * v.ra * v.sbb) / (rho2 * rho2);
-    const T xi2 = gz2 / (R(4) * pow(R(3.0 * kPi * kPi) * rho, R(2.0 / 3.0)));
+    const T xi2 = gz2 / (R(4) * pow3(R(3.0 * kPi * kPi) * rho, 2));
     const T zz2 = z * z;
     const T C0 = R(0.53) + R(0.87) * zz2 + R(0.50) * zz2 * zz2 + R(2.26) * zz2 * zz2 * zz2;
-    const T den = R(1) + xi2 * (pow(opz, R(-4.0 / 3.0)) + pow(omz, R(-4.0 / 3.0))) * R(0.5);
+    const T den = R(1) + xi2 * (pow3(opz, -4) + pow3(omz, -4)) * R(0.5);
     const T den2 = den * den;
     const T C = C0 / (den2 * den2);
     const T rr[2] = {v.ra, v.rb};
@@ -471,13 +492,13 @@ CGB_HDN T fx_r2scan(const T& n, const T& sig, const T& tau) {
     const R C2 = R(-kR2Dfx * (1.0 - 1.174));
     const T p = p_red<T, R>(n, sig);
     const T tauw = sig / (R(8) * n);
-    const T tunif = R(0.3 * 9.570780000627305) * pow(n, R(5.0 / 3.0));
+    const T tunif = R(0.3 * 9.570780000627305) * pow3(n, 5);
     const T ab = (tau - tauw) / (tunif + R(kR2Eta) * tauw);
     const R dp24 = R(kR2Dp2 * kR2Dp2 * kR2Dp2 * kR2Dp2);
     const T x = (Ceta * C2 * exp(-(p * p) / dp24) + mu_ak) * p;
     const T hx1 = R(1) + k1 - k1 / (R(1) + x / k1);
     const T fx = r2_fx<T, R>(ab);
-    const T gx = R(1) - exp(-a1 / pow(p, R(0.25)));
+    const T gx = R(1) - exp(-a1 / sqrt(sqrt(p)));
     return (hx1 + fx * (hx0 - hx1)) * gx;
 }
 
@@ -489,12 +510,12 @@ CGB_HDN T e_r2scan_c(const XIn<T>& v) {
     rs_zeta<T, R>(v, rho, rs, z, opz, omz);
     const T sig = v.saa + R(2) * v.sab + v.sbb;
     const T tau = v.ta + v.tb;
-    const T phi = (pow(opz, R(2.0 / 3.0)) + pow(omz, R(2.0 / 3.0))) * R(0.5);
+    const T phi = (pow3(opz, 2) + pow3(omz, 2)) * R(0.5);
     const T phi3 = phi * phi * phi;
-    const T ds = (pow(opz, R(5.0 / 3.0)) + pow(omz, R(5.0 / 3.0))) * R(0.5);
-    const T dxz = (pow(opz, R(4.0 / 3.0)) + pow(omz, R(4.0 / 3.0))) * R(0.5);
+    const T ds = (pow3(opz, 5) + pow3(omz, 5)) * R(0.5);
+    const T dxz = (pow3(opz, 4) + pow3(omz, 4)) * R(0.5);
     const T p = p_red<T, R>(rho, sig);
-    const T kf = pow(R(3.0 * kPi * kPi) * rho, R(1.0 / 3.0));
+    const T kf = pow3(R(3.0 * kPi * kPi) * rho, 1);
     const T t2 = sig * R(kPi) / (R(16) * phi * phi * kf * rho * rho);
     T de1;
     const T e1 = pw_eps<T, R>(rs, z, opz, omz, &de1);
@@ -508,17 +529,17 @@ CGB_HDN T e_r2scan_c(const XIn<T>& v) {
     const T z2 = z * z, z4 = z2 * z2;
     const T Gc = (R(1) - R(2.3631) * (dxz - R(1))) * (R(1) - z4 * z4 * z4);
     const T w0 = exp(-elda0 / b1c) - R(1);
-    const T ginf = pow(R(1) + R(4) * chi * p, R(-0.25));
+    const T ginf = R(1) / sqrt(sqrt(R(1) + R(4) * chi * p));
     const T H0 = b1c * log(R(1) + w0 * (R(1) - ginf));
     const T e0 = (elda0 + H0) * Gc;
     const R dp24 = R(kR2Dp2 * kR2Dp2 * kR2Dp2 * kR2Dp2);
     const T dy = R(kR2Dfc) / (R(27) * gamma * ds * phi3 * w1) *
                  (R(20) * rs * (delda0 * Gc - de1) - R(45 * kR2Eta) * (elda0 * Gc - e1)) * p * exp(-(p * p) / dp24);
-    const T g = pow(R(1) + R(4) * (y - dy), R(-0.25));
+    const T g = R(1) / sqrt(sqrt(R(1) + R(4) * (y - dy)));
     const T H1 = gamma * phi3 * log(R(1) + w1 * (R(1) - g));
     const T ec1 = e1 + H1;
     const T tauw = sig / (R(8) * rho);
-    const T tunif = R(0.3 * 9.570780000627305) * pow(rho, R(5.0 / 3.0)) * ds;
+    const T tunif = R(0.3 * 9.570780000627305) * pow3(rho, 5) * ds;
     const T ab = (tau - tauw) / (tunif + R(kR2Eta) * tauw);
     const T fc = r2_fc<T, R>(ab);
     return rho * (ec1 + fc * (e0 - ec1));
@@ -819,6 +840,12 @@ CGB_HD Jet2<R, N> sqrt(const Jet2<R, N>& a) {
 template <class R, int N>
 CGB_HD Jet2<R, N> pow(const Jet2<R, N>& a, R p) {
     const R f = Scal<R>::pow_(a.v, p);
+    const R i = R(1) / a.v;
+    return chain2(a, f, p * f * i, p * (p - R(1)) * f * i * i);
+}
+template <class R, int N>
+CGB_HD Jet2<R, N> pow3(const Jet2<R, N>& a, int k) {
+    const R f = pow_third(a.v, k), p = R(k) / R(3);
     const R i = R(1) / a.v;
     return chain2(a, f, p * f * i, p * (p - R(1)) * f * i * i);
 }

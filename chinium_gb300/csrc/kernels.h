@@ -37,6 +37,13 @@ void launch_ao(int nblocks, const BlockDesc* d_blocks, const int* d_block_shells
 void launch_density_fp64(int nblocks, const BlockDesc* d_blocks, const int* d_basis_lists, int nbasis,
                          int nspin, int type, const double* D, const double* ao, long Gp, double* rho,
                          double* rho1, double* tau, cudaStream_t s);
+// The same in float-float arithmetic on the FP32 pipe (~1e-14 relative), from
+// D and the AO store split into float pairs by launch_split_ff: the
+// incremental build's reference densities.
+void launch_split_ff(long n, const double* src, float2* dst, cudaStream_t s);
+void launch_density_ff(int nblocks, const BlockDesc* d_blocks, const int* d_basis_lists, int nbasis, int nspin,
+                       int type, const float2* D, const float2* ao, long Gp, double* rho, double* rho1, double* tau,
+                       cudaStream_t s);
 
 // XC nuclear-gradient partials with the grid fixed (LDA / GGA): part[s][list entry][t]
 // = -2 sum_g [d_t phi U + sum_r d_t d_r phi f_r T] for the block function at that list entry

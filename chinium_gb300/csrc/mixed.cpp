@@ -671,9 +671,9 @@ void Grid::build_incremental(const double* dD, const Functional& f, double* dE, 
         return;
     }
     if (anchor == 2) {
-        // FP64 densities, functional and E_xc; V from the full coefficients
-        // on the tensor cores
-        density_device(dD);
+        // float-float (FP64-level) densities, FP64 functional and E_xc; V
+        // from the full coefficients on the tensor cores
+        density_device(dD, true);
         evaluate(f);
         energy_device(dE);
         alloc_refs();

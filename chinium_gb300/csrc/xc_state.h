@@ -59,6 +59,8 @@ struct Grid {
     DevBuf<BlockDesc> d_blocks;
     DevBuf<int> d_lists, d_shell_lists;
     DevBuf<double> d_ao;
+    DevBuf<float2> d_ao_ff, d_D_ff;  // float-float copies for the reference densities of incremental builds
+    int ao_ff_order = -1;            // AO order d_ao_ff was split from (-1: none)
     DevBuf<double> d_rho, d_rho1, d_tau, d_sigma, d_eps, d_vrho, d_vsigma, d_vtau, d_fcoef, d_partial, d_scalar;
     DevBuf<double> d_D, d_V;
 
@@ -74,7 +76,7 @@ struct Grid {
     DevShells dev_shells() const;
     void get_ao(int derivative);
     void ensure_work();
-    void density_device(const double* dD);
+    void density_device(const double* dD, bool float_float = false);
     void evaluate(const Functional& f, double float_above = __builtin_huge_val());
     void energy_device(double* dE);
     void fock_device(double* dV, int family);

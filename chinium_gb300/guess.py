@@ -416,14 +416,42 @@ def predict_density(model, Z, xyz, basis, S, nocc, bf16=True, D_base=None, metri
     D = assemble_blocks(pr, Y, Uas, Ubs, first, count, n)
     D = 0.5 * (D + D.T)
     if model.residual:
-        D = D + D_base
-    # purification: occupied natural orbitals in the overlap metric
+        D = D + (D_base.result() if hasattr(D_base, "result") else D_base)
+    # purification: the projector onto the nocc most occupied natural orbitals
+    # in the overlap metric -- by McWeeny iterations P <- 3P^2 - 2P^3 (GEMMs
+    # only; the same projector when exactly nocc occupations exceed 1/2),
+    # else (or when the orbitals are wanted) by diagonalisation
     _, Xh, Sh = metric or overlap_metric(S)
-    occ, C = np.linalg.eigh(Sh @ D @ Sh)
+    P = 0.5 * (Sh @ D @ Sh)
+    if not return_orbitals:
+        converged = False
+        for _ in range(12):
+            P2 = P @ P
+            if np.abs(P2 - P).max() < 1e-12:
+                converged = True
+                break
+            P = 3.0 * P2 - 2.0 * (P2 @ P)
+        if converged and abs(np.trace(P) - nocc) < 1e-8:
+            P = 0.5 * (P + P.T)
+            return 2.0 * (Xh @ P @ Xh)
+        P = 0.5 * (Sh @ D @ Sh)
+    occ, C = np.linalg.eigh(P)
     Cn = Xh @ C[:, np.argsort(occ)[::-1]]
     Co = Cn[:, :nocc]
     D = 2.0 * Co @ Co.T
     return (D, Cn) if return_orbitals else D
+
+
+_WORKER = None
+
+
+def _worker():
+    """One background thread for the guess's SAP base (created on first use)."""
+    global _WORKER
+    if _WORKER is None:
+        from concurrent.futures import ThreadPoolExecutor
+        _WORKER = ThreadPoolExecutor(max_workers=1, thread_name_prefix="sap-guess")
+    return _WORKER
 
 
 def guess_density(model, Z, xyz, ctx, bf16=True, precision="fp64", return_orbitals=False):
@@ -436,7 +464,11 @@ def guess_density(model, Z, xyz, ctx, bf16=True, precision="fp64", return_orbita
     metric = overlap_metric(ctx["S"], ctx)
     # tensor-core V_SAP only for a well-conditioned overlap (as the SCF's own SAP guess)
     prec = precision if ctx.get("S_min", 0.0) >= 1e-3 else "fp64"
-    base = sap_density(ctx["grid"], ctx["H"], ctx["S"], nocc, metric, prec) if model.residual else None
+    # the SAP base (V_SAP on the GPU, then a host diagonalisation) on a worker
+    # thread while this one forms the pair features, runs the network and
+    # assembles the blocks (both release the interpreter lock in their
+    # library calls)
+    base = _worker().submit(sap_density, ctx["grid"], ctx["H"], ctx["S"], nocc, metric, prec) if model.residual else None
     return predict_density(model, Z, xyz, ctx["basis"], ctx["S"], nocc, bf16=bf16, D_base=base, metric=metric,
                            return_orbitals=return_orbitals)
 

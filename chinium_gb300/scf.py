@@ -304,7 +304,7 @@ def occupations(Z, charge, mult):
 def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, mult=1, precision="fp64",
             guess="sap", conv_energy=1e-8, conv_grad=1e-6, max_iter=100, diis_size=20, screen=0.0,
             eri_threshold=1e-12, anchor_every=0, context=None, verbose=False, jk_device="engine", anchor="fp64",
-            adiis_until=1e-1, rotate_below=1e-1, callback=None, reanchor_above=1.0, fp32_potentials=False,
+            adiis_until=1e-1, rotate_below=1e-1, callback=None, reanchor_above=1.0, fp32_potentials=True,
             orbitals=None):
     """Kohn-Sham SCF.  precision: "fp64" (plain XC build every iteration) or
     "mixed" (incremental tensor-core XC builds after a first build that sets
@@ -314,7 +314,8 @@ def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, m
     tensor-core build, whose density error stays in E_xc at first order).
     fp32_potentials: the incremental builds' functional takes FP32 potentials
     where the density is above the mixed config's func_float_above (FP64
-    energy density everywhere).
+    energy density everywhere), as a full mixed build does; False keeps the
+    potentials in FP64 too.
     guess: "sap", "core", "learned" (the per-atom-pair network, with the SAP
     guess as fallback: for molecules outside the model's elements / basis, for
     open shells, and when the SCF started from it has not converged within
@@ -363,6 +364,7 @@ def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, m
     b, S, H, jk, Enuc, g = ctx["basis"], ctx["S"], ctx["H"], ctx["jk"], ctx["Enuc"], ctx["grid"]
     n = b.nbasis
     X = overlap_metric(S, ctx)[0]
+    SX = S @ X
     timings["setup"] = time.perf_counter() - t_start
 
     def solve(F):
@@ -462,19 +464,23 @@ def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, m
         else:
             J = jk.coulomb_end(J_pending)
         timings["jk"] += time.perf_counter() - t0
+        t0 = time.perf_counter()
+        HJ = H + J
         if unrestricted:
-            Fs = [H + J - exx * Ks[s] + Vxc[s] for s in range(2)]
-            E = (np.sum(Dtot * H) + 0.5 * np.sum(Dtot * J) - 0.5 * exx * (np.sum(Ds[0] * Ks[0]) + np.sum(Ds[1] * Ks[1]))
+            Fs = [HJ + Vxc[s] - exx * Ks[s] if exx else HJ + Vxc[s] for s in range(2)]
+            E = (np.vdot(Dtot, H) + 0.5 * np.vdot(Dtot, J) - 0.5 * exx * (np.vdot(Ds[0], Ks[0]) + np.vdot(Ds[1], Ks[1]))
                  + Exc + Enuc)
         else:
-            Fs = [H + J - 0.5 * exx * Ks[0] + Vxc[0]]
-            E = np.sum(Dtot * H) + 0.5 * np.sum(Dtot * J) - 0.25 * exx * np.sum(Dtot * Ks[0]) + Exc + Enuc
+            Fs = [HJ + Vxc[0] - 0.5 * exx * Ks[0] if exx else HJ + Vxc[0]]
+            E = np.vdot(Dtot, H) + 0.5 * np.vdot(Dtot, J) - 0.25 * exx * np.vdot(Dtot, Ks[0]) + Exc + Enuc
         errs = []
         for F, D in zip(Fs, Ds):
-            FDS = F @ D @ S  # S D F = (F D S)^T for symmetric F, D, S
-            errs.append(X.T @ (FDS - FDS.T) @ X)
+            # X^T (F D S - S D F) X; S D F = (F D S)^T for symmetric F, D, S
+            Mc = X.T @ (F @ (D @ SX))
+            errs.append(Mc - Mc.T)
         gmax = max(np.abs(e).max() for e in errs)
         dE = None if E_old is None else E - E_old
+        timings["fock"] = timings.get("fock", 0.0) + time.perf_counter() - t0
         history.append((E, gmax))
         if callback is not None:
             callback(it, Ds, Exc, Vxc, E)
@@ -484,8 +490,10 @@ def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, m
             converged = True
             break
         E_old = E
+        t0 = time.perf_counter()
         diis.push(Fs, errs, Ds, E)
         Fx = diis.extrapolate_adiis() if adiis_until > 0 and gmax > adiis_until else diis.extrapolate()
+        timings["diis"] = timings.get("diis", 0.0) + time.perf_counter() - t0
         t0 = time.perf_counter()
         occs = (na, nb) if unrestricted else (na,)
         rotate = rotate_below > 0 and gmax < rotate_below and Cs is not None

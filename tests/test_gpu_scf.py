@@ -144,6 +144,9 @@ def test_incremental_anchor_kinds_and_fp32_potentials():
     assert E3 == Em and np.abs(V3 - Vm[0]).max() < 1e-12
     E64, V64 = g.build(xc, [D1])
     V64 = V64[0]
+    # anchor 2's float-float densities with the FP64 functional: E_xc as the FP64 build
+    E2, _ = inc(D1, 2)
+    assert abs(E2 - E64) < 1e-10, E2 - E64
     out = {}
     for anchor in (2, 3):
         for flag in (0, 16):
