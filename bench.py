@@ -393,42 +393,42 @@ def run_alkanes(args):
 SCF_METRIC = "SCF wall time to 1e-8 Eh, (H2O)_8 RKS PBE/def2-SVP SG-2, mixed + learned guess"
 
 
-def run_scf_water(args):
-    """Held-out water octamers (seeded, disjoint from the guess's training
-    seeds): full Kohn-Sham SCFs to 1e-8 Eh with (a) plain FP64 XC builds from
-    the SAP guess — with the reference's unscreened blocks and with block
-    screening 1e-11 — and (b) incremental mixed builds from the learned guess
-    (its SAP base on the tensor cores; references from screened FP64
-    densities with a tensor-core V), plus the other combinations.  Integrals,
-    the overlap metric and the grids are shared setup (repulsion integrals
-    computed on the GPU and resident in HBM); the timed SCF includes the guess
-    and every iteration (XC build, J/K contraction, DIIS, diagonalisation)."""
-    import torch
+def scf_water_legs(nmols, molecules=None, grid="SG-2", legs_cfg=None):
+    """Full Kohn-Sham SCFs to 1e-8 Eh (PBE/def2-SVP) of seeded held-out water
+    octamers (disjoint from the guess's training seeds) or of the given
+    molecules: (a) plain FP64 XC builds from the SAP guess -- with the
+    reference's unscreened blocks and with block screening 1e-11 -- and from
+    the learned guess, and (b) incremental mixed builds from the learned guess
+    (its SAP base on the tensor cores; references from float-float densities
+    with a tensor-core V), plus the other combinations.  Integrals, the overlap
+    metric and the grids are shared setup (repulsion integrals computed on the
+    GPU and resident in HBM); the timed SCF includes the guess and every
+    iteration (XC build, J/K contraction, DIIS, orbital update).  Returns the
+    per-leg means and the speed-ups."""
     import chinium_gb300 as cg
     from chinium_gb300 import guess as G
     from chinium_gb300 import molecules as M
     from chinium_gb300.scf import run_scf
-    torch.cuda.set_device(0)
-    mols = M.water_clusters(args.scf_mols, seed=424242, kmin=8, kmax=8)
+    mols = molecules or M.water_clusters(nmols, seed=424242, kmin=8, kmax=8)
     model = G.load(G.DEFAULT_WEIGHTS)
     # (XC precision, guess, reference build of the incremental mixed SCF, FP64 block screening).
     # Screening 0 is the reference's semantics (every function in every block); 1e-11 drops the shells
     # below 1e-11 on a block, which leaves E_xc unchanged to 1e-14 Eh here and makes FP64 builds 2.4x faster.
-    legs_cfg = {"fp64_sap": ("fp64", "sap", "fp64", 0.0), "fp64_sap_screened": ("fp64", "sap", "fp64", 1e-11),
-                "fp64_learned": ("fp64", "learned", "fp64", 0.0),
-                "fp64_learned_screened": ("fp64", "learned", "fp64", 1e-11),
-                "mixed_sap": ("mixed", "sap", "density", 1e-11), "mixed_learned": ("mixed", "learned", "density", 1e-11),
-                "mixed_learned_unscreened_anchor": ("mixed", "learned", "density", 0.0)}
+    legs_cfg = legs_cfg or {
+        "fp64_sap": ("fp64", "sap", "fp64", 0.0), "fp64_sap_screened": ("fp64", "sap", "fp64", 1e-11),
+        "fp64_learned": ("fp64", "learned", "fp64", 0.0), "fp64_learned_screened": ("fp64", "learned", "fp64", 1e-11),
+        "mixed_sap": ("mixed", "sap", "density", 1e-11), "mixed_learned": ("mixed", "learned", "density", 1e-11),
+        "mixed_learned_unscreened_anchor": ("mixed", "learned", "density", 0.0)}
     legs = {k: [] for k in legs_cfg}
     dE = []
     t_setup = 0.0
     xc = cg.ExchangeCorrelation().Read("PBE")
     for Z, xyz in mols:
-        kw = dict(functional="PBE", grid="SG-2", jk_device="engine")
+        kw = dict(functional="PBE", grid=grid, jk_device="engine")
         t0 = time.perf_counter()
         ctxs = {}
-        for scr in (0.0, 1e-11):  # integrals shared; one grid (AO store, mixed tiles) per screening
-            ctx = {k: v for k, v in ctxs[0.0].items() if not k.startswith("grid")} if ctxs else None
+        for scr in sorted({v[3] for v in legs_cfg.values()}):  # integrals shared; one grid per screening
+            ctx = {k: v for k, v in next(iter(ctxs.values())).items() if not k.startswith("grid")} if ctxs else None
             warm = run_scf(Z, xyz, precision="fp64", guess="core", max_iter=1, context=ctx, screen=scr, **kw)
             ctxs[scr] = warm.context
             ctxs[scr]["grid"].build(xc, [warm.D[0]], precision=cg.PRECISION_MIXED)  # mixed tiles, AO planes
@@ -452,16 +452,49 @@ def run_scf_water(args):
                 "diag_s": float(np.mean([x["diag_s"] for x in v])),
                 "max_abs_dE_vs_fp64_sap": float(max(x["dE"] for x in v))} for k, v in legs.items()}
     value = summ["mixed_learned"]["wall_s"]
-    line = {"metric": SCF_METRIC, "value": value, "unit": "s", "n_gpus": 1, "steps": len(mols), "warmup": 0,
+    best = min((v["wall_s"], k) for k, v in summ.items() if k.startswith("fp64"))
+    return {"molecules": len(mols), "legs": summ, "setup_s_per_molecule": t_setup / len(mols),
+            "mixed_learned_s": value, "speedup_vs_plain_fp64_sap": summ["fp64_sap"]["wall_s"] / value,
+            "speedup_vs_screened_fp64_sap": summ["fp64_sap_screened"]["wall_s"] / value
+            if "fp64_sap_screened" in summ else None,
+            "best_fp64_leg": best[1], "speedup_vs_best_fp64": best[0] / value,
+            "max_abs_dE_total_vs_plain_fp64": float(max(dE))}
+
+
+def run_scf_water(args):
+    """The SCF line of held-out water octamers (scf_water_legs)."""
+    import torch
+    torch.cuda.set_device(0)
+    r = scf_water_legs(args.scf_mols)
+    value = r["mixed_learned_s"]
+    line = {"metric": SCF_METRIC, "value": value, "unit": "s", "n_gpus": 1, "steps": r["molecules"], "warmup": 0,
             "ms_per_step": value * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
             "dtype": "bf16x3 (split) + f64 accumulation (XC); f64 elsewhere", "data": "synthetic",
-            "config": {"workload": "(H2O)_8 water clusters (seed 424242), RKS PBE/def2-SVP SG-2, SCF to 1e-8 Eh",
-                       "molecules": len(mols), "legs": summ, "setup_s_per_molecule": t_setup / len(mols),
-                       "speedup_vs_plain_fp64_sap": summ["fp64_sap"]["wall_s"] / value,
-                       "speedup_vs_screened_fp64_sap": summ["fp64_sap_screened"]["wall_s"] / value,
-                       "speedup_vs_best_fp64": min(v["wall_s"] for k, v in summ.items() if k.startswith("fp64")) / value,
-                       "max_abs_dE_total_vs_plain_fp64": float(max(dE))}}
+            "config": dict({"workload": "(H2O)_8 water clusters (seed 424242), RKS PBE/def2-SVP SG-2, SCF to 1e-8 Eh"},
+                           **r)}
     print(json.dumps(line), flush=True)
+
+
+def scf_summaries():
+    """SCF results carried by the default line (a few seconds each): the
+    (H2O)_8 SG-2 legs on two held-out octamers, the single water of the
+    plain-path configuration (PBE/def2-SVP SG-1 from the SAP guess, FP64)
+    beside its mixed + learned SCF, and the learned guess on 24 held-out
+    clusters of 2-8 waters (SG-1, mixed SCFs, SAP vs learned start)."""
+    import types
+    from chinium_gb300 import molecules as M
+    from chinium_gb300 import learn_guess as LG
+    from chinium_gb300 import guess as G
+    out = {"scf_water8_sg2": scf_water_legs(2)}
+    h2o = scf_water_legs(1, molecules=[M.h2o()], grid="SG-1", legs_cfg={
+        "fp64_sap": ("fp64", "sap", "fp64", 0.0), "fp64_learned": ("fp64", "learned", "fp64", 0.0),
+        "mixed_learned": ("mixed", "learned", "density", 0.0)})
+    out["scf_h2o_sg1"] = h2o
+    a = types.SimpleNamespace(test=24, kmin=2, kmax=8, test_kmax=8, functional="PBE", jk="engine", precision="mixed")
+    t0 = time.perf_counter()
+    rows = LG.evaluate(G.load(G.DEFAULT_WEIGHTS), a, lambda s: None)
+    out["learned_guess_24_heldout_sg1"] = dict(LG.summarize(rows), eval_s=time.perf_counter() - t0)
+    return out
 
 
 JK_METRIC = "Coulomb (J) builds/s, (H2O)8 def2-SVP, repulsion integrals on the GPU (in-core)"
@@ -825,6 +858,7 @@ def main():
     ap.add_argument("--scf-mols", type=int, default=4)
     ap.add_argument("--fp64-mols", type=int, default=0, help="alkanes64: molecules checked in FP64 (0 = all)")
     ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--no-scf", action="store_true", help="c18: leave out the SCF and learned-guess results")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -1048,6 +1082,8 @@ def main():
             line["config"]["abs_dE_xc_fp64_vs_oracle"] = abs(E64 - arm.E)
             line["config"]["max_abs_dV_xc_fp64_vs_oracle"] = float(max(
                 np.abs(V64h[s_].T - arm.F[s_]).max() for s_ in range(ns)))
+    if rank == 0 and args.workload == "c18" and not args.no_scf:
+        line["scf"] = scf_summaries()
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
