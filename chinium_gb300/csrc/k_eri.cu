@@ -482,7 +482,10 @@ void launch_coulomb_dense(int n, int nmat, long long ld, const double* M, const 
     const float2* Mf = reinterpret_cast<const float2*>(M);
     coulomb_pack_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(n, nmat, ld, D, xf);
     CGB_CUDA(cudaGetLastError());
-    const unsigned blocks = persistent_blocks(ld, 8);
+    // one CTA per 8 rows (not persistent): CTAs retire every few microseconds,
+    // so kernels of a higher-priority stream (an SCF's XC build beside J) get
+    // SMs without waiting for the whole GEMV
+    const unsigned blocks = (unsigned)((ld + 7) / 8);
     for (int m0 = 0; m0 < nmat; m0 += kGemvMaxVec) {
         const int nm = nmat - m0 < kGemvMaxVec ? nmat - m0 : kGemvMaxVec;
         const float2* xm = xf + m0 * ld;

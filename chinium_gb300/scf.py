@@ -358,7 +358,8 @@ def run_scf(Z, xyz, basis="def2-svp", functional="PBE", grid="SG-1", charge=0, m
             # iteration (torch's or the engine's stream) runs alongside it
             import torch
             torch.cuda.synchronize()
-            ctx["grid_stream"] = torch.cuda.Stream()
+            # a higher priority than the J/K stream: the XC build is the longer of the two
+            ctx["grid_stream"] = torch.cuda.Stream(priority=-1)
             g.set_stream(ctx["grid_stream"].cuda_stream)
         ctx["grid"], ctx["grid_key"] = g, key
     b, S, H, jk, Enuc, g = ctx["basis"], ctx["S"], ctx["H"], ctx["jk"], ctx["Enuc"], ctx["grid"]
