@@ -38,29 +38,49 @@ def _binom(n, k):
     return math.comb(n, k) if 0 <= k <= n else 0
 
 
+_SH_TABLES = {}
+
+
+def _solid_harmonic_table(l):
+    """Monomial exponents (a, b, c), a + b + c = l, and the (2l+1) x nmono
+    coefficients of the real solid harmonics S_lm (m = -l..l) in them,
+    Helgaker-Jorgensen-Olsen normalisation (S_l0 = r^l P_l(cos theta))."""
+    if l not in _SH_TABLES:
+        exps = [(a, b, l - a - b) for a in range(l, -1, -1) for b in range(l - a, -1, -1)]
+        col = {e: i for i, e in enumerate(exps)}
+        T = np.zeros((2 * l + 1, len(exps)))
+        for m in range(-l, l + 1):
+            am = abs(m)
+            vm2 = 1 if m < 0 else 0
+            N = 1.0 / (2 ** am * math.factorial(l)) * math.sqrt(
+                2.0 * math.factorial(l + am) * math.factorial(l - am) / (2.0 if m == 0 else 1.0))
+            vmax2 = 2 * math.floor(am / 2 - vm2 / 2) + vm2
+            for t in range((l - am) // 2 + 1):
+                for u in range(t + 1):
+                    for v2 in range(vm2, vmax2 + 1, 2):
+                        sgn = -1.0 if (t + (v2 - vm2) // 2) % 2 else 1.0
+                        C = sgn * 0.25 ** t * _binom(l, t) * _binom(l - t, am + t) * _binom(t, u) * _binom(am, v2)
+                        a, b, c = 2 * t + am - 2 * u - v2, 2 * u + v2, l - 2 * t - am
+                        if a < 0 or b < 0 or c < 0:
+                            continue
+                        T[m + l, col[(a, b, c)]] += N * C
+        _SH_TABLES[l] = (exps, T)
+    return _SH_TABLES[l]
+
+
 def solid_harmonics(l, xyz):
     """Real solid harmonics S_lm (m = -l..l), Helgaker-Jorgensen-Olsen
     normalisation (S_l0 = r^l P_l(cos theta)); xyz (K, 3) -> (2l+1, K)."""
+    exps, T = _solid_harmonic_table(l)
     x, y, z = xyz[:, 0], xyz[:, 1], xyz[:, 2]
-    out = np.zeros((2 * l + 1, len(xyz)))
-    for m in range(-l, l + 1):
-        am = abs(m)
-        vm2 = 1 if m < 0 else 0
-        N = 1.0 / (2 ** am * math.factorial(l)) * math.sqrt(
-            2.0 * math.factorial(l + am) * math.factorial(l - am) / (2.0 if m == 0 else 1.0))
-        vmax2 = 2 * math.floor(am / 2 - vm2 / 2) + vm2
-        acc = np.zeros(len(xyz))
-        for t in range((l - am) // 2 + 1):
-            for u in range(t + 1):
-                for v2 in range(vm2, vmax2 + 1, 2):
-                    sgn = -1.0 if (t + (v2 - vm2) // 2) % 2 else 1.0
-                    C = sgn * 0.25 ** t * _binom(l, t) * _binom(l - t, am + t) * _binom(t, u) * _binom(am, v2)
-                    a, b, c = 2 * t + am - 2 * u - v2, 2 * u + v2, l - 2 * t - am
-                    if a < 0 or b < 0 or c < 0:
-                        continue
-                    acc = acc + C * x ** a * y ** b * z ** c
-        out[m + l] = N * acc
-    return out
+    px = [np.ones_like(x)]
+    py, pz = [np.ones_like(y)], [np.ones_like(z)]
+    for _ in range(l):
+        px.append(px[-1] * x)
+        py.append(py[-1] * y)
+        pz.append(pz[-1] * z)
+    mono = np.stack([px[a] * py[b] * pz[c] for a, b, c in exps])
+    return T @ mono
 
 
 _RNG_PTS = np.random.default_rng(12345).normal(size=(32, 3))
@@ -83,7 +103,7 @@ def shell_rotations(shell_type, Qs):
     if shell_type == 1:  # Cartesian x, y, z
         return np.ascontiguousarray(np.transpose(Qs, (0, 2, 1)))
     l = -shell_type
-    pts = np.einsum("kj,pjm->pkm", _RNG_PTS, Qs).reshape(-1, 3)  # rows r^T Q
+    pts = np.matmul(_RNG_PTS, Qs).reshape(-1, 3)  # rows r^T Q
     A = solid_harmonics(l, pts).reshape(2 * l + 1, P, len(_RNG_PTS)).transpose(1, 0, 2)
     return A @ _sample_pinv(l)
 
@@ -173,14 +193,18 @@ def frames_and_features(Z, xyz, pr):
     Z = np.asarray(Z)
     n = len(xyz)
     dist = np.linalg.norm(xyz[:, None, :] - xyz[None, :, :], axis=2)
-    orders = [np.lexsort((np.arange(n), np.round(dist[a], 6))) for a in range(n)]
+    # per atom, all atoms by distance (ties within 1e-6 bohr by index), as _by_distance
+    orders = np.lexsort((np.broadcast_to(np.arange(n), (n, n)), np.round(dist, 6)), axis=-1)
     P = len(pr)
-    A = np.array([a for a, _ in pr])
-    B = np.array([b for _, b in pr])
-    neigh = -np.ones((P, N_NEIGH + 2), dtype=np.int64)
-    for p, (a, b) in enumerate(pr):
-        o = [int(i) for i in orders[a] if i != a and i != b][:N_NEIGH + 2]
-        neigh[p, :len(o)] = o
+    prs = np.asarray(pr, dtype=np.int64).reshape(P, 2)
+    A, B = prs[:, 0], prs[:, 1]
+    # the first N_NEIGH + 2 atoms of a's order other than a and b (-1 when the molecule has fewer)
+    O = orders[A]
+    keep = (O != A[:, None]) & (O != B[:, None])
+    sel = np.argsort(~keep, axis=1, kind="stable")[:, :N_NEIGH + 2]
+    neigh = np.where(np.take_along_axis(keep, sel, 1), np.take_along_axis(O, sel, 1), -1)
+    if neigh.shape[1] < N_NEIGH + 2:
+        neigh = np.pad(neigh, ((0, 0), (0, N_NEIGH + 2 - neigh.shape[1])), constant_values=-1)
     ra = xyz[A]
     same = A == B
     # frame: z along a->b (on site: toward the nearest neighbour), x toward the next reference atom
@@ -201,14 +225,16 @@ def frames_and_features(Z, xyz, pr):
     oh = lambda zz: np.stack([(zz == e).astype(np.float64) for e in ELEMENTS], axis=1)
     dab = dist[A, B]
     cols = [oh(Z[A]), oh(Z[B]), same[:, None].astype(np.float64), dab[:, None], np.exp(-dab)[:, None]]
-    for k in range(N_NEIGH):
-        i = neigh[:, k]
-        ok = (i >= 0)[:, None]
-        ii = np.maximum(i, 0)
-        di = dist[A, ii]
-        w = _cut(di)
-        loc = np.einsum("pji,pj->pi", Qs, xyz[ii] - ra) * w[:, None]
-        cols += [np.where(ok, loc, 0.0), np.where(ok, (w / (1.0 + di))[:, None], 0.0), np.where(ok, oh(Z[ii]), 0.0)]
+    # the N_NEIGH nearest others, all at once: (local position x cutoff weight, weight / (1 + d), element)
+    ii = neigh[:, :N_NEIGH]
+    ok = (ii >= 0)[:, :, None]
+    iic = np.maximum(ii, 0)
+    di = dist[A[:, None], iic]
+    w = _cut(di)
+    loc = np.matmul(xyz[iic] - ra[:, None, :], Qs) * w[:, :, None]
+    ohk = np.stack([(Z[iic] == e).astype(np.float64) for e in ELEMENTS], axis=2)
+    per = np.where(ok, np.concatenate([loc, (w / (1.0 + di))[:, :, None], ohk], axis=2), 0.0)
+    cols.append(per.reshape(P, -1))
     return Qs, np.concatenate(cols, axis=1).astype(np.float32)
 
 
@@ -273,18 +299,39 @@ def dataset(Z, xyz, basis, D):
 
 
 def _pair_rotations(types, pr, Qs):
-    """Per pair (a, b): the atom rotations of a and b in the pair's frame,
-    computed in one batch per distinct shell layout."""
-    Ua, Ub = [None] * len(pr), [None] * len(pr)
-    for side, out in ((0, Ua), (1, Ub)):
-        groups = {}
-        for p, ab in enumerate(pr):
-            groups.setdefault(tuple(types[ab[side]]), []).append(p)
-        for layout, idx in groups.items():
-            U = atom_rotations(list(layout), Qs[idx])
-            for k, p in enumerate(idx):
-                out[p] = U[k]
-    return Ua, Ub
+    """Per pair (a, b): the atom rotations of a and b in the pair's frame.
+    Each shell type's rotation is computed once for all frames, and each
+    distinct atom layout's block-diagonal matrices once from those."""
+    per_type = {t: shell_rotations(t, Qs) for t in sorted({t for ts in types for t in ts})}
+    by_layout = {}
+    for ts in {tuple(ts) for ts in types}:
+        blocks = [per_type[t] for t in ts]
+        n = sum(b.shape[1] for b in blocks)
+        U = np.zeros((len(Qs), n, n))
+        o = 0
+        for b in blocks:
+            k = b.shape[1]
+            U[:, o:o + k, o:o + k] = b
+            o += k
+        by_layout[ts] = U
+    keys_a = [tuple(types[a]) for a, _ in pr]
+    keys_b = [tuple(types[b]) for _, b in pr]
+    return _PairRotations(by_layout, keys_a), _PairRotations(by_layout, keys_b)
+
+
+class _PairRotations(list):
+    """Per-pair rotation matrices (a list, item p for pair p) that can also
+    gather the pairs of one layout at once: take(idx) -> (len(idx), n, n)."""
+
+    def __init__(self, by_layout, keys):
+        super().__init__(by_layout[k][p] for p, k in enumerate(keys))
+        self._by_layout, self._keys = by_layout, keys
+
+    def take(self, idx):
+        ks = {self._keys[p] for p in idx}
+        if len(ks) != 1:
+            return np.stack([self[p] for p in idx])
+        return self._by_layout[ks.pop()][idx]
 
 
 # ------------------------------------------------------------------ network
@@ -387,8 +434,8 @@ def assemble_blocks(pr, Y, Uas, Ubs, first, count, n):
     fa, fb = np.array([first[a] for a in A]), np.array([first[b] for b in B])
     for ca, cb in sorted(set(zip(ca_all.tolist(), cb_all.tolist()))):
         idx = np.nonzero((ca_all == ca) & (cb_all == cb))[0]
-        Ua = np.stack([Uas[p] for p in idx])
-        Ub = np.stack([Ubs[p] for p in idx])
+        Ua = Uas.take(idx) if hasattr(Uas, "take") else np.stack([Uas[p] for p in idx])
+        Ub = Ubs.take(idx) if hasattr(Ubs, "take") else np.stack([Ubs[p] for p in idx])
         blk = np.transpose(Ua, (0, 2, 1)) @ Y[idx, :ca, :cb].astype(np.float64) @ Ub
         rows = fa[idx][:, None] + np.arange(ca)
         cols = fb[idx][:, None] + np.arange(cb)
@@ -416,7 +463,7 @@ def predict_density(model, Z, xyz, basis, S, nocc, bf16=True, D_base=None, metri
     D = assemble_blocks(pr, Y, Uas, Ubs, first, count, n)
     D = 0.5 * (D + D.T)
     if model.residual:
-        D = D + (D_base.result() if hasattr(D_base, "result") else D_base)
+        D = D + D_base
     # purification: the projector onto the nocc most occupied natural orbitals
     # in the overlap metric -- by McWeeny iterations P <- 3P^2 - 2P^3 (GEMMs
     # only; the same projector when exactly nocc occupations exceed 1/2),
@@ -427,11 +474,11 @@ def predict_density(model, Z, xyz, basis, S, nocc, bf16=True, D_base=None, metri
         converged = False
         for _ in range(12):
             P2 = P @ P
-            if np.abs(P2 - P).max() < 1e-12:
+            if np.abs(P2 - P).max() < 1e-11:
                 converged = True
                 break
             P = 3.0 * P2 - 2.0 * (P2 @ P)
-        if converged and abs(np.trace(P) - nocc) < 1e-8:
+        if converged and abs(np.trace(P) - nocc) < 1e-7:
             P = 0.5 * (P + P.T)
             return 2.0 * (Xh @ P @ Xh)
         P = 0.5 * (Sh @ D @ Sh)
@@ -440,18 +487,6 @@ def predict_density(model, Z, xyz, basis, S, nocc, bf16=True, D_base=None, metri
     Co = Cn[:, :nocc]
     D = 2.0 * Co @ Co.T
     return (D, Cn) if return_orbitals else D
-
-
-_WORKER = None
-
-
-def _worker():
-    """One background thread for the guess's SAP base (created on first use)."""
-    global _WORKER
-    if _WORKER is None:
-        from concurrent.futures import ThreadPoolExecutor
-        _WORKER = ThreadPoolExecutor(max_workers=1, thread_name_prefix="sap-guess")
-    return _WORKER
 
 
 def guess_density(model, Z, xyz, ctx, bf16=True, precision="fp64", return_orbitals=False):
@@ -464,11 +499,7 @@ def guess_density(model, Z, xyz, ctx, bf16=True, precision="fp64", return_orbita
     metric = overlap_metric(ctx["S"], ctx)
     # tensor-core V_SAP only for a well-conditioned overlap (as the SCF's own SAP guess)
     prec = precision if ctx.get("S_min", 0.0) >= 1e-3 else "fp64"
-    # the SAP base (V_SAP on the GPU, then a host diagonalisation) on a worker
-    # thread while this one forms the pair features, runs the network and
-    # assembles the blocks (both release the interpreter lock in their
-    # library calls)
-    base = _worker().submit(sap_density, ctx["grid"], ctx["H"], ctx["S"], nocc, metric, prec) if model.residual else None
+    base = sap_density(ctx["grid"], ctx["H"], ctx["S"], nocc, metric, prec) if model.residual else None
     return predict_density(model, Z, xyz, ctx["basis"], ctx["S"], nocc, bf16=bf16, D_base=base, metric=metric,
                            return_orbitals=return_orbitals)
 
