@@ -578,9 +578,15 @@ def run_c18_mixed(args):
     g = cg.Grid(b, wl["grid"])
     g.setType(xc.type)
     g.getAO(0)
+    if args.v_operands:  # 1: operands split inside the kernels (as for batches whose planes do not fit)
+        g.set_mixed_config(v_operands=args.v_operands)
     D = model_density(b.nbasis, wl["nocc"])
     for _ in range(args.warmup):
         g.build(xc, [D], precision=cg.PRECISION_MIXED)
+    g.profile(True)
+    g.build(xc, [D], precision=cg.PRECISION_MIXED)
+    kms = g.kernel_ms()
+    g.profile(False)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.steps):
@@ -590,7 +596,9 @@ def run_c18_mixed(args):
                       "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
                       "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                       "dtype": "bf16x3 (split) + f64 accumulation", "data": "synthetic",
-                      "config": {"workload": wl["name"], "E_xc": E}}), flush=True)
+                      "config": {"workload": wl["name"], "E_xc": E, "v_operands": args.v_operands,
+                                 "kernel_ms": dict(zip(("density", "functional", "energy", "v_operand",
+                                                        "v_partials", "v_reduction"), kms))}}), flush=True)
 
 
 C18_SCF_METRIC = "SCF wall time to 1e-8 Eh, C18 RKS B3LYP/def2-TZVP SG-2, mixed vs plain FP64 XC"
@@ -859,6 +867,8 @@ def main():
     ap.add_argument("--fp64-mols", type=int, default=0, help="alkanes64: molecules checked in FP64 (0 = all)")
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--no-scf", action="store_true", help="c18: leave out the SCF and learned-guess results")
+    ap.add_argument("--v-operands", type=int, default=0, choices=[0, 1, 2],
+                    help="c18-mixed: operand form of the tensor-core kernels (0 by free memory, 1 split in-kernel, 2 pre-split)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -454,7 +454,7 @@ __global__ void __launch_bounds__(kThreads, 1) density_tc_kernel(const __grid_co
                     v[f] = tc::lds32f(rf + (f * 128 + ct) * 4);
                     mx = fmaxf(mx, fabsf(v[f]));
                 }
-                e = tc::fixed_exponent((double)mx);
+                e = tc::fixed_exponent_f(mx);
             }
             warp_arrive(&sm.rempty[0]);
             const int s = uu & 1;
@@ -1110,7 +1110,7 @@ __global__ void __launch_bounds__(128) split_store_fixed_kernel(const float* __r
     const float* src = e32 + (size_t)c * n + (size_t)sl * 64 * 128 + g;
     float mx = 0.f;
     for (int f = 0; f < 64; f++) mx = fmaxf(mx, fabsf(src[(size_t)f * 128]));
-    const int e = tc::fixed_exponent((double)mx);
+    const int e = tc::fixed_exponent_f(mx);
     bf16* dst = e16d + (size_t)(c * 3) * n + (size_t)sl * 64 * 128 + g;
     for (int f = 0; f < 64; f++) {
         bf16 h, m, l;

@@ -273,24 +273,52 @@ __device__ __forceinline__ void split3_fixed(double x, int e, __nv_bfloat16& h, 
 // 2^k as a float for -126 <= k <= 127.
 __device__ __forceinline__ float pow2f(int k) { return __int_as_float((127 + k) << 23); }
 
+// fixed_exponent of a float group maximum from its bits (no FP64): the same
+// value as ilogb for every float >= 2^-100.
+__device__ __forceinline__ int fixed_exponent_f(float maxabs) {
+    return maxabs >= 0x1p-100f ? (int)((__float_as_uint(maxabs) >> 23) & 0xffu) - 127 : kFixedZero;
+}
+
+// x rounded to the nearest integer, ties to even (as rintf), for |x| < 2^22:
+// adding and removing 1.5 * 2^23 on the FMA pipe (rintf runs on the
+// eight-times-slower conversion pipe).
+__device__ __forceinline__ float round_small(float x) {
+    const float big = 12582912.f;  // 1.5 * 2^23
+    return __fsub_rn(__fadd_rn(x, big), big);
+}
+
+// The BF16 of a float whose low 16 significand bits are zero (exact: the top
+// half of its bits), without a conversion instruction.
+__device__ __forceinline__ __nv_bfloat16 bf16_exact(float x) {
+    return __ushort_as_bfloat16((unsigned short)(__float_as_uint(x) >> 16));
+}
+
 // split3_fixed for a float x, in float arithmetic: every step is exact (scaling
 // by powers of two within the normal range, rounding to an integer, exact
-// differences), so it gives the same slices as the double version.  Needs
-// -100 <= e <= 103 or e == kFixedZero (fixed_exponent of a float group).
+// differences), so it gives the same slices as the double version.  The
+// scaled values are below 2^8 in magnitude, so round_small rounds them, and
+// each slice has at most 8 significant bits, so bf16_exact converts it.
+// Needs -100 <= e <= 103 or e == kFixedZero (fixed_exponent of a float group).
 __device__ __forceinline__ void split3_fixed_f(float x, int e, __nv_bfloat16& h, __nv_bfloat16& m,
                                                __nv_bfloat16& l) {
     if (e == kFixedZero) {
         h = m = l = __float2bfloat16_rn(0.f);
         return;
     }
-    const float a = rintf(x * pow2f(7 - e)) * pow2f(e - 7);
-    const float r1 = x - a;
-    const float b = rintf(r1 * pow2f(15 - e)) * pow2f(e - 15);
-    const float r2 = r1 - b;
-    const float c = rintf(r2 * pow2f(23 - e)) * pow2f(e - 23);
-    h = __float2bfloat16_rn(a);
-    m = __float2bfloat16_rn(b);
-    l = __float2bfloat16_rn(c);
+    // slice = round_small(v * 2^k) * 2^-k as two exact FMAs: t = v 2^k + B
+    // rounds the (exact) scaled value to an integer offset by B = 1.5 * 2^23,
+    // and t 2^-k - B 2^-k is that integer times 2^-k, exactly representable
+    const float big = 12582912.f;
+    const float s1 = pow2f(7 - e), s2 = pow2f(15 - e), s3 = pow2f(23 - e);
+    const float i1 = pow2f(e - 7), i2 = pow2f(e - 15), i3 = pow2f(e - 23);
+    const float a = __fmaf_rn(__fmaf_rn(x, s1, big), i1, -big * i1);
+    const float r1 = __fsub_rn(x, a);
+    const float b = __fmaf_rn(__fmaf_rn(r1, s2, big), i2, -big * i2);
+    const float r2 = __fsub_rn(r1, b);
+    const float c = __fmaf_rn(__fmaf_rn(r2, s3, big), i3, -big * i3);
+    h = bf16_exact(a);
+    m = bf16_exact(b);
+    l = bf16_exact(c);
 }
 
 }  // namespace tc
