@@ -178,16 +178,7 @@ __device__ __forceinline__ void store_chunk(uint32_t planes, int r, int j, const
 __device__ __forceinline__ void store_chunk_fixed(uint32_t planes, int r, int j, const float* v, int e) {
     uint32_t hh[4], mm[4], ll[4];
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
-        bf16 h0, m0, l0, h1, m1, l1;
-        tc::split3_fixed_f(v[2 * k], e, h0, m0, l0);
-        tc::split3_fixed_f(v[2 * k + 1], e, h1, m1, l1);
-        const __nv_bfloat162 H = __halves2bfloat162(h0, h1), Mv = __halves2bfloat162(m0, m1),
-                             Lv = __halves2bfloat162(l0, l1);
-        hh[k] = *reinterpret_cast<const uint32_t*>(&H);
-        mm[k] = *reinterpret_cast<const uint32_t*>(&Mv);
-        ll[k] = *reinterpret_cast<const uint32_t*>(&Lv);
-    }
+    for (int k = 0; k < 4; k++) tc::split3_fixed_f2(make_float2(v[2 * k], v[2 * k + 1]), e, hh[k], mm[k], ll[k]);
     const uint32_t off = (uint32_t)r * 128u + ((uint32_t)(j ^ (r & 7)) << 4);
     tc::sts128(planes + off, make_uint4(hh[0], hh[1], hh[2], hh[3]));
     tc::sts128(planes + kPlaneA + off, make_uint4(mm[0], mm[1], mm[2], mm[3]));
