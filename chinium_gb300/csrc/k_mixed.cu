@@ -141,18 +141,19 @@ __device__ __forceinline__ void conv_publish(uint64_t* full) {
     warp_arrive(full);
 }
 
-// Three-term split of 8 consecutive K-elements into one 16-byte chunk per plane.
+// Three-term split of 8 consecutive K-elements into one 16-byte chunk per plane
+// (round to nearest at each term; the residuals in packed FP32x2 arithmetic).
 __device__ __forceinline__ void split8(const float* v, uint4& h, uint4& m, uint4& l) {
     uint32_t hh[4], mm[4], ll[4];
+    const float2 neg1 = make_float2(-1.f, -1.f);
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-        const float a = v[2 * k], b = v[2 * k + 1];
-        const __nv_bfloat162 H = __floats2bfloat162_rn(a, b);
-        const float2 Hf = __bfloat1622float2(H);
-        const float ra = a - Hf.x, rb = b - Hf.y;
-        const __nv_bfloat162 Mv = __floats2bfloat162_rn(ra, rb);
-        const float2 Mf = __bfloat1622float2(Mv);
-        const __nv_bfloat162 Lv = __floats2bfloat162_rn(ra - Mf.x, rb - Mf.y);
+        const float2 a = make_float2(v[2 * k], v[2 * k + 1]);
+        const __nv_bfloat162 H = __floats2bfloat162_rn(a.x, a.y);
+        const float2 r = __ffma2_rn(__bfloat1622float2(H), neg1, a);  // a - H, exact
+        const __nv_bfloat162 Mv = __floats2bfloat162_rn(r.x, r.y);
+        const float2 r2 = __ffma2_rn(__bfloat1622float2(Mv), neg1, r);
+        const __nv_bfloat162 Lv = __floats2bfloat162_rn(r2.x, r2.y);
         hh[k] = *reinterpret_cast<const uint32_t*>(&H);
         mm[k] = *reinterpret_cast<const uint32_t*>(&Mv);
         ll[k] = *reinterpret_cast<const uint32_t*>(&Lv);
