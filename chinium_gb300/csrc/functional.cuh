@@ -32,6 +32,71 @@ namespace xcf {
 #define CGB_HDN __host__ __device__ __noinline__
 #endif
 
+// ------------------------------------------------------------ float-float
+// ff: a value held as hi + lo, two floats with |lo| <= ulp(hi) / 2 (48-bit
+// significand), so FP64-level arithmetic runs on the FP32 pipe (64x GB300's
+// FP64 rate).  The error-free transformations are Knuth's TwoSum, Dekker's
+// Fast2Sum and the FMA product, combined as in the QD library (Hida, Li and
+// Bailey 2001): accurate addition, multiplication, long division.  Used for
+// the mixed path's FP64-level energy density.
+struct ff {
+    float hi, lo;
+    CGB_HD ff() : hi(0.f), lo(0.f) {}
+    CGB_HD ff(float h, float l) : hi(h), lo(l) {}
+    CGB_HD ff(double x) : hi((float)x), lo((float)(x - (double)(float)x)) {}
+    CGB_HD ff(int x) : ff((double)x) {}
+};
+CGB_HD void ff_two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+CGB_HD void ff_fast_two_sum(float a, float b, float& s, float& e) {  // |a| >= |b|
+    s = a + b;
+    e = b - (s - a);
+}
+CGB_HD ff operator+(ff a, ff b) {
+    float s, e, t, f;
+    ff_two_sum(a.hi, b.hi, s, e);
+    ff_two_sum(a.lo, b.lo, t, f);
+    e += t;
+    ff_fast_two_sum(s, e, s, e);
+    e += f;
+    ff_fast_two_sum(s, e, s, e);
+    return ff(s, e);
+}
+CGB_HD ff operator-(ff a) { return ff(-a.hi, -a.lo); }
+CGB_HD ff operator-(ff a, ff b) { return a + (-b); }
+CGB_HD ff operator*(ff a, ff b) {
+    const float p = a.hi * b.hi;
+    float e = fmaf(a.hi, b.hi, -p);  // the product's rounding error, exactly
+    e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e));
+    float s;
+    ff_fast_two_sum(p, e, s, e);
+    return ff(s, e);
+}
+CGB_HD ff operator/(ff a, ff b) {
+    const float q1 = a.hi / b.hi;
+    ff r = a - b * ff(q1, 0.f);
+    const float q2 = r.hi / b.hi;
+    r = r - b * ff(q2, 0.f);
+    const float q3 = r.hi / b.hi;
+    float s, e;
+    ff_fast_two_sum(q1, q2, s, e);
+    return ff(s, e) + ff(q3, 0.f);
+}
+CGB_HD ff& operator+=(ff& a, ff b) { return a = a + b; }
+CGB_HD ff& operator-=(ff& a, ff b) { return a = a - b; }
+CGB_HD ff& operator*=(ff& a, ff b) { return a = a * b; }
+CGB_HD ff& operator/=(ff& a, ff b) { return a = a / b; }
+CGB_HD bool operator<(ff a, ff b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+CGB_HD bool operator>(ff a, ff b) { return b < a; }
+CGB_HD bool operator<=(ff a, ff b) { return !(b < a); }
+CGB_HD bool operator>=(ff a, ff b) { return !(a < b); }
+CGB_HD double ff_value(ff a) { return (double)a.hi + (double)a.lo; }
+// x 2^k, exact (both parts scaled).
+CGB_HD ff ff_ldexp(ff a, int k) { return ff(ldexpf(a.hi, k), ldexpf(a.lo, k)); }
+
 template <class R, int N>
 struct Dual {
     R v;
@@ -62,6 +127,53 @@ struct Scal<float> {
     static CGB_HD float cbrt_(float x) { return ::cbrtf(x); }
     static CGB_HD float atan_(float x) { return ::atanf(x); }
     static CGB_HD float asinh_(float x) { return ::asinhf(x); }
+};
+
+// Elementary functions in float-float, each from the FP32 function's value by
+// one Newton step (quadratic: 2^-23 -> ~2^-46) or, for exp, by argument
+// reduction: exp(a) = 2^k (1 + s)^(2^9) with r = a - k ln2, s = expm1(r / 512)
+// from its Taylor series, then s <- s (s + 2) nine times (the QD library's
+// method; squaring 1 + s in that form keeps the small part's relative
+// accuracy).  atan and asinh (VWN's and Becke 88's) go through FP64.
+template <>
+struct Scal<ff> {
+    static CGB_HD ff exp_(ff a) {
+        if (a.hi > 88.f) return ff(INFINITY, 0.f);
+        if (a.hi < -87.f) return ff(0.f, 0.f);
+        // r = a - k ln2 with ln2 = c1 + c2 (Cody and Waite): c1 has 16 significant
+        // bits, so k c1 (|k| <= 127) is exact in one float; c2 is the rest in ff
+        const float k = rintf(a.hi * 1.44269504f);
+        const float c1 = 0.693145751953125f;
+        const ff c2(1.4286068203094172321214581765680755e-06);
+        const ff r = ff_ldexp((a - ff(k * c1, 0.f)) - ff(k, 0.f) * c2, -9);
+        // expm1(r) for |r| <= ln2 / 1024: r + r^2/2 + ... + r^6/720 (next term < 2^-80)
+        ff s = r * (ff(1.0) + r * (ff(0.5) + r * (ff(1.0 / 6.0) + r * (ff(1.0 / 24.0) +
+                     r * (ff(1.0 / 120.0) + r * ff(1.0 / 720.0))))));
+        for (int i = 0; i < 9; i++) s = s * (s + ff(2.0));
+        return ff_ldexp(ff(1.0) + s, (int)k);
+    }
+    static CGB_HD ff log_(ff a) {
+        // Newton on exp: x1 = x0 + a exp(-x0) - 1
+        const float x0 = logf(a.hi);
+        return ff(x0, 0.f) + a * exp_(ff(-x0, 0.f)) - ff(1.0);
+    }
+    static CGB_HD ff sqrt_(ff a) {
+        if (!(a.hi > 0.f)) return ff(0.f, 0.f);
+        const float x = sqrtf(a.hi);
+        const ff X(x, 0.f);
+        const ff r = a - X * X;
+        return X + ff(r.hi * (0.5f / x), 0.f);
+    }
+    static CGB_HD ff cbrt_(ff a) {
+        if (a.hi == 0.f) return ff(0.f, 0.f);
+        const float x = cbrtf(a.hi);
+        const ff X(x, 0.f);
+        const ff r = a - X * X * X;
+        return X + ff(r.hi / (3.f * x * x), 0.f);
+    }
+    static CGB_HD ff atan_(ff a) { return ff(::atan(ff_value(a))); }
+    static CGB_HD ff asinh_(ff a) { return ff(::asinh(ff_value(a))); }
+    static CGB_HD ff pow_(ff a, ff p) { return ff(::pow(ff_value(a), ff_value(p))); }
 };
 
 // value / derivative-propagation primitives

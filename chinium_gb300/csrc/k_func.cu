@@ -39,10 +39,11 @@ __device__ double cta_sum(double v) {
 
 // MODE 1: only the points whose total density is >= float_above: the
 // potentials in FP32 (forward-mode derivatives of the FP32 expression) and
-// the energy density eps in FP64 (the value alone) -- float constants and
-// float k/3 exponents shift an FP32 eps systematically by 1e-8..1e-7
-// relative, which E_xc = sum w rho eps would accumulate, while V takes
-// FP32-level errors;
+// the energy density eps at FP64 level (the value alone, in float-float
+// arithmetic on the FP32 pipe; in FP64 at a point where that overflows
+// FP32's range) -- float constants and float k/3 exponents shift an FP32 eps
+// systematically by 1e-8..1e-7 relative, which E_xc = sum w rho eps would
+// accumulate, while V takes FP32-level errors;
 // MODE 2: only the others, in FP64 (float_above = +inf: every point).  The
 // mixed path runs both launches (separate kernels: each gets the registers
 // and occupancy of its own precision); accumulate adds the CTA's energy
@@ -81,7 +82,12 @@ __global__ void __launch_bounds__(kThreads) functional_kernel(xcf::FuncDesc f, l
             if (MODE == 1) {  // mixed path: FP32 potentials, FP64 eps, above the low-density bound
                 float ef, df[3] = {0, 0, 0};
                 xcf::eval_unpol<float, FAM>(f, (float)r, (float)s, (float)t, ef, df);
-                xcf::eval_unpol_value<double, FAM>(f, r, s, t, e);
+                // the energy density in float-float (FP64-level, on the FP32 pipe);
+                // FP64 where an intermediate left FP32's exponent range
+                xcf::ff eff;
+                xcf::eval_unpol_value<xcf::ff, FAM>(f, xcf::ff(r), xcf::ff(s), xcf::ff(t), eff);
+                e = xcf::ff_value(eff);
+                if (!isfinite(e)) xcf::eval_unpol_value<double, FAM>(f, r, s, t, e);
                 for (int i = 0; i < 3; i++) dv[i] = df[i];
             } else {
                 xcf::eval_unpol<double, FAM>(f, r, s, t, e, dv);
@@ -122,7 +128,11 @@ __global__ void __launch_bounds__(kThreads) functional_kernel(xcf::FuncDesc f, l
                 float inf_[7], ef, df[7] = {0, 0, 0, 0, 0, 0, 0};
                 for (int i = 0; i < 7; i++) inf_[i] = (float)in[i];
                 xcf::eval_pol<float, FAM>(f, inf_, ef, df);
-                xcf::eval_pol_value<double, FAM>(f, in, e);
+                xcf::ff inff[7], eff;
+                for (int i = 0; i < 7; i++) inff[i] = xcf::ff(in[i]);
+                xcf::eval_pol_value<xcf::ff, FAM>(f, inff, eff);
+                e = xcf::ff_value(eff);
+                if (!isfinite(e)) xcf::eval_pol_value<double, FAM>(f, in, e);
                 for (int i = 0; i < 7; i++) dv[i] = df[i];
             } else {
                 xcf::eval_pol<double, FAM>(f, in, e, dv);
