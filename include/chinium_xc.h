@@ -321,8 +321,9 @@ int xc_build_response(xc_grid* g, xc_functional* f, const double* D, int nspin, 
  * the functional and E_xc are FP64 on the reconstructed densities.  The
  * tensor-core error is relative to the change since the previous call, so it
  * vanishes as an SCF converges.  anchor resets the references: 1 (or the
- * first call on a grid with anchor 0) by a full FP64 build; 2 by FP64
- * densities, functional and E_xc with V on the tensor cores (about half the
+ * first call on a grid with anchor 0) by a full FP64 build; 2 by densities
+ * at FP64 level (float-float arithmetic on the FP32 pipe, ~1e-14 relative),
+ * the FP64 functional and E_xc, with V on the tensor cores (a fraction of the
  * cost: an error in V moves a converged SCF energy only at second order,
  * while E_xc takes the density's error at first order); 3 by a full
  * tensor-core build (as xc_build with XC_PRECISION_MIXED: the densities'
