@@ -130,11 +130,14 @@ struct Scal<float> {
 };
 
 // Elementary functions in float-float, each from the FP32 function's value by
-// one Newton step (quadratic: 2^-23 -> ~2^-46) or, for exp, by argument
-// reduction: exp(a) = 2^k (1 + s)^(2^9) with r = a - k ln2, s = expm1(r / 512)
-// from its Taylor series, then s <- s (s + 2) nine times (the QD library's
-// method; squaring 1 + s in that form keeps the small part's relative
-// accuracy).  atan and asinh (VWN's and Becke 88's) go through FP64.
+// one Newton step (quadratic: 2^-23 -> ~2^-46; log after reducing its
+// argument to [1/sqrt 2, sqrt 2)) or, for exp, by argument reduction:
+// exp(a) = 2^k (1 + s)^(2^9) with r = a - k ln2, s = expm1(r / 512) from its
+// Taylor series, then s <- s (s + 2) nine times (the QD library's method;
+// squaring 1 + s in that form keeps the small part's relative accuracy).
+// atan and asinh (VWN's and Becke 88's) go through FP64.  Accuracy ~1e-14
+// relative while results stay well inside FP32's range (lo is a normal float
+// down to |hi| ~ 1e-31: exp arguments above about -70).
 template <>
 struct Scal<ff> {
     static CGB_HD ff exp_(ff a) {
@@ -153,9 +156,17 @@ struct Scal<ff> {
         return ff_ldexp(ff(1.0) + s, (int)k);
     }
     static CGB_HD ff log_(ff a) {
-        // Newton on exp: x1 = x0 + a exp(-x0) - 1
-        const float x0 = logf(a.hi);
-        return ff(x0, 0.f) + a * exp_(ff(-x0, 0.f)) - ff(1.0);
+        // a = m 2^e with m in [1/sqrt 2, sqrt 2): log a = e ln2 + log m, and log m
+        // by one Newton step on exp from logf(m) (error ~ (2^-24 |log m|)^2 / 2)
+        int e;
+        const float f = frexpf(a.hi, &e);  // a.hi = f 2^e, f in [1/2, 1)
+        if (f < 0.70710678f) e -= 1;
+        const ff m = ff_ldexp(a, -e);
+        const float x0 = logf(m.hi);
+        const ff lm = ff(x0, 0.f) + m * exp_(ff(-x0, 0.f)) - ff(1.0);
+        const float c1 = 0.693145751953125f;  // ln2 = c1 + c2 as in exp_ (e c1 exact)
+        const ff c2(1.4286068203094172321214581765680755e-06);
+        return (ff((float)e * c1, 0.f) + ff((float)e, 0.f) * c2) + lm;
     }
     static CGB_HD ff sqrt_(ff a) {
         if (!(a.hi > 0.f)) return ff(0.f, 0.f);
