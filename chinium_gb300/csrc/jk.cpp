@@ -51,7 +51,16 @@ struct JkEngine {
                                               // in 8-byte elements); results (FP64)
     DevBuf<double> d_ints;                    // in-core integrals, or the direct-mode chunk buffer
     DevBuf<double> d_D, d_rawJ, d_rawK, d_J, d_K;
+    // in-core exchange by bra-pair chunks (launch_jk_slab): chunks grouped by
+    // the bra pair's na + nb, largest first
+    DevBuf<longlong2> d_chunks;
+    std::vector<int> cls_rows;
+    std::vector<long long> cls_c0;
     int nmat_alloc = 0;
+    bool slab_fits(int nmat) const {
+        return !cls_rows.empty() && jk_slab_bytes(cls_rows[0], n, nmat) <= kJkSlabMaxBytes;
+    }
+    void make_chunks(const std::vector<int2>& quart);
     EriDev dev() const { return EriDev{d_pairs.p, d_pp_p.p, d_pp_P.p, d_ep.p, d_boys.p}; }
     void setup(const BasisSet& b, double thr, double max_bytes);
     void build_device(int nmat, const double* dD, double* dJ, double* dK);
@@ -59,6 +68,7 @@ struct JkEngine {
 
 namespace {
 constexpr double kPrimCut = 1e-20;
+constexpr long long kSlabChunk = 2048;  // quartets per exchange chunk at most
 
 inline int nfunc_of(const Shell& s) { return shell_size(s.type); }
 }  // namespace
@@ -186,13 +196,16 @@ void JkEngine::setup(const BasisSet& b, double thr, double max_bytes) {
         npair += npair & 1;  // even row stride (16-byte rows for the GEMV)
         CGB_CUDA(cudaStreamSynchronize(stream));
         CGB_CUDA(cudaMemGetInfo(&freeb, &totalb));
-        dense_j = (double)npair * npair * sizeof(double) <= 0.25 * (double)freeb;
+        // (and the operator plus the integrals within the caller's budget)
+        const double mbytes = (double)npair * npair * sizeof(double);
+        dense_j = mbytes <= 0.25 * (double)freeb && (double)nints * sizeof(double) + mbytes <= budget;
         if (dense_j) {
             d_M.alloc((size_t)npair * npair);
             d_M.zero(stream);
             launch_coulomb_scatter(dev(), d_quartets.p, d_off.p, nquartets, d_ints.p, npair, d_M.p, stream);
             launch_coulomb_split((long long)npair * npair, d_M.p, stream);
         }
+        make_chunks(quart);
         CGB_CUDA(cudaStreamSynchronize(stream));
     } else {
         // chunks of consecutive quartets whose blocks fit in the chunk buffer
@@ -212,6 +225,34 @@ void JkEngine::setup(const BasisSet& b, double thr, double max_bytes) {
         chunk_ints = cap;
         d_ints.alloc(cap);
     }
+}
+
+void JkEngine::make_chunks(const std::vector<int2>& quart) {
+    // the quartets of a bra pair are consecutive (bra-major list); runs of at
+    // most kSlabChunk of them, grouped by the bra pair's na + nb
+    std::vector<std::vector<longlong2>> by_rows(2 * (2 * kEriMaxL + 1) + 1);
+    const long long nq = (long long)quart.size();
+    for (long long q = 0; q < nq;) {
+        const int i = quart[q].x;
+        long long e = q;
+        while (e < nq && quart[e].x == i) e++;
+        const int rows = pairs[i].na + pairs[i].nb;
+        for (long long c = q; c < e; c += kSlabChunk)
+            by_rows[rows].push_back(make_longlong2(c, std::min(e, c + kSlabChunk)));
+        q = e;
+    }
+    std::vector<longlong2> all;
+    cls_rows.clear();
+    cls_c0.clear();
+    for (int rows = (int)by_rows.size() - 1; rows >= 0; rows--) {
+        if (by_rows[rows].empty()) continue;
+        cls_rows.push_back(rows);
+        cls_c0.push_back((long long)all.size());
+        all.insert(all.end(), by_rows[rows].begin(), by_rows[rows].end());
+    }
+    cls_c0.push_back((long long)all.size());
+    d_chunks.upload(all.data(), all.size(), stream);
+    CGB_CUDA(cudaStreamSynchronize(stream));
 }
 
 void JkEngine::build_device(int nmat, const double* dD, double* dJ, double* dK) {
@@ -236,13 +277,19 @@ void JkEngine::build_device(int nmat, const double* dD, double* dJ, double* dK) 
             }
             launch_coulomb_dense(n, nmat, npair, d_M.p, dD, d_x.p, d_y.p, dJ, stream);
         }
-        if (rK)
+        if (rK && slab_fits(nmat))
+            launch_jk_slab(dev(), d_quartets.p, d_off.p, d_chunks.p, cls_rows, cls_c0, d_ints.p, n, nmat, dD, nullptr,
+                           rK, stream);
+        else if (rK)
             launch_jk_contract(dev(), d_quartets.p, d_off.p, 0, nquartets, 0, d_ints.p, n, nmat, dD, nullptr, rK,
                                stream);
         launch_jk_symmetrise(n, nmat, nullptr, rK, nullptr, dK, stream);
         return;
     }
-    if (incore) {
+    if (incore && rK && slab_fits(nmat)) {
+        launch_jk_slab(dev(), d_quartets.p, d_off.p, d_chunks.p, cls_rows, cls_c0, d_ints.p, n, nmat, dD, rJ, rK,
+                       stream);
+    } else if (incore) {
         launch_jk_contract(dev(), d_quartets.p, d_off.p, 0, nquartets, 0, d_ints.p, n, nmat, dD, rJ, rK, stream);
     } else {
         for (size_t c = 0; c + 1 < chunk_q.size(); c++) {

@@ -262,6 +262,129 @@ __global__ void __launch_bounds__(32 * kJkWarps) jk_contract_kernel(EriDev e, co
     }
 }
 
+// Exchange by bra pair (in-core list).  The quartets of one bra pair
+// P = (a, b) are consecutive in the list, and every exchange element they
+// feed lies in a row of shell a or of shell b: K(a, c), K(a, d), K(b, c),
+// K(b, d).  A CTA takes one run of them (a chunk), adds its K contributions
+// into a shared-memory slab of those na + nb rows x n columns (per matrix)
+// and its J(a, b) contributions into a small shared buffer, and adds both to
+// the raw accumulators once at the end: one FP64 global atomic per touched
+// slab element instead of one per element and quartet.  The J(c, d)
+// contributions (a different ket pair per quartet) stay global atomics.
+// Warps take the chunk's quartets in turn, lanes the sub-block elements, as
+// in jk_contract_kernel.  Shared layout: nmat x kNf^2 J(a, b) entries, then
+// nmat x rows x n slab entries (rows = na + nb <= rows_cap, the launch's
+// size).
+template <bool kJ>
+__global__ void __launch_bounds__(32 * kJkWarps) jk_slab_kernel(EriDev e, const int2* __restrict__ quartets,
+                                                                const long long* __restrict__ out_off,
+                                                                const longlong2* __restrict__ chunks, int rows_cap,
+                                                                const double* __restrict__ ints, int n, int nmat,
+                                                                const double* __restrict__ D,
+                                                                double* __restrict__ rawJ,
+                                                                double* __restrict__ rawK) {
+    extern __shared__ double sm_slab[];
+    const longlong2 ch = chunks[blockIdx.x];
+    const int2 pq0 = quartets[ch.x];
+    const EriPair P = e.pairs[pq0.x];
+    const int na = P.na, nb = P.nb, sa = P.fa, sb = P.fb, rows = na + nb;
+    if (rows > rows_cap) return;  // chunks are grouped by rows on the host; never taken
+    const int slab = rows * n;
+    const size_t nn = (size_t)n * n;
+    double* __restrict__ j1 = sm_slab;                        // [m][ia * nb + ib]
+    double* __restrict__ ks = sm_slab + (size_t)nmat * kNf * kNf;  // [m][row][col]
+    for (int t = threadIdx.x; t < nmat * (kNf * kNf + slab); t += blockDim.x) sm_slab[t] = 0.0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const double fab = sa == sb ? 0.5 : 1.0;
+    const int nJ1 = na * nb;
+    for (long long q = ch.x + (threadIdx.x >> 5); q < ch.y; q += kJkWarps) {
+        const int2 pq = quartets[q];
+        const EriPair Q = e.pairs[pq.y];
+        const int nc = Q.na, nd = Q.nb, sc = Q.fa, sd = Q.fb;
+        const double* __restrict__ blk = ints + out_off[q];
+        double f = fab;
+        if (sc == sd) f *= 0.5;
+        if (pq.x == pq.y) f *= 0.5;
+        const int nJ2 = nc * nd, nK1 = na * nc, nK2 = nb * nd, nK3 = na * nd;
+        const int nJ = kJ ? nJ1 + nJ2 : 0;
+        const int tot = nJ + nK1 + nK2 + nK3 + nb * nc;
+        const int sab = nb * nc * nd, sbb = nc * nd;  // strides of ia, ib in the block
+        for (int m = 0; m < nmat; m++) {
+            const double* __restrict__ Dm = D + m * nn;
+            double* __restrict__ km = ks + (size_t)m * slab;
+            for (int k = lane; k < tot; k += 32) {
+                double acc = 0.0;
+                double* dst;
+                if (k < nJ && k < nJ1) {  // J(a, b) += f sum_cd I D(c, d): shared
+                    const int ia = k / nb, ib = k - ia * nb;
+                    const double* bl = blk + ia * sab + ib * sbb;
+                    for (int ic = 0; ic < nc; ic++)
+                        for (int id = 0; id < nd; id++)
+                            acc = fma(__ldg(bl + ic * nd + id), __ldg(Dm + (size_t)(sc + ic) * n + sd + id), acc);
+                    dst = j1 + m * kNf * kNf + k;
+                } else if (k < nJ) {  // J(c, d) += f sum_ab I D(a, b): global
+                    const int r = k - nJ1, ic = r / nd, id = r - ic * nd;
+                    const double* bl = blk + ic * nd + id;
+                    for (int ia = 0; ia < na; ia++)
+                        for (int ib = 0; ib < nb; ib++)
+                            acc = fma(__ldg(bl + ia * sab + ib * sbb), __ldg(Dm + (size_t)(sa + ia) * n + sb + ib), acc);
+                    dst = rawJ + m * nn + (size_t)(sc + ic) * n + sd + id;
+                } else {
+                    int r = k - nJ;
+                    if (r < nK1) {  // K(a, c) += f sum_bd I D(b, d): slab row ia
+                        const int ia = r / nc, ic = r - ia * nc;
+                        for (int ib = 0; ib < nb; ib++)
+                            for (int id = 0; id < nd; id++)
+                                acc = fma(__ldg(blk + ia * sab + ib * sbb + ic * nd + id),
+                                          __ldg(Dm + (size_t)(sb + ib) * n + sd + id), acc);
+                        dst = km + ia * n + sc + ic;
+                    } else if ((r -= nK1) < nK2) {  // K(b, d) += f sum_ac I D(a, c): slab row na + ib
+                        const int ib = r / nd, id = r - ib * nd;
+                        for (int ia = 0; ia < na; ia++)
+                            for (int ic = 0; ic < nc; ic++)
+                                acc = fma(__ldg(blk + ia * sab + ib * sbb + ic * nd + id),
+                                          __ldg(Dm + (size_t)(sa + ia) * n + sc + ic), acc);
+                        dst = km + (na + ib) * n + sd + id;
+                    } else if ((r -= nK2) < nK3) {  // K(a, d) += f sum_bc I D(b, c): slab row ia
+                        const int ia = r / nd, id = r - ia * nd;
+                        for (int ib = 0; ib < nb; ib++)
+                            for (int ic = 0; ic < nc; ic++)
+                                acc = fma(__ldg(blk + ia * sab + ib * sbb + ic * nd + id),
+                                          __ldg(Dm + (size_t)(sb + ib) * n + sc + ic), acc);
+                        dst = km + ia * n + sd + id;
+                    } else {  // K(b, c) += f sum_ad I D(a, d): slab row na + ib
+                        r -= nK3;
+                        const int ib = r / nc, ic = r - ib * nc;
+                        for (int ia = 0; ia < na; ia++)
+                            for (int id = 0; id < nd; id++)
+                                acc = fma(__ldg(blk + ia * sab + ib * sbb + ic * nd + id),
+                                          __ldg(Dm + (size_t)(sa + ia) * n + sd + id), acc);
+                        dst = km + (na + ib) * n + sc + ic;
+                    }
+                }
+                atomicAdd(dst, f * acc);
+            }
+        }
+    }
+    __syncthreads();
+    // slab row r < na is function sa + r, row na + r' is function sb + r'
+    for (int t = threadIdx.x; t < nmat * slab; t += blockDim.x) {
+        const double v = ks[t];
+        if (v == 0.0) continue;  // columns no ket of the chunk touched
+        const int m = t / slab, r = t - m * slab, row = r / n, col = r - row * n;
+        const int fn = row < na ? sa + row : sb + (row - na);
+        atomicAdd(rawK + m * nn + (size_t)fn * n + col, v);
+    }
+    if (kJ) {
+        for (int t = threadIdx.x; t < nmat * nJ1; t += blockDim.x) {
+            const int m = t / nJ1, r = t - m * nJ1, ia = r / nb, ib = r - ia * nb;
+            const double v = j1[m * kNf * kNf + r];
+            if (v != 0.0) atomicAdd(rawJ + m * nn + (size_t)(sa + ia) * n + sb + ib, v);
+        }
+    }
+}
+
 // Dense Coulomb operator of small molecules: M[(mu nu), (la si)] =
 // (mu nu|la si) over packed pairs mu >= nu (p = mu (mu + 1) / 2 + nu), filled
 // once from the in-core quartet blocks (warp per quartet, both (P, Q) and
@@ -416,6 +539,10 @@ __global__ void jk_symmetrise_kernel(int n, int nmat, const double* __restrict__
 
 void set_eri_kernel_attributes() {
     CGB_CUDA(cudaFuncSetAttribute(eri_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(EriSmem)));
+    CGB_CUDA(cudaFuncSetAttribute(jk_slab_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)kJkSlabMaxBytes));
+    CGB_CUDA(cudaFuncSetAttribute(jk_slab_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)kJkSlabMaxBytes));
     static bool tables = false;
     if (!tables) {
         unsigned h[kHMax];
@@ -452,6 +579,30 @@ void launch_jk_contract(const EriDev& e, const int2* quartets, const long long* 
     jk_contract_kernel<<<blocks, 32 * kJkWarps, 0, s>>>(e, quartets, out_off, q0, nq, base, ints, n, nmat, D, rawJ,
                                                       rawK);
     CGB_CUDA(cudaGetLastError());
+}
+
+size_t jk_slab_bytes(int rows, int n, int nmat) {
+    return (size_t)nmat * ((size_t)kNf * kNf + (size_t)rows * n) * sizeof(double);
+}
+
+void launch_jk_slab(const EriDev& e, const int2* quartets, const long long* out_off, const longlong2* chunks,
+                    const std::vector<int>& cls_rows, const std::vector<long long>& cls_c0, const double* ints, int n,
+                    int nmat, const double* D, double* rawJ, double* rawK, cudaStream_t s) {
+    CGB_CHECK(rawK && cls_c0.size() == cls_rows.size() + 1, XC_ERR_INTERNAL, "bad exchange slab launch");
+    for (size_t k = 0; k < cls_rows.size(); k++) {
+        const long long nc = cls_c0[k + 1] - cls_c0[k];
+        if (nc <= 0) continue;
+        const size_t bytes = jk_slab_bytes(cls_rows[k], n, nmat);
+        CGB_CHECK(bytes <= kJkSlabMaxBytes && nc < (1LL << 31), XC_ERR_INTERNAL, "exchange slab too large");
+        const longlong2* c = chunks + cls_c0[k];
+        if (rawJ)
+            jk_slab_kernel<true><<<(unsigned)nc, 32 * kJkWarps, bytes, s>>>(e, quartets, out_off, c, cls_rows[k], ints,
+                                                                            n, nmat, D, rawJ, rawK);
+        else
+            jk_slab_kernel<false><<<(unsigned)nc, 32 * kJkWarps, bytes, s>>>(e, quartets, out_off, c, cls_rows[k],
+                                                                             ints, n, nmat, D, nullptr, rawK);
+        CGB_CUDA(cudaGetLastError());
+    }
 }
 
 static unsigned persistent_blocks(long long items, int per_block) {

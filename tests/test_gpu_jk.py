@@ -82,6 +82,27 @@ def test_direct_mode_equals_incore(case):
     assert np.abs(Ja - Jr).max() < TOL and np.abs(Ka[0] - Kr).max() < TOL
 
 
+def test_incore_without_dense_coulomb(case):
+    """A budget that holds the integrals but not the dense Coulomb operator
+    (the path of large molecules): J and K both from the in-core blocks,
+    exchange summed per bra pair in shared memory; equal to the reference and
+    to the dense-operator build.  J alone takes the per-quartet kernel."""
+    name, b, eri = case
+    n = b.nbasis
+    a = JKEngine(b, threshold=0.0)
+    c = JKEngine(b, threshold=0.0, max_bytes=8.0 * a.info()["integrals"])
+    assert c.info()["incore"]
+    Ds = [sym_density(n, 5), sym_density(n, 6)]
+    Jc, Kc = c.end(c.begin(Ds, True))
+    Ja, Ka = a.end(a.begin(Ds, True))
+    J0, K0 = reference_jk(eri, Ds[0])
+    J1, K1 = reference_jk(eri, Ds[1])
+    assert np.abs(Jc - (J0 + J1)).max() <= TOL
+    assert max(np.abs(Kc[0] - K0).max(), np.abs(Kc[1] - K1).max()) <= TOL
+    assert np.abs(Jc - Ja).max() < 1e-12 and np.abs(Kc[1] - Ka[1]).max() < 1e-12
+    assert np.abs(c.coulomb(Ds[0]) - J0).max() <= TOL
+
+
 def test_host_buffer_entry_point(case):
     name, b, eri = case
     n = b.nbasis
