@@ -607,8 +607,9 @@ C18_SCF_METRIC = "SCF wall time to 1e-8 Eh, C18 RKS B3LYP/def2-TZVP SG-2, mixed 
 def run_c18_scf(args):
     """cyclo[18]carbon, restricted B3LYP/def2-TZVP (558 functions) on SG-2:
     full Kohn-Sham SCFs to 1e-8 Eh from the SAP guess, Coulomb and exact
-    exchange from the library's GPU integrals (4.3e9 unique integrals kept in
-    HBM, computed once in the shared set-up).  Legs: the plain FP64 XC build
+    exchange from the library's GPU integrals (4.9e9 unique integrals of 8.1e7
+    shell quartets, computed in FP64 once in the shared set-up and kept in
+    HBM as float-float pairs).  Legs: the plain FP64 XC build
     every iteration (per-block shell screening 1e-11, the same energies as
     unscreened to 1e-14 Eh) and incremental tensor-core XC builds (references
     from FP64 densities).  The timed SCF includes the guess and every
@@ -637,7 +638,8 @@ def run_c18_scf(args):
     value = legs["mixed"]["wall_s"]
     line = {"metric": C18_SCF_METRIC, "value": value, "unit": "s", "n_gpus": 1, "steps": 1, "warmup": 0,
             "ms_per_step": value * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-            "dtype": "bf16x3 (split) + f64 accumulation (XC); f64 integrals, J/K, DIIS", "data": "synthetic",
+            "dtype": "bf16x3 (split) + f64 accumulation (XC); f64 integrals, J/K in float-float (48-bit) "
+                     "on the FP32 pipe, f64 DIIS", "data": "synthetic",
             "config": {"workload": "C18 RKS B3LYP/def2-TZVP SG-2, SCF to 1e-8 Eh from the SAP guess",
                        "setup_s": t_setup, "integrals": jk_info, "legs": legs,
                        "speedup_vs_plain_fp64": legs["fp64"]["wall_s"] / value,

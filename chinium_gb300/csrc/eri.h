@@ -62,18 +62,22 @@ void launch_jk_contract(const EriDev& e, const int2* quartets, const long long* 
                         long long base, const double* ints, int n, int nmat, const double* D, double* rawJ,
                         double* rawK, cudaStream_t s);
 
-// Exchange (rawK, required) and, when rawJ is given, Coulomb of the in-core
-// list (base 0) by bra-pair chunks: chunks[c] = [first, end) quartets of one
-// bra pair, at most a few thousand; the chunks are grouped by the bra pair's
-// na + nb, class k (na + nb = cls_rows[k]) holding chunks cls_c0[k] ..
-// cls_c0[k + 1] - 1.  One CTA per chunk sums its exchange contributions in
-// a shared-memory slab of jk_slab_bytes(rows, n, nmat) bytes, which must not
-// exceed kJkSlabMaxBytes.  Same raw accumulators as launch_jk_contract.
+// Coulomb and / or exchange (rawJ, rawK; either may be null) of the in-core
+// list (base 0) from the float-float store (the FP64 blocks split in place
+// by launch_coulomb_split, which nothing else reads afterwards) by bra-pair
+// chunks: chunks[c] = [first, end) quartets of one bra pair, at most a few
+// thousand; the chunks are grouped by the bra pair's na + nb, class k
+// (na + nb = cls_rows[k]) holding chunks cls_c0[k] .. cls_c0[k + 1] - 1.
+// D (FP64, nmat x n x n) is split into Dff (same size in float pairs) first.
+// One CTA per chunk sums its exchange contributions in a shared-memory slab
+// of jk_slab_bytes(rows, n, m) bytes for m matrices at a time, which must
+// not exceed kJkSlabMaxBytes for m = 1.  Same raw accumulators as
+// launch_jk_contract.
 constexpr size_t kJkSlabMaxBytes = 200 * 1024;
 size_t jk_slab_bytes(int rows, int n, int nmat);
 void launch_jk_slab(const EriDev& e, const int2* quartets, const long long* out_off, const longlong2* chunks,
-                    const std::vector<int>& cls_rows, const std::vector<long long>& cls_c0, const double* ints, int n,
-                    int nmat, const double* D, double* rawJ, double* rawK, cudaStream_t s);
+                    const std::vector<int>& cls_rows, const std::vector<long long>& cls_c0, const float2* ints, int n,
+                    int nmat, const double* D, float2* Dff, double* rawJ, double* rawK, cudaStream_t s);
 
 // Dense Coulomb operator M (ld x ld, ld = n (n + 1) / 2 rounded up to even,
 // packed pairs mu >= nu) from the in-core blocks of all quartets; M must

@@ -51,15 +51,16 @@ struct JkEngine {
                                               // in 8-byte elements); results (FP64)
     DevBuf<double> d_ints;                    // in-core integrals, or the direct-mode chunk buffer
     DevBuf<double> d_D, d_rawJ, d_rawK, d_J, d_K;
-    // in-core exchange by bra-pair chunks (launch_jk_slab): chunks grouped by
-    // the bra pair's na + nb, largest first
+    // in-core J / K by bra-pair chunks (launch_jk_slab) from the store split
+    // into float-float pairs, when one matrix's slab of the largest bra
+    // shells fits in shared memory: chunks grouped by the bra pair's na + nb,
+    // largest first
+    bool ff_store = false;
     DevBuf<longlong2> d_chunks;
     std::vector<int> cls_rows;
     std::vector<long long> cls_c0;
+    DevBuf<float2> d_Dff;
     int nmat_alloc = 0;
-    bool slab_fits(int nmat) const {
-        return !cls_rows.empty() && jk_slab_bytes(cls_rows[0], n, nmat) <= kJkSlabMaxBytes;
-    }
     void make_chunks(const std::vector<int2>& quart);
     EriDev dev() const { return EriDev{d_pairs.p, d_pp_p.p, d_pp_P.p, d_ep.p, d_boys.p}; }
     void setup(const BasisSet& b, double thr, double max_bytes);
@@ -206,6 +207,8 @@ void JkEngine::setup(const BasisSet& b, double thr, double max_bytes) {
             launch_coulomb_split((long long)npair * npair, d_M.p, stream);
         }
         make_chunks(quart);
+        ff_store = jk_slab_bytes(cls_rows[0], n, 1) <= kJkSlabMaxBytes;
+        if (ff_store) launch_coulomb_split(nints, d_ints.p, stream);  // after the scatter read the FP64 blocks
         CGB_CUDA(cudaStreamSynchronize(stream));
     } else {
         // chunks of consecutive quartets whose blocks fit in the chunk buffer
@@ -266,6 +269,25 @@ void JkEngine::build_device(int nmat, const double* dD, double* dJ, double* dK) 
     double* rK = dK ? d_rawK.p : nullptr;
     if (rJ) CGB_CUDA(cudaMemsetAsync(rJ, 0, nn * nmat * sizeof(double), stream));
     if (rK) CGB_CUDA(cudaMemsetAsync(rK, 0, nn * nmat * sizeof(double), stream));
+    if (incore && ff_store) {
+        if (d_Dff.n < nn * nmat) d_Dff.alloc(nn * nmat);
+        const float2* I = reinterpret_cast<const float2*>(d_ints.p);
+        if (dense_j && dJ) {
+            if (nmat > dense_nmat) {
+                d_x.alloc((size_t)npair * nmat);
+                d_x.zero(stream);  // pad entries stay zero
+                d_y.alloc((size_t)npair * nmat);
+                dense_nmat = nmat;
+            }
+            launch_coulomb_dense(n, nmat, npair, d_M.p, dD, d_x.p, d_y.p, dJ, stream);
+            rJ = nullptr;  // J written straight into dJ
+        }
+        if (rJ || rK)
+            launch_jk_slab(dev(), d_quartets.p, d_off.p, d_chunks.p, cls_rows, cls_c0, I, n, nmat, dD, d_Dff.p, rJ,
+                           rK, stream);
+        launch_jk_symmetrise(n, nmat, rJ, rK, rJ ? dJ : nullptr, dK, stream);
+        return;
+    }
     if (incore && dense_j) {
         // J from the dense operator (written straight into dJ); K from the blocks
         if (dJ) {
@@ -277,19 +299,13 @@ void JkEngine::build_device(int nmat, const double* dD, double* dJ, double* dK) 
             }
             launch_coulomb_dense(n, nmat, npair, d_M.p, dD, d_x.p, d_y.p, dJ, stream);
         }
-        if (rK && slab_fits(nmat))
-            launch_jk_slab(dev(), d_quartets.p, d_off.p, d_chunks.p, cls_rows, cls_c0, d_ints.p, n, nmat, dD, nullptr,
-                           rK, stream);
-        else if (rK)
+        if (rK)
             launch_jk_contract(dev(), d_quartets.p, d_off.p, 0, nquartets, 0, d_ints.p, n, nmat, dD, nullptr, rK,
                                stream);
         launch_jk_symmetrise(n, nmat, nullptr, rK, nullptr, dK, stream);
         return;
     }
-    if (incore && rK && slab_fits(nmat)) {
-        launch_jk_slab(dev(), d_quartets.p, d_off.p, d_chunks.p, cls_rows, cls_c0, d_ints.p, n, nmat, dD, rJ, rK,
-                       stream);
-    } else if (incore) {
+    if (incore) {
         launch_jk_contract(dev(), d_quartets.p, d_off.p, 0, nquartets, 0, d_ints.p, n, nmat, dD, rJ, rK, stream);
     } else {
         for (size_t c = 0; c + 1 < chunk_q.size(); c++) {

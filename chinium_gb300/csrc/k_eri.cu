@@ -11,9 +11,13 @@
 // and the bra contraction I[ab][cd] += pre sum_h Ep_ab[ab][h] X[cd][h].
 // The block of pure integrals [fa][fb][fc][fd] is written once.
 //
-// jk_contract_kernel: one warp per quartet block; each lane forms elements
-// of the six J / K sub-blocks it feeds (2 J, 4 K), scaled by the quartet's
-// degeneracy, with one FP64 atomic per element.  Small molecules take J from
+// jk_slab_kernel (in-core store, split once into float-float pairs): one CTA
+// per run of quartets of one bra pair; lanes form elements of the six J / K
+// sub-blocks each quartet feeds (2 J, 4 K) in float-float arithmetic on the
+// FP32 pipe, the exchange elements summed in a shared-memory slab of the bra
+// shells' rows and added to HBM once per run.  jk_contract_kernel (FP64
+// store: integral-direct chunks, or slabs too large for shared memory): one
+// warp per quartet block, one FP64 atomic per element.  Small molecules take J from
 // a dense Coulomb operator over function pairs filled once from the blocks
 // (coulomb_scatter_kernel, then split into float-float pairs) and a GEMV per
 // build in float-float arithmetic on the FP32 pipe (coulomb_gemv_kernel).
@@ -262,129 +266,6 @@ __global__ void __launch_bounds__(32 * kJkWarps) jk_contract_kernel(EriDev e, co
     }
 }
 
-// Exchange by bra pair (in-core list).  The quartets of one bra pair
-// P = (a, b) are consecutive in the list, and every exchange element they
-// feed lies in a row of shell a or of shell b: K(a, c), K(a, d), K(b, c),
-// K(b, d).  A CTA takes one run of them (a chunk), adds its K contributions
-// into a shared-memory slab of those na + nb rows x n columns (per matrix)
-// and its J(a, b) contributions into a small shared buffer, and adds both to
-// the raw accumulators once at the end: one FP64 global atomic per touched
-// slab element instead of one per element and quartet.  The J(c, d)
-// contributions (a different ket pair per quartet) stay global atomics.
-// Warps take the chunk's quartets in turn, lanes the sub-block elements, as
-// in jk_contract_kernel.  Shared layout: nmat x kNf^2 J(a, b) entries, then
-// nmat x rows x n slab entries (rows = na + nb <= rows_cap, the launch's
-// size).
-template <bool kJ>
-__global__ void __launch_bounds__(32 * kJkWarps) jk_slab_kernel(EriDev e, const int2* __restrict__ quartets,
-                                                                const long long* __restrict__ out_off,
-                                                                const longlong2* __restrict__ chunks, int rows_cap,
-                                                                const double* __restrict__ ints, int n, int nmat,
-                                                                const double* __restrict__ D,
-                                                                double* __restrict__ rawJ,
-                                                                double* __restrict__ rawK) {
-    extern __shared__ double sm_slab[];
-    const longlong2 ch = chunks[blockIdx.x];
-    const int2 pq0 = quartets[ch.x];
-    const EriPair P = e.pairs[pq0.x];
-    const int na = P.na, nb = P.nb, sa = P.fa, sb = P.fb, rows = na + nb;
-    if (rows > rows_cap) return;  // chunks are grouped by rows on the host; never taken
-    const int slab = rows * n;
-    const size_t nn = (size_t)n * n;
-    double* __restrict__ j1 = sm_slab;                        // [m][ia * nb + ib]
-    double* __restrict__ ks = sm_slab + (size_t)nmat * kNf * kNf;  // [m][row][col]
-    for (int t = threadIdx.x; t < nmat * (kNf * kNf + slab); t += blockDim.x) sm_slab[t] = 0.0;
-    __syncthreads();
-    const int lane = threadIdx.x & 31;
-    const double fab = sa == sb ? 0.5 : 1.0;
-    const int nJ1 = na * nb;
-    for (long long q = ch.x + (threadIdx.x >> 5); q < ch.y; q += kJkWarps) {
-        const int2 pq = quartets[q];
-        const EriPair Q = e.pairs[pq.y];
-        const int nc = Q.na, nd = Q.nb, sc = Q.fa, sd = Q.fb;
-        const double* __restrict__ blk = ints + out_off[q];
-        double f = fab;
-        if (sc == sd) f *= 0.5;
-        if (pq.x == pq.y) f *= 0.5;
-        const int nJ2 = nc * nd, nK1 = na * nc, nK2 = nb * nd, nK3 = na * nd;
-        const int nJ = kJ ? nJ1 + nJ2 : 0;
-        const int tot = nJ + nK1 + nK2 + nK3 + nb * nc;
-        const int sab = nb * nc * nd, sbb = nc * nd;  // strides of ia, ib in the block
-        for (int m = 0; m < nmat; m++) {
-            const double* __restrict__ Dm = D + m * nn;
-            double* __restrict__ km = ks + (size_t)m * slab;
-            for (int k = lane; k < tot; k += 32) {
-                double acc = 0.0;
-                double* dst;
-                if (k < nJ && k < nJ1) {  // J(a, b) += f sum_cd I D(c, d): shared
-                    const int ia = k / nb, ib = k - ia * nb;
-                    const double* bl = blk + ia * sab + ib * sbb;
-                    for (int ic = 0; ic < nc; ic++)
-                        for (int id = 0; id < nd; id++)
-                            acc = fma(__ldg(bl + ic * nd + id), __ldg(Dm + (size_t)(sc + ic) * n + sd + id), acc);
-                    dst = j1 + m * kNf * kNf + k;
-                } else if (k < nJ) {  // J(c, d) += f sum_ab I D(a, b): global
-                    const int r = k - nJ1, ic = r / nd, id = r - ic * nd;
-                    const double* bl = blk + ic * nd + id;
-                    for (int ia = 0; ia < na; ia++)
-                        for (int ib = 0; ib < nb; ib++)
-                            acc = fma(__ldg(bl + ia * sab + ib * sbb), __ldg(Dm + (size_t)(sa + ia) * n + sb + ib), acc);
-                    dst = rawJ + m * nn + (size_t)(sc + ic) * n + sd + id;
-                } else {
-                    int r = k - nJ;
-                    if (r < nK1) {  // K(a, c) += f sum_bd I D(b, d): slab row ia
-                        const int ia = r / nc, ic = r - ia * nc;
-                        for (int ib = 0; ib < nb; ib++)
-                            for (int id = 0; id < nd; id++)
-                                acc = fma(__ldg(blk + ia * sab + ib * sbb + ic * nd + id),
-                                          __ldg(Dm + (size_t)(sb + ib) * n + sd + id), acc);
-                        dst = km + ia * n + sc + ic;
-                    } else if ((r -= nK1) < nK2) {  // K(b, d) += f sum_ac I D(a, c): slab row na + ib
-                        const int ib = r / nd, id = r - ib * nd;
-                        for (int ia = 0; ia < na; ia++)
-                            for (int ic = 0; ic < nc; ic++)
-                                acc = fma(__ldg(blk + ia * sab + ib * sbb + ic * nd + id),
-                                          __ldg(Dm + (size_t)(sa + ia) * n + sc + ic), acc);
-                        dst = km + (na + ib) * n + sd + id;
-                    } else if ((r -= nK2) < nK3) {  // K(a, d) += f sum_bc I D(b, c): slab row ia
-                        const int ia = r / nd, id = r - ia * nd;
-                        for (int ib = 0; ib < nb; ib++)
-                            for (int ic = 0; ic < nc; ic++)
-                                acc = fma(__ldg(blk + ia * sab + ib * sbb + ic * nd + id),
-                                          __ldg(Dm + (size_t)(sb + ib) * n + sc + ic), acc);
-                        dst = km + ia * n + sd + id;
-                    } else {  // K(b, c) += f sum_ad I D(a, d): slab row na + ib
-                        r -= nK3;
-                        const int ib = r / nc, ic = r - ib * nc;
-                        for (int ia = 0; ia < na; ia++)
-                            for (int id = 0; id < nd; id++)
-                                acc = fma(__ldg(blk + ia * sab + ib * sbb + ic * nd + id),
-                                          __ldg(Dm + (size_t)(sa + ia) * n + sd + id), acc);
-                        dst = km + (na + ib) * n + sc + ic;
-                    }
-                }
-                atomicAdd(dst, f * acc);
-            }
-        }
-    }
-    __syncthreads();
-    // slab row r < na is function sa + r, row na + r' is function sb + r'
-    for (int t = threadIdx.x; t < nmat * slab; t += blockDim.x) {
-        const double v = ks[t];
-        if (v == 0.0) continue;  // columns no ket of the chunk touched
-        const int m = t / slab, r = t - m * slab, row = r / n, col = r - row * n;
-        const int fn = row < na ? sa + row : sb + (row - na);
-        atomicAdd(rawK + m * nn + (size_t)fn * n + col, v);
-    }
-    if (kJ) {
-        for (int t = threadIdx.x; t < nmat * nJ1; t += blockDim.x) {
-            const int m = t / nJ1, r = t - m * nJ1, ia = r / nb, ib = r - ia * nb;
-            const double v = j1[m * kNf * kNf + r];
-            if (v != 0.0) atomicAdd(rawJ + m * nn + (size_t)(sa + ia) * n + sb + ib, v);
-        }
-    }
-}
-
 // Dense Coulomb operator of small molecules: M[(mu nu), (la si)] =
 // (mu nu|la si) over packed pairs mu >= nu (p = mu (mu + 1) / 2 + nu), filled
 // once from the in-core quartet blocks (warp per quartet, both (P, Q) and
@@ -459,6 +340,172 @@ __device__ __forceinline__ void ff_fma(float mh, float ml, float xh, float xl, f
     const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(p, z));
     s = t;
     c = __fadd_rn(c, __fadd_rn(__fadd_rn(err, e), __fmaf_rn(mh, xl, __fmul_rn(ml, xh))));
+}
+
+// float -> double from the bit pattern (integer pipe; GB300's FP64 pipe,
+// which also converts, runs at 1/64 of the FP32 rate).  Normal numbers are
+// exact; zero and subnormals (below 1.2e-38) give 0.
+__device__ __forceinline__ double f32_to_f64(float x) {
+    const unsigned u = __float_as_uint(x);
+    const unsigned ex = (u >> 23) & 0xffu;
+    if (ex == 0) return 0.0;
+    const unsigned long long b = ((unsigned long long)(u & 0x80000000u) << 32) |
+                                 ((unsigned long long)(ex + 896u) << 52) |
+                                 ((unsigned long long)(u & 0x7fffffu) << 29);
+    return __longlong_as_double((long long)b);
+}
+
+// FP64 value of the float-float pair (s, c) scaled by f, a power of two
+// (exact in FP32): one FP64 add.
+__device__ __forceinline__ double ff_scaled(float s, float c, float f) {
+    return f32_to_f64(s * f) + f32_to_f64(c * f);
+}
+
+// Exchange and Coulomb by bra pair (in-core list, float-float store).  The
+// quartets of one bra pair P = (a, b) are consecutive in the list, and every
+// exchange element they feed lies in a row of shell a or of shell b:
+// K(a, c), K(a, d), K(b, c), K(b, d).  A CTA takes one run of them (a
+// chunk), adds its K contributions into a shared-memory slab of those
+// na + nb rows x n columns (per matrix) and its J(a, b) contributions into a
+// small shared buffer, and adds both to the raw accumulators once at the
+// end: one FP64 global atomic per touched slab element instead of one per
+// element and quartet.  The J(c, d) contributions (a different ket pair per
+// quartet) stay global atomics.  Warps take the chunk's quartets in turn,
+// lanes the sub-block elements (one slice sum of the block times D each, as
+// in jk_contract_kernel).  The integrals and densities are float-float pairs
+// (hi, lo) and the slice sums run in float-float on the FP32 pipe; each sum
+// enters the FP64 slab with one FP64 add.  Shared layout: nmat x kNf^2
+// J(a, b) entries, then (kK) nmat x rows x n slab entries (rows = na + nb
+// <= rows_cap, the launch's size).
+template <bool kJ, bool kK>
+__global__ void __launch_bounds__(32 * kJkWarps) jk_slab_kernel(EriDev e, const int2* __restrict__ quartets,
+                                                                const long long* __restrict__ out_off,
+                                                                const longlong2* __restrict__ chunks, int rows_cap,
+                                                                const float2* __restrict__ ints, int n, int nmat,
+                                                                const float2* __restrict__ D,
+                                                                double* __restrict__ rawJ,
+                                                                double* __restrict__ rawK) {
+    extern __shared__ double sm_slab[];
+    const longlong2 ch = chunks[blockIdx.x];
+    const int2 pq0 = quartets[ch.x];
+    const EriPair P = e.pairs[pq0.x];
+    const int na = P.na, nb = P.nb, sa = P.fa, sb = P.fb, rows = na + nb;
+    if (kK && rows > rows_cap) return;  // chunks are grouped by rows on the host; never taken
+    const int slab = kK ? rows * n : 0;
+    const size_t nn = (size_t)n * n;
+    double* __restrict__ j1 = sm_slab;                             // [m][ia * nb + ib]
+    double* __restrict__ ks = sm_slab + (size_t)nmat * kNf * kNf;  // [m][row][col]
+    for (int t = threadIdx.x; t < nmat * (kNf * kNf + slab); t += blockDim.x) sm_slab[t] = 0.0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const float fab = sa == sb ? 0.5f : 1.0f;
+    const int nJ1 = na * nb;
+    for (long long q = ch.x + (threadIdx.x >> 5); q < ch.y; q += kJkWarps) {
+        const int2 pq = quartets[q];
+        const EriPair Q = e.pairs[pq.y];
+        const int nc = Q.na, nd = Q.nb, sc = Q.fa, sd = Q.fb;
+        const float2* __restrict__ blk = ints + out_off[q];
+        float f = fab;
+        if (sc == sd) f *= 0.5f;
+        if (pq.x == pq.y) f *= 0.5f;
+        const int nJ2 = nc * nd, nK1 = na * nc, nK2 = nb * nd, nK3 = na * nd;
+        const int nJ = kJ ? nJ1 + nJ2 : 0;
+        const int tot = nJ + (kK ? nK1 + nK2 + nK3 + nb * nc : 0);
+        const int sab = nb * nc * nd, sbb = nc * nd;  // strides of ia, ib in the block
+        for (int m = 0; m < nmat; m++) {
+            const float2* __restrict__ Dm = D + m * nn;
+            double* __restrict__ km = ks + (size_t)m * slab;
+            for (int k = lane; k < tot; k += 32) {
+                float s = 0.f, c = 0.f;
+                double* dst;
+                if (k < nJ && k < nJ1) {  // J(a, b) += f sum_cd I D(c, d): shared
+                    const int ia = k / nb, ib = k - ia * nb;
+                    const float2* bl = blk + ia * sab + ib * sbb;
+                    for (int ic = 0; ic < nc; ic++)
+                        for (int id = 0; id < nd; id++) {
+                            const float2 v = bl[ic * nd + id], x = Dm[(size_t)(sc + ic) * n + sd + id];
+                            ff_fma(v.x, v.y, x.x, x.y, s, c);
+                        }
+                    dst = j1 + m * kNf * kNf + k;
+                } else if (k < nJ) {  // J(c, d) += f sum_ab I D(a, b): global
+                    const int r = k - nJ1, ic = r / nd, id = r - ic * nd;
+                    const float2* bl = blk + ic * nd + id;
+                    for (int ia = 0; ia < na; ia++)
+                        for (int ib = 0; ib < nb; ib++) {
+                            const float2 v = bl[ia * sab + ib * sbb], x = Dm[(size_t)(sa + ia) * n + sb + ib];
+                            ff_fma(v.x, v.y, x.x, x.y, s, c);
+                        }
+                    dst = rawJ + m * nn + (size_t)(sc + ic) * n + sd + id;
+                } else {
+                    int r = k - nJ;
+                    if (r < nK1) {  // K(a, c) += f sum_bd I D(b, d): slab row ia
+                        const int ia = r / nc, ic = r - ia * nc;
+                        for (int ib = 0; ib < nb; ib++)
+                            for (int id = 0; id < nd; id++) {
+                                const float2 v = blk[ia * sab + ib * sbb + ic * nd + id];
+                                const float2 x = Dm[(size_t)(sb + ib) * n + sd + id];
+                                ff_fma(v.x, v.y, x.x, x.y, s, c);
+                            }
+                        dst = km + ia * n + sc + ic;
+                    } else if ((r -= nK1) < nK2) {  // K(b, d) += f sum_ac I D(a, c): slab row na + ib
+                        const int ib = r / nd, id = r - ib * nd;
+                        for (int ia = 0; ia < na; ia++)
+                            for (int ic = 0; ic < nc; ic++) {
+                                const float2 v = blk[ia * sab + ib * sbb + ic * nd + id];
+                                const float2 x = Dm[(size_t)(sa + ia) * n + sc + ic];
+                                ff_fma(v.x, v.y, x.x, x.y, s, c);
+                            }
+                        dst = km + (na + ib) * n + sd + id;
+                    } else if ((r -= nK2) < nK3) {  // K(a, d) += f sum_bc I D(b, c): slab row ia
+                        const int ia = r / nd, id = r - ia * nd;
+                        for (int ib = 0; ib < nb; ib++)
+                            for (int ic = 0; ic < nc; ic++) {
+                                const float2 v = blk[ia * sab + ib * sbb + ic * nd + id];
+                                const float2 x = Dm[(size_t)(sb + ib) * n + sc + ic];
+                                ff_fma(v.x, v.y, x.x, x.y, s, c);
+                            }
+                        dst = km + ia * n + sd + id;
+                    } else {  // K(b, c) += f sum_ad I D(a, d): slab row na + ib
+                        r -= nK3;
+                        const int ib = r / nc, ic = r - ib * nc;
+                        for (int ia = 0; ia < na; ia++)
+                            for (int id = 0; id < nd; id++) {
+                                const float2 v = blk[ia * sab + ib * sbb + ic * nd + id];
+                                const float2 x = Dm[(size_t)(sa + ia) * n + sd + id];
+                                ff_fma(v.x, v.y, x.x, x.y, s, c);
+                            }
+                        dst = km + (na + ib) * n + sc + ic;
+                    }
+                }
+                atomicAdd(dst, ff_scaled(s, c, f));
+            }
+        }
+    }
+    __syncthreads();
+    if constexpr (kK) {
+        // slab row r < na is function sa + r, row na + r' is function sb + r'
+        for (int t = threadIdx.x; t < nmat * slab; t += blockDim.x) {
+            const double v = ks[t];
+            if (v == 0.0) continue;  // columns no ket of the chunk touched
+            const int m = t / slab, r = t - m * slab, row = r / n, col = r - row * n;
+            const int fn = row < na ? sa + row : sb + (row - na);
+            atomicAdd(rawK + m * nn + (size_t)fn * n + col, v);
+        }
+    }
+    if constexpr (kJ) {
+        for (int t = threadIdx.x; t < nmat * nJ1; t += blockDim.x) {
+            const int m = t / nJ1, r = t - m * nJ1, ia = r / nb, ib = r - ia * nb;
+            const double v = j1[m * kNf * kNf + r];
+            if (v != 0.0) atomicAdd(rawJ + m * nn + (size_t)(sa + ia) * n + sb + ib, v);
+        }
+    }
+}
+
+// nmat densities (FP64) -> float-float pairs, out of place
+__global__ void jk_split_density_kernel(long long count, const double* __restrict__ D, float2* __restrict__ out) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+         i += (long long)gridDim.x * blockDim.x)
+        out[i] = ff_split(D[i]);
 }
 
 // y[m] = M x[m] for NM <= 4 vectors in one pass over M (npair rows of
@@ -539,9 +586,11 @@ __global__ void jk_symmetrise_kernel(int n, int nmat, const double* __restrict__
 
 void set_eri_kernel_attributes() {
     CGB_CUDA(cudaFuncSetAttribute(eri_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(EriSmem)));
-    CGB_CUDA(cudaFuncSetAttribute(jk_slab_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    CGB_CUDA(cudaFuncSetAttribute(jk_slab_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)kJkSlabMaxBytes));
-    CGB_CUDA(cudaFuncSetAttribute(jk_slab_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    CGB_CUDA(cudaFuncSetAttribute(jk_slab_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)kJkSlabMaxBytes));
+    CGB_CUDA(cudaFuncSetAttribute(jk_slab_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)kJkSlabMaxBytes));
     static bool tables = false;
     if (!tables) {
@@ -586,22 +635,40 @@ size_t jk_slab_bytes(int rows, int n, int nmat) {
 }
 
 void launch_jk_slab(const EriDev& e, const int2* quartets, const long long* out_off, const longlong2* chunks,
-                    const std::vector<int>& cls_rows, const std::vector<long long>& cls_c0, const double* ints, int n,
-                    int nmat, const double* D, double* rawJ, double* rawK, cudaStream_t s) {
-    CGB_CHECK(rawK && cls_c0.size() == cls_rows.size() + 1, XC_ERR_INTERNAL, "bad exchange slab launch");
+                    const std::vector<int>& cls_rows, const std::vector<long long>& cls_c0, const float2* ints, int n,
+                    int nmat, const double* D, float2* Dff, double* rawJ, double* rawK, cudaStream_t s) {
+    CGB_CHECK((rawJ || rawK) && cls_c0.size() == cls_rows.size() + 1, XC_ERR_INTERNAL, "bad exchange slab launch");
+    const size_t nn = (size_t)n * n;
+    const long long count = (long long)nn * nmat;
+    jk_split_density_kernel<<<(unsigned)std::min<long long>((count + 255) / 256, 4096), 256, 0, s>>>(count, D, Dff);
+    CGB_CUDA(cudaGetLastError());
     for (size_t k = 0; k < cls_rows.size(); k++) {
         const long long nc = cls_c0[k + 1] - cls_c0[k];
         if (nc <= 0) continue;
-        const size_t bytes = jk_slab_bytes(cls_rows[k], n, nmat);
-        CGB_CHECK(bytes <= kJkSlabMaxBytes && nc < (1LL << 31), XC_ERR_INTERNAL, "exchange slab too large");
+        CGB_CHECK(nc < (1LL << 31), XC_ERR_INTERNAL, "too many exchange chunks");
+        const int rows = rawK ? cls_rows[k] : 0;
+        // matrices per launch: as many as the slab holds (at least one)
+        int mg = nmat;
+        while (mg > 1 && jk_slab_bytes(rows, n, mg) > kJkSlabMaxBytes) mg--;
+        const size_t bytes = jk_slab_bytes(rows, n, mg);
+        CGB_CHECK(bytes <= kJkSlabMaxBytes, XC_ERR_INTERNAL, "exchange slab too large");
         const longlong2* c = chunks + cls_c0[k];
-        if (rawJ)
-            jk_slab_kernel<true><<<(unsigned)nc, 32 * kJkWarps, bytes, s>>>(e, quartets, out_off, c, cls_rows[k], ints,
-                                                                            n, nmat, D, rawJ, rawK);
-        else
-            jk_slab_kernel<false><<<(unsigned)nc, 32 * kJkWarps, bytes, s>>>(e, quartets, out_off, c, cls_rows[k],
-                                                                             ints, n, nmat, D, nullptr, rawK);
-        CGB_CUDA(cudaGetLastError());
+        for (int m0 = 0; m0 < nmat; m0 += mg) {
+            const int nm = std::min(mg, nmat - m0);
+            const float2* Dm = Dff + m0 * nn;
+            double* Jm = rawJ ? rawJ + m0 * nn : nullptr;
+            double* Km = rawK ? rawK + m0 * nn : nullptr;
+            if (Jm && Km)
+                jk_slab_kernel<true, true><<<(unsigned)nc, 32 * kJkWarps, bytes, s>>>(e, quartets, out_off, c, rows,
+                                                                                      ints, n, nm, Dm, Jm, Km);
+            else if (Km)
+                jk_slab_kernel<false, true><<<(unsigned)nc, 32 * kJkWarps, bytes, s>>>(e, quartets, out_off, c, rows,
+                                                                                       ints, n, nm, Dm, nullptr, Km);
+            else
+                jk_slab_kernel<true, false><<<(unsigned)nc, 32 * kJkWarps, bytes, s>>>(e, quartets, out_off, c, rows,
+                                                                                       ints, n, nm, Dm, Jm, nullptr);
+            CGB_CUDA(cudaGetLastError());
+        }
     }
 }
 
