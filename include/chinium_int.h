@@ -46,7 +46,14 @@ int xc_eri(const xc_basis* b, double* eri, double schwarz_threshold);
  * threshold -1 at SelfConsistentField.cpp:47; 0 does the same here).  The
  * integrals are computed once and kept in HBM when they take at most
  * max_bytes (0: half of the free device memory); otherwise every build
- * recomputes them in chunks (integral-direct). */
+ * recomputes them in chunks (integral-direct).  Kept integrals of a small
+ * molecule also fill a dense Coulomb operator over function pairs when it
+ * fits in the same budget and a quarter of the free memory.  In-core builds
+ * contract in float-float arithmetic (FP64 integrals and densities held as
+ * pairs of floats, 48 significant bits, sums of products on the FP32 pipe;
+ * J and K agree with FP64 contractions to ~1e-13 relative) when one
+ * matrix's exchange rows of the largest shell pair fit in shared memory
+ * (n up to ~1800 functions with f shells); other builds run in FP64. */
 typedef struct xc_jk xc_jk;
 int xc_jk_create(const xc_basis* b, double threshold, double max_bytes, xc_jk** out);
 int xc_jk_destroy(xc_jk* jk);
