@@ -62,6 +62,7 @@ struct JkEngine {
     DevBuf<float2> d_Dff;
     int nmat_alloc = 0;
     void make_chunks(const std::vector<int2>& quart);
+    void dense_coulomb(int nmat, const double* dD, double* dJ);  // J from the dense operator into dJ
     EriDev dev() const { return EriDev{d_pairs.p, d_pp_p.p, d_pp_P.p, d_ep.p, d_boys.p}; }
     void setup(const BasisSet& b, double thr, double max_bytes);
     void build_device(int nmat, const double* dD, double* dJ, double* dK);
@@ -258,6 +259,16 @@ void JkEngine::make_chunks(const std::vector<int2>& quart) {
     CGB_CUDA(cudaStreamSynchronize(stream));
 }
 
+void JkEngine::dense_coulomb(int nmat, const double* dD, double* dJ) {
+    if (nmat > dense_nmat) {
+        d_x.alloc((size_t)npair * nmat);
+        d_x.zero(stream);  // pad entries stay zero
+        d_y.alloc((size_t)npair * nmat);
+        dense_nmat = nmat;
+    }
+    launch_coulomb_dense(n, nmat, npair, d_M.p, dD, d_x.p, d_y.p, dJ, stream);
+}
+
 void JkEngine::build_device(int nmat, const double* dD, double* dJ, double* dK) {
     const size_t nn = (size_t)n * n;
     if (nmat > nmat_alloc) {
@@ -265,47 +276,21 @@ void JkEngine::build_device(int nmat, const double* dD, double* dJ, double* dK) 
         d_rawK.alloc(nn * nmat);
         nmat_alloc = nmat;
     }
-    double* rJ = dJ ? d_rawJ.p : nullptr;
+    // J from the dense operator (straight into dJ) where there is one, else
+    // from the blocks into the raw accumulator with K
+    const bool j_dense = incore && dense_j && dJ;
+    double* rJ = dJ && !j_dense ? d_rawJ.p : nullptr;
     double* rK = dK ? d_rawK.p : nullptr;
     if (rJ) CGB_CUDA(cudaMemsetAsync(rJ, 0, nn * nmat * sizeof(double), stream));
     if (rK) CGB_CUDA(cudaMemsetAsync(rK, 0, nn * nmat * sizeof(double), stream));
+    if (j_dense) dense_coulomb(nmat, dD, dJ);
     if (incore && ff_store) {
-        if (d_Dff.n < nn * nmat) d_Dff.alloc(nn * nmat);
-        const float2* I = reinterpret_cast<const float2*>(d_ints.p);
-        if (dense_j && dJ) {
-            if (nmat > dense_nmat) {
-                d_x.alloc((size_t)npair * nmat);
-                d_x.zero(stream);  // pad entries stay zero
-                d_y.alloc((size_t)npair * nmat);
-                dense_nmat = nmat;
-            }
-            launch_coulomb_dense(n, nmat, npair, d_M.p, dD, d_x.p, d_y.p, dJ, stream);
-            rJ = nullptr;  // J written straight into dJ
+        if (rJ || rK) {
+            if (d_Dff.n < nn * nmat) d_Dff.alloc(nn * nmat);
+            launch_jk_slab(dev(), d_quartets.p, d_off.p, d_chunks.p, cls_rows, cls_c0,
+                           reinterpret_cast<const float2*>(d_ints.p), n, nmat, dD, d_Dff.p, rJ, rK, stream);
         }
-        if (rJ || rK)
-            launch_jk_slab(dev(), d_quartets.p, d_off.p, d_chunks.p, cls_rows, cls_c0, I, n, nmat, dD, d_Dff.p, rJ,
-                           rK, stream);
-        launch_jk_symmetrise(n, nmat, rJ, rK, rJ ? dJ : nullptr, dK, stream);
-        return;
-    }
-    if (incore && dense_j) {
-        // J from the dense operator (written straight into dJ); K from the blocks
-        if (dJ) {
-            if (nmat > dense_nmat) {
-                d_x.alloc((size_t)npair * nmat);
-                d_x.zero(stream);  // pad entries stay zero
-                d_y.alloc((size_t)npair * nmat);
-                dense_nmat = nmat;
-            }
-            launch_coulomb_dense(n, nmat, npair, d_M.p, dD, d_x.p, d_y.p, dJ, stream);
-        }
-        if (rK)
-            launch_jk_contract(dev(), d_quartets.p, d_off.p, 0, nquartets, 0, d_ints.p, n, nmat, dD, nullptr, rK,
-                               stream);
-        launch_jk_symmetrise(n, nmat, nullptr, rK, nullptr, dK, stream);
-        return;
-    }
-    if (incore) {
+    } else if (incore) {
         launch_jk_contract(dev(), d_quartets.p, d_off.p, 0, nquartets, 0, d_ints.p, n, nmat, dD, rJ, rK, stream);
     } else {
         for (size_t c = 0; c + 1 < chunk_q.size(); c++) {
@@ -317,7 +302,7 @@ void JkEngine::build_device(int nmat, const double* dD, double* dJ, double* dK) 
                                stream);
         }
     }
-    launch_jk_symmetrise(n, nmat, rJ, rK, dJ, dK, stream);
+    launch_jk_symmetrise(n, nmat, rJ, rK, rJ ? dJ : nullptr, dK, stream);
 }
 
 }  // namespace cgb
