@@ -71,6 +71,13 @@ struct JkEngine {
 namespace {
 constexpr double kPrimCut = 1e-20;
 constexpr long long kSlabChunk = 2048;  // quartets per exchange chunk at most
+// The slab kernel pays one shared-memory FP64 add (the warp waits for it)
+// per sub-block element, the per-quartet kernel one global atomic add (not
+// waited for) and FP64 products.  Measured: C18 def2-TZVP, 61 integrals per
+// quartet, J + K 0.18 s (slab) vs 0.23 s; (H2O)8 def2-SVP, 13 per quartet,
+// K 7.3 ms (slab) vs 4.7 ms.  The slab kernel is taken from this average up
+// (between the measured points; the crossover itself was not measured).
+constexpr double kSlabMinIntsPerQuartet = 24.0;
 
 inline int nfunc_of(const Shell& s) { return shell_size(s.type); }
 }  // namespace
@@ -208,7 +215,8 @@ void JkEngine::setup(const BasisSet& b, double thr, double max_bytes) {
             launch_coulomb_split((long long)npair * npair, d_M.p, stream);
         }
         make_chunks(quart);
-        ff_store = jk_slab_bytes(cls_rows[0], n, 1) <= kJkSlabMaxBytes;
+        ff_store = jk_slab_bytes(cls_rows[0], n, 1) <= kJkSlabMaxBytes &&
+                   (double)nints >= kSlabMinIntsPerQuartet * (double)nquartets;
         if (ff_store) launch_coulomb_split(nints, d_ints.p, stream);  // after the scatter read the FP64 blocks
         CGB_CUDA(cudaStreamSynchronize(stream));
     } else {

@@ -51,9 +51,10 @@ int xc_eri(const xc_basis* b, double* eri, double schwarz_threshold);
  * fits in the same budget and a quarter of the free memory.  In-core builds
  * contract in float-float arithmetic (FP64 integrals and densities held as
  * pairs of floats, 48 significant bits, sums of products on the FP32 pipe;
- * J and K agree with FP64 contractions to ~1e-13 relative) when one
- * matrix's exchange rows of the largest shell pair fit in shared memory
- * (n up to ~1800 functions with f shells); other builds run in FP64. */
+ * J and K agree with FP64 contractions to ~1e-13 relative) when the shell
+ * quartets average at least 24 integrals (basis sets with d and f shells)
+ * and one matrix's exchange rows of the largest shell pair fit in shared
+ * memory (n up to ~1800 functions with f shells); other builds run in FP64. */
 typedef struct xc_jk xc_jk;
 int xc_jk_create(const xc_basis* b, double threshold, double max_bytes, xc_jk** out);
 int xc_jk_destroy(xc_jk* jk);

@@ -84,9 +84,11 @@ def test_direct_mode_equals_incore(case):
 
 def test_incore_without_dense_coulomb(case):
     """A budget that holds the integrals but not the dense Coulomb operator
-    (the path of large molecules): J and K both from the in-core blocks,
-    exchange summed per bra pair in shared memory; equal to the reference and
-    to the dense-operator build.  J alone takes the per-quartet kernel."""
+    (the path of large molecules): J and K both from the in-core blocks
+    (h2o_tzvp, 28 integrals per quartet: float-float store, exchange summed
+    per bra pair in shared memory; the others: FP64 per-quartet kernel);
+    equal to the reference and to the dense-operator build, also for J
+    alone."""
     name, b, eri = case
     n = b.nbasis
     a = JKEngine(b, threshold=0.0)
