@@ -1,0 +1,85 @@
+"""The oracle's functionals (the libxc ids the reference's ExchangeCorrelation
+reads, src/ExchangeCorrelation.cpp:18-248) pinned without libxc: exchange and
+correlation energies of the hydrogen atom's exact ground-state density
+rho = exp(-2 r) / pi (one electron, fully spin-polarized; its kinetic energy
+density is the von Weizsaecker one, tau = |grad rho|^2 / (8 rho) = rho / 2),
+against values that follow from the functionals' definitions or that their
+authors published:
+
+- Slater exchange: -(81/512) 3^(1/3) 2^(4/3) pi^(-2/3) = -0.268037 in closed
+  form (spin scaling, and the integral of rho^(4/3) is 27 / (64 pi^(1/3)));
+- TPSS exchange: the exact -5/16, a norm its two constants were fitted to
+  (Tao, Perdew, Staroverov, Scuseria, PRL 91, 146401 (2003));
+- r2SCAN exchange: -5/16, SCAN's hydrogen-atom norm that r2SCAN keeps
+  (Furness, Kaplan, Ning, Perdew, Sun, JPCL 11, 8208 (2020));
+- B88 exchange -0.3098 (Becke, PRA 38, 3098 (1988)), PBE exchange -0.3059
+  and PBE correlation -0.0060 (Perdew, Burke, Ernzerhof, PRL 77, 3865 (1996)),
+  published to four decimals; both PBE parameter sets (ids 101/130 and the
+  reference's PBE.df ids 321/322, 2e-7 Eh apart here) meet them;
+- LYP, TPSS and r2SCAN correlation: zero for any one-electron density, by
+  construction.
+
+The CUDA functionals agree with the oracle's on points to 1e-9 relative for
+99 % of them and 1e-8 wherever a spin density is above 1e-12
+(tests/test_gpu_parity.py), so this pins them too.  CPU only."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+# radial Gauss-Legendre quadrature on r = x / (1 - x), x in (0, 1): the
+# energies below are converged to 1e-12 with 800 nodes
+_x, _w = np.polynomial.legendre.leggauss(800)
+_t = 0.5 * (_x + 1.0)
+R = _t / (1.0 - _t)
+W = 4.0 * np.pi * R**2 * 0.5 * _w / (1.0 - _t) ** 2
+RHO = np.exp(-2.0 * R) / np.pi
+
+
+def exchange_polarized(ids):
+    """E_x[rho, 0] = E_x[2 rho] / 2 (spin scaling), through the unpolarized
+    evaluation: density 2 rho, sigma = |grad 2 rho|^2 = 16 rho^2, tau = rho."""
+    n = 2.0 * RHO
+    eps = O.functional(ids, 1, [n], [16.0 * RHO**2], [RHO])[0]
+    return 0.5 * np.sum(W * n * eps)
+
+
+def energy_polarized(ids):
+    """E[rho, 0] through the spin-polarized evaluation (rho_down = 0)."""
+    z = np.zeros_like(RHO)
+    eps = O.functional(ids, 2, [RHO, z], [4.0 * RHO**2, z, z], [0.5 * RHO, z])[0]
+    return np.sum(W * RHO * eps)
+
+
+def test_quadrature_holds_one_electron():
+    assert abs(np.sum(W * RHO) - 1.0) < 1e-12
+
+
+def test_slater_exchange_closed_form():
+    ref = -(81.0 / 512.0) * 3.0 ** (1 / 3) * 2.0 ** (4 / 3) * np.pi ** (-2 / 3)
+    assert abs(exchange_polarized([1]) - ref) < 1e-12
+    assert abs(energy_polarized([1]) - ref) < 1e-12
+
+
+@pytest.mark.parametrize("name,ids,ref,tol", [
+    ("TPSS", [202], -5.0 / 16.0, 1e-6),
+    ("r2SCAN", [497], -5.0 / 16.0, 5e-6),
+    ("B88", [106], -0.3098, 5e-5),
+    ("PBE", [101], -0.3059, 5e-5),
+    ("PBE, the reference's PBE.df id", [321], -0.3059, 5e-5),
+])
+def test_exchange_of_the_hydrogen_atom(name, ids, ref, tol):
+    ex = exchange_polarized(ids)
+    assert abs(ex - ref) < tol, (name, ex)
+    # the spin-polarized evaluation with an empty minority channel agrees
+    assert abs(energy_polarized(ids) - ex) < 1e-10
+
+
+@pytest.mark.parametrize("ids", [[130], [322]])
+def test_pbe_correlation_of_the_hydrogen_atom(ids):
+    assert abs(energy_polarized(ids) - (-0.0060)) < 5e-5
+
+
+@pytest.mark.parametrize("name,ids", [("LYP", [131]), ("TPSS", [231]), ("r2SCAN", [498])])
+def test_one_electron_correlation_vanishes(name, ids):
+    assert abs(energy_polarized(ids)) < 1e-10, name
