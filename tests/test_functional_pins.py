@@ -83,3 +83,20 @@ def test_pbe_correlation_of_the_hydrogen_atom(ids):
 @pytest.mark.parametrize("name,ids", [("LYP", [131]), ("TPSS", [231]), ("r2SCAN", [498])])
 def test_one_electron_correlation_vanishes(name, ids):
     assert abs(energy_polarized(ids)) < 1e-10, name
+
+
+@pytest.mark.parametrize("zeta", [0.0, 1.0])
+def test_vwn5_and_pw92_fits_of_the_uniform_gas_agree(zeta):
+    """VWN5 (id 7) and PW92 (PBE correlation at zero gradient, id 130: the
+    reduction itself is tested in test_oracle.py) are independent fits to the
+    same quantum Monte Carlo correlation energies of the uniform electron
+    gas; they agree to ~0.5 % from r_s = 0.1 to 50, unpolarized and fully
+    polarized (a coefficient typed wrong in either shows far beyond that)."""
+    rs = np.array([0.1, 0.5, 1.0, 2.0, 3.0, 5.0, 10.0, 20.0, 50.0])
+    n = 3.0 / (4.0 * np.pi * rs**3)
+    na, nb = n * (1 + zeta) / 2, n * (1 - zeta) / 2
+    z = np.zeros_like(n)
+    vwn = O.functional([7], 2, [na, nb], [z, z, z])[0]
+    pw = O.functional([130], 2, [na, nb], [z, z, z])[0]
+    assert np.all(pw < 0)
+    assert np.all(np.abs(vwn / pw - 1.0) < 6.5e-3), np.abs(vwn / pw - 1.0).max()
