@@ -14,7 +14,11 @@
 // fit in the memory budget they are computed once and kept in HBM
 // ("in-core", as the reference keeps RepulsionInts in memory); otherwise
 // each build recomputes them chunk by chunk ("direct").  A build contracts
-// every quartet block with the density matrices into J and K.
+// every quartet block with the density matrices into J and K: in-core stores
+// of large quartets (>= 24 integrals on average) are split once into
+// float-float pairs and contracted per bra pair on the FP32 pipe
+// (jk_slab_kernel); the others per quartet in FP64 (jk_contract_kernel).
+// Small molecules take J from a dense Coulomb operator instead.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
