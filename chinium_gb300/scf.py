@@ -275,6 +275,8 @@ def cayley_update(C, F, nocc):
     occupied one (within 1e-3 Eh): the occupations would no longer follow the
     aufbau order, and the caller diagonalises instead."""
     m = C.shape[1]
+    if nocc == 0 or nocc == m:
+        return C.copy()  # an empty or full spin channel: no occupied-virtual block to rotate
     Co, Cv = C[:, :nocc], C[:, nocc:]
     FC = F @ C
     e_o = np.einsum("ij,ij->j", Co, FC[:, :nocc])

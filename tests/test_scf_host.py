@@ -148,3 +148,63 @@ def test_cayley_closed_form_matches_the_explicit_transform():
     want = C @ np.linalg.solve(np.eye(n) - 0.5 * K, np.eye(n) + 0.5 * K)
     np.testing.assert_allclose(got, want, atol=1e-12)
     np.testing.assert_allclose(got.T @ S @ got, np.eye(n), atol=1e-11)
+
+
+def _host_hf(monkeypatch, Z, xyz, basis, mult):
+    """Hartree-Fock through run_scf with the XC build switched off and the
+    host integrals (as in the test above)."""
+    import chinium_gb300 as cg
+    from chinium_gb300 import molecules as M
+    from chinium_gb300 import scf
+
+    class NoXC:
+        EXX = 1.0
+        type = 0
+
+        def __init__(self, spin=1):
+            pass
+
+        def Read(self, name):
+            return self
+
+    class NoXCGrid:
+        def __init__(self, n):
+            self.n = n
+
+        def build(self, xc, D, precision=0):
+            return 0.0, [np.zeros((self.n, self.n)) for _ in D]
+
+    monkeypatch.setattr(scf, "ExchangeCorrelation", NoXC)
+    xyz = np.asarray(xyz, dtype=np.float64).reshape(-1, 3)
+    b = cg.Basis(Z, xyz, basis)
+    S, T, V = scf.one_electron(b)
+    nspin = 2 if mult != 1 else 1
+    ctx = {"basis": b, "S": S, "H": T + V, "jk": scf.JK(scf.repulsion(b, 0.0)), "grid": NoXCGrid(b.nbasis),
+           "Enuc": M.nuclear_repulsion(Z, xyz), "grid_key": ("grid", nspin, "HF", "SG-1", 0.0)}
+    r = scf.run_scf(Z, xyz, basis=basis, functional="HF", mult=mult, guess="core", context=ctx,
+                    conv_energy=1e-11, jk_device="cpu")
+    assert r.converged
+    return r, S, T + V
+
+
+def test_one_electron_hartree_fock_is_the_core_eigenvalue(monkeypatch):
+    """For one electron, Coulomb and exchange cancel exactly (J = K of the
+    same spin density), so the UHF energy of the hydrogen atom is the lowest
+    eigenvalue of the core Hamiltonian in the basis: a check of the host
+    integrals' J / K, the unrestricted Fock assembly and the energy
+    expression; variationally above the exact -1/2 Eh."""
+    import scipy.linalg as sl
+    for basis in ("def2-svp", "def2-tzvp"):
+        r, S, H = _host_hf(monkeypatch, [1], [0.0, 0.0, 0.0], basis, mult=2)
+        e0 = sl.eigh(H, S, eigvals_only=True)[0]
+        assert abs(r.energy - e0) < 1e-10, (basis, r.energy, e0)
+        assert -0.5 < r.energy < -0.499
+
+
+def test_helium_hartree_fock_above_the_limit(monkeypatch):
+    """RHF of the helium atom: variationally above the numerical Hartree-Fock
+    limit, -2.8616800 Eh, and within 2 mEh of it in def2-TZVP, whose helium
+    set is 3s1p (the integrals, J - K / 2 of a two-electron closed shell and
+    the SCF together; a wrong sign or scale of J or K moves it by ~1 Eh)."""
+    r, _, _ = _host_hf(monkeypatch, [2], [0.0, 0.0, 0.0], "def2-tzvp", mult=1)
+    assert -2.8616800 < r.energy < -2.8596800, r.energy
