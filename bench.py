@@ -59,6 +59,25 @@ def workload_density(wl, nbasis):
     return [0.5 * model_density(nbasis, no, seed=k) for k, no in enumerate(wl["nocc"])]
 
 
+def max_over_ranks(t, world, device):
+    """The slowest rank's time, the whole job's clock when every rank runs an
+    independent replica (all-reduce MAX of one FP64 scalar on the process
+    group; NCCL on the GPUs, gloo in the CPU tests); world 1 returns t."""
+    if world <= 1:
+        return t
+    import torch
+    import torch.distributed as dist
+    x = torch.tensor([t], dtype=torch.float64, device=device)
+    dist.all_reduce(x, op=dist.ReduceOp.MAX)
+    return float(x.item())
+
+
+def whole_job_rate(world, units_per_rank_step, steps, t_max):
+    """Units all ranks processed per second: weak scaling, every rank handles
+    units_per_rank_step per step, over the slowest rank's time."""
+    return world * units_per_rank_step * steps / t_max
+
+
 def clocks_start(path):
     try:
         f = open(path, "w")
@@ -1017,9 +1036,7 @@ def main():
     t_dev = time_builds(torch, grid, xc, dD, dE, dV, precision, args.steps, stream)
     if world > 1:
         torch.distributed.barrier()
-        t = torch.tensor([t_dev], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_dev = float(t.item())
+    t_dev = max_over_ranks(t_dev, world, "cuda")
     clocks = clocks_stop(cp, cf, clk_path) if rank == 0 else None
 
     # end to end through the public host-buffer call: pinned D in, E and V out
@@ -1027,16 +1044,18 @@ def main():
     Vh = torch.zeros((ns, n, n), dtype=torch.float64).pin_memory()
     Eh = ctypes.c_double()
     torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         check(lib().xc_build(grid._h, xc._h, ctypes.c_void_p(Dh.data_ptr()), ns, precision, ctypes.byref(Eh),
                              ctypes.c_void_p(Vh.data_ptr())))
     torch.cuda.synchronize()
-    t_e2e = time.perf_counter() - t0
+    t_e2e = max_over_ranks(time.perf_counter() - t0, world, "cuda")
 
     G = info["npoints"]  # real points (the reference's padded blocks carry zero-weight copies)
-    value = world * G * args.steps / t_dev
-    e2e = world * G * args.steps / t_e2e
+    value = whole_job_rate(world, G, args.steps, t_dev)
+    e2e = whole_job_rate(world, G, args.steps, t_e2e)
     plain = G * plain_steps / t_plain
     peaks = measured_peaks()
 
