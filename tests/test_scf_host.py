@@ -208,3 +208,29 @@ def test_helium_hartree_fock_above_the_limit(monkeypatch):
     the SCF together; a wrong sign or scale of J or K moves it by ~1 Eh)."""
     r, _, _ = _host_hf(monkeypatch, [2], [0.0, 0.0, 0.0], "def2-tzvp", mult=1)
     assert -2.8616800 < r.energy < -2.8596800, r.energy
+
+
+def test_unrestricted_adiis_and_rotations_reach_the_diagonalisation_fixed_point(monkeypatch):
+    """UHF of the OH radical (doublet; both spin channels occupied, unequal):
+    the ADIIS start and Cayley rotations per spin reach the energy of plain
+    CDIIS with a diagonalisation every iteration."""
+    r_rot, _, _ = _host_hf(monkeypatch, [8, 1], [0, 0, 0, 0, 0, 1.83], "def2-svp", mult=2)  # defaults
+    import chinium_gb300 as cg
+    from chinium_gb300 import molecules as M
+    from chinium_gb300 import scf
+    Z, xyz = [8, 1], np.array([[0, 0, 0], [0, 0, 1.83]], dtype=np.float64)
+    b = cg.Basis(Z, xyz, "def2-svp")
+    S, T, V = scf.one_electron(b)
+
+    class NoXCGrid:
+        def build(self, xc, D, precision=0):
+            return 0.0, [np.zeros((b.nbasis, b.nbasis)) for _ in D]
+
+    ctx = {"basis": b, "S": S, "H": T + V, "jk": scf.JK(scf.repulsion(b, 0.0)), "grid": NoXCGrid(),
+           "Enuc": M.nuclear_repulsion(Z, xyz), "grid_key": ("grid", 2, "HF", "SG-1", 0.0)}
+    r_plain = scf.run_scf(Z, xyz, basis="def2-svp", functional="HF", mult=2, guess="core", context=ctx,
+                          conv_energy=1e-10, jk_device="cpu", adiis_until=0.0, rotate_below=0.0)
+    assert r_plain.converged and r_plain.timings.get("rotations", 0) == 0
+    assert r_rot.timings.get("rotations", 0) > 0
+    assert abs(r_rot.energy - r_plain.energy) < 1e-9
+    assert -75.2 < r_rot.energy < -75.1
