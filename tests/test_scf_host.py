@@ -3,6 +3,7 @@ its kept inner products against a from-scratch restatement of Pulay's
 commutator DIIS (src/DIIS/CDIIS.cpp:24-47), and the packed-pair Coulomb
 contraction used by the HBM-resident J."""
 import numpy as np
+import pytest
 
 from chinium_gb300.scf import DIIS
 
@@ -234,3 +235,62 @@ def test_unrestricted_adiis_and_rotations_reach_the_diagonalisation_fixed_point(
     assert r_rot.timings.get("rotations", 0) > 0
     assert abs(r_rot.energy - r_plain.energy) < 1e-9
     assert -75.2 < r_rot.energy < -75.1
+
+
+def _hf_atom(monkeypatch, Z, sets):
+    """RHF of a closed-shell atom in an uncontracted even-tempered basis
+    (sets: [(type, exponents)]), XC off, host integrals."""
+    import chinium_gb300 as cg
+    from chinium_gb300 import scf
+
+    class NoXC:
+        EXX = 1.0
+        type = 0
+
+        def __init__(self, spin=1):
+            pass
+
+        def Read(self, name):
+            return self
+
+    monkeypatch.setattr(scf, "ExchangeCorrelation", NoXC)
+    types, exps = [], []
+    for t, ex in sets:
+        types += [t] * len(ex)
+        exps += list(ex)
+    xyz = np.zeros((1, 3))
+    b = cg.Basis.from_shells([Z], xyz, [0] * len(types), types, [1] * len(types), exps, [1.0] * len(exps),
+                             normalize=True)
+    S, T, V = scf.one_electron(b)
+
+    class NoXCGrid:
+        def build(self, xc, D, precision=0):
+            return 0.0, [np.zeros((b.nbasis, b.nbasis)) for _ in D]
+
+    ctx = {"basis": b, "S": S, "H": T + V, "jk": scf.JK(scf.repulsion(b, 0.0)), "grid": NoXCGrid(), "Enuc": 0.0,
+           "grid_key": ("grid", 1, "HF", "SG-1", 0.0)}
+    r = scf.run_scf([Z], xyz, functional="HF", guess="core", context=ctx, conv_energy=1e-11, jk_device="cpu",
+                    max_iter=200)
+    assert r.converged
+    return r.energy
+
+
+def _even(a0, beta, k):
+    return [a0 * beta ** i for i in range(k)]
+
+
+@pytest.mark.parametrize("Z,sets,limit,window", [
+    # numerical Hartree-Fock limits of the atoms; the s (and, for neon, p)
+    # even-tempered sets reach them from above within the window
+    (2, [(0, _even(0.02, 2.2, 22))], -2.8616799956, 2e-7),
+    (4, [(0, _even(0.01, 2.0, 28))], -14.5730231683, 3e-7),
+    (10, [(0, _even(0.05, 2.0, 28)), (1, _even(0.04, 2.0, 17))], -128.5470981, 2e-6),
+])
+def test_closed_shell_atoms_reach_the_hartree_fock_limit(monkeypatch, Z, sets, limit, window):
+    """He, Be and Ne RHF in large uncontracted even-tempered s / p bases:
+    above the numerical Hartree-Fock limit (variational) and within a few
+    1e-7 Eh (He, Be) or 2e-6 Eh (Ne) of it: the host McMurchie-Davidson s and
+    p integrals, their J / K contraction and the SCF energy expression against
+    an independent physical number."""
+    E = _hf_atom(monkeypatch, Z, sets)
+    assert limit - 1e-9 < E < limit + window, (Z, E, E - limit)
