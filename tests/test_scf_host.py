@@ -294,3 +294,21 @@ def test_closed_shell_atoms_reach_the_hartree_fock_limit(monkeypatch, Z, sets, l
     an independent physical number."""
     E = _hf_atom(monkeypatch, Z, sets)
     assert limit - 1e-9 < E < limit + window, (Z, E, E - limit)
+
+
+def test_hartree_fock_energy_is_invariant_under_rigid_motion(monkeypatch):
+    """H2O / def2-TZVP (d and f shells on oxygen) rotated at random and
+    translated: the overlap matrix changes element by element but the RHF
+    energy does not (to 1e-10 Eh), which a wrong solid-harmonic transform
+    or d / f integral would break."""
+    from scipy.spatial.transform import Rotation
+    from chinium_gb300 import molecules as M
+    Z, xyz = M.h2o()
+    xyz = np.asarray(xyz, dtype=np.float64).reshape(-1, 3)
+    R = Rotation.random(random_state=3).as_matrix()
+    moved = xyz @ R.T + np.array([0.7, -1.3, 2.1])
+    r0, S0, _ = _host_hf(monkeypatch, Z, xyz, "def2-tzvp", mult=1)
+    r1, S1, _ = _host_hf(monkeypatch, Z, moved, "def2-tzvp", mult=1)
+    assert np.abs(S0 - S1).max() > 0.1
+    assert np.abs(np.linalg.eigvalsh(S0) - np.linalg.eigvalsh(S1)).max() < 1e-12
+    assert abs(r0.energy - r1.energy) < 1e-10, (r0.energy, r1.energy)
