@@ -33,10 +33,12 @@ def xc_host(tmp_path_factory):
                         "-o", exe], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
 
-    def run(ids, ns, inputs):
-        """inputs: (npoints, 3) restricted or (npoints, 7) unrestricted;
-        returns eps (npoints,) and dv (npoints, 3 or 7)."""
-        head = "%d %d %s" % (ns, len(ids), " ".join(str(i) for i in ids))
+    def run(ids, ns, inputs, mode="v"):
+        """mode "v": inputs (npoints, 3) restricted or (npoints, 7)
+        unrestricted; returns eps (npoints,) and dv (npoints, 3 or 7).
+        mode "f" (LDA / GGA): inputs (npoints, 2) or (npoints, 5); returns
+        eps and the potentials followed by the second derivatives."""
+        head = "%s %d %d %s" % (mode, ns, len(ids), " ".join(str(i) for i in ids))
         text = "".join(head + " " + " ".join("%.17g" % v for v in row) + "\n" for row in inputs)
         out = subprocess.run([exe], input=text, capture_output=True, text=True, check=True).stdout
         vals = np.array([[float(v) for v in line.split()] for line in out.strip().splitlines()])
@@ -93,6 +95,59 @@ def test_library_matches_the_oracle_on_points(xc_host, ids, ns):
         # methods' roundings and the formulas' cancellations
         assert np.quantile(err, 0.99) < 1e-10, (name, np.quantile(err, 0.99))
         assert err.max() < 1e-7, (name, err.max())
+
+
+def moderate_points(ns, n, rng):
+    """Densities 1e-3 .. 1e2 with ordinary reduced gradients: the region where
+    the oracle's second derivatives (Richardson differences of its exact
+    complex-step gradients) are accurate to ~1e-9."""
+    if ns == 1:
+        rho = 10 ** rng.uniform(-3, 2, n)
+        return np.stack([rho, rho ** (8 / 3) * 10 ** rng.uniform(-2, 1, n)], axis=1)
+    ra = 10 ** rng.uniform(-3, 2, n)
+    rb = ra * 10 ** rng.uniform(-1, 0.5, n)
+    saa = ra ** (8 / 3) * 10 ** rng.uniform(-2, 1, n)
+    sbb = rb ** (8 / 3) * 10 ** rng.uniform(-2, 1, n)
+    sab = np.sqrt(saa * sbb) * rng.uniform(-0.9, 0.9, n)
+    return np.stack([ra, rb, saa, sab, sbb], axis=1)
+
+
+# input index pairs of the second-derivative components (libxc layouts)
+PAIRS = {1: [(0, 0), (0, 1), (1, 1)],
+         2: [(0, 0), (0, 1), (1, 1)] + [(a, s) for a in (0, 1) for s in (2, 3, 4)] +
+            [(2, 2), (2, 3), (2, 4), (3, 3), (3, 4), (4, 4)]}
+
+
+@pytest.mark.parametrize("ns", [1, 2])
+@pytest.mark.parametrize("ids", [i for i in ID_SETS if O.family(i) <= 1], ids=lambda s: "+".join(map(str, s)))
+def test_library_second_derivatives_match_the_oracle(xc_host, ids, ns):
+    """The response's kernel f_xc: second-derivative jets of the library
+    against the oracle's, each component scaled by its two inputs
+    (rho^2, rho sigma, sigma^2, ...) and compared with the energy density:
+    a measure that also holds where a component vanishes identically (LYP is
+    linear in the sigmas)."""
+    rng = np.random.default_rng(12)
+    inp = moderate_points(ns, 300, rng)
+    _, out = xc_host(ids, ns, inp, mode="f")
+    npot = 2 if ns == 1 else 5
+    got = out[:, npot:].T  # (3 or 15, npoints)
+    if ns == 1:
+        ref = np.concatenate(O.functional_fxc(ids, 1, inp[:, 0], inp[:, 1]), axis=0)
+        eden = sum(np.abs(O.functional([i], 1, inp[:, 0], inp[:, 1])[0].ravel()) for i in ids) * inp[:, 0]
+    else:
+        ref = np.concatenate(O.functional_fxc(ids, 2, inp[:, 0:2].T, inp[:, 2:5].T), axis=0)
+        eden = sum(np.abs(O.functional([i], 2, inp[:, 0:2].T, inp[:, 2:5].T)[0].ravel()) for i in ids) * \
+            (inp[:, 0] + inp[:, 1])
+    u = np.abs(inp.T).copy()
+    if ns == 2:
+        u[3] = np.abs(inp[:, 3]) + np.sqrt(inp[:, 2] * inp[:, 4])  # sigma_ab's scale
+    pairs = PAIRS[ns]
+    if O.family(ids) == 0:  # LDA: v2rho2 only
+        pairs = pairs[:1] if ns == 1 else pairs[:3]
+    for k, (i, j) in enumerate(pairs):
+        err = np.abs(got[k] - ref[k]) * u[i] * u[j] / eden
+        # measured ~5e-13 at most
+        assert np.quantile(err, 0.99) < 1e-11 and err.max() < 1e-10, (k, np.quantile(err, 0.99), err.max())
 
 
 def _hydrogen():
